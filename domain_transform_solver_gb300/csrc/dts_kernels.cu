@@ -1,0 +1,613 @@
+// DTS kernels for sm_103a: guide ingest, window-bound search, the fused
+// X+Y half-step iteration, the domain-transform filter pass with the
+// confidence epilogue, and small helpers for downloads.
+//
+// Key fact used throughout: the edge weights dH, dV are >= 1
+// (sqrt(1 + nonnegative)), so a window of the reference's linear search
+// (src/domain_transform_filter.cuh:7-28) never reaches further than
+// floor(sigma)+1 pixels from its centre.  Every pass is therefore a
+// bounded-radius stencil over a tile plus halo held in shared memory: no
+// global prefix sums, no transposes, no long-row cancellation.
+#include "../../include/dtsgb.h"
+#include "color.cuh"
+#include "dtsgb_internal.cuh"
+
+namespace dtsgb {
+
+namespace {
+
+constexpr int kThreads = 256;
+// kINV255Sq, src/domain_transform_common_kernels.cuh:10 (a float constant).
+__device__ __constant__ float c_inv255sq = (float)0.0000153787;
+
+// dH / dV integrand of src/domain_transform_common_kernels.cuh:71-116:
+// sqrt(SSD4(a-b) * kINV255Sq * r * r + 1) with r = sigma_{x|y} / sigma_r,
+// evaluated in the order nvcc compiles the reference expression.
+__device__ __forceinline__ float edge_weight(uchar4 a, uchar4 b, float ratio) {
+  const int d0 = (int)a.x - (int)b.x, d1 = (int)a.y - (int)b.y;
+  const int d2 = (int)a.z - (int)b.z, d3 = (int)a.w - (int)b.w;
+  const float ssd = (float)(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3);
+  float t = __fmul_rn(ssd, c_inv255sq);
+  t = __fmul_rn(t, ratio);
+  return __fsqrt_rn(__fmaf_rn(t, ratio, 1.0f));
+}
+
+__global__ void k_color_convert_flat(uchar4* __restrict__ g, long long n,
+                                     int cs) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    g[i] = convert_pixel(g[i], cs);
+}
+
+// ---------------------------------------------------------------------------
+// Window bounds (a4).  One CTA per TWxTH tile.  Shared memory holds dH for
+// the tile rows over columns [x0-rx+1, x0+TW+rx-1) and dV for the tile
+// columns over rows [y0-ry+1, y0+TH+ry-1), rx = floor(sigma_x)+1.
+// Lower bound: the largest i < p with sum_{j=i+1..p} w(j) > sigma, else p-1.
+// Upper bound: (the smallest i > p, i < limit, with sum_{j=p+1..i} w(j) >
+// sigma) - 1, else p.  limit is W for X and min(W,H) (reference quirk) or H
+// for Y.  A negative ratio stands for an all-zero domain transform (no
+// differential computed yet): every window is the pixel itself.
+// ---------------------------------------------------------------------------
+template <int TW, int TH>
+__global__ void __launch_bounds__(kThreads)
+    k_bounds(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
+             const uchar4* __restrict__ guide, uint32_t* __restrict__ bounds,
+             float ratio_x, float ratio_y, float sig_x, float sig_y, int rx,
+             int ry, int ref_y_limit) {
+  extern __shared__ float sm[];
+  const Tile t = tiles[blockIdx.x];
+  const Inst in = insts[t.inst];
+  const int W = in.w, H = in.h, P = in.pitch;
+  const uchar4* g = guide + in.off;
+  const int DW = TW + 2 * rx - 1;
+  const int DR = TH + 2 * ry - 1;
+  float* sH = sm;            // TH x DW
+  float* sV = sm + TH * DW;  // DR x TW
+  const uchar4 zero = make_uchar4(0, 0, 0, 0);
+  for (int i = threadIdx.x; i < TH * DW; i += blockDim.x) {
+    const int r = i / DW, c = i - r * DW;
+    const int x = t.x0 - rx + 1 + c, y = t.y0 + r;
+    float w = 0.f;
+    if (x >= 0 && x < W && y < H) {
+      const uchar4 cur = g[(long long)y * P + x];
+      const uchar4 prev = x > 0 ? g[(long long)y * P + x - 1] : zero;
+      w = ratio_x < 0.f ? 0.f : edge_weight(cur, prev, ratio_x);
+    }
+    sH[i] = w;
+  }
+  for (int i = threadIdx.x; i < DR * TW; i += blockDim.x) {
+    const int r = i / TW, c = i - r * TW;
+    const int x = t.x0 + c, y = t.y0 - ry + 1 + r;
+    float w = 0.f;
+    if (x < W && y >= 0 && y < H) {
+      const uchar4 cur = g[(long long)y * P + x];
+      const uchar4 prev = y > 0 ? g[(long long)(y - 1) * P + x] : zero;
+      w = ratio_y < 0.f ? 0.f : edge_weight(cur, prev, ratio_y);
+    }
+    sV[i] = w;
+  }
+  __syncthreads();
+  const int ylim = ref_y_limit ? min(W, H) : H;
+  uint32_t* bo = bounds + in.off;
+  for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+    const int r = i / TW, c = i - r * TW;
+    const int x = t.x0 + c, y = t.y0 + r;
+    if (x >= W || y >= H) continue;
+    const float* row = sH + r * DW + (c + rx - 1);  // row[0] = dH(x)
+    int dlx = 1, dux = 0, dly = 1, duy = 0;
+    float acc = 0.f;
+    for (int k = 1; k <= rx && x - k >= 0; ++k) {
+      acc += row[1 - k];
+      if (acc > sig_x) {
+        dlx = k;
+        break;
+      }
+    }
+    acc = 0.f;
+    for (int k = 1; k <= rx && x + k < W; ++k) {
+      acc += row[k];
+      if (acc > sig_x) {
+        dux = k - 1;
+        break;
+      }
+    }
+    const float* col = sV + (r + ry - 1) * TW + c;  // col[0] = dV(y)
+    acc = 0.f;
+    for (int k = 1; k <= ry && y - k >= 0; ++k) {
+      acc += col[(1 - k) * TW];
+      if (acc > sig_y) {
+        dly = k;
+        break;
+      }
+    }
+    acc = 0.f;
+    for (int k = 1; k <= ry && y + k < ylim; ++k) {
+      acc += col[k * TW];
+      if (acc > sig_y) {
+        duy = k - 1;
+        break;
+      }
+    }
+    bo[(long long)y * P + x] = pack_bounds(dlx, dux, dly, duy);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// One solver iteration (a6/a7): the X half-step followed by the Y half-step
+// in one kernel.  A CTA owns a TWxTH output tile and stages the previous
+// iterate over the tile plus a halo of floor(sigma) on all sides.  The X
+// half-step is evaluated for the tile columns over the tile rows plus the
+// vertical halo (those rows feed the Y windows), kept in shared memory, and
+// the Y half-step writes the tile.  HBM traffic per pixel and iteration:
+// read v, t, c, bounds; write v.
+//   X: v' = v - s*(lambda*(v - B_x) + 0.5*g),
+//      g = 2*(c/n)*(v - t) (L2) or (c/n)*(v-t)/sqrt((v-t)^2 + 1e-6)
+//   Y: v' = v - s*lambda*(v - B_y)
+// (src/domain_transform_solver.cuh:12-116).  With overwrite in (0,1), the
+// target replaces v where c > overwrite before each half-step
+// (src/domain_transform_solver.cu:126-130, 160-164).
+// ---------------------------------------------------------------------------
+template <typename TS, int MODE, int TW, int TH>
+__global__ void __launch_bounds__(kThreads)
+    k_dts_iter(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
+               const float* __restrict__ vin, float* __restrict__ vout,
+               const TS* __restrict__ tgt, const TS* __restrict__ cnf,
+               const uint32_t* __restrict__ bnd, float lambda, float step,
+               float overwrite, int hx, int hy) {
+  extern __shared__ float sm[];
+  const Tile t = tiles[blockIdx.x];
+  const Inst in = insts[t.inst];
+  const int W = in.w, H = in.h, P = in.pitch;
+  const long long off = in.off;
+  const int SW = TW + 2 * hx, SR = TH + 2 * hy;
+  float* sv = sm;            // SR x SW previous iterate
+  float* sx = sm + SR * SW;  // SR x TW after the X half-step
+  const bool over = overwrite > 0.f && overwrite < 1.f;
+  const int gx0 = t.x0 - hx, gy0 = t.y0 - hy;
+  for (int i = threadIdx.x; i < SR * SW; i += blockDim.x) {
+    const int r = i / SW, c = i - r * SW;
+    const int x = gx0 + c, y = gy0 + r;
+    float v = 0.f;
+    if (x >= 0 && x < W && y >= 0 && y < H) {
+      const long long p = off + (long long)y * P + x;
+      v = __ldg(vin + p);
+      if (over && load_f(cnf + p) > overwrite) v = load_f(tgt + p);
+    }
+    sv[i] = v;
+  }
+  __syncthreads();
+  const float slam = step * lambda;
+  for (int i = threadIdx.x; i < SR * TW; i += blockDim.x) {
+    const int r = i / TW, c = i - r * TW;
+    const int x = t.x0 + c, y = gy0 + r;
+    float out = 0.f;
+    if (x < W && y >= 0 && y < H) {
+      const long long p = off + (long long)y * P + x;
+      const uint32_t b = __ldg(bnd + p);
+      // radii clamped to the staged halo: a window never reads outside it
+      const int dl = min((int)(b & 0xff), hx + 1), du = min((int)((b >> 8) & 0xff), hx);
+      const float* row = sv + r * SW + (c + hx);
+      float s = 0.f;
+      for (int k = 1 - dl; k <= du; ++k) s += row[k];
+      const float nf = (float)(dl + du);
+      const float B = __fdiv_rn(s, nf);
+      const float v = row[0];
+      const float tv = load_f(tgt + p), cv = load_f(cnf + p);
+      const float cn = __fdiv_rn(cv, nf);
+      const float d = v - tv;
+      float g;
+      if (MODE == 0) {
+        g = 2.f * cn * d;
+      } else {
+        g = __fdiv_rn(cn * d, __fsqrt_rn(__fmaf_rn(d, d, 1e-6f)));
+      }
+      out = __fmaf_rn(step, -__fmaf_rn(lambda, v - B, 0.5f * g), v);
+      if (over && cv > overwrite) out = tv;
+    }
+    sx[i] = out;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+    const int r = i / TW, c = i - r * TW;
+    const int x = t.x0 + c, y = t.y0 + r;
+    if (x >= W || y >= H) continue;
+    const long long p = off + (long long)y * P + x;
+    const uint32_t b = __ldg(bnd + p);
+    const int dl = min((int)((b >> 16) & 0xff), hy + 1), du = min((int)(b >> 24), hy);
+    const float* col = sx + (r + hy) * TW + c;
+    float s = 0.f;
+    for (int k = 1 - dl; k <= du; ++k) s += col[k * TW];
+    const float B = __fdiv_rn(s, (float)(dl + du));
+    const float v = col[0];
+    vout[p] = __fmaf_rn(-slam, v - B, v);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Filter pass (a5): X box mean then Y box mean over NCH channels sharing the
+// windows (src/domain_transform_filter.cuh:30-71).  With CONF the Y result
+// is not stored; instead the confidence epilogue of
+// src/domain_transform_solver.cu:21-44 is applied to (ch0, ch1) =
+// (DT(t), DT(t^2)).
+// ---------------------------------------------------------------------------
+template <int NCH, bool CONF, typename TS, int TW, int TH>
+__global__ void __launch_bounds__(kThreads)
+    k_filter(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
+             const float* __restrict__ in0, const float* __restrict__ in1,
+             float* __restrict__ out0, float* __restrict__ out1,
+             const uint32_t* __restrict__ bnd, int hx, int hy,
+             TS* __restrict__ conf_out, float scale, int left_clear) {
+  extern __shared__ float sm[];
+  const Tile t = tiles[blockIdx.x];
+  const Inst in = insts[t.inst];
+  const int W = in.w, H = in.h, P = in.pitch;
+  const long long off = in.off;
+  const int SW = TW + 2 * hx, SR = TH + 2 * hy;
+  float* sv[NCH];
+  float* sx[NCH];
+  for (int ch = 0; ch < NCH; ++ch) {
+    sv[ch] = sm + ch * (SR * SW + SR * TW);
+    sx[ch] = sv[ch] + SR * SW;
+  }
+  const float* src[2] = {in0, in1};
+  const int gx0 = t.x0 - hx, gy0 = t.y0 - hy;
+  for (int i = threadIdx.x; i < SR * SW; i += blockDim.x) {
+    const int r = i / SW, c = i - r * SW;
+    const int x = gx0 + c, y = gy0 + r;
+    const bool ok = x >= 0 && x < W && y >= 0 && y < H;
+    const long long p = off + (long long)y * P + x;
+#pragma unroll
+    for (int ch = 0; ch < NCH; ++ch) sv[ch][i] = ok ? __ldg(src[ch] + p) : 0.f;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < SR * TW; i += blockDim.x) {
+    const int r = i / TW, c = i - r * TW;
+    const int x = t.x0 + c, y = gy0 + r;
+    float res[NCH];
+#pragma unroll
+    for (int ch = 0; ch < NCH; ++ch) res[ch] = 0.f;
+    if (x < W && y >= 0 && y < H) {
+      const long long p = off + (long long)y * P + x;
+      const uint32_t b = __ldg(bnd + p);
+      // radii clamped to the staged halo: a window never reads outside it
+      const int dl = min((int)(b & 0xff), hx + 1), du = min((int)((b >> 8) & 0xff), hx);
+      const float nf = (float)(dl + du);
+#pragma unroll
+      for (int ch = 0; ch < NCH; ++ch) {
+        const float* row = sv[ch] + r * SW + (c + hx);
+        float s = 0.f;
+        for (int k = 1 - dl; k <= du; ++k) s += row[k];
+        res[ch] = __fdiv_rn(s, nf);
+      }
+    }
+#pragma unroll
+    for (int ch = 0; ch < NCH; ++ch) sx[ch][i] = res[ch];
+  }
+  __syncthreads();
+  float* dst[2] = {out0, out1};
+  for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+    const int r = i / TW, c = i - r * TW;
+    const int x = t.x0 + c, y = t.y0 + r;
+    if (x >= W || y >= H) continue;
+    const long long p = off + (long long)y * P + x;
+    const uint32_t b = __ldg(bnd + p);
+    const int dl = min((int)((b >> 16) & 0xff), hy + 1), du = min((int)(b >> 24), hy);
+    const float nf = (float)(dl + du);
+    float res[NCH];
+#pragma unroll
+    for (int ch = 0; ch < NCH; ++ch) {
+      const float* col = sx[ch] + (r + hy) * TW + c;
+      float s = 0.f;
+      for (int k = 1 - dl; k <= du; ++k) s += col[k * TW];
+      res[ch] = __fdiv_rn(s, nf);
+    }
+    if (CONF) {
+      float cv = 0.f;
+      if (x > left_clear) {
+        const float var = res[1] - res[0] * res[0];
+        cv = (var < 0.f || !isfinite(var)) ? 0.f : expf(-var * scale);
+      }
+      conf_out[p] = store_cast<TS>(cv);
+      // keep DT(t^2) as the filter's last result (the reference leaves it in
+      // its var buffer)
+      dst[1][p] = res[1];
+      dst[0][p] = res[0];
+    } else {
+#pragma unroll
+      for (int ch = 0; ch < NCH; ++ch) dst[ch][p] = res[ch];
+    }
+  }
+}
+
+template <typename TS>
+__global__ void k_to_float(const Inst* __restrict__ insts, int n_inst,
+                           const TS* __restrict__ src, float* __restrict__ dst,
+                           float* __restrict__ dst_sq) {
+  const Inst in = insts[blockIdx.y];
+  const long long n = (long long)in.pitch * in.h;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float v = load_f(src + in.off + i);
+    dst[in.off + i] = v;
+    if (dst_sq) dst_sq[in.off + i] = v * v;
+  }
+}
+
+template <typename TS>
+__global__ void k_from_float(const float* __restrict__ src, TS* __restrict__ dst,
+                             long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    dst[i] = store_cast<TS>(src[i]);
+}
+
+template <typename TS>
+__global__ void k_fill(TS* __restrict__ dst, long long n, float v) {
+  const TS val = store_cast<TS>(v);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    dst[i] = val;
+}
+
+__global__ void k_differential(const Inst* __restrict__ insts,
+                               const uchar4* __restrict__ guide, float ratio,
+                               int axis, float* __restrict__ out) {
+  const Inst in = insts[blockIdx.y];
+  const long long n = (long long)in.w * in.h;
+  const uchar4 zero = make_uchar4(0, 0, 0, 0);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(i / in.w), x = (int)(i - (long long)y * in.w);
+    const long long p = in.off + (long long)y * in.pitch + x;
+    const uchar4 cur = guide[p];
+    uchar4 prev = zero;
+    if (axis == 0 && x > 0) prev = guide[p - 1];
+    if (axis == 1 && y > 0) prev = guide[p - in.pitch];
+    out[p] = edge_weight(cur, prev, ratio);
+  }
+}
+
+// Row-wise inclusive prefix sum, one warp per row, Kahan-compensated carry
+// between 32-element chunks.
+__global__ void k_row_prefix(const Inst* __restrict__ insts,
+                             const float* __restrict__ in,
+                             float* __restrict__ out) {
+  const Inst I = insts[blockIdx.y];
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= I.h) return;
+  const float* src = in + I.off + (long long)warp * I.pitch;
+  float* dst = out + I.off + (long long)warp * I.pitch;
+  float carry = 0.f, comp = 0.f;
+  for (int x0 = 0; x0 < I.w; x0 += 32) {
+    const int x = x0 + lane;
+    float v = x < I.w ? src[x] : 0.f;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float n = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += n;
+    }
+    if (x < I.w) dst[x] = carry + v;
+    const float total = __shfl_sync(0xffffffffu, v, 31);
+    const float yk = total - comp;
+    const float tk = carry + yk;
+    comp = (tk - carry) - yk;
+    carry = tk;
+  }
+}
+
+__global__ void k_unpack_bounds(const Inst* __restrict__ insts,
+                                const uint32_t* __restrict__ bnd, int axis,
+                                int32_t* __restrict__ l, int32_t* __restrict__ u) {
+  const Inst in = insts[blockIdx.y];
+  const long long n = (long long)in.w * in.h;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(i / in.w), x = (int)(i - (long long)y * in.w);
+    const uint32_t b = bnd[in.off + (long long)y * in.pitch + x];
+    const int pos = axis == 0 ? x : y;
+    const int dl = axis == 0 ? (b & 0xff) : ((b >> 16) & 0xff);
+    const int du = axis == 0 ? ((b >> 8) & 0xff) : (b >> 24);
+    l[i] = pos - dl;
+    u[i] = pos + du;
+  }
+}
+
+int grid_for(long long n, int threads = kThreads) {
+  long long b = (n + threads - 1) / threads;
+  if (b > 152 * 16) b = 152 * 16;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+template <typename F>
+int set_smem(F* f, size_t bytes) {
+  if (bytes > 48 * 1024) {
+    DTSGB_CUDA(cudaFuncSetAttribute(
+        f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  }
+  return DTSGB_OK;
+}
+
+constexpr size_t kMaxSmem = 227 * 1024;
+
+}  // namespace
+
+int launch_color_convert_flat(uchar4* guide, long long n, int color_space,
+                              cudaStream_t s) {
+  if (color_space == DTSGB_RGB || n <= 0) return DTSGB_OK;
+  k_color_convert_flat<<<grid_for(n), kThreads, 0, s>>>(guide, n, color_space);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
+int launch_bounds(const DtsLaunch& L, const uchar4* guide, uint32_t* bounds,
+                  float ratio_x, float ratio_y, float sigma_x, float sigma_y,
+                  int ref_y_limit, cudaStream_t s) {
+  const int rx = (int)floorf(sigma_x) + 1, ry = (int)floorf(sigma_y) + 1;
+  if (rx > 255 || ry > 255)
+    return fail(DTSGB_ERR_UNSUPPORTED, "sigma >= 255 is not supported");
+  const int TW = kBoundsTW, TH = kBoundsTH;
+  const size_t smem =
+      sizeof(float) * ((size_t)TH * (TW + 2 * rx - 1) + (size_t)(TH + 2 * ry - 1) * TW);
+  if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "sigma too large");
+  int st = set_smem(k_bounds<TW, TH>, smem);
+  if (st) return st;
+  ProfScope ps(s, DTSGB_K_BOUNDS);
+  k_bounds<TW, TH><<<L.n_tiles, kThreads, smem, s>>>(
+      L.d_inst, L.d_tiles, guide, bounds, ratio_x, ratio_y, sigma_x, sigma_y,
+      rx, ry, ref_y_limit);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
+template <typename TS, int MODE>
+static int launch_iter_t(const DtsLaunch& L, const float* vin, float* vout,
+                         const void* target, const void* conf,
+                         const uint32_t* bounds, float lambda, float step,
+                         float overwrite, int hx, int hy, cudaStream_t s) {
+  const int TW = kIterTW, TH = kIterTH;
+  const size_t smem = sizeof(float) * ((size_t)(TH + 2 * hy) * (TW + 2 * hx) +
+                                       (size_t)(TH + 2 * hy) * TW);
+  if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "sigma_z too large");
+  int st = set_smem(k_dts_iter<TS, MODE, TW, TH>, smem);
+  if (st) return st;
+  ProfScope ps(s, DTSGB_K_DTS_ITER);
+  k_dts_iter<TS, MODE, TW, TH><<<L.n_tiles, kThreads, smem, s>>>(
+      L.d_inst, L.d_tiles, vin, vout, (const TS*)target, (const TS*)conf,
+      bounds, lambda, step, overwrite, hx, hy);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
+int launch_dts_iter(const DtsLaunch& L, Storage st, IterMode mode,
+                    const float* vin, float* vout, const void* target,
+                    const void* conf, const uint32_t* bounds, float lambda,
+                    float step, float overwrite, int hx, int hy,
+                    cudaStream_t s) {
+  if (st == Storage::F32) {
+    if (mode == IterMode::L2)
+      return launch_iter_t<float, 0>(L, vin, vout, target, conf, bounds, lambda,
+                                     step, overwrite, hx, hy, s);
+    return launch_iter_t<float, 1>(L, vin, vout, target, conf, bounds, lambda,
+                                   step, overwrite, hx, hy, s);
+  }
+  if (mode == IterMode::L2)
+    return launch_iter_t<__nv_bfloat16, 0>(L, vin, vout, target, conf, bounds,
+                                           lambda, step, overwrite, hx, hy, s);
+  return launch_iter_t<__nv_bfloat16, 1>(L, vin, vout, target, conf, bounds,
+                                         lambda, step, overwrite, hx, hy, s);
+}
+
+int launch_target_to_float(const DtsLaunch& L, Storage st, const void* src,
+                           float* dst, float* dst_sq, cudaStream_t s) {
+  dim3 grid(64, L.n_inst);
+  ProfScope ps(s, DTSGB_K_DTS_OTHER);
+  if (st == Storage::F32)
+    k_to_float<float><<<grid, kThreads, 0, s>>>(L.d_inst, L.n_inst,
+                                                 (const float*)src, dst, dst_sq);
+  else
+    k_to_float<__nv_bfloat16><<<grid, kThreads, 0, s>>>(
+        L.d_inst, L.n_inst, (const __nv_bfloat16*)src, dst, dst_sq);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
+int launch_init_var(const DtsLaunch& L, Storage st, const void* target,
+                    float* v, cudaStream_t s) {
+  return launch_target_to_float(L, st, target, v, nullptr, s);
+}
+
+int launch_storage_from_float(const Inst*, int, Storage st, const float* src,
+                              void* dst, long long n, cudaStream_t s) {
+  if (st == Storage::F32) {
+    DTSGB_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(float),
+                               cudaMemcpyDeviceToDevice, s));
+    return DTSGB_OK;
+  }
+  k_from_float<__nv_bfloat16><<<grid_for(n), kThreads, 0, s>>>(
+      src, (__nv_bfloat16*)dst, n);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
+int launch_fill_storage(Storage st, void* dst, long long n, float value,
+                        cudaStream_t s) {
+  if (st == Storage::F32)
+    k_fill<float><<<grid_for(n), kThreads, 0, s>>>((float*)dst, n, value);
+  else
+    k_fill<__nv_bfloat16><<<grid_for(n), kThreads, 0, s>>>(
+        (__nv_bfloat16*)dst, n, value);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
+template <int NCH, bool CONF, typename TS>
+static int launch_filter_t(const DtsLaunch& L, const float* in0,
+                           const float* in1, float* out0, float* out1,
+                           const uint32_t* bounds, int hx, int hy,
+                           void* conf_out, float scale, int left_clear,
+                           cudaStream_t s) {
+  const int TW = kIterTW, TH = kIterTH;
+  const size_t smem = NCH * sizeof(float) *
+                      ((size_t)(TH + 2 * hy) * (TW + 2 * hx) + (size_t)(TH + 2 * hy) * TW);
+  if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "filter sigma too large");
+  int st = set_smem(k_filter<NCH, CONF, TS, TW, TH>, smem);
+  if (st) return st;
+  ProfScope ps(s, DTSGB_K_FILTER);
+  k_filter<NCH, CONF, TS, TW, TH><<<L.n_tiles, kThreads, smem, s>>>(
+      L.d_inst, L.d_tiles, in0, in1, out0, out1, bounds, hx, hy, (TS*)conf_out,
+      scale, left_clear);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
+int launch_filter_pass(const DtsLaunch& L, int nch, const float* in0,
+                       const float* in1, float* out0, float* out1,
+                       const uint32_t* bounds, int hx, int hy, Storage st,
+                       void* conf_out, float scale, int left_clear,
+                       cudaStream_t s) {
+  if (conf_out) {
+    if (st == Storage::F32)
+      return launch_filter_t<2, true, float>(L, in0, in1, out0, out1, bounds, hx,
+                                             hy, conf_out, scale, left_clear, s);
+    return launch_filter_t<2, true, __nv_bfloat16>(L, in0, in1, out0, out1,
+                                                   bounds, hx, hy, conf_out,
+                                                   scale, left_clear, s);
+  }
+  if (nch == 2)
+    return launch_filter_t<2, false, float>(L, in0, in1, out0, out1, bounds, hx,
+                                            hy, nullptr, 0.f, 0, s);
+  return launch_filter_t<1, false, float>(L, in0, nullptr, out0, nullptr, bounds,
+                                          hx, hy, nullptr, 0.f, 0, s);
+}
+
+int launch_differential(const DtsLaunch& L, const uchar4* guide, float ratio,
+                        int axis, float* out, cudaStream_t s) {
+  k_differential<<<dim3(64, L.n_inst), kThreads, 0, s>>>(L.d_inst, guide, ratio,
+                                                         axis, out);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
+int launch_row_prefix(const Inst* h_inst, const Inst* d_inst, int n_inst,
+                      const float* in, float* out, cudaStream_t s) {
+  int max_h = 1;
+  for (int i = 0; i < n_inst; ++i) max_h = max_h > h_inst[i].h ? max_h : h_inst[i].h;
+  const int warps_per_block = kThreads / 32;
+  dim3 grid((max_h + warps_per_block - 1) / warps_per_block, n_inst);
+  k_row_prefix<<<grid, kThreads, 0, s>>>(d_inst, in, out);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
+int launch_unpack_bounds(const DtsLaunch& L, const uint32_t* bounds, int axis,
+                         int32_t* l, int32_t* u, cudaStream_t s) {
+  k_unpack_bounds<<<dim3(64, L.n_inst), kThreads, 0, s>>>(L.d_inst, bounds, axis,
+                                                          l, u);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
+}  // namespace dtsgb

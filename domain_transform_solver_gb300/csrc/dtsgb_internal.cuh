@@ -1,0 +1,152 @@
+// Internal declarations shared by the CUDA translation units of libdtsgb.
+// Nothing here is part of the public C ABI (include/dtsgb.h).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+namespace dtsgb {
+
+// ---------------------------------------------------------------------------
+// Layout of one image instance in HBM.  Every per-pixel plane of a solver
+// (guide, target, confidence, window bounds, iterates) uses the same
+// element offset and row pitch, so one descriptor addresses all of them.
+// The pitch is the width rounded up to 32 elements so that every row starts
+// on a 128-byte boundary for 4-byte planes.
+// ---------------------------------------------------------------------------
+struct Inst {
+  int w, h, pitch, pad;
+  long long off;  // element offset of pixel (0,0)
+};
+
+// One 2D tile of an instance for the tiled DTS kernels.
+struct Tile {
+  int inst, x0, y0, pad;
+};
+
+// Packed per-pixel window bounds: the window along an axis is the half-open
+// index range (p - dl, p + du], i.e. pixels p-dl+1 .. p+du, n = dl + du.
+//   bits  0- 7 dl_x, 8-15 du_x, 16-23 dl_y, 24-31 du_y
+__host__ __device__ inline uint32_t pack_bounds(int dlx, int dux, int dly,
+                                                int duy) {
+  return (uint32_t)dlx | ((uint32_t)dux << 8) | ((uint32_t)dly << 16) |
+         ((uint32_t)duy << 24);
+}
+
+// Storage types for target / confidence.
+enum class Storage : int { F32 = 0, BF16 = 1 };
+
+template <typename T>
+__device__ __forceinline__ float load_f(const T* p);
+template <>
+__device__ __forceinline__ float load_f<float>(const float* p) {
+  return __ldg(p);
+}
+template <>
+__device__ __forceinline__ float load_f<__nv_bfloat16>(const __nv_bfloat16* p) {
+  return __bfloat162float(__ldg(p));
+}
+
+template <typename T>
+__device__ __forceinline__ T store_cast(float v);
+template <>
+__device__ __forceinline__ float store_cast<float>(float v) {
+  return v;
+}
+template <>
+__device__ __forceinline__ __nv_bfloat16 store_cast<__nv_bfloat16>(float v) {
+  return __float2bfloat16_rn(v);
+}
+
+// ---------------------------------------------------------------------------
+// Status handling.
+// ---------------------------------------------------------------------------
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define DTSGB_CUDA(call)                                  \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return ::dtsgb::cuda_fail(e_, #call); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Kernel timing (profile.cu): no-ops unless enabled through the C ABI.
+// ---------------------------------------------------------------------------
+void prof_begin(cudaStream_t s, int kernel_id);
+void prof_end(cudaStream_t s, int kernel_id);
+
+struct ProfScope {
+  cudaStream_t s;
+  int id;
+  ProfScope(cudaStream_t s_, int id_) : s(s_), id(id_) { prof_begin(s, id); }
+  ~ProfScope() { prof_end(s, id); }
+};
+
+// ---------------------------------------------------------------------------
+// DTS launchers (dts_kernels.cu).  All take device pointers and a stream and
+// return a DTSGB_* status.
+// ---------------------------------------------------------------------------
+struct DtsLaunch {
+  const Inst* d_inst;   // device instance table
+  const Tile* d_tiles;  // device tile table for the tile shape in use
+  int n_tiles;
+  int n_inst;
+};
+
+// Tile shapes (compile-time in the kernels).
+constexpr int kBoundsTW = 32, kBoundsTH = 32;
+constexpr int kIterTW = 64, kIterTH = 64;
+
+int launch_color_convert(const Inst* h_inst, const Inst* d_inst, int n_inst,
+                         uchar4* guide, int color_space, cudaStream_t s);
+// in-place conversion over a flat run of n pixels (ignores pitch padding)
+int launch_color_convert_flat(uchar4* guide, long long n, int color_space,
+                              cudaStream_t s);
+
+int launch_bounds(const DtsLaunch& L, const uchar4* guide, uint32_t* bounds,
+                  float ratio_x, float ratio_y, float sigma_x, float sigma_y,
+                  int ref_y_limit, cudaStream_t s);
+
+enum class IterMode : int { L2 = 0, CHARB = 1 };
+int launch_dts_iter(const DtsLaunch& L, Storage st, IterMode mode,
+                    const float* vin, float* vout, const void* target,
+                    const void* conf, const uint32_t* bounds, float lambda,
+                    float step, float overwrite, int halo_x, int halo_y,
+                    cudaStream_t s);
+// v = target (as float), optionally overwritten nowhere: the initial iterate.
+int launch_init_var(const DtsLaunch& L, Storage st, const void* target,
+                    float* v, cudaStream_t s);
+
+// Box pass of the domain-transform filter over nch channels sharing bounds.
+// When conf_out is non-null (confidence epilogue), nch must be 2 and the
+// result written is exp(-(ch1 - ch0^2) * scale) (0 for x <= left_clear or a
+// negative / non-finite variance) into conf_out (storage st).
+int launch_filter_pass(const DtsLaunch& L, int nch, const float* in0,
+                       const float* in1, float* out0, float* out1,
+                       const uint32_t* bounds, int halo_x, int halo_y,
+                       Storage st, void* conf_out, float scale,
+                       int left_clear, cudaStream_t s);
+
+// Helpers for the filter / confidence paths.
+int launch_target_to_float(const DtsLaunch& L, Storage st, const void* src,
+                           float* dst, float* dst_sq, cudaStream_t s);
+int launch_storage_from_float(const Inst* h_inst, int n_inst, Storage st,
+                              const float* src, void* dst, long long n,
+                              cudaStream_t s);
+int launch_fill_storage(Storage st, void* dst, long long n, float value,
+                        cudaStream_t s);
+
+// Debug / download helpers.
+int launch_differential(const DtsLaunch& L, const uchar4* guide, float ratio,
+                        int axis, float* out, cudaStream_t s);
+int launch_row_prefix(const Inst* h_inst, const Inst* d_inst, int n_inst,
+                      const float* in, float* out, cudaStream_t s);
+int launch_unpack_bounds(const DtsLaunch& L, const uint32_t* bounds, int axis,
+                         int32_t* l, int32_t* u, cudaStream_t s);
+
+}  // namespace dtsgb

@@ -1,0 +1,51 @@
+// Internal HFBS declarations (not part of the C ABI).
+#pragma once
+
+#include "dtsgb_internal.cuh"
+
+namespace dtsgb {
+
+// One HFBS instance: its image plane (shared layout with the DTS planes)
+// and its bilateral grid.
+struct HInst {
+  int w, h, pitch;
+  int gx, gy, gl;
+  // pad faces written by the reference's FillGrid (g % 8 != 0 and inside
+  // the max-size allocation); they read the last fill value of the buffer
+  int cov_x, cov_y, cov_l;
+  // luma bin == gl is stored (and read back by the slice) only when the
+  // z = gl plane lies inside the allocation
+  int ovf_stored;
+  long long pix_off;    // element offset of pixel (0,0)
+  long long grid_off;   // element offset of voxel (0,0,0)
+  long long plane_off;  // element offset of the overflow count plane
+};
+
+// Solver parameters shared by a batch (HFBSGridParams minus the grid dims).
+struct HParams {
+  float sigma_x, sigma_y, sigma_l, lambda, alpha, beta;
+  int bistoch_iter_max, optim_iter_max;
+  float neg_exp_beta;
+};
+
+// Device buffers and sizes of a batch of HFBS instances.
+struct HfbsBatch {
+  const HInst* d_inst;
+  int n_inst;
+  long long max_voxels, max_pixels, max_cells, max_lines;
+  int max_gl;
+  const uchar4* guide;
+  const float* target;
+  const float* conf;
+  float* out;
+  float *count, *csum, *b, *n0, *n1, *invA, *z0, *z1, *h, *t0, *t1, *t2, *ovf;
+  // optional debug copies (single-instance class API)
+  bool keep_debug;
+  size_t grid_bytes;
+  float *dbg_norm, *dbg_blur_c, *dbg_z_init, *dbg_z_final;
+};
+
+// Enqueue the whole HFBS::Optimize sequence (splat .. slice) on a stream.
+int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s);
+
+}  // namespace dtsgb

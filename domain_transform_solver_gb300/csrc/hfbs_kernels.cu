@@ -1,0 +1,374 @@
+// HFBS kernels for sm_103a (Mazumdar et al. bilateral-grid solver as the
+// reference implements it, src/hfbs.cu:65-427).
+//
+// Every kernel handles a batch of independent instances: blockIdx.y selects
+// the instance, blockIdx.x strides over its pixels / voxels / lines (CTAs
+// past the end of a small instance exit at once).  Grids are dense
+// gx*gy*gl float arrays, x fastest.  Reads outside the interior follow the
+// reference's buffers (see hfbs_internal.cuh / the oracle): index -1 reads 0
+// (zero boundary mode), index g reads the pad value of that buffer.
+//
+// The splat is atomic-free and deterministic: one thread per spatial cell
+// walks the cell's pixels in row-major order and bins them into per-thread
+// luma histograms held in shared memory.
+#include "../../include/dtsgb.h"
+#include "dtsgb_internal.cuh"
+#include "hfbs_internal.cuh"
+
+namespace dtsgb {
+
+namespace {
+
+constexpr int kT = 256;
+
+__device__ __forceinline__ long long gidx(const HInst& I, int x, int y, int z) {
+  return I.grid_off + ((long long)z * I.gy + y) * I.gx + x;
+}
+
+// First pixel index p >= 0 with floorf(p * 1.0f / sigma) >= cell (the
+// reference's bin of pixel p, src/hfbs.cu:82-83); n if none.
+__device__ __forceinline__ int cell_start(int cell, float sigma, int n) {
+  int p = (int)ceilf((float)cell * sigma) - 2;
+  if (p < 0) p = 0;
+  if (p > n) p = n;
+  while (p < n && (int)floorf((float)p * 1.0f / sigma) < cell) ++p;
+  while (p > 0 && (int)floorf((float)(p - 1) * 1.0f / sigma) >= cell) --p;
+  return p;
+}
+
+// a12: SplatBAndC + BistochastasizeSetup (src/hfbs.cu:72-120).  Bins
+// (floor(x/sx), floor(y/sy), floor(L/sl)) with L the .x channel; sums of
+// c*t, c and 1 per bin.  Luma bin == gl lands in the overflow plane.
+__global__ void __launch_bounds__(64)
+    k_splat(const HInst* __restrict__ insts, const uchar4* __restrict__ guide,
+            const float* __restrict__ tgt, const float* __restrict__ cnf,
+            float* __restrict__ count, float* __restrict__ csum,
+            float* __restrict__ b, float* __restrict__ ovf, HParams p) {
+  extern __shared__ float sh[];
+  const HInst I = insts[blockIdx.y];
+  const int ncell = I.gx * I.gy;
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gl = I.gl;
+  // per-thread histograms: [bin][3] strided by blockDim for conflict-free use
+  float* hist = sh;
+  const int T = blockDim.x;
+  if (blockIdx.x * blockDim.x >= ncell) return;
+  for (int k = 0; k < 3 * gl; ++k) hist[k * T + threadIdx.x] = 0.f;
+  float ovf_cnt = 0.f;
+  if (cell < ncell) {
+    const int bx = cell % I.gx, by = cell / I.gx;
+    const int xs = cell_start(bx, p.sigma_x, I.w), xe = cell_start(bx + 1, p.sigma_x, I.w);
+    const int ys = cell_start(by, p.sigma_y, I.h), ye = cell_start(by + 1, p.sigma_y, I.h);
+    for (int y = ys; y < ye; ++y) {
+      const long long row = I.pix_off + (long long)y * I.pitch;
+      for (int x = xs; x < xe; ++x) {
+        const uchar4 g = guide[row + x];
+        const int bl = (int)floorf((float)g.x * 1.0f / p.sigma_l);
+        const float c = cnf[row + x];
+        const float ct = c * tgt[row + x];
+        if (bl < gl) {
+          hist[(3 * bl + 0) * T + threadIdx.x] += ct;
+          hist[(3 * bl + 1) * T + threadIdx.x] += c;
+          hist[(3 * bl + 2) * T + threadIdx.x] += 1.f;
+        } else {
+          ovf_cnt += 1.f;
+        }
+      }
+    }
+    for (int z = 0; z < gl; ++z) {
+      const long long gi = gidx(I, bx, by, z);
+      b[gi] = hist[(3 * z + 0) * T + threadIdx.x];
+      csum[gi] = hist[(3 * z + 1) * T + threadIdx.x];
+      count[gi] = hist[(3 * z + 2) * T + threadIdx.x];
+    }
+    ovf[I.plane_off + cell] = I.ovf_stored ? ovf_cnt : 0.f;
+  }
+}
+
+__global__ void k_fill_ones(const HInst* __restrict__ insts, float* __restrict__ a) {
+  const HInst I = insts[blockIdx.y];
+  const long long n = (long long)I.gx * I.gy * I.gl;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    a[I.grid_off + i] = 1.f;
+}
+
+// a13: one BistochastasizeOptimize step (src/hfbs.cu:126-155):
+// n' = sqrt(n * (count + 1e-5) / (2n + sum6 nbr n + 1e-5)).  Faces covered by
+// FillGrid read `pad`, all other out-of-grid reads 0.
+__global__ void k_bistoch(const HInst* __restrict__ insts,
+                          const float* __restrict__ src, float* __restrict__ dst,
+                          const float* __restrict__ count, float pad) {
+  const HInst I = insts[blockIdx.y];
+  const int gx = I.gx, gy = I.gy, gl = I.gl;
+  const long long n = (long long)gx * gy * gl;
+  const float px = I.cov_x ? pad : 0.f, py = I.cov_y ? pad : 0.f,
+              pz = I.cov_l ? pad : 0.f;
+  const float* s = src + I.grid_off;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % gx);
+    const long long t = i / gx;
+    const int y = (int)(t % gy), z = (int)(t / gy);
+    const long long sy = gx, sz = (long long)gx * gy;
+    const float v = s[i];
+    float nb = x > 0 ? s[i - 1] : 0.f;
+    nb += x + 1 < gx ? s[i + 1] : px;
+    nb += y > 0 ? s[i - sy] : 0.f;
+    nb += y + 1 < gy ? s[i + sy] : py;
+    nb += z > 0 ? s[i - sz] : 0.f;
+    nb += z + 1 < gl ? s[i + sz] : pz;
+    const float blurred = 2.f * v + nb;
+    const float cnt = count[I.grid_off + i];
+    dst[I.grid_off + i] =
+        __fsqrt_rn(__fdiv_rn(v * (cnt + 0.00001f), blurred + 0.00001f));
+  }
+}
+
+// a14: CalcInvDiagA (src/hfbs.cu:159-195):
+// invA = 1 / max(1e-3, lambda*(count - 2 n^2) + sum c).
+__global__ void k_inv_diag(const HInst* __restrict__ insts,
+                           const float* __restrict__ count,
+                           const float* __restrict__ csum,
+                           const float* __restrict__ norm,
+                           float* __restrict__ invA, float lambda) {
+  const HInst I = insts[blockIdx.y];
+  const long long n = (long long)I.gx * I.gy * I.gl;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long g = I.grid_off + i;
+    const float nv = norm[g];
+    const float diag = lambda * (count[g] - 2.f * nv * nv) + csum[g];
+    invA[g] = (float)(1.0 / fmax(1e-3, (double)diag));
+  }
+}
+
+// a15: Laplace sweep along one axis for two fields at once (src/hfbs.cu:
+// 355-427): d(i) = sum_j beta^|i-j| s(j), forward then backward recursion,
+// one thread per grid line.
+__global__ void k_laplace(const HInst* __restrict__ insts, int axis,
+                          const float* __restrict__ s0, float* __restrict__ d0,
+                          const float* __restrict__ s1, float* __restrict__ d1,
+                          float beta) {
+  const HInst I = insts[blockIdx.y];
+  const int gx = I.gx, gy = I.gy, gl = I.gl;
+  int len, na, nlines;
+  long long stride;
+  if (axis == 0) {
+    len = gx; stride = 1; na = gy; nlines = gy * gl;
+  } else if (axis == 1) {
+    len = gy; stride = gx; na = gx; nlines = gx * gl;
+  } else {
+    len = gl; stride = (long long)gx * gy; na = gx; nlines = gx * gy;
+  }
+  for (int line = blockIdx.x * blockDim.x + threadIdx.x; line < nlines;
+       line += gridDim.x * blockDim.x) {
+    const int a = line % na, bb = line / na;
+    long long base;
+    if (axis == 0) base = ((long long)bb * gy + a) * gx;
+    else if (axis == 1) base = (long long)bb * gx * gy + a;
+    else base = (long long)bb * gx + a;
+    base += I.grid_off;
+    for (int f = 0; f < 2; ++f) {
+      const float* s = f ? s1 : s0;
+      float* d = f ? d1 : d0;
+      float r = s[base];
+      d[base] = r;
+      for (int i = 1; i < len; ++i) {
+        r = __fmaf_rn(beta, r, s[base + i * stride]);
+        d[base + i * stride] = r;
+      }
+      r = s[base + (long long)(len - 1) * stride];
+      for (int i = len - 2; i >= 0; --i) {
+        r = beta * r;
+        d[base + i * stride] = d[base + i * stride] + r;
+        r = r + s[base + i * stride];
+      }
+    }
+  }
+}
+
+// InitZ<true> (src/hfbs.cu:337-353): z = blur(b) / (blur(c) + 1e-7); h = 0.
+__global__ void k_init_z(const HInst* __restrict__ insts,
+                         const float* __restrict__ blur_b,
+                         const float* __restrict__ blur_c, float* __restrict__ z,
+                         float* __restrict__ h) {
+  const HInst I = insts[blockIdx.y];
+  const long long n = (long long)I.gx * I.gy * I.gl;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long g = I.grid_off + i;
+    z[g] = (float)((double)blur_b[g] / ((double)blur_c[g] + 1e-7));
+    h[g] = 0.f;
+  }
+}
+
+// a16: SolveHFBS heavy-ball step (src/hfbs.cu:201-239).
+__global__ void k_solve(const HInst* __restrict__ insts,
+                        const float* __restrict__ zs, float* __restrict__ zd,
+                        float* __restrict__ h, const float* __restrict__ norm,
+                        const float* __restrict__ b,
+                        const float* __restrict__ invA, float lambda,
+                        float alpha, float beta) {
+  const HInst I = insts[blockIdx.y];
+  const int gx = I.gx, gy = I.gy, gl = I.gl;
+  const long long n = (long long)gx * gy * gl;
+  const float* z = zs + I.grid_off;
+  const float* nn = norm + I.grid_off;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % gx);
+    const long long t = i / gx;
+    const int y = (int)(t % gy), zz = (int)(t / gy);
+    const long long sy = gx, sz = (long long)gx * gy;
+    float d = 0.f;
+    if (x > 0) d += z[i - 1] * nn[i - 1];
+    if (x + 1 < gx) d += z[i + 1] * nn[i + 1];
+    if (y > 0) d += z[i - sy] * nn[i - sy];
+    if (y + 1 < gy) d += z[i + sy] * nn[i + sy];
+    if (zz > 0) d += z[i - sz] * nn[i - sz];
+    if (zz + 1 < gl) d += z[i + sz] * nn[i + sz];
+    const long long g = I.grid_off + i;
+    const float q = (b[g] + lambda * nn[i] * d) * invA[g];
+    const float zc = z[i];
+    const float grad = zc - q;
+    const float gc = fabsf(grad) > 1.345f ? copysignf(1.f, grad) : grad;
+    const float hn = __fmaf_rn(beta, h[g], gc);
+    h[g] = hn;
+    zd[g] = zc - alpha * hn;
+  }
+}
+
+// a17: SliceSolution<true> (src/hfbs.cu:246-330): count-weighted trilinear
+// interpolation of z at (x/sx, y/sy, L/sl).
+__global__ void k_slice(const HInst* __restrict__ insts,
+                        const uchar4* __restrict__ guide,
+                        const float* __restrict__ count,
+                        const float* __restrict__ ovf,
+                        const float* __restrict__ z, float* __restrict__ out,
+                        HParams p) {
+  const HInst I = insts[blockIdx.y];
+  const long long npx = (long long)I.w * I.h;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(i / I.w), x = (int)(i - (long long)y * I.w);
+    const long long pp = I.pix_off + (long long)y * I.pitch + x;
+    const float fx = (float)x * 1.0f / p.sigma_x;
+    const float fy = (float)y * 1.0f / p.sigma_y;
+    const float fz = (float)guide[pp].x * 1.0f / p.sigma_l;
+    const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
+    const float wx = fx - x0, wy = fy - y0, wz = fz - z0;
+    float num[2][2], den[2][2];
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+      for (int dy = 0; dy < 2; ++dy) {
+        float ns = 0.f, ds = 0.f;
+#pragma unroll
+        for (int dx = 0; dx < 2; ++dx) {
+          const int ix = (int)x0 + dx, iy = (int)y0 + dy, iz = (int)z0 + dz;
+          float cnt = 0.f, zv = 0.f;
+          if (ix < I.gx && iy < I.gy && iz < I.gl) {
+            const long long g = gidx(I, ix, iy, iz);
+            cnt = count[g];
+            zv = z[g];
+          } else if (ix < I.gx && iy < I.gy && iz == I.gl) {
+            cnt = ovf[I.plane_off + (long long)iy * I.gx + ix];
+          }
+          const float w = dx ? wx : 1.f - wx;
+          ns += cnt * zv * w;
+          ds += cnt * w;
+        }
+        num[dz][dy] = ns;
+        den[dz][dy] = ds;
+      }
+    const float c0 = num[0][0] * (1.f - wy) + num[0][1] * wy;
+    const float c1 = num[1][0] * (1.f - wy) + num[1][1] * wy;
+    const float c0m = den[0][0] * (1.f - wy) + den[0][1] * wy;
+    const float c1m = den[1][0] * (1.f - wy) + den[1][1] * wy;
+    out[pp] = __fdiv_rn(c0 * (1.f - wz) + c1 * wz, c0m * (1.f - wz) + c1m * wz);
+  }
+}
+
+int blocks_for(long long n) {
+  long long b = (n + kT - 1) / kT;
+  if (b > 152 * 8) b = 152 * 8;
+  return b < 1 ? 1 : (int)b;
+}
+
+}  // namespace
+
+int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
+  const int ni = B.n_inst;
+  const dim3 gv(blocks_for(B.max_voxels), ni);
+  const dim3 gp(blocks_for(B.max_pixels), ni);
+  const dim3 gc((B.max_cells + 63) / 64, ni);
+  const size_t splat_smem = sizeof(float) * 3 * (size_t)B.max_gl * 64;
+  if (splat_smem > 48 * 1024)
+    DTSGB_CUDA(cudaFuncSetAttribute(
+        k_splat, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)splat_smem));
+  prof_begin(s, DTSGB_K_HFBS_SPLAT);
+  k_splat<<<gc, 64, splat_smem, s>>>(B.d_inst, B.guide, B.target, B.conf,
+                                     B.count, B.csum, B.b, B.ovf, p);
+  DTSGB_CUDA(cudaGetLastError());
+  prof_end(s, DTSGB_K_HFBS_SPLAT);
+  // bistochastization ping-pong: even iterations read the buffer filled with
+  // ones, whose covered pad faces hold 1
+  k_fill_ones<<<gv, kT, 0, s>>>(B.d_inst, B.n0);
+  float* src = B.n0;
+  float* dst = B.n1;
+  for (int it = 0; it < p.bistoch_iter_max; ++it) {
+    prof_begin(s, DTSGB_K_HFBS_BISTOCH);
+    k_bistoch<<<gv, kT, 0, s>>>(B.d_inst, src, dst, B.count,
+                                (it % 2 == 0) ? 1.f : 0.f);
+    prof_end(s, DTSGB_K_HFBS_BISTOCH);
+    float* t = src;
+    src = dst;
+    dst = t;
+  }
+  float* norm = src;
+  float* spare = dst;
+  prof_begin(s, DTSGB_K_HFBS_OTHER);
+  k_inv_diag<<<gv, kT, 0, s>>>(B.d_inst, B.count, B.csum, norm, B.invA,
+                               p.lambda);
+  // Laplace blur of (c, b): X -> Y -> Z.
+  const dim3 gl_lines(blocks_for(B.max_lines), ni);
+  k_laplace<<<gl_lines, kT, 0, s>>>(B.d_inst, 0, B.csum, B.t0, B.b, B.t1,
+                                    p.neg_exp_beta);
+  k_laplace<<<gl_lines, kT, 0, s>>>(B.d_inst, 1, B.t0, B.t2, B.t1, spare,
+                                    p.neg_exp_beta);
+  k_laplace<<<gl_lines, kT, 0, s>>>(B.d_inst, 2, B.t2, B.t0, spare, B.t1,
+                                    p.neg_exp_beta);
+  // blur_c = t0, blur_b = t1
+  k_init_z<<<gv, kT, 0, s>>>(B.d_inst, B.t1, B.t0, B.z0, B.h);
+  prof_end(s, DTSGB_K_HFBS_OTHER);
+  if (B.keep_debug) {
+    DTSGB_CUDA(cudaMemcpyAsync(B.dbg_blur_c, B.t0, B.grid_bytes,
+                               cudaMemcpyDeviceToDevice, s));
+    DTSGB_CUDA(cudaMemcpyAsync(B.dbg_z_init, B.z0, B.grid_bytes,
+                               cudaMemcpyDeviceToDevice, s));
+    DTSGB_CUDA(cudaMemcpyAsync(B.dbg_norm, norm, B.grid_bytes,
+                               cudaMemcpyDeviceToDevice, s));
+  }
+  float* zs = B.z0;
+  float* zd = B.z1;
+  for (int it = 0; it < p.optim_iter_max; ++it) {
+    prof_begin(s, DTSGB_K_HFBS_SOLVE);
+    k_solve<<<gv, kT, 0, s>>>(B.d_inst, zs, zd, B.h, norm, B.b, B.invA, p.lambda,
+                              p.alpha, p.beta);
+    prof_end(s, DTSGB_K_HFBS_SOLVE);
+    float* t = zs;
+    zs = zd;
+    zd = t;
+  }
+  if (B.keep_debug)
+    DTSGB_CUDA(cudaMemcpyAsync(B.dbg_z_final, zs, B.grid_bytes,
+                               cudaMemcpyDeviceToDevice, s));
+  prof_begin(s, DTSGB_K_HFBS_SLICE);
+  k_slice<<<gp, kT, 0, s>>>(B.d_inst, B.guide, B.count, B.ovf, zs, B.out, p);
+  prof_end(s, DTSGB_K_HFBS_SLICE);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
+}  // namespace dtsgb

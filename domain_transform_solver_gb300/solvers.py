@@ -1,0 +1,394 @@
+"""Python mirror of the reference's solver classes over libdtsgb's C ABI.
+
+Class, method and argument names follow the reference C++ API
+(src/domain_transform_filter.h, src/domain_transform_solver.h, src/hfbs.h,
+src/edge_aware_solver.h) so a user of the reference finds the same calls:
+
+    solver = DomainTransformSolver(ImageDim(640, 480))
+    solver.SetImageDim(ImageDim(640, 480))
+    solver.ClearAll()
+    solver.InitFrame(COLOR_SPACE.YCbCr, rgba, target, confidence)
+    solver.ComputeColorSpaceDifferential(DomainFilterParams(8, 8, 0.1))
+    solver.IntegrateColorDifferentials()
+    solver.Optimize(DomainOptimizeParams(num_iterations=10, ...))
+    out = solver.Download(ImageType.OPTIMIZED_QUANTITY)
+
+Images are numpy arrays: RGBA uint8 (H, W, 4) and float32 (H, W).  Errors
+raise DtsgbError instead of printing; the HFBS "grid too large" case warns
+and copies the target to the output, like the reference.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import warnings
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import (ConfParams, DtsgbError, FilterParams, HfbsParams,
+                   OptimizeParams, check)
+
+__all__ = [
+    "ImageDim", "ImageType", "COLOR_SPACE", "RobustLoss", "DomainFilterParams",
+    "DomainFilterParamsVec1", "DomainOptimizeParams", "HFBSGridParams",
+    "DomainTransformFilter", "DomainTransformSolver", "HFBS", "DtsOptions",
+    "HfbsOptions", "Solve", "EdgeAwareOptimize", "DtsgbError",
+    "FLAG_BF16_STORAGE", "FLAG_FIX_Y_LIMIT",
+]
+
+FLAG_BF16_STORAGE = 0x1
+FLAG_FIX_Y_LIMIT = 0x2
+FLAG_FILTER_ONLY = 0x4
+
+
+@dataclass
+class ImageDim:  # src/domain_transform_common.h:7-17
+    width: int = 100
+    height: int = 200
+
+    def Transpose(self) -> "ImageDim":
+        return ImageDim(self.height, self.width)
+
+
+class ImageType(enum.IntEnum):  # src/domain_transform_common.h:20-28
+    COLOR_IMAGE = 0
+    DIFFERENTIAL = 1
+    INTEGRAL = 2
+    TARGET = 3
+    CONFIDENCE = 4
+    OPTIMIZED_QUANTITY = 5
+    TEST = 6
+
+
+class COLOR_SPACE(enum.IntEnum):  # src/domain_transform_common.h:32
+    RGB = 0
+    YCbCr = 1
+    YYY = 2
+
+
+class RobustLoss(enum.IntEnum):  # src/domain_transform_optimize.h:8
+    L1 = 0
+    L2 = 1
+    CHARBONNIER = 2
+
+
+@dataclass
+class DomainFilterParams:  # DomainFilterParamsVec<0>, filter_params.h:8-27
+    sigma_x: float = 8.0
+    sigma_y: float = 8.0
+    sigma_r: float = 0.2
+
+    def _c(self) -> FilterParams:
+        return FilterParams(self.sigma_x, self.sigma_y, self.sigma_r)
+
+
+@dataclass
+class DomainFilterParamsVec1:  # DomainFilterParamsVec<1>
+    sigma_x: float = 8.0
+    sigma_y: float = 8.0
+    sigma_r: float = 0.2
+    sigmas: list = field(default_factory=lambda: [16.0, 0.0])
+
+    def _c(self) -> ConfParams:
+        s = list(self.sigmas) + [0.0, 0.0]
+        return ConfParams(self.sigma_x, self.sigma_y, self.sigma_r,
+                          (ctypes.c_float * 2)(s[0], s[1]))
+
+
+@dataclass
+class DomainOptimizeParams:  # src/domain_transform_optimize.h:29-50
+    num_iterations: int = 3
+    loss: RobustLoss = RobustLoss.L2
+    lambda_: float = 1.0
+    sigma_z: float = 100.0
+    step_size: float = 0.99
+    photo_consis_lambda: float = 1.0
+    DT_lambda: float = 0.2
+
+    def _c(self) -> OptimizeParams:
+        return OptimizeParams(int(self.num_iterations), int(self.loss),
+                              self.lambda_, self.sigma_z, self.step_size,
+                              self.photo_consis_lambda, self.DT_lambda)
+
+
+@dataclass
+class HFBSGridParams:  # src/hfbs.h:18-60
+    sigma_x: float = 8.0
+    sigma_y: float = 8.0
+    sigma_l: float = 4.0
+    lambda_: float = 8.0
+    alpha: float = 1.0
+    beta: float = 0.9
+    bistoch_iter_max: int = 20
+    optim_iter_max: int = 140
+    neg_exp_beta: float = 0.9
+    grid_x: int = 1
+    grid_y: int = 1
+    grid_l: int = 1
+
+    def _c(self) -> HfbsParams:
+        return HfbsParams(self.sigma_x, self.sigma_y, self.sigma_l,
+                          self.lambda_, self.alpha, self.beta,
+                          int(self.bistoch_iter_max), int(self.optim_iter_max),
+                          self.neg_exp_beta, self.grid_x, self.grid_y,
+                          self.grid_l)
+
+
+def _ptr(a) -> ctypes.c_void_p | None:
+    if a is None:
+        return None
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _f32(a, shape) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.size != shape[0] * shape[1]:
+        raise ValueError(f"expected {shape[0]}x{shape[1]} floats, got {a.shape}")
+    return a
+
+
+def _rgba(a, shape) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.uint8)
+    if a.size != shape[0] * shape[1] * 4:
+        raise ValueError(f"expected {shape[0]}x{shape[1]}x4 bytes, got {a.shape}")
+    return a
+
+
+class DomainTransformFilter:
+    """src/domain_transform_filter.h:19-70."""
+
+    _flags_base = FLAG_FILTER_ONLY
+
+    def __init__(self, max_image_dims: ImageDim, flags: int = 0):
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(self._lib.dtsgb_dts_create(max_image_dims.width,
+                                         max_image_dims.height,
+                                         flags | self._flags_base,
+                                         ctypes.byref(h)))
+        self._h = h
+        self.max_image_dims_ = ImageDim(max_image_dims.width, max_image_dims.height)
+        self.image_dims_ = ImageDim(max_image_dims.width, max_image_dims.height)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.dtsgb_dts_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def SetStream(self, stream_handle: int | None) -> None:
+        check(self._lib.dtsgb_dts_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
+
+    def SetImageDim(self, image_dim: ImageDim) -> None:
+        check(self._lib.dtsgb_dts_set_image_dim(self._h, image_dim.width,
+                                                image_dim.height))
+        self.image_dims_ = ImageDim(image_dim.width, image_dim.height)
+
+    def _shape(self):
+        return (self.image_dims_.height, self.image_dims_.width)
+
+    def InitFrame(self, color_space: COLOR_SPACE, color_image) -> None:
+        rgba = _rgba(color_image, self._shape())
+        check(self._lib.dtsgb_dts_init_frame(self._h, int(color_space),
+                                             _ptr(rgba), None, None))
+
+    def Filter(self, filter_params: DomainFilterParams, input_, num_iter: int = 3):
+        inp = _f32(input_, self._shape())
+        out = np.empty(self._shape(), np.float32)
+        check(self._lib.dtsgb_dts_filter(self._h, ctypes.byref(filter_params._c()),
+                                         _ptr(inp), _ptr(out), int(num_iter)))
+        return out
+
+    def Download(self, image_type: ImageType) -> np.ndarray:
+        h, w = self._shape()
+        if int(image_type) == ImageType.COLOR_IMAGE:
+            out = np.zeros((h, w, 4), np.uint8)
+        else:
+            out = np.zeros((h, w), np.float32)
+        check(self._lib.dtsgb_dts_download(self._h, int(image_type), _ptr(out)))
+        return out
+
+    def ClearAll(self) -> None:
+        check(self._lib.dtsgb_dts_clear_all(self._h))
+
+    def ComputeColorSpaceDifferential(self, params: DomainFilterParams) -> None:
+        check(self._lib.dtsgb_dts_compute_differential(self._h, ctypes.byref(params._c())))
+
+    def IntegrateColorDifferentials(self) -> None:
+        check(self._lib.dtsgb_dts_integrate(self._h))
+
+    def DebugBounds(self, axis: int, sigma: float):
+        """Window bounds (l, u] the kernels use for one sigma (tests)."""
+        h, w = self._shape()
+        l = np.empty((h, w), np.int32)
+        u = np.empty((h, w), np.int32)
+        check(self._lib.dtsgb_dts_debug_bounds(self._h, int(axis), float(sigma),
+                                               _ptr(l), _ptr(u)))
+        return l, u
+
+
+class DomainTransformSolver(DomainTransformFilter):
+    """src/domain_transform_solver.h:34-85."""
+
+    _flags_base = 0
+
+    def InitFrame(self, color_space: COLOR_SPACE, color_image, target=None,
+                  confidence=None) -> None:
+        shape = self._shape()
+        rgba = _rgba(color_image, shape)
+        t = _f32(target, shape) if target is not None else None
+        c = _f32(confidence, shape) if confidence is not None else None
+        check(self._lib.dtsgb_dts_init_frame(self._h, int(color_space), _ptr(rgba),
+                                             _ptr(t), _ptr(c)))
+
+    def Optimize(self, optimize_params: DomainOptimizeParams,
+                 overwrite_target_above_conf: float = -1) -> None:
+        check(self._lib.dtsgb_dts_optimize(self._h, ctypes.byref(optimize_params._c()),
+                                           float(overwrite_target_above_conf)))
+
+    def ComputeConfidence(self, conf_params: DomainFilterParamsVec1,
+                          left_side_clear_width: int) -> None:
+        check(self._lib.dtsgb_dts_compute_confidence(
+            self._h, ctypes.byref(conf_params._c()), int(left_side_clear_width)))
+
+
+class HFBS:
+    """src/hfbs.h:99-150."""
+
+    def __init__(self, max_image_dims: ImageDim, max_grid_x: int,
+                 max_grid_y: int, max_grid_l: int, flags: int = 0):
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(self._lib.dtsgb_hfbs_create(max_image_dims.width,
+                                          max_image_dims.height, max_grid_x,
+                                          max_grid_y, max_grid_l, flags,
+                                          ctypes.byref(h)))
+        self._h = h
+        self.image_dim_ = ImageDim(max_image_dims.width, max_image_dims.height)
+        self.grid_params_ = HFBSGridParams()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.dtsgb_hfbs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def SetStream(self, stream_handle: int | None) -> None:
+        check(self._lib.dtsgb_hfbs_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
+
+    def _shape(self):
+        return (self.image_dim_.height, self.image_dim_.width)
+
+    def SetImageDim(self, image_dim: ImageDim) -> None:
+        check(self._lib.dtsgb_hfbs_set_image_dim(self._h, image_dim.width,
+                                                 image_dim.height))
+        self.image_dim_ = ImageDim(image_dim.width, image_dim.height)
+
+    def InitFrame(self, color_space: COLOR_SPACE, color_image, target,
+                  confidence=None) -> None:
+        shape = self._shape()
+        rgba = _rgba(color_image, shape)
+        t = _f32(target, shape)
+        c = _f32(confidence, shape) if confidence is not None else None
+        check(self._lib.dtsgb_hfbs_init_frame(self._h, int(color_space), _ptr(rgba),
+                                              _ptr(t), _ptr(c)))
+
+    def SetFilterParams(self, grid_params: HFBSGridParams) -> None:
+        self.grid_params_ = grid_params
+        check(self._lib.dtsgb_hfbs_set_filter_params(self._h,
+                                                     ctypes.byref(grid_params._c())))
+
+    def ClearAll(self) -> None:
+        check(self._lib.dtsgb_hfbs_clear_all(self._h))
+
+    def Optimize(self) -> None:
+        st = check(self._lib.dtsgb_hfbs_optimize(self._h), allow_warning=True)
+        if st == _lib.DTSGB_WARN_GRID_TOO_LARGE:
+            warnings.warn(self._lib.dtsgb_last_error().decode())
+
+    def GridDims(self):
+        gx, gy, gl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(self._lib.dtsgb_hfbs_grid_dims(self._h, ctypes.byref(gx),
+                                             ctypes.byref(gy), ctypes.byref(gl)))
+        return gx.value, gy.value, gl.value
+
+    def DebugGrid(self, which: int) -> np.ndarray:
+        gx, gy, gl = self.GridDims()
+        out = np.empty((gl, gy, gx), np.float32)
+        check(self._lib.dtsgb_hfbs_debug_grid(self._h, int(which), _ptr(out)))
+        return out
+
+    def Download(self, image_type: ImageType) -> np.ndarray:
+        out = np.zeros(self._shape(), np.float32)
+        check(self._lib.dtsgb_hfbs_download(self._h, int(image_type), _ptr(out)))
+        return out
+
+
+# ---- generic solve API, src/edge_aware_solver.h:13-90 (cv::Mat-free) -------
+@dataclass
+class DtsOptions:
+    filter_options: DomainFilterParams = field(default_factory=DomainFilterParams)
+    optim_options: DomainOptimizeParams = field(default_factory=DomainOptimizeParams)
+    conf_params: DomainFilterParamsVec1 = field(default_factory=DomainFilterParamsVec1)
+    color_space: COLOR_SPACE = COLOR_SPACE.YCbCr
+    image_dims: ImageDim = field(default_factory=ImageDim)
+    overwrite_target_above_conf: float = -1
+
+
+@dataclass
+class HfbsOptions:
+    grid_params: HFBSGridParams = field(default_factory=HFBSGridParams)
+    color_space: COLOR_SPACE = COLOR_SPACE.YCbCr
+    image_dims: ImageDim = field(default_factory=ImageDim)
+    overwrite_target_above_conf: float = -1
+
+
+def Solve(options, compute_confidence: bool, solver) -> None:
+    """Solve<DtsOptions> / Solve<HfbsOptions>, edge_aware_solver.h:37-55."""
+    if isinstance(options, DtsOptions):
+        solver.ComputeColorSpaceDifferential(options.filter_options)
+        solver.IntegrateColorDifferentials()
+        if compute_confidence:
+            solver.ComputeConfidence(options.conf_params, 0)
+        solver.Optimize(options.optim_options, options.overwrite_target_above_conf)
+    elif isinstance(options, HfbsOptions):
+        solver.Optimize()
+    else:
+        raise TypeError("options must be DtsOptions or HfbsOptions")
+
+
+def EdgeAwareOptimize(rgba_image, target_image, confidence, options, solver):
+    """EdgeAwareOptimize, edge_aware_solver.h:59-90, without OpenCV: returns
+    (solution, host wall time in ms of Solve plus the blocking Download).
+    bench.py times the solve alone with CUDA events."""
+    import time
+
+    solver.SetImageDim(options.image_dims)
+    solver.ClearAll()
+    if isinstance(solver, HFBS):
+        solver.SetFilterParams(options.grid_params)
+    solver.InitFrame(options.color_space, rgba_image, target_image, confidence)
+    t0 = time.perf_counter()
+    Solve(options, confidence is None, solver)
+    out = solver.Download(ImageType.OPTIMIZED_QUANTITY)
+    return out, (time.perf_counter() - t0) * 1e3

@@ -1,0 +1,230 @@
+/*
+ * libdtsgb -- C ABI of the GB300-native Domain Transform Solver (DTS) and
+ * Hardware-Friendly Bilateral Solver (HFBS).
+ *
+ * Every entry point returns an int status (DTSGB_OK = 0); no call prints,
+ * exits or aborts.  dtsgb_last_error() returns a description of the last
+ * failure on the calling thread.  Arguments are plain pointers and sizes:
+ *   - "host" pointers are ordinary (pageable or pinned) host memory, copied
+ *     synchronously like the reference's libcua View/CopyTo;
+ *   - "device" pointers are CUDA device memory of the current device;
+ *   - compute calls are asynchronous on the handle's stream (set with
+ *     *_set_stream; by default a stream owned by the handle), exactly like
+ *     the reference's kernel launches, and every download synchronises.
+ *
+ * Each declaration names the reference interface it replaces.  The reference
+ * paths are relative to akashbapat/domain_transform_solver.
+ */
+#ifndef DTSGB_H_
+#define DTSGB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DTSGB_API __attribute__((visibility("default")))
+
+/* ---- status codes -------------------------------------------------------*/
+#define DTSGB_OK 0
+#define DTSGB_ERR_INVALID_ARGUMENT 1 /* null handle / pointer, bad enum      */
+#define DTSGB_ERR_INVALID_DIMS 2     /* SetImageDim outside the allocation   */
+#define DTSGB_ERR_UNSUPPORTED 3      /* parameter outside the kernels' range */
+#define DTSGB_ERR_CUDA 4             /* a CUDA runtime call failed           */
+#define DTSGB_ERR_OUT_OF_MEMORY 5
+#define DTSGB_ERR_TOO_SMALL 6        /* image below the supported minimum    */
+/* HFBS grid larger than the allocation: target copied to the output
+ * (src/hfbs.cu:594-611).  A warning: the call still completed. */
+#define DTSGB_WARN_GRID_TOO_LARGE 100
+
+/* ---- enums, values identical to the reference -----------------------------
+ * ImageType    src/domain_transform_common.h:20-28
+ * COLOR_SPACE  src/domain_transform_common.h:32
+ * RobustLoss   src/domain_transform_optimize.h:8                          */
+enum {
+  DTSGB_COLOR_IMAGE = 0,
+  DTSGB_DIFFERENTIAL = 1,
+  DTSGB_INTEGRAL = 2,
+  DTSGB_TARGET = 3,
+  DTSGB_CONFIDENCE = 4,
+  DTSGB_OPTIMIZED_QUANTITY = 5,
+  DTSGB_TEST = 6
+};
+enum { DTSGB_RGB = 0, DTSGB_YCBCR = 1, DTSGB_YYY = 2 };
+enum { DTSGB_L1 = 0, DTSGB_L2 = 1, DTSGB_CHARBONNIER = 2 };
+
+/* ---- creation flags -------------------------------------------------------*/
+/* Store target and confidence as BF16 (rounded once at upload); all
+ * arithmetic stays FP32. */
+#define DTSGB_FLAG_BF16_STORAGE 0x1u
+/* Search the Y-pass window up to the image height instead of reproducing the
+ * reference's width limit (src/domain_transform_filter.cuh:22). */
+#define DTSGB_FLAG_FIX_Y_LIMIT 0x2u
+/* HFBS only: keep the filter-only (DomainTransformFilter) download set. */
+#define DTSGB_FLAG_FILTER_ONLY 0x4u
+
+/* ---- parameter structs, field order of the reference ----------------------*/
+/* DomainFilterParams = DomainFilterParamsVec<0>,
+ * src/domain_transform_filter_params.h:8-27 (sigmas[] unused at N=0). */
+typedef struct {
+  float sigma_x, sigma_y, sigma_r;
+} dtsgb_filter_params;
+
+/* DomainFilterParamsVec<1>: sigmas[0] is the confidence sigma. */
+typedef struct {
+  float sigma_x, sigma_y, sigma_r;
+  float sigmas[2];
+} dtsgb_conf_params;
+
+/* DomainOptimizeParams, src/domain_transform_optimize.h:29-50. */
+typedef struct {
+  int num_iterations;
+  int loss;
+  float lambda;
+  float sigma_z;
+  float step_size;
+  float photo_consis_lambda;
+  float DT_lambda;
+} dtsgb_optimize_params;
+
+/* HFBSGridParams, src/hfbs.h:18-60 (grid_* are outputs of optimize). */
+typedef struct {
+  float sigma_x, sigma_y, sigma_l, lambda, alpha, beta;
+  int bistoch_iter_max, optim_iter_max;
+  float neg_exp_beta;
+  int grid_x, grid_y, grid_l;
+} dtsgb_hfbs_params;
+
+DTSGB_API const char* dtsgb_last_error(void);
+DTSGB_API int dtsgb_version(void);
+
+/* ---- kernel timing (new; no reference counterpart) ------------------------
+ * When enabled, every launch of the kernels below is bracketed by CUDA
+ * events recorded on the stream it is launched on; read() synchronises on
+ * those events and returns the launch count and summed duration. */
+enum {
+  DTSGB_K_BOUNDS = 0,   /* window-bound search from the guide          */
+  DTSGB_K_DTS_ITER = 1, /* fused X+Y solver iteration                  */
+  DTSGB_K_FILTER = 2,   /* filter / confidence box pass                */
+  DTSGB_K_HFBS_SPLAT = 3,
+  DTSGB_K_HFBS_BISTOCH = 4,
+  DTSGB_K_HFBS_SOLVE = 5,
+  DTSGB_K_HFBS_OTHER = 6,
+  DTSGB_K_HFBS_SLICE = 7,
+  DTSGB_K_DTS_OTHER = 8, /* iterate init, conversions                 */
+  DTSGB_K_COUNT = 9
+};
+DTSGB_API int dtsgb_profile_enable(int enable);
+DTSGB_API int dtsgb_profile_reset(void);
+DTSGB_API int dtsgb_profile_read(int kernel_id, int* launches, double* total_ms);
+
+/* ===========================================================================
+ * DTS: DomainTransformFilter (src/domain_transform_filter.h:19-70) and
+ * DomainTransformSolver (src/domain_transform_solver.h:34-85) over one handle.
+ * ===========================================================================*/
+typedef struct dtsgb_dts_s* dtsgb_dts_t;
+
+/* DomainTransformFilter(const ImageDim&) / DomainTransformSolver(const
+ * ImageDim&): allocates every buffer at max_w x max_h. */
+DTSGB_API int dtsgb_dts_create(int max_w, int max_h, unsigned flags,
+                               dtsgb_dts_t* out);
+/* ~DomainTransformSolver */
+DTSGB_API int dtsgb_dts_destroy(dtsgb_dts_t h);
+/* (new) stream for all later work of this handle; NULL = own stream. */
+DTSGB_API int dtsgb_dts_set_stream(dtsgb_dts_t h, void* cuda_stream);
+/* SetImageDim, src/domain_transform_filter.h:31 (invalid dims: error, the
+ * previous dims stay, as the reference ignores them). */
+DTSGB_API int dtsgb_dts_set_image_dim(dtsgb_dts_t h, int width, int height);
+/* InitFrame(color_space, color_image)            filter.h:36
+ * InitFrame(color_space, color, target, conf)    solver.h:52
+ * rgba: host W*H*4 bytes; target may be NULL (filter only); confidence NULL
+ * means all ones. */
+DTSGB_API int dtsgb_dts_init_frame(dtsgb_dts_t h, int color_space,
+                                   const void* rgba, const float* target,
+                                   const float* confidence);
+/* (new) same with device pointers (dense rows, no pitch). */
+DTSGB_API int dtsgb_dts_init_frame_device(dtsgb_dts_t h, int color_space,
+                                          const void* rgba,
+                                          const float* target,
+                                          const float* confidence);
+/* ComputeColorSpaceDifferential, filter.h:53 / solver.h:57. */
+DTSGB_API int dtsgb_dts_compute_differential(dtsgb_dts_t h,
+                                             const dtsgb_filter_params* p);
+/* IntegrateColorDifferentials, filter.h:57 / solver.h:60. */
+DTSGB_API int dtsgb_dts_integrate(dtsgb_dts_t h);
+/* Filter(params, input, output, num_iter), filter.h:41: host in/out. */
+DTSGB_API int dtsgb_dts_filter(dtsgb_dts_t h, const dtsgb_filter_params* p,
+                               const float* input, float* output,
+                               int num_iter);
+/* ComputeConfidence(conf_params, left_side_clear_width), solver.h:74. */
+DTSGB_API int dtsgb_dts_compute_confidence(dtsgb_dts_t h,
+                                           const dtsgb_conf_params* p,
+                                           int left_side_clear_width);
+/* Optimize(optimize_params, overwrite_target_above_conf), solver.h:66. */
+DTSGB_API int dtsgb_dts_optimize(dtsgb_dts_t h,
+                                 const dtsgb_optimize_params* p,
+                                 float overwrite_target_above_conf);
+/* Download(image_type, image), filter.h:46 / solver.h:69: host dst.
+ * COLOR_IMAGE -> W*H*4 bytes, other types -> W*H floats. */
+DTSGB_API int dtsgb_dts_download(dtsgb_dts_t h, int image_type, void* image);
+/* (new) same into device memory (async on the handle's stream). */
+DTSGB_API int dtsgb_dts_download_device(dtsgb_dts_t h, int image_type,
+                                        void* image);
+/* ClearAll, filter.h:49 / solver.h:78. */
+DTSGB_API int dtsgb_dts_clear_all(dtsgb_dts_t h);
+/* (new, tests) window bounds the kernels use for one sigma on the current
+ * domain transform; axis 0 = X, 1 = Y.  l, u: host W*H int32 each; the
+ * window is the index range (l, u] along the axis. */
+DTSGB_API int dtsgb_dts_debug_bounds(dtsgb_dts_t h, int axis, float sigma,
+                                     int32_t* l, int32_t* u);
+/* (new, tests) colour conversion of n host RGBA pixels through the GPU. */
+DTSGB_API int dtsgb_debug_color_convert(int color_space, const void* in,
+                                        void* out, long long n);
+
+/* ===========================================================================
+ * HFBS: class HFBS, src/hfbs.h:99-150.
+ * ===========================================================================*/
+typedef struct dtsgb_hfbs_s* dtsgb_hfbs_t;
+
+/* HFBS(max_image_dims, max_grid_x, max_grid_y, max_grid_l), hfbs.h:107. */
+DTSGB_API int dtsgb_hfbs_create(int max_w, int max_h, int max_grid_x,
+                                int max_grid_y, int max_grid_l,
+                                unsigned flags, dtsgb_hfbs_t* out);
+DTSGB_API int dtsgb_hfbs_destroy(dtsgb_hfbs_t h);
+DTSGB_API int dtsgb_hfbs_set_stream(dtsgb_hfbs_t h, void* cuda_stream);
+/* SetImageDim, hfbs.h:115. */
+DTSGB_API int dtsgb_hfbs_set_image_dim(dtsgb_hfbs_t h, int width, int height);
+/* InitFrame(color_space, color_image, target, confidence), hfbs.h:121. */
+DTSGB_API int dtsgb_hfbs_init_frame(dtsgb_hfbs_t h, int color_space,
+                                    const void* rgba, const float* target,
+                                    const float* confidence);
+DTSGB_API int dtsgb_hfbs_init_frame_device(dtsgb_hfbs_t h, int color_space,
+                                           const void* rgba,
+                                           const float* target,
+                                           const float* confidence);
+/* SetFilterParams, hfbs.h:125. */
+DTSGB_API int dtsgb_hfbs_set_filter_params(dtsgb_hfbs_t h,
+                                           const dtsgb_hfbs_params* p);
+/* ClearAll, hfbs.h:129. */
+DTSGB_API int dtsgb_hfbs_clear_all(dtsgb_hfbs_t h);
+/* Optimize, hfbs.h:132.  Returns DTSGB_WARN_GRID_TOO_LARGE when the grid
+ * exceeds the allocation (the target is copied to the output). */
+DTSGB_API int dtsgb_hfbs_optimize(dtsgb_hfbs_t h);
+/* Download(image_type, image), hfbs.h:136: TARGET, CONFIDENCE,
+ * OPTIMIZED_QUANTITY (W*H floats, host). */
+DTSGB_API int dtsgb_hfbs_download(dtsgb_hfbs_t h, int image_type, float* image);
+DTSGB_API int dtsgb_hfbs_download_device(dtsgb_hfbs_t h, int image_type,
+                                         float* image);
+/* (new) grid dims of the last optimize. */
+DTSGB_API int dtsgb_hfbs_grid_dims(dtsgb_hfbs_t h, int* gx, int* gy, int* gl);
+/* (new, tests) one intermediate grid of the last optimize into host memory,
+ * gx*gy*gl floats, x fastest: 0 splat count, 1 splat of c, 2 b,
+ * 3 splat_norm, 4 inv_diag_A, 5 blurred c, 6 initial z, 7 final z. */
+DTSGB_API int dtsgb_hfbs_debug_grid(dtsgb_hfbs_t h, int which, float* dst);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DTSGB_H_ */

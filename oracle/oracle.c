@@ -1,0 +1,953 @@
+/*
+ * CPU oracle for the DTS / HFBS hot path -- TEST INFRASTRUCTURE ONLY.
+ * See oracle.h for what it is, how it is built and why parity is unpinned.
+ * Every function cites the reference file:line it restates.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define EXPORT __attribute__((visibility("default")))
+
+#if defined(ORA_REAL_IS_FLOAT)
+#define R_SQRT sqrtf
+#define R_FMA fmaf
+#define R_EXP expf
+#else
+#define R_SQRT sqrt
+#define R_FMA fma
+#define R_EXP exp
+#endif
+
+EXPORT int ora_real_bytes(void) { return (int)sizeof(REAL); }
+
+/* ======================================================================
+ * a1. Colour conversion -- src/color_space.cuh:11-40.
+ * The reference evaluates double expressions and converts to unsigned char
+ * (truncation toward zero; every value lies in [0, 255.5]).
+ *   Y  = R*0.299 + 0.587*G + 0.114*B              (color_space.cuh:19,36)
+ *   Cb = 128 - R*0.168736 - 0.331264*G + 0.5*B     (color_space.cuh:20)
+ *   Cr = 128 + R*0.5 - 0.418688*G - 0.081312*B     (color_space.cuh:21)
+ * contract selects the evaluation order:
+ *   0: every multiply and add rounded on its own;
+ *   1: nvcc's default contraction with the first product of Y fused,
+ *      Y = fma(0.114,B, fma(R,0.299, 0.587*G));
+ *   2: the same but the second product of Y fused,
+ *      Y = fma(0.114,B, fma(0.587,G, R*0.299)).
+ * Cb and Cr have one contraction order only:
+ *      Cb = fma(0.5,B, fma(-0.331264,G, fma(-R,0.168736,128)))
+ *      Cr = fma(-0.081312,B, fma(-0.418688,G, fma(R,0.5,128)))
+ * ====================================================================== */
+static double ora_y_expr(int r, int g, int b, int contract) {
+  const double R = r, G = g, B = b;
+  if (contract == 0) {
+    volatile double t1 = R * 0.299, t2 = 0.587 * G, t3 = 0.114 * B;
+    volatile double s = t1 + t2;
+    return s + t3;
+  }
+  if (contract == 1) return fma(0.114, B, fma(R, 0.299, 0.587 * G));
+  return fma(0.114, B, fma(0.587, G, R * 0.299));
+}
+static double ora_cb_expr(int r, int g, int b, int contract) {
+  const double R = r, G = g, B = b;
+  if (contract == 0) {
+    volatile double t1 = R * 0.168736, t2 = 0.331264 * G, t3 = 0.5 * B;
+    volatile double s = 128.0 - t1;
+    s = s - t2;
+    return s + t3;
+  }
+  return fma(0.5, B, fma(-0.331264, G, fma(-R, 0.168736, 128.0)));
+}
+static double ora_cr_expr(int r, int g, int b, int contract) {
+  const double R = r, G = g, B = b;
+  if (contract == 0) {
+    volatile double t1 = R * 0.5, t2 = 0.418688 * G, t3 = 0.081312 * B;
+    volatile double s = 128.0 + t1;
+    s = s - t2;
+    return s - t3;
+  }
+  return fma(-0.081312, B, fma(-0.418688, G, fma(R, 0.5, 128.0)));
+}
+static uint8_t ora_to_u8(double v) { return (uint8_t)(int)v; }
+
+EXPORT void ora_color_convert(int color_space, int contract, const uint8_t* in,
+                              uint8_t* out, int64_t n) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    const int r = in[4 * i], g = in[4 * i + 1], b = in[4 * i + 2];
+    const uint8_t a = in[4 * i + 3];
+    uint8_t o0 = (uint8_t)r, o1 = (uint8_t)g, o2 = (uint8_t)b;
+    if (color_space == ORA_YCBCR) {
+      o0 = ora_to_u8(ora_y_expr(r, g, b, contract));
+      o1 = ora_to_u8(ora_cb_expr(r, g, b, contract));
+      o2 = ora_to_u8(ora_cr_expr(r, g, b, contract));
+    } else if (color_space == ORA_YYY) {
+      o0 = o1 = o2 = ora_to_u8(ora_y_expr(r, g, b, contract));
+    }
+    out[4 * i] = o0;
+    out[4 * i + 1] = o1;
+    out[4 * i + 2] = o2;
+    out[4 * i + 3] = a;
+  }
+}
+
+/* ======================================================================
+ * DTS state: the buffers of DomainTransformFilterStruct
+ * (src/domain_transform_filter_struct.cuh:10-63) and
+ * DomainTransformSolverStruct (src/domain_transform_solver_struct.cuh:10-29),
+ * stored densely (row pitch = current width) and in natural orientation
+ * (the reference stores ct_V and the Y sums transposed; only the layout
+ * differs).
+ * ====================================================================== */
+#define ORA_MAX_OVR 16
+struct ora_dts {
+  int max_w, max_h, w, h;
+  int ref_y_limit, contract;
+  uint8_t* color;
+  REAL *dH, *dV, *ctH, *ctV, *var, *target, *conf;
+  int n_ovr;
+  int ovr_axis[ORA_MAX_OVR];
+  float ovr_sigma[ORA_MAX_OVR];
+  int32_t *ovr_l[ORA_MAX_OVR], *ovr_u[ORA_MAX_OVR];
+};
+
+static REAL* ora_alloc_real(size_t n) { return (REAL*)calloc(n, sizeof(REAL)); }
+
+EXPORT ora_dts* ora_dts_create(int max_w, int max_h) {
+  ora_dts* s = (ora_dts*)calloc(1, sizeof(ora_dts));
+  const size_t n = (size_t)max_w * max_h;
+  s->max_w = s->w = max_w;
+  s->max_h = s->h = max_h;
+  s->ref_y_limit = 1;
+  s->contract = ORA_CONTRACT_NVCC;
+  s->color = (uint8_t*)calloc(n * 4, 1);
+  s->dH = ora_alloc_real(n);
+  s->dV = ora_alloc_real(n);
+  s->ctH = ora_alloc_real(n);
+  s->ctV = ora_alloc_real(n);
+  s->var = ora_alloc_real(n);
+  s->target = ora_alloc_real(n);
+  s->conf = ora_alloc_real(n);
+  return s;
+}
+
+EXPORT void ora_dts_clear_bounds_override(ora_dts* s) {
+  for (int i = 0; i < s->n_ovr; ++i) {
+    free(s->ovr_l[i]);
+    free(s->ovr_u[i]);
+  }
+  s->n_ovr = 0;
+}
+
+EXPORT void ora_dts_destroy(ora_dts* s) {
+  if (!s) return;
+  ora_dts_clear_bounds_override(s);
+  free(s->color);
+  free(s->dH);
+  free(s->dV);
+  free(s->ctH);
+  free(s->ctV);
+  free(s->var);
+  free(s->target);
+  free(s->conf);
+  free(s);
+}
+
+EXPORT void ora_dts_set_compat(ora_dts* s, int ref_y_limit, int contract) {
+  s->ref_y_limit = ref_y_limit;
+  s->contract = contract;
+}
+
+/* DomainTransformFilter::SetImageDim -- src/domain_transform_filter.cu:114-122
+ * (invalid dims are reported and ignored). */
+EXPORT int ora_dts_set_image_dim(ora_dts* s, int w, int h) {
+  if (w > 0 && w <= s->max_w && h > 0 && h <= s->max_h) {
+    s->w = w;
+    s->h = h;
+    return 0;
+  }
+  return -1;
+}
+
+/* ClearAll -- src/domain_transform_filter.cu:202-216,
+ * src/domain_transform_solver.cu:248-255. */
+EXPORT void ora_dts_clear_all(ora_dts* s) {
+  const size_t n = (size_t)s->max_w * s->max_h;
+  memset(s->color, 0, n * 4);
+  memset(s->dH, 0, n * sizeof(REAL));
+  memset(s->dV, 0, n * sizeof(REAL));
+  memset(s->ctH, 0, n * sizeof(REAL));
+  memset(s->ctV, 0, n * sizeof(REAL));
+  memset(s->var, 0, n * sizeof(REAL));
+  memset(s->target, 0, n * sizeof(REAL));
+  memset(s->conf, 0, n * sizeof(REAL));
+}
+
+/* InitFrame -- src/domain_transform_filter.cu:18-49 and
+ * src/domain_transform_solver.cu:46-61 (confidence NULL -> all ones). */
+EXPORT void ora_dts_init_frame(ora_dts* s, int color_space, const uint8_t* rgba,
+                               const float* target, const float* confidence) {
+  const int64_t n = (int64_t)s->w * s->h;
+  ora_color_convert(color_space, s->contract, rgba, s->color, n);
+  if (target)
+    for (int64_t i = 0; i < n; ++i) s->target[i] = (REAL)target[i];
+  if (confidence) {
+    for (int64_t i = 0; i < n; ++i) s->conf[i] = (REAL)confidence[i];
+  } else {
+    const size_t nmax = (size_t)s->max_w * s->max_h;
+    for (size_t i = 0; i < nmax; ++i) s->conf[i] = 1;
+  }
+}
+
+/* a2. dHdx / dVdy -- src/domain_transform_common_kernels.cuh:71-116 and
+ * ComputeColorSpaceDifferential, src/domain_transform_filter.cu:92-110.
+ * The backward neighbour of column 0 / row 0 is read through a surface with
+ * zero boundary mode, i.e. (0,0,0,0). */
+static const float kInv255Sq = (float)0.0000153787; /* common_kernels.cuh:10 */
+
+static REAL ora_edge(const uint8_t* a, const uint8_t* b, float ratio) {
+  int ssd = 0;
+  for (int k = 0; k < 4; ++k) {
+    const int d = (int)a[k] - (int)b[k];
+    ssd += d * d;
+  }
+  REAL t = (REAL)ssd * (REAL)kInv255Sq;
+  t = t * (REAL)ratio;
+  return R_SQRT(R_FMA(t, (REAL)ratio, (REAL)1));
+}
+
+EXPORT void ora_dts_differential(ora_dts* s, float sigma_x, float sigma_y,
+                                 float sigma_r) {
+  const float rx = sigma_x / sigma_r, ry = sigma_y / sigma_r;
+  const int W = s->w, H = s->h;
+  static const uint8_t zero4[4] = {0, 0, 0, 0};
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < H; ++y) {
+    for (int x = 0; x < W; ++x) {
+      const uint8_t* cur = s->color + 4 * ((size_t)y * W + x);
+      const uint8_t* left = x > 0 ? cur - 4 : zero4;
+      const uint8_t* up = y > 0 ? cur - 4 * (size_t)W : zero4;
+      s->dH[(size_t)y * W + x] = ora_edge(cur, left, rx);
+      s->dV[(size_t)y * W + x] = ora_edge(cur, up, ry);
+    }
+  }
+}
+
+/* a3. IntegrateColorDifferentials -- src/domain_transform_filter.cu:85-90,
+ * src/domain_transform_common_functions.h:44-99: inclusive prefix sums of dH
+ * along rows (ct_H) and of dV along columns (ct_V).  The reference sums with
+ * a CUB block scan; the oracle sums sequentially. */
+static void ora_row_prefix(const REAL* in, REAL* out, int W, int H) {
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < H; ++y) {
+    REAL acc = 0;
+    for (int x = 0; x < W; ++x) {
+      acc += in[(size_t)y * W + x];
+      out[(size_t)y * W + x] = acc;
+    }
+  }
+}
+static void ora_col_prefix(const REAL* in, REAL* out, int W, int H) {
+#pragma omp parallel for schedule(static)
+  for (int x = 0; x < W; ++x) {
+    REAL acc = 0;
+    for (int y = 0; y < H; ++y) {
+      acc += in[(size_t)y * W + x];
+      out[(size_t)y * W + x] = acc;
+    }
+  }
+}
+
+EXPORT void ora_dts_integrate(ora_dts* s) {
+  ora_row_prefix(s->dH, s->ctH, s->w, s->h);
+  ora_col_prefix(s->dV, s->ctV, s->w, s->h);
+}
+
+/* a4. LinearSearchLowerAndUpperBound2DX -- src/domain_transform_filter.cuh:7-28.
+ *   lower = first i <= p (descending) with ct(p) - sigma > ct(i), else p-1;
+ *   upper = (first i >= p, i < limit, with ct(p) + sigma < ct(i)) - 1, else p.
+ * ct(i) is ct[i*stride]; n is the number of valid entries along the axis.
+ * limit may exceed n (the Y-pass quirk); entries past n read as zero in the
+ * reference's zero-filled allocation and never satisfy the upper test, so
+ * the effective limit is min(limit, n). */
+static void ora_search(const REAL* ct, size_t stride, int p, int n, int limit,
+                       REAL sigma, int32_t* lo, int32_t* up, REAL* margin) {
+  const REAL val = ct[(size_t)p * stride];
+  const REAL lthr = val - sigma, uthr = val + sigma;
+  int l = p - 1, u = p;
+  REAL m = INFINITY, d;
+  int found = 0;
+  for (int i = p; i >= 0; --i) {
+    if (lthr > ct[(size_t)i * stride]) {
+      l = i;
+      found = 1;
+      break;
+    }
+  }
+  if (found) {
+    d = lthr - ct[(size_t)l * stride];
+    if (d < m) m = d;
+    d = ct[(size_t)(l + 1) * stride] - lthr;
+    if (d < m) m = d;
+  } else {
+    d = ct[0] - lthr;
+    if (d < m) m = d;
+  }
+  const int lim = limit < n ? limit : n;
+  found = 0;
+  int i;
+  for (i = p; i < lim; ++i) {
+    if (uthr < ct[(size_t)i * stride]) {
+      u = i - 1;
+      found = 1;
+      break;
+    }
+  }
+  if (found) {
+    d = ct[(size_t)i * stride] - uthr;
+    if (d < m) m = d;
+    d = uthr - ct[(size_t)(i - 1) * stride];
+    if (d < m) m = d;
+  } else if (p < lim) {
+    d = uthr - ct[(size_t)(lim - 1) * stride];
+    if (d < m) m = d;
+  }
+  *lo = l;
+  *up = u;
+  if (margin) *margin = m;
+}
+
+static int ora_y_limit(const ora_dts* s) {
+  return s->ref_y_limit ? s->w : s->h;
+}
+
+EXPORT void ora_dts_bounds(const ora_dts* s, int axis, float sigma, int32_t* l,
+                           int32_t* u, REAL* margin) {
+  const int W = s->w, H = s->h;
+  if (axis == 0) {
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        const size_t k = (size_t)y * W + x;
+        ora_search(s->ctH + (size_t)y * W, 1, x, W, W, (REAL)sigma, l + k,
+                   u + k, margin ? margin + k : NULL);
+      }
+  } else {
+    const int lim = ora_y_limit(s);
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < W; ++x)
+      for (int y = 0; y < H; ++y) {
+        const size_t k = (size_t)y * W + x;
+        ora_search(s->ctV + x, (size_t)W, y, H, lim, (REAL)sigma, l + k, u + k,
+                   margin ? margin + k : NULL);
+      }
+  }
+}
+
+EXPORT void ora_dts_add_bounds_override(ora_dts* s, int axis, float sigma,
+                                        const int32_t* l, const int32_t* u) {
+  if (s->n_ovr >= ORA_MAX_OVR) return;
+  const size_t n = (size_t)s->w * s->h;
+  const int k = s->n_ovr++;
+  s->ovr_axis[k] = axis;
+  s->ovr_sigma[k] = sigma;
+  s->ovr_l[k] = (int32_t*)malloc(n * sizeof(int32_t));
+  s->ovr_u[k] = (int32_t*)malloc(n * sizeof(int32_t));
+  memcpy(s->ovr_l[k], l, n * sizeof(int32_t));
+  memcpy(s->ovr_u[k], u, n * sizeof(int32_t));
+}
+
+/* Bounds for one pass: the override for (axis, sigma) if present, else the
+ * reference search.  Caller frees. */
+static void ora_pass_bounds(const ora_dts* s, int axis, float sigma,
+                            int32_t** l, int32_t** u) {
+  const size_t n = (size_t)s->w * s->h;
+  *l = (int32_t*)malloc(n * sizeof(int32_t));
+  *u = (int32_t*)malloc(n * sizeof(int32_t));
+  for (int k = 0; k < s->n_ovr; ++k) {
+    if (s->ovr_axis[k] == axis && s->ovr_sigma[k] == sigma) {
+      memcpy(*l, s->ovr_l[k], n * sizeof(int32_t));
+      memcpy(*u, s->ovr_u[k], n * sizeof(int32_t));
+      return;
+    }
+  }
+  ora_dts_bounds(s, axis, sigma, *l, *u, NULL);
+}
+
+/* Window mean (S(u) - S(l)) / (u - l) over a prefix sum S along one axis;
+ * S(-1) reads the slot before the row in the reference (pitch padding); the
+ * oracle defines it as 0. */
+static REAL ora_window_mean(const REAL* S, size_t stride, int l, int u) {
+  const REAL su = S[(size_t)u * stride];
+  const REAL sl = l >= 0 ? S[(size_t)l * stride] : (REAL)0;
+  return (su - sl) / (REAL)(u - l);
+}
+
+/* a5. FilterX / FilterY -- src/domain_transform_filter.cuh:30-71. */
+static void ora_box_pass(const ora_dts* s, int axis, const REAL* in, REAL* out,
+                         const int32_t* l, const int32_t* u) {
+  const int W = s->w, H = s->h;
+  const size_t n = (size_t)W * H;
+  REAL* S = ora_alloc_real(n);
+  if (axis == 0) {
+    ora_row_prefix(in, S, W, H);
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        const size_t k = (size_t)y * W + x;
+        out[k] = ora_window_mean(S + (size_t)y * W, 1, l[k], u[k]);
+      }
+  } else {
+    ora_col_prefix(in, S, W, H);
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        const size_t k = (size_t)y * W + x;
+        out[k] = ora_window_mean(S + x, (size_t)W, l[k], u[k]);
+      }
+  }
+  free(S);
+}
+
+/* DomainTransformFilter::Filter -- src/domain_transform_filter.cu:124-188:
+ * recompute the DT for these sigmas, then num_iter x {X box, Y box} with the
+ * sigma schedule: iteration 0 unscaled, iteration i>=1 scaled by
+ * 3*2^(N-i-1)/sqrt(4^N-1) (computed in double, stored as float). */
+static void ora_filter_buffers(ora_dts* s, float sx, float sy, float sr,
+                               const REAL* in, REAL* out, int num_iter) {
+  ora_dts_differential(s, sx, sy, sr);
+  ora_dts_integrate(s);
+  const size_t n = (size_t)s->w * s->h;
+  REAL* a = ora_alloc_real(n);
+  REAL* b = ora_alloc_real(n);
+  memcpy(a, in, n * sizeof(REAL));
+  for (int it = 0; it < num_iter; ++it) {
+    float sig_x = sx, sig_y = sy;
+    if (it != 0) {
+      const float mult = (float)(3 * pow(2.0, (double)(num_iter - (it + 1))) /
+                                 sqrt(pow(4.0, (double)num_iter) - 1));
+      sig_x *= mult;
+      sig_y *= mult;
+    }
+    int32_t *l, *u;
+    ora_pass_bounds(s, 0, sig_x, &l, &u);
+    ora_box_pass(s, 0, a, b, l, u);
+    free(l);
+    free(u);
+    ora_pass_bounds(s, 1, sig_y, &l, &u);
+    ora_box_pass(s, 1, b, a, l, u);
+    free(l);
+    free(u);
+  }
+  memcpy(s->var, a, n * sizeof(REAL));
+  memcpy(out, a, n * sizeof(REAL));
+  free(a);
+  free(b);
+}
+
+EXPORT void ora_dts_filter(ora_dts* s, float sx, float sy, float sr,
+                           const float* in, REAL* out, int num_iter) {
+  const size_t n = (size_t)s->w * s->h;
+  REAL* tmp = ora_alloc_real(n);
+  for (size_t i = 0; i < n; ++i) tmp[i] = (REAL)in[i];
+  ora_filter_buffers(s, sx, sy, sr, tmp, out, num_iter);
+  free(tmp);
+}
+
+/* a8. ComputeConfidence -- src/domain_transform_solver.cu:206-246 and
+ * ComputeConfidenceKernel :21-44.  conf = exp(-(DT(t^2)-DT(t)^2)*0.5/s0^2)
+ * for x > left_clear (so column 0 is always cleared), 0 when the variance is
+ * negative or not finite.  The two Filter calls leave the DT of the
+ * confidence sigmas in place for any later Optimize. */
+EXPORT void ora_dts_compute_confidence(ora_dts* s, float sx, float sy, float sr,
+                                       float sigma0, int left_clear) {
+  const int W = s->w, H = s->h;
+  const size_t n = (size_t)W * H;
+  REAL* dtz = ora_alloc_real(n);
+  REAL* sq = ora_alloc_real(n);
+  REAL* dtz2 = ora_alloc_real(n);
+  ora_filter_buffers(s, sx, sy, sr, s->target, dtz, 3);
+  for (size_t i = 0; i < n; ++i) sq[i] = s->target[i] * s->target[i];
+  ora_filter_buffers(s, sx, sy, sr, sq, dtz2, 3);
+  const float scale = 0.5f / (sigma0 * sigma0);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const size_t k = (size_t)y * W + x;
+      REAL c = 0;
+      if (x > left_clear) {
+        const REAL var = dtz2[k] - dtz[k] * dtz[k];
+        c = (var < 0 || !isfinite(var)) ? (REAL)0 : R_EXP(-var * (REAL)scale);
+      }
+      s->conf[k] = c;
+    }
+  free(dtz);
+  free(sq);
+  free(dtz2);
+}
+
+/* a6/a7. DomainTransformSolver::Optimize -- src/domain_transform_solver.cu:
+ * 100-202 with OptimizeX / OptimizeY, src/domain_transform_solver.cuh:12-116.
+ *   X: v' = v - s*(lambda*(v - B_x) + 0.5*g),
+ *      g = 2*(c/n)*(v-t)                  (L2)
+ *      g = (c/n)*(v-t)/sqrt((v-t)^2+1e-6) (Charbonnier)
+ *   Y: v' = v - s*lambda*(v - B_y)
+ * sigma is sigma_z in every iteration (kDMIter = 1).  RobustLoss::L1 has no
+ * kernel in either switch, so the result stays the target.  With
+ * overwrite in (0,1) the target is copied over v where c > overwrite before
+ * each half-step (CopyVariableFlagGreaterThanThresh, common_kernels.cuh:36-50).
+ */
+EXPORT void ora_dts_optimize(ora_dts* s, int num_iterations, int loss,
+                             float lambda, float sigma_z, float step,
+                             float overwrite) {
+  const int W = s->w, H = s->h;
+  const size_t n = (size_t)W * H;
+  REAL* v = ora_alloc_real(n);
+  REAL* S = ora_alloc_real(n);
+  memcpy(v, s->target, n * sizeof(REAL));
+  const int do_over = overwrite > 0 && overwrite < 1;
+  if (loss != ORA_L2 && loss != ORA_CHARBONNIER) {
+    memcpy(s->var, v, n * sizeof(REAL));
+    free(v);
+    free(S);
+    return;
+  }
+  int32_t *lx, *ux, *ly, *uy;
+  ora_pass_bounds(s, 0, sigma_z, &lx, &ux);
+  ora_pass_bounds(s, 1, sigma_z, &ly, &uy);
+  const REAL lam = lambda, st = step;
+  for (int it = 0; it < num_iterations; ++it) {
+    if (do_over)
+      for (size_t k = 0; k < n; ++k)
+        if (s->conf[k] > (REAL)overwrite) v[k] = s->target[k];
+    ora_row_prefix(v, S, W, H);
+    REAL* vx = ora_alloc_real(n);
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y) {
+      for (int x = 0; x < W; ++x) {
+        const size_t k = (size_t)y * W + x;
+        const int l = lx[k], u = ux[k];
+        const REAL B = ora_window_mean(S + (size_t)y * W, 1, l, u);
+        const REAL cn = s->conf[k] / (REAL)(u - l);
+        const REAL d = v[k] - s->target[k];
+        REAL g;
+        if (loss == ORA_L2)
+          g = 2 * cn * d;
+        else
+          g = cn * d / R_SQRT(d * d + (REAL)0.000001);
+        const REAL stepv = -(lam * (v[k] - B) + (REAL)0.5 * g);
+        vx[k] = v[k] + st * stepv;
+      }
+    }
+    memcpy(v, vx, n * sizeof(REAL));
+    free(vx);
+    if (do_over)
+      for (size_t k = 0; k < n; ++k)
+        if (s->conf[k] > (REAL)overwrite) v[k] = s->target[k];
+    ora_col_prefix(v, S, W, H);
+    REAL* vy = ora_alloc_real(n);
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        const size_t k = (size_t)y * W + x;
+        const REAL B = ora_window_mean(S + x, (size_t)W, ly[k], uy[k]);
+        vy[k] = v[k] + st * (-(lam * (v[k] - B)));
+      }
+    memcpy(v, vy, n * sizeof(REAL));
+    free(vy);
+  }
+  memcpy(s->var, v, n * sizeof(REAL));
+  free(lx);
+  free(ux);
+  free(ly);
+  free(uy);
+  free(v);
+  free(S);
+}
+
+/* Download -- src/domain_transform_filter.cu:51-74 and
+ * src/domain_transform_solver.cu:63-87. */
+EXPORT void ora_dts_download(const ora_dts* s, int type, void* dst) {
+  const size_t n = (size_t)s->w * s->h;
+  switch (type) {
+    case ORA_COLOR_IMAGE:
+      memcpy(dst, s->color, n * 4);
+      break;
+    case ORA_DIFFERENTIAL:
+      memcpy(dst, s->dH, n * sizeof(REAL));
+      break;
+    case ORA_INTEGRAL:
+      memcpy(dst, s->ctH, n * sizeof(REAL));
+      break;
+    case ORA_TARGET:
+      memcpy(dst, s->target, n * sizeof(REAL));
+      break;
+    case ORA_CONFIDENCE:
+      memcpy(dst, s->conf, n * sizeof(REAL));
+      break;
+    case ORA_OPTIMIZED_QUANTITY:
+      memcpy(dst, s->var, n * sizeof(REAL));
+      break;
+    default:
+      break;
+  }
+}
+
+/* ======================================================================
+ * HFBS -- src/hfbs.h:18-150, src/hfbs.cu:17-759.
+ * Grids are dense gx*gy*gl (x fastest).  Reads outside the interior follow
+ * the reference's buffers:
+ *  - index -1 on any axis: surface read with zero boundary mode -> 0;
+ *  - index g on an axis (the pad plane): FillGrid (hfbs.cu:33-61) writes
+ *    pad planes only where its 8^3-block launch reaches them, i.e. when
+ *    g % 8 != 0 and the plane lies inside the max-size allocation; such a
+ *    "covered" face holds the last fill value of that buffer.  In the
+ *    bistochastization ping-pong (hfbs.cu:644-662) the source is `scratch`
+ *    (filled with 1) on even iterations and `splat_norm` (filled with 0) on
+ *    odd ones, so covered faces read 1 on even iterations, 0 otherwise.
+ *    Every other pad read in the solve and slice is 0;
+ *  - bins with luma bin == gl (sigma_l dividing 255) land in the z = gl pad
+ *    plane of the splat buffers (if inside the allocation) and are read back
+ *    only by the slice.
+ * ====================================================================== */
+struct ora_hfbs {
+  int max_w, max_h, max_gx, max_gy, max_gl, w, h;
+  int contract;
+  ora_hfbs_params p;
+  uint8_t* color;
+  REAL *target, *conf, *optim;
+  int gx, gy, gl;
+  REAL* grids[ORA_G_COUNT];
+  REAL* overflow_count; /* gx*gy, the z = gl plane of splat_sum */
+};
+
+EXPORT ora_hfbs* ora_hfbs_create(int max_w, int max_h, int max_gx, int max_gy,
+                                 int max_gl) {
+  ora_hfbs* s = (ora_hfbs*)calloc(1, sizeof(ora_hfbs));
+  const size_t n = (size_t)max_w * max_h;
+  s->max_w = s->w = max_w;
+  s->max_h = s->h = max_h;
+  s->max_gx = max_gx;
+  s->max_gy = max_gy;
+  s->max_gl = max_gl;
+  s->contract = ORA_CONTRACT_NVCC;
+  /* HFBSGridParams defaults, src/hfbs.h:18-60. */
+  s->p.sigma_x = 8.0f;
+  s->p.sigma_y = 8.0f;
+  s->p.sigma_l = 4.0f;
+  s->p.lambda = 8.0f;
+  s->p.alpha = 1.0f;
+  s->p.beta = 0.9f;
+  s->p.bistoch_iter_max = 20;
+  s->p.optim_iter_max = 140;
+  s->p.neg_exp_beta = 0.9f;
+  s->p.grid_x = s->p.grid_y = s->p.grid_l = 1;
+  s->color = (uint8_t*)calloc(n * 4, 1);
+  s->target = ora_alloc_real(n);
+  s->conf = ora_alloc_real(n);
+  s->optim = ora_alloc_real(n);
+  return s;
+}
+
+static void ora_hfbs_free_grids(ora_hfbs* s) {
+  for (int i = 0; i < ORA_G_COUNT; ++i) {
+    free(s->grids[i]);
+    s->grids[i] = NULL;
+  }
+  free(s->overflow_count);
+  s->overflow_count = NULL;
+}
+
+EXPORT void ora_hfbs_destroy(ora_hfbs* s) {
+  if (!s) return;
+  ora_hfbs_free_grids(s);
+  free(s->color);
+  free(s->target);
+  free(s->conf);
+  free(s->optim);
+  free(s);
+}
+
+EXPORT void ora_hfbs_set_compat(ora_hfbs* s, int contract) {
+  s->contract = contract;
+}
+
+/* HFBS::SetImageDim -- src/hfbs.cu:527-538. */
+EXPORT int ora_hfbs_set_image_dim(ora_hfbs* s, int w, int h) {
+  if (h > s->max_h || w > s->max_w) return -1;
+  s->w = w;
+  s->h = h;
+  return 0;
+}
+
+EXPORT void ora_hfbs_set_params(ora_hfbs* s, const ora_hfbs_params* p) {
+  s->p = *p;
+}
+
+/* HFBS::ClearAll -- src/hfbs.cu:745-759. */
+EXPORT void ora_hfbs_clear_all(ora_hfbs* s) {
+  const size_t n = (size_t)s->max_w * s->max_h;
+  memset(s->color, 0, n * 4);
+  memset(s->target, 0, n * sizeof(REAL));
+  memset(s->conf, 0, n * sizeof(REAL));
+  memset(s->optim, 0, n * sizeof(REAL));
+}
+
+/* HFBS::InitFrame -- src/hfbs.cu:498-525, 540-553. */
+EXPORT void ora_hfbs_init_frame(ora_hfbs* s, int color_space,
+                                const uint8_t* rgba, const float* target,
+                                const float* confidence) {
+  const int64_t n = (int64_t)s->w * s->h;
+  ora_color_convert(color_space, s->contract, rgba, s->color, n);
+  if (target)
+    for (int64_t i = 0; i < n; ++i) s->target[i] = (REAL)target[i];
+  if (confidence) {
+    for (int64_t i = 0; i < n; ++i) s->conf[i] = (REAL)confidence[i];
+  } else {
+    const size_t nmax = (size_t)s->max_w * s->max_h;
+    for (size_t i = 0; i < nmax; ++i) s->conf[i] = 1;
+  }
+}
+
+#define GI(x, y, z) (((size_t)(z) * gy + (y)) * gx + (x))
+
+/* Laplace sweeps -- src/hfbs.cu:355-427: along one axis,
+ *   forward  r = s(0); d(0) = r; r = s(i) + beta*r; d(i) = r
+ *   backward r = s(g-1); r = beta*r; d(i) += r; r += s(i)  (i = g-2 .. 0)
+ * i.e. d(i) = sum_j beta^|i-j| s(j). */
+static void ora_laplace(const REAL* src, REAL* dst, int gx, int gy, int gl,
+                        int axis, REAL beta) {
+  const int len = axis == 0 ? gx : (axis == 1 ? gy : gl);
+  const size_t stride = axis == 0 ? 1 : (axis == 1 ? (size_t)gx : (size_t)gx * gy);
+  const int na = axis == 0 ? gy : gx, nb = axis == 2 ? gy : gl;
+#pragma omp parallel for schedule(static)
+  for (int bidx = 0; bidx < nb; ++bidx)
+    for (int aidx = 0; aidx < na; ++aidx) {
+      size_t base;
+      if (axis == 0) base = GI(0, aidx, bidx);
+      else if (axis == 1) base = GI(aidx, 0, bidx);
+      else base = GI(aidx, bidx, 0);
+      REAL r = src[base];
+      dst[base] = r;
+      for (int i = 1; i < len; ++i) {
+        r = R_FMA(beta, r, src[base + i * stride]);
+        dst[base + i * stride] = r;
+      }
+      r = src[base + (size_t)(len - 1) * stride];
+      for (int i = len - 2; i >= 0; --i) {
+        r = beta * r;
+        dst[base + i * stride] = dst[base + i * stride] + r;
+        r = r + src[base + i * stride];
+      }
+    }
+}
+
+/* HFBS::Optimize -- src/hfbs.cu:586-743. */
+EXPORT int ora_hfbs_optimize(ora_hfbs* s) {
+  const int W = s->w, H = s->h;
+  ora_hfbs_params* p = &s->p;
+  /* grid sizes, hfbs.cu:589-591 (float division for x/y, double for l) */
+  p->grid_x = (int)ceilf((float)W / p->sigma_x);
+  p->grid_y = (int)ceilf((float)H / p->sigma_y);
+  p->grid_l = (int)ceil(255.0 / (double)p->sigma_l);
+  const int gx = p->grid_x, gy = p->grid_y, gl = p->grid_l;
+  s->gx = gx;
+  s->gy = gy;
+  s->gl = gl;
+  ora_hfbs_free_grids(s);
+  if (gx > s->max_gx || gy > s->max_gy || gl > s->max_gl) {
+    /* hfbs.cu:594-611: report and copy target to the output. */
+    memcpy(s->optim, s->target, (size_t)W * H * sizeof(REAL));
+    return 1;
+  }
+  const size_t ng = (size_t)gx * gy * gl;
+  for (int i = 0; i < ORA_G_COUNT; ++i) s->grids[i] = ora_alloc_real(ng);
+  s->overflow_count = ora_alloc_real((size_t)gx * gy);
+  REAL* count = s->grids[ORA_G_SPLAT_SUM];
+  REAL* csum = s->grids[ORA_G_SPLAT_C];
+  REAL* b = s->grids[ORA_G_B];
+  REAL* norm = s->grids[ORA_G_SPLAT_NORM];
+  REAL* invA = s->grids[ORA_G_INV_DIAG_A];
+  REAL* blur_c = s->grids[ORA_G_BLUR_C];
+  REAL* zinit = s->grids[ORA_G_Z_INIT];
+  REAL* zfin = s->grids[ORA_G_Z_FINAL];
+  const int ovf_stored = gl < s->max_gl;
+
+  /* a12. SplatBAndC + BistochastasizeSetup, hfbs.cu:72-120 (nearest bin;
+   * bin of luma from the .x channel). */
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const size_t k = (size_t)y * W + x;
+      const int bx = (int)floorf((float)x * 1.0f / p->sigma_x);
+      const int by = (int)floorf((float)y * 1.0f / p->sigma_y);
+      const int bl = (int)floorf((float)s->color[4 * k] * 1.0f / p->sigma_l);
+      const REAL c = s->conf[k];
+      const REAL ct = c * s->target[k];
+      if (bl < gl) {
+        const size_t g = GI(bx, by, bl);
+        b[g] += ct;
+        csum[g] += c;
+        count[g] += 1;
+      } else if (ovf_stored) {
+        s->overflow_count[(size_t)by * gx + bx] += 1;
+      }
+    }
+
+  /* a13. bistochastization, hfbs.cu:126-155 and :644-666. */
+  const int cov_x = (gx % 8 != 0) && (gx < s->max_gx);
+  const int cov_y = (gy % 8 != 0) && (gy < s->max_gy);
+  const int cov_l = (gl % 8 != 0) && (gl < s->max_gl);
+  REAL* src = ora_alloc_real(ng);
+  REAL* dst = ora_alloc_real(ng);
+  for (size_t i = 0; i < ng; ++i) src[i] = 1;
+  for (int it = 0; it < p->bistoch_iter_max; ++it) {
+    const REAL pad = (it % 2 == 0) ? (REAL)1 : (REAL)0;
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < gl; ++z)
+      for (int y = 0; y < gy; ++y)
+        for (int x = 0; x < gx; ++x) {
+          REAL nb = 0;
+          nb += x > 0 ? src[GI(x - 1, y, z)] : (REAL)0;
+          nb += x + 1 < gx ? src[GI(x + 1, y, z)] : (cov_x ? pad : (REAL)0);
+          nb += y > 0 ? src[GI(x, y - 1, z)] : (REAL)0;
+          nb += y + 1 < gy ? src[GI(x, y + 1, z)] : (cov_y ? pad : (REAL)0);
+          nb += z > 0 ? src[GI(x, y, z - 1)] : (REAL)0;
+          nb += z + 1 < gl ? src[GI(x, y, z + 1)] : (cov_l ? pad : (REAL)0);
+          const REAL v = src[GI(x, y, z)];
+          const REAL blurred = 2 * v + nb;
+          dst[GI(x, y, z)] =
+              R_SQRT(v * (count[GI(x, y, z)] + (REAL)0.00001f) /
+                     (blurred + (REAL)0.00001f));
+        }
+    REAL* t = src;
+    src = dst;
+    dst = t;
+  }
+  memcpy(norm, src, ng * sizeof(REAL));
+
+  /* a14. CalcInvDiagA, hfbs.cu:159-195 (the splat of c was saved in
+   * inv_diag_A by BistochastasizeSetup). */
+  for (size_t i = 0; i < ng; ++i) {
+    const REAL diag = (REAL)p->lambda * (count[i] - 2 * norm[i] * norm[i]) + csum[i];
+    const REAL m = diag > (REAL)1e-3 ? diag : (REAL)1e-3;
+    invA[i] = (REAL)1 / m;
+  }
+
+  /* a15. Laplace blur of c (-> blur_c) and of b (-> z), InitZ<true>,
+   * hfbs.cu:676-719. */
+  const REAL nb_beta = p->neg_exp_beta;
+  ora_laplace(csum, dst, gx, gy, gl, 0, nb_beta);
+  ora_laplace(dst, src, gx, gy, gl, 1, nb_beta);
+  ora_laplace(src, blur_c, gx, gy, gl, 2, nb_beta);
+  ora_laplace(b, dst, gx, gy, gl, 0, nb_beta);
+  ora_laplace(dst, src, gx, gy, gl, 1, nb_beta);
+  ora_laplace(src, zinit, gx, gy, gl, 2, nb_beta);
+  for (size_t i = 0; i < ng; ++i) zinit[i] = zinit[i] / (blur_c[i] + (REAL)1e-7);
+
+  /* a16. SolveHFBS heavy-ball iterations, hfbs.cu:201-239 and :720-732.
+   * Neighbours outside the interior read 0. */
+  REAL* h = ora_alloc_real(ng);
+  REAL* zs = src;
+  REAL* zd = dst;
+  memcpy(zs, zinit, ng * sizeof(REAL));
+  const REAL lam = p->lambda, beta = p->beta, alpha = p->alpha;
+  for (int it = 0; it < p->optim_iter_max; ++it) {
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < gl; ++z)
+      for (int y = 0; y < gy; ++y)
+        for (int x = 0; x < gx; ++x) {
+          REAL d = 0;
+          if (x > 0) d += zs[GI(x - 1, y, z)] * norm[GI(x - 1, y, z)];
+          if (x + 1 < gx) d += zs[GI(x + 1, y, z)] * norm[GI(x + 1, y, z)];
+          if (y > 0) d += zs[GI(x, y - 1, z)] * norm[GI(x, y - 1, z)];
+          if (y + 1 < gy) d += zs[GI(x, y + 1, z)] * norm[GI(x, y + 1, z)];
+          if (z > 0) d += zs[GI(x, y, z - 1)] * norm[GI(x, y, z - 1)];
+          if (z + 1 < gl) d += zs[GI(x, y, z + 1)] * norm[GI(x, y, z + 1)];
+          const size_t g = GI(x, y, z);
+          const REAL q = (b[g] + lam * norm[g] * d) * invA[g];
+          const REAL zc = zs[g];
+          const REAL grad = zc - q;
+          const REAL gc = fabs((double)grad) > 1.345 ? (grad > 0 ? (REAL)1 : (REAL)-1)
+                                                     : grad;
+          const REAL hn = beta * h[g] + gc;
+          h[g] = hn;
+          zd[g] = zc - alpha * hn;
+        }
+    REAL* t = zs;
+    zs = zd;
+    zd = t;
+  }
+  memcpy(zfin, zs, ng * sizeof(REAL));
+  free(h);
+  free(src);
+  free(dst);
+
+  /* a17. SliceSolution<true>, hfbs.cu:246-330: count-weighted trilinear
+   * interpolation; positions and weights in float as in the reference. */
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const size_t k = (size_t)y * W + x;
+      const float fxp = (float)x * 1.0f / p->sigma_x;
+      const float fyp = (float)y * 1.0f / p->sigma_y;
+      const float fzp = (float)s->color[4 * k] * 1.0f / p->sigma_l;
+      const float x0 = floorf(fxp), y0 = floorf(fyp), z0 = floorf(fzp);
+      const REAL wx = (REAL)(fxp - x0), wy = (REAL)(fyp - y0), wz = (REAL)(fzp - z0);
+      REAL num[2][2], den[2][2];
+      for (int dz = 0; dz < 2; ++dz)
+        for (int dy = 0; dy < 2; ++dy) {
+          REAL nsum = 0, dsum = 0;
+          for (int dx = 0; dx < 2; ++dx) {
+            const int ix = (int)x0 + dx, iy = (int)y0 + dy, iz = (int)z0 + dz;
+            REAL cnt = 0, zv = 0;
+            if (ix < gx && iy < gy && iz < gl) {
+              cnt = count[GI(ix, iy, iz)];
+              zv = zfin[GI(ix, iy, iz)];
+            } else if (ix < gx && iy < gy && iz == gl && ovf_stored) {
+              cnt = s->overflow_count[(size_t)iy * gx + ix];
+            }
+            const REAL wxx = dx ? wx : (REAL)1 - wx;
+            nsum += cnt * zv * wxx;
+            dsum += cnt * wxx;
+          }
+          num[dz][dy] = nsum;
+          den[dz][dy] = dsum;
+        }
+      const REAL c0 = num[0][0] * ((REAL)1 - wy) + num[0][1] * wy;
+      const REAL c1 = num[1][0] * ((REAL)1 - wy) + num[1][1] * wy;
+      const REAL c0m = den[0][0] * ((REAL)1 - wy) + den[0][1] * wy;
+      const REAL c1m = den[1][0] * ((REAL)1 - wy) + den[1][1] * wy;
+      s->optim[k] = (c0 * ((REAL)1 - wz) + c1 * wz) / (c0m * ((REAL)1 - wz) + c1m * wz);
+    }
+  return 0;
+}
+
+/* HFBS::Download -- src/hfbs.cu:555-576. */
+EXPORT void ora_hfbs_download(const ora_hfbs* s, int type, REAL* dst) {
+  const size_t n = (size_t)s->w * s->h;
+  switch (type) {
+    case ORA_TARGET:
+      memcpy(dst, s->target, n * sizeof(REAL));
+      break;
+    case ORA_CONFIDENCE:
+      memcpy(dst, s->conf, n * sizeof(REAL));
+      break;
+    case ORA_OPTIMIZED_QUANTITY:
+      memcpy(dst, s->optim, n * sizeof(REAL));
+      break;
+    default:
+      break;
+  }
+}
+
+EXPORT void ora_hfbs_grid_dims(const ora_hfbs* s, int* gx, int* gy, int* gl) {
+  *gx = s->gx;
+  *gy = s->gy;
+  *gl = s->gl;
+}
+
+EXPORT void ora_hfbs_grid(const ora_hfbs* s, int which, REAL* dst) {
+  if (which < 0 || which >= ORA_G_COUNT || !s->grids[which]) return;
+  memcpy(dst, s->grids[which], (size_t)s->gx * s->gy * s->gl * sizeof(REAL));
+}

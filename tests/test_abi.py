@@ -1,0 +1,35 @@
+"""CPU checks of the drop-in boundary: libdtsgb.so builds for sm_103a, loads
+without a GPU, and exports every entry point include/dtsgb.h declares.  No
+compute call is made here."""
+import ctypes
+
+from domain_transform_solver_gb300 import _lib
+
+
+def test_header_declares_the_reference_surface():
+    names = set(_lib.declared_symbols())
+    for n in ["dtsgb_dts_create", "dtsgb_dts_init_frame", "dtsgb_dts_optimize",
+              "dtsgb_dts_filter", "dtsgb_dts_compute_confidence",
+              "dtsgb_dts_download", "dtsgb_dts_clear_all",
+              "dtsgb_dts_set_image_dim", "dtsgb_dts_compute_differential",
+              "dtsgb_dts_integrate", "dtsgb_hfbs_create", "dtsgb_hfbs_init_frame",
+              "dtsgb_hfbs_set_filter_params", "dtsgb_hfbs_optimize",
+              "dtsgb_hfbs_download", "dtsgb_hfbs_clear_all",
+              "dtsgb_hfbs_set_image_dim", "dtsgb_last_error"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(dts):
+    lib = ctypes.CDLL(str(_lib.LIB_PATH))
+    missing = [n for n in _lib.declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_error_string_before_any_call(dts):
+    lib = _lib.load()
+    assert lib.dtsgb_version() >= 1
+    # a null handle is rejected without touching the GPU
+    assert lib.dtsgb_dts_set_image_dim(None, 10, 10) == _lib.DTSGB_ERR_INVALID_ARGUMENT
+    assert b"null" in lib.dtsgb_last_error()
+    assert lib.dtsgb_hfbs_optimize(None) == _lib.DTSGB_ERR_INVALID_ARGUMENT
+    assert lib.dtsgb_dts_create(0, 10, 0, None) == _lib.DTSGB_ERR_INVALID_ARGUMENT

@@ -1,0 +1,97 @@
+"""GPU parity of the HFBS path against the FP64 oracle, through the C ABI."""
+import warnings
+
+import numpy as np
+import pytest
+
+import parity as P
+
+pytestmark = pytest.mark.gpu
+
+PARAMS = dict(sigma_x=8.0, sigma_y=8.0, sigma_l=16.0, lambda_=8.0, alpha=1.0,
+              beta=0.9, bistoch_iter_max=20, optim_iter_max=64, neg_exp_beta=0.9)
+
+
+def _run(D, rgba, t, c, cs, params, max_grid):
+    h, w = t.shape
+    s = D.HFBS(D.ImageDim(w, h), *max_grid)
+    s.SetImageDim(D.ImageDim(w, h))
+    s.SetFilterParams(D.HFBSGridParams(**params))
+    s.ClearAll()
+    s.InitFrame(D.COLOR_SPACE(cs), rgba, t, c)
+    s.Optimize()
+    return s.Download(D.ImageType.OPTIMIZED_QUANTITY), s
+
+
+def _parity(D, O, rgba, t, c, cs, params, max_grid):
+    out, s = _run(D, rgba, t, c, cs, params, max_grid)
+    ref, o, st = O.hfbs_solve(rgba, t, c, cs, params, max_grid=max_grid)
+    assert st == 0
+    assert s.GridDims() == o.grid_dims()
+    # bin assignment is integer work: counts bit-exact
+    assert np.array_equal(s.DebugGrid(0), o.grid("splat_sum").astype(np.float32))
+    for k, name in ((1, "splat_c"), (2, "b"), (3, "splat_norm"), (4, "inv_diag_A"),
+                    (7, "z_final")):
+        g, r = s.DebugGrid(k), o.grid(name)
+        scale = max(1.0, float(np.abs(r).max()))
+        assert np.abs(g - r).max() <= 1e-4 * scale, name
+    rng_t = P.target_range(t)
+    fin = np.isfinite(ref)
+    assert np.array_equal(np.isfinite(out), fin)
+    err = np.abs(out[fin] - ref[fin])
+    assert err.max() <= P.TOL_REL * rng_t, (err.max(), rng_t)
+    return out
+
+
+def test_cfg1_colorization_u_and_v(gpu_ready, oracle_mod):
+    from domain_transform_solver_gb300 import workloads as W
+    u, v = W.colorization_instance()
+    _parity(gpu_ready, oracle_mod, u.rgba, u.target, u.confidence, 0, PARAMS,
+            (80, 60, 16))
+    _parity(gpu_ready, oracle_mod, u.rgba, v, u.confidence, 0, PARAMS, (96, 96, 32))
+
+
+@pytest.mark.parametrize("w,h,sl,mg", [
+    (70, 30, 40.0, (64, 64, 64)),     # covered pad faces on x, y, l
+    (64, 64, 16.0, (8, 8, 16)),       # grid equal to the allocation
+    (50, 20, 15.0, (64, 64, 64)),     # luma bin 17 = gl stored in the pad plane
+    (50, 20, 15.0, (64, 64, 17)),     # ... or dropped (NaN slices, like the ref)
+    (9, 300, 8.0, (8, 64, 64)),
+    (333, 7, 25.0, (64, 8, 16)),
+])
+def test_pad_and_overflow_quirks(gpu_ready, oracle_mod, w, h, sl, mg):
+    rng = np.random.default_rng(w * h)
+    g = rng.integers(0, 256, (h, w, 4)).astype(np.uint8)
+    g[..., 3] = 255
+    g[0, :5, 0] = 255
+    t = rng.uniform(-0.5, 0.5, (h, w)).astype(np.float32)
+    c = (rng.random((h, w)) < 0.4).astype(np.float32)
+    p = dict(PARAMS, sigma_l=sl, bistoch_iter_max=9, optim_iter_max=17)
+    _parity(gpu_ready, oracle_mod, g, t, c, 0, p, mg)
+
+
+def test_ycbcr_depth_default_confidence(gpu_ready, oracle_mod):
+    from domain_transform_solver_gb300 import workloads as W
+    inst = W.depth_sr_instance(21, 320, 240, n_poly=15)
+    _parity(gpu_ready, oracle_mod, inst.rgba, (inst.target - 5) * 12.8, None, 1,
+            dict(PARAMS, optim_iter_max=40), (40, 30, 16))
+
+
+def test_grid_too_large_copies_target(gpu_ready):
+    D = gpu_ready
+    rng = np.random.default_rng(3)
+    g = rng.integers(0, 256, (32, 64, 4)).astype(np.uint8)
+    t = rng.random((32, 64)).astype(np.float32)
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        out, _ = _run(D, g, t, None, 0, PARAMS, (4, 4, 16))
+    assert any("too large" in str(x.message) for x in w)
+    assert np.array_equal(out, t)
+
+
+def test_deterministic(gpu_ready):
+    from domain_transform_solver_gb300 import workloads as W
+    u, v = W.colorization_instance()
+    a, _ = _run(gpu_ready, u.rgba, u.target, u.confidence, 0, PARAMS, (80, 60, 16))
+    b, _ = _run(gpu_ready, u.rgba, u.target, u.confidence, 0, PARAMS, (80, 60, 16))
+    assert np.array_equal(a, b)
