@@ -116,6 +116,19 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_hfbs_download_device": ([vp, i, vp], i),
         "dtsgb_hfbs_grid_dims": ([vp, P(i), P(i), P(i)], i),
         "dtsgb_hfbs_debug_grid": ([vp, i, vp], i),
+        "dtsgb_profile_enable": ([i], i),
+        "dtsgb_profile_reset": ([], i),
+        "dtsgb_profile_read": ([i, P(i), P(ctypes.c_double)], i),
+        "dtsgb_batch_create": ([i, P(i), P(i), u, pvp], i),
+        "dtsgb_batch_destroy": ([vp], i),
+        "dtsgb_batch_set_stream": ([vp, vp], i),
+        "dtsgb_batch_use_graphs": ([vp, i], i),
+        "dtsgb_batch_upload": ([vp, i, pvp, pvp, pvp], i),
+        "dtsgb_batch_upload_device": ([vp, i, pvp, pvp, pvp], i),
+        "dtsgb_batch_solve_dts": ([vp, P(FilterParams), P(OptimizeParams), f], i),
+        "dtsgb_batch_solve_hfbs": ([vp, P(HfbsParams)], i),
+        "dtsgb_batch_download": ([vp, i, pvp], i),
+        "dtsgb_batch_download_device": ([vp, i, pvp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name, None)

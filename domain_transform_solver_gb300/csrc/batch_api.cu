@@ -1,0 +1,512 @@
+// Batched DTS / HFBS over many images of uneven size (C ABI in
+// include/dtsgb.h).  All instances live in one arena: plane k of instance i
+// starts at element offset off_i (rows pitched to 32 elements), and every
+// kernel launch covers every instance through the instance and tile tables,
+// so a solve costs the same number of launches for 1 or 1000 images.  The
+// fixed launch sequence of each solve can be captured as a CUDA graph and
+// replayed (the iteration counts are fixed and nothing depends on data).
+//
+// HFBS instances of a batch behave like HFBS objects whose max grid exceeds
+// their grid on every axis (as in the reference's CLIs): pad faces of axes
+// with g % 8 != 0 are covered, and the luma-overflow plane is stored.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/dtsgb.h"
+#include "dtsgb_internal.cuh"
+#include "hfbs_internal.cuh"
+
+using namespace dtsgb;
+
+namespace {
+
+struct Graph {
+  cudaGraphExec_t exec = nullptr;
+  std::vector<char> key;
+};
+
+template <typename T>
+void key_append(std::vector<char>& k, const T& v) {
+  const char* p = reinterpret_cast<const char*>(&v);
+  k.insert(k.end(), p, p + sizeof(T));
+}
+
+enum { HG_COUNT = 0, HG_CSUM, HG_B, HG_N0, HG_N1, HG_INVA, HG_Z0, HG_Z1, HG_H,
+       HG_T0, HG_T1, HG_T2, HG_NUM };
+
+}  // namespace
+
+struct dtsgb_batch_s {
+  int n = 0;
+  unsigned flags = 0;
+  Storage st = Storage::F32;
+  int ref_y = 1;
+  std::vector<Inst> inst;
+  long long total = 0;
+  int max_w = 0, max_h = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  uchar4* guide = nullptr;
+  void* target = nullptr;
+  void* conf = nullptr;
+  uint32_t* bounds = nullptr;
+  float* v[2] = {nullptr, nullptr};
+  float* hout = nullptr;
+  float* scratch = nullptr;
+  Inst* d_inst = nullptr;
+  Tile* d_tb = nullptr;
+  Tile* d_ti = nullptr;
+  int ntb = 0, nti = 0;
+  int dts_res = -1;
+  bool hfbs_done = false;
+  bool use_graphs = true;
+  Graph g_dts, g_hfbs;
+  std::vector<HInst> hinst;
+  HInst* d_hinst = nullptr;
+  float* hg[HG_NUM] = {};
+  long long gcap = 0;
+  float* ovf = nullptr;
+  long long ocap = 0;
+
+  size_t tsize() const { return st == Storage::F32 ? 4 : 2; }
+};
+
+namespace {
+
+void drop_graph(dtsgb_batch_t b, Graph& g) {
+  if (g.exec) {
+    cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+  }
+  prof_drop_captured(&g);
+  g.key.clear();
+}
+
+void batch_free(dtsgb_batch_t b) {
+  drop_graph(b, b->g_dts);
+  drop_graph(b, b->g_hfbs);
+  dfree(b->guide);
+  dfree(b->target);
+  dfree(b->conf);
+  dfree(b->bounds);
+  dfree(b->v[0]);
+  dfree(b->v[1]);
+  dfree(b->hout);
+  dfree(b->scratch);
+  dfree(b->d_inst);
+  dfree(b->d_tb);
+  dfree(b->d_ti);
+  dfree(b->d_hinst);
+  for (auto& p : b->hg) dfree(p);
+  dfree(b->ovf);
+  if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+  b->stream = nullptr;
+}
+
+// Run `enqueue` directly, or through the solve's CUDA graph (captured on the
+// first call with this key, replayed afterwards).
+template <typename F>
+int run_graph(dtsgb_batch_t b, Graph& g, std::vector<char> key, F enqueue) {
+  if (!b->use_graphs) return enqueue();
+  key_append(key, prof_enabled());
+  if (g.exec && g.key == key) {
+    DTSGB_CUDA(cudaGraphLaunch(g.exec, b->stream));
+    return DTSGB_OK;
+  }
+  drop_graph(b, g);
+  prof_set_capture_tag(&g);
+  cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) {
+    prof_set_capture_tag(nullptr);
+    return cuda_fail(e, "cudaStreamBeginCapture");
+  }
+  int st = enqueue();
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(b->stream, &graph);
+  prof_set_capture_tag(nullptr);
+  if (st) {
+    if (graph) cudaGraphDestroy(graph);
+    prof_drop_captured(&g);
+    return st;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    g.exec = nullptr;
+    prof_drop_captured(&g);
+    return cuda_fail(e, "cudaGraphInstantiate");
+  }
+  g.key = key;
+  DTSGB_CUDA(cudaGraphLaunch(g.exec, b->stream));
+  return DTSGB_OK;
+}
+
+int upload_plane(dtsgb_batch_t b, int i, const float* src, void* dst,
+                 cudaMemcpyKind kind) {
+  const Inst& I = b->inst[i];
+  const size_t wb = (size_t)I.w * 4;
+  if (b->st == Storage::F32) {
+    DTSGB_CUDA(cudaMemcpy2DAsync((float*)dst + I.off, (size_t)I.pitch * 4, src, wb,
+                                 wb, I.h, kind, b->stream));
+  } else {
+    DTSGB_CUDA(cudaMemcpy2DAsync(b->scratch + I.off, (size_t)I.pitch * 4, src, wb,
+                                 wb, I.h, kind, b->stream));
+  }
+  return DTSGB_OK;
+}
+
+int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
+                 const float* const* target, const float* const* conf,
+                 cudaMemcpyKind kind) {
+  if (!b || !rgba || !target) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  if (cs < DTSGB_RGB || cs > DTSGB_YYY)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "invalid color space");
+  for (int i = 0; i < b->n; ++i)
+    if (!rgba[i] || !target[i])
+      return fail(DTSGB_ERR_INVALID_ARGUMENT, "null image pointer");
+  int st;
+  for (int i = 0; i < b->n; ++i) {
+    const Inst& I = b->inst[i];
+    const size_t wb = (size_t)I.w * 4;
+    DTSGB_CUDA(cudaMemcpy2DAsync(b->guide + I.off, (size_t)I.pitch * 4, rgba[i], wb,
+                                 wb, I.h, kind, b->stream));
+  }
+  st = launch_color_convert_flat(b->guide, b->total, cs, b->stream);
+  if (st) return st;
+  // target
+  for (int i = 0; i < b->n; ++i)
+    if ((st = upload_plane(b, i, target[i], b->target, kind))) return st;
+  if (b->st == Storage::BF16 &&
+      (st = launch_storage_from_float(nullptr, 0, b->st, b->scratch, b->target,
+                                      b->total, b->stream)))
+    return st;
+  // confidence (missing -> ones)
+  bool any_conf = false;
+  for (int i = 0; i < b->n; ++i) {
+    const Inst& I = b->inst[i];
+    if (conf && conf[i]) {
+      any_conf = true;
+      if ((st = upload_plane(b, i, conf[i], b->conf, kind))) return st;
+    } else if (b->st == Storage::F32) {
+      if ((st = launch_fill_storage(Storage::F32, (float*)b->conf + I.off,
+                                    (long long)I.pitch * I.h, 1.f, b->stream)))
+        return st;
+    } else {
+      if ((st = launch_fill_storage(Storage::F32, b->scratch + I.off,
+                                    (long long)I.pitch * I.h, 1.f, b->stream)))
+        return st;
+    }
+  }
+  (void)any_conf;
+  if (b->st == Storage::BF16 &&
+      (st = launch_storage_from_float(nullptr, 0, b->st, b->scratch, b->conf,
+                                      b->total, b->stream)))
+    return st;
+  b->dts_res = -1;
+  b->hfbs_done = false;
+  if (kind == cudaMemcpyHostToDevice) DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+  return DTSGB_OK;
+}
+
+int ensure_hfbs_buffers(dtsgb_batch_t b, long long voxels, long long planes) {
+  if (voxels > b->gcap) {
+    for (auto& p : b->hg) dfree(p);
+    b->gcap = 0;
+    for (int k = 0; k < HG_NUM; ++k) {
+      int st = dalloc(&b->hg[k], (size_t)voxels);
+      if (st) return st;
+    }
+    b->gcap = voxels;
+    drop_graph(b, b->g_hfbs);
+  }
+  if (planes > b->ocap) {
+    dfree(b->ovf);
+    int st = dalloc(&b->ovf, (size_t)planes);
+    if (st) return st;
+    b->ocap = planes;
+    drop_graph(b, b->g_hfbs);
+  }
+  return DTSGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+DTSGB_API int dtsgb_batch_create(int n, const int* widths, const int* heights,
+                                 unsigned flags, dtsgb_batch_t* out) {
+  if (!out || !widths || !heights || n <= 0)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "bad batch description");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i)
+    if (widths[i] <= 0 || heights[i] <= 0)
+      return fail(DTSGB_ERR_INVALID_DIMS, "instance dims must be positive");
+  dtsgb_batch_t b = new dtsgb_batch_s();
+  b->n = n;
+  b->flags = flags;
+  b->st = (flags & DTSGB_FLAG_BF16_STORAGE) ? Storage::BF16 : Storage::F32;
+  b->ref_y = (flags & DTSGB_FLAG_FIX_Y_LIMIT) ? 0 : 1;
+  std::vector<Tile> tb, ti;
+  long long off = 0;
+  for (int i = 0; i < n; ++i) {
+    Inst I{widths[i], heights[i], round_up(widths[i], 32), 0, off};
+    b->inst.push_back(I);
+    off += (long long)I.pitch * I.h;
+    b->max_w = std::max(b->max_w, I.w);
+    b->max_h = std::max(b->max_h, I.h);
+    for (int y = 0; y < I.h; y += kBoundsTH)
+      for (int x = 0; x < I.w; x += kBoundsTW) tb.push_back(Tile{i, x, y, 0});
+    for (int y = 0; y < I.h; y += kIterTH)
+      for (int x = 0; x < I.w; x += kIterTW) ti.push_back(Tile{i, x, y, 0});
+  }
+  b->total = off;
+  b->ntb = (int)tb.size();
+  b->nti = (int)ti.size();
+  int st = DTSGB_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete b;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  b->own_stream = true;
+  const size_t T = (size_t)b->total;
+  if (!st) st = dalloc(&b->guide, T);
+  if (!st) st = dalloc((char**)&b->target, T * b->tsize());
+  if (!st) st = dalloc((char**)&b->conf, T * b->tsize());
+  if (!st) st = dalloc(&b->bounds, T);
+  if (!st) st = dalloc(&b->v[0], T);
+  if (!st) st = dalloc(&b->v[1], T);
+  if (!st) st = dalloc(&b->hout, T);
+  if (!st && b->st == Storage::BF16) st = dalloc(&b->scratch, T);
+  if (!st) st = dalloc(&b->d_inst, (size_t)n);
+  if (!st) st = dalloc(&b->d_tb, tb.size());
+  if (!st) st = dalloc(&b->d_ti, ti.size());
+  if (!st) st = dalloc(&b->d_hinst, (size_t)n);
+  if (!st) {
+    e = cudaMemcpy(b->d_inst, b->inst.data(), n * sizeof(Inst), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_tb, tb.data(), tb.size() * sizeof(Tile), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_ti, ti.data(), ti.size() * sizeof(Tile), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) st = cuda_fail(e, "batch tables");
+  }
+  if (st) {
+    batch_free(b);
+    delete b;
+    return st;
+  }
+  *out = b;
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_batch_destroy(dtsgb_batch_t b) {
+  if (!b) return DTSGB_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  batch_free(b);
+  delete b;
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_batch_set_stream(dtsgb_batch_t b, void* stream) {
+  if (!b) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null handle");
+  DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+  if (b->own_stream) cudaStreamDestroy(b->stream);
+  b->own_stream = false;
+  b->stream = (cudaStream_t)stream;
+  if (!stream) {
+    DTSGB_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    b->own_stream = true;
+  }
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_batch_use_graphs(dtsgb_batch_t b, int enable) {
+  if (!b) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null handle");
+  b->use_graphs = enable != 0;
+  if (!b->use_graphs) {
+    drop_graph(b, b->g_dts);
+    drop_graph(b, b->g_hfbs);
+  }
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
+                                 const float* const* target,
+                                 const float* const* conf) {
+  return batch_upload(b, cs, rgba, target, conf, cudaMemcpyHostToDevice);
+}
+
+DTSGB_API int dtsgb_batch_upload_device(dtsgb_batch_t b, int cs,
+                                        const void* const* rgba,
+                                        const float* const* target,
+                                        const float* const* conf) {
+  return batch_upload(b, cs, rgba, target, conf, cudaMemcpyDeviceToDevice);
+}
+
+DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b, const dtsgb_filter_params* f,
+                                    const dtsgb_optimize_params* p,
+                                    float overwrite) {
+  if (!b || !f || !p) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  if (!finite_pos(f->sigma_x) || !finite_pos(f->sigma_y) || !finite_pos(f->sigma_r))
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "filter sigmas must be finite, positive");
+  if (p->loss < DTSGB_L1 || p->loss > DTSGB_CHARBONNIER)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "invalid loss");
+  if (p->num_iterations < 0)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "num_iterations < 0");
+  if (!finite_pos(p->sigma_z) || p->sigma_z >= 254.f)
+    return fail(DTSGB_ERR_UNSUPPORTED, "sigma_z must be in (0, 254)");
+  const float rx = f->sigma_x / f->sigma_r, ry = f->sigma_y / f->sigma_r;
+  const int halo = (int)std::floor(p->sigma_z);
+  const bool iterate = p->loss != DTSGB_L1 && p->num_iterations > 0;
+  const DtsLaunch Lb{b->d_inst, b->d_tb, b->ntb, b->n};
+  const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n};
+  int res = 0;
+  auto enqueue = [&]() -> int {
+    int st = launch_init_var(Li, b->st, b->target, b->v[0], b->stream);
+    if (st || !iterate) return st;
+    st = launch_bounds(Lb, b->guide, b->bounds, rx, ry, p->sigma_z, p->sigma_z,
+                       b->ref_y, b->stream);
+    if (st) return st;
+    const IterMode mode = p->loss == DTSGB_L2 ? IterMode::L2 : IterMode::CHARB;
+    int a = 0;
+    for (int it = 0; it < p->num_iterations; ++it) {
+      st = launch_dts_iter(Li, b->st, mode, b->v[a], b->v[1 - a], b->target,
+                           b->conf, b->bounds, p->lambda, p->step_size, overwrite,
+                           halo, halo, b->stream);
+      if (st) return st;
+      a = 1 - a;
+    }
+    return DTSGB_OK;
+  };
+  res = iterate ? (p->num_iterations % 2) : 0;
+  std::vector<char> key;
+  key_append(key, *f);
+  key_append(key, *p);
+  key_append(key, overwrite);
+  int st = run_graph(b, b->g_dts, key, enqueue);
+  if (st) return st;
+  b->dts_res = res;
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p) {
+  if (!b || !p) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  if (!finite_pos(p->sigma_x) || !finite_pos(p->sigma_y) || !finite_pos(p->sigma_l))
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "grid sigmas must be finite, positive");
+  if (p->bistoch_iter_max < 0 || p->optim_iter_max < 0)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "iteration counts must be >= 0");
+  const int gl = (int)std::ceil(255.0 / (double)p->sigma_l);
+  if (gl > 256) return fail(DTSGB_ERR_UNSUPPORTED, "more than 256 luma bins");
+  std::vector<HInst> hi(b->n);
+  long long goff = 0, poff = 0, max_vox = 0, max_px = 0, max_cells = 0, max_lines = 0;
+  for (int i = 0; i < b->n; ++i) {
+    const Inst& I = b->inst[i];
+    HInst& H = hi[i];
+    H.w = I.w;
+    H.h = I.h;
+    H.pitch = I.pitch;
+    H.gx = (int)std::ceil((float)I.w / p->sigma_x);
+    H.gy = (int)std::ceil((float)I.h / p->sigma_y);
+    H.gl = gl;
+    H.cov_x = H.gx % 8 != 0;
+    H.cov_y = H.gy % 8 != 0;
+    H.cov_l = H.gl % 8 != 0;
+    H.ovf_stored = 1;
+    H.pix_off = I.off;
+    H.grid_off = goff;
+    H.plane_off = poff;
+    const long long vox = (long long)H.gx * H.gy * H.gl;
+    goff += round_up_ll(vox, 32);
+    poff += round_up_ll((long long)H.gx * H.gy, 32);
+    max_vox = std::max(max_vox, vox);
+    max_px = std::max(max_px, (long long)I.w * I.h);
+    max_cells = std::max(max_cells, (long long)H.gx * H.gy);
+    max_lines = std::max({max_lines, (long long)H.gy * H.gl, (long long)H.gx * H.gl,
+                          (long long)H.gx * H.gy});
+  }
+  int st = ensure_hfbs_buffers(b, goff, poff);
+  if (st) return st;
+  const bool same_tables =
+      b->hinst.size() == hi.size() &&
+      std::memcmp(b->hinst.data(), hi.data(), hi.size() * sizeof(HInst)) == 0;
+  if (!same_tables) {
+    b->hinst = hi;
+    DTSGB_CUDA(cudaMemcpyAsync(b->d_hinst, b->hinst.data(), hi.size() * sizeof(HInst),
+                               cudaMemcpyHostToDevice, b->stream));
+    DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+  }
+  HfbsBatch B{};
+  B.d_inst = b->d_hinst;
+  B.n_inst = b->n;
+  B.max_voxels = max_vox;
+  B.max_pixels = max_px;
+  B.max_cells = max_cells;
+  B.max_lines = max_lines;
+  B.max_gl = gl;
+  B.guide = b->guide;
+  B.target = b->target;
+  B.conf = b->conf;
+  B.st = b->st;
+  B.out = b->hout;
+  B.count = b->hg[HG_COUNT];
+  B.csum = b->hg[HG_CSUM];
+  B.b = b->hg[HG_B];
+  B.n0 = b->hg[HG_N0];
+  B.n1 = b->hg[HG_N1];
+  B.invA = b->hg[HG_INVA];
+  B.z0 = b->hg[HG_Z0];
+  B.z1 = b->hg[HG_Z1];
+  B.h = b->hg[HG_H];
+  B.t0 = b->hg[HG_T0];
+  B.t1 = b->hg[HG_T1];
+  B.t2 = b->hg[HG_T2];
+  B.ovf = b->ovf;
+  B.keep_debug = false;
+  HParams hp{p->sigma_x, p->sigma_y, p->sigma_l, p->lambda, p->alpha, p->beta,
+             p->bistoch_iter_max, p->optim_iter_max, p->neg_exp_beta};
+  std::vector<char> key;
+  key_append(key, hp);
+  st = run_graph(b, b->g_hfbs, key, [&]() { return hfbs_enqueue_solve(B, hp, b->stream); });
+  if (st) return st;
+  b->hfbs_done = true;
+  return DTSGB_OK;
+}
+
+static int batch_download(dtsgb_batch_t b, int which, float* const* dst,
+                          cudaMemcpyKind kind) {
+  if (!b || !dst) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  const float* src = nullptr;
+  if (which == 0) {
+    if (b->dts_res < 0) return fail(DTSGB_ERR_INVALID_ARGUMENT, "no DTS solve yet");
+    src = b->v[b->dts_res];
+  } else if (which == 1) {
+    if (!b->hfbs_done) return fail(DTSGB_ERR_INVALID_ARGUMENT, "no HFBS solve yet");
+    src = b->hout;
+  } else {
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "which must be 0 (DTS) or 1 (HFBS)");
+  }
+  for (int i = 0; i < b->n; ++i) {
+    if (!dst[i]) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null output pointer");
+    const Inst& I = b->inst[i];
+    const size_t wb = (size_t)I.w * 4;
+    DTSGB_CUDA(cudaMemcpy2DAsync(dst[i], wb, src + I.off, (size_t)I.pitch * 4, wb, I.h,
+                                 kind, b->stream));
+  }
+  if (kind == cudaMemcpyDeviceToHost) DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_batch_download(dtsgb_batch_t b, int which, float* const* dst) {
+  return batch_download(b, which, dst, cudaMemcpyDeviceToHost);
+}
+
+DTSGB_API int dtsgb_batch_download_device(dtsgb_batch_t b, int which,
+                                          float* const* dst) {
+  return batch_download(b, which, dst, cudaMemcpyDeviceToDevice);
+}
+
+}  // extern "C"

@@ -37,46 +37,19 @@ int cuda_fail(cudaError_t e, const char* what) {
   return DTSGB_ERR_CUDA;
 }
 
+float filter_sigma_multiplier(int it, int n) {
+  if (it == 0) return 1.f;
+  return (float)(3 * std::pow(2.0, (double)(n - (it + 1))) /
+                 std::sqrt(std::pow(4.0, (double)n) - 1));
+}
+
 namespace {
-
-int round_up(int v, int m) { return (v + m - 1) / m * m; }
-
-bool finite_pos(float v) { return std::isfinite(v) && v > 0.f; }
-
-// Device allocation helper: zero-initialised.
-template <typename T>
-int dalloc(T** p, size_t count) {
-  *p = nullptr;
-  if (count == 0) count = 1;
-  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
-  if (e != cudaSuccess) {
-    *p = nullptr;
-    return cuda_fail(e, "cudaMalloc");
-  }
-  e = cudaMemset(*p, 0, count * sizeof(T));
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
-  return DTSGB_OK;
-}
-template <typename T>
-void dfree(T*& p) {
-  if (p) cudaFree((void*)p);
-  p = nullptr;
-}
 
 std::vector<Tile> make_tiles(int w, int h, int tw, int th) {
   std::vector<Tile> t;
   for (int y = 0; y < h; y += th)
     for (int x = 0; x < w; x += tw) t.push_back(Tile{0, x, y, 0});
   return t;
-}
-
-// sigma multiplier of DomainTransformFilter::Filter,
-// src/domain_transform_filter.cu:142-152: 1 at iteration 0, else
-// 3*2^(N-i-1)/sqrt(4^N-1) evaluated in double and stored as float.
-float filter_sigma_multiplier(int it, int n) {
-  if (it == 0) return 1.f;
-  return (float)(3 * std::pow(2.0, (double)(n - (it + 1))) /
-                 std::sqrt(std::pow(4.0, (double)n) - 1));
 }
 
 }  // namespace
@@ -805,6 +778,7 @@ DTSGB_API int dtsgb_hfbs_optimize(dtsgb_hfbs_t h) {
   B.guide = h->guide;
   B.target = h->target;
   B.conf = h->conf;
+  B.st = Storage::F32;
   B.out = h->out;
   B.count = h->g[G_COUNT];
   B.csum = h->g[G_CSUM];

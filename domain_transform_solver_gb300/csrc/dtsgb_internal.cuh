@@ -75,10 +75,47 @@ int cuda_fail(cudaError_t e, const char* what);
   } while (0)
 
 // ---------------------------------------------------------------------------
+// Host helpers shared by the API translation units.
+// ---------------------------------------------------------------------------
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+inline long long round_up_ll(long long v, long long m) { return (v + m - 1) / m * m; }
+inline bool finite_pos(float v) { return v == v && v > 0.f && v < 3.4e38f; }
+
+// Zero-initialised device allocation; returns a DTSGB_* status.
+template <typename T>
+int dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    (void)cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? (set_error("cudaMalloc: out of memory"), 5)
+                                          : cuda_fail(e, "cudaMalloc");
+  }
+  e = cudaMemset(*p, 0, count * sizeof(T));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
+  return 0;
+}
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+// sigma multiplier of DomainTransformFilter::Filter
+// (src/domain_transform_filter.cu:142-152): 1 at iteration 0, else
+// 3*2^(N-i-1)/sqrt(4^N-1) evaluated in double and stored as float.
+float filter_sigma_multiplier(int it, int n);
+
+// ---------------------------------------------------------------------------
 // Kernel timing (profile.cu): no-ops unless enabled through the C ABI.
 // ---------------------------------------------------------------------------
 void prof_begin(cudaStream_t s, int kernel_id);
 void prof_end(cudaStream_t s, int kernel_id);
+bool prof_enabled();
+void prof_set_capture_tag(const void* tag);
+void prof_drop_captured(const void* tag);
 
 struct ProfScope {
   cudaStream_t s;

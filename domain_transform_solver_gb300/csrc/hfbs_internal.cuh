@@ -35,8 +35,9 @@ struct HfbsBatch {
   long long max_voxels, max_pixels, max_cells, max_lines;
   int max_gl;
   const uchar4* guide;
-  const float* target;
-  const float* conf;
+  const void* target;  // storage type st
+  const void* conf;
+  Storage st;
   float* out;
   float *count, *csum, *b, *n0, *n1, *invA, *z0, *z1, *h, *t0, *t1, *t2, *ovf;
   // optional debug copies (single-instance class API)

@@ -39,9 +39,10 @@ __device__ __forceinline__ int cell_start(int cell, float sigma, int n) {
 // a12: SplatBAndC + BistochastasizeSetup (src/hfbs.cu:72-120).  Bins
 // (floor(x/sx), floor(y/sy), floor(L/sl)) with L the .x channel; sums of
 // c*t, c and 1 per bin.  Luma bin == gl lands in the overflow plane.
+template <typename TS>
 __global__ void __launch_bounds__(64)
     k_splat(const HInst* __restrict__ insts, const uchar4* __restrict__ guide,
-            const float* __restrict__ tgt, const float* __restrict__ cnf,
+            const TS* __restrict__ tgt, const TS* __restrict__ cnf,
             float* __restrict__ count, float* __restrict__ csum,
             float* __restrict__ b, float* __restrict__ ovf, HParams p) {
   extern __shared__ float sh[];
@@ -64,8 +65,8 @@ __global__ void __launch_bounds__(64)
       for (int x = xs; x < xe; ++x) {
         const uchar4 g = guide[row + x];
         const int bl = (int)floorf((float)g.x * 1.0f / p.sigma_l);
-        const float c = cnf[row + x];
-        const float ct = c * tgt[row + x];
+        const float c = load_f(cnf + row + x);
+        const float ct = c * load_f(tgt + row + x);
         if (bl < gl) {
           hist[(3 * bl + 0) * T + threadIdx.x] += ct;
           hist[(3 * bl + 1) * T + threadIdx.x] += c;
@@ -304,12 +305,24 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   const dim3 gp(blocks_for(B.max_pixels), ni);
   const dim3 gc((B.max_cells + 63) / 64, ni);
   const size_t splat_smem = sizeof(float) * 3 * (size_t)B.max_gl * 64;
-  if (splat_smem > 48 * 1024)
-    DTSGB_CUDA(cudaFuncSetAttribute(
-        k_splat, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)splat_smem));
   prof_begin(s, DTSGB_K_HFBS_SPLAT);
-  k_splat<<<gc, 64, splat_smem, s>>>(B.d_inst, B.guide, B.target, B.conf,
-                                     B.count, B.csum, B.b, B.ovf, p);
+  if (B.st == Storage::F32) {
+    if (splat_smem > 48 * 1024)
+      DTSGB_CUDA(cudaFuncSetAttribute(k_splat<float>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)splat_smem));
+    k_splat<float><<<gc, 64, splat_smem, s>>>(
+        B.d_inst, B.guide, (const float*)B.target, (const float*)B.conf, B.count,
+        B.csum, B.b, B.ovf, p);
+  } else {
+    if (splat_smem > 48 * 1024)
+      DTSGB_CUDA(cudaFuncSetAttribute(k_splat<__nv_bfloat16>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)splat_smem));
+    k_splat<__nv_bfloat16><<<gc, 64, splat_smem, s>>>(
+        B.d_inst, B.guide, (const __nv_bfloat16*)B.target,
+        (const __nv_bfloat16*)B.conf, B.count, B.csum, B.b, B.ovf, p);
+  }
   DTSGB_CUDA(cudaGetLastError());
   prof_end(s, DTSGB_K_HFBS_SPLAT);
   // bistochastization ping-pong: even iterations read the buffer filled with

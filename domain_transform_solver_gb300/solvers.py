@@ -35,7 +35,7 @@ __all__ = [
     "DomainFilterParamsVec1", "DomainOptimizeParams", "HFBSGridParams",
     "DomainTransformFilter", "DomainTransformSolver", "HFBS", "DtsOptions",
     "HfbsOptions", "Solve", "EdgeAwareOptimize", "DtsgbError",
-    "FLAG_BF16_STORAGE", "FLAG_FIX_Y_LIMIT",
+    "FLAG_BF16_STORAGE", "FLAG_FIX_Y_LIMIT", "Batch",
 ]
 
 FLAG_BF16_STORAGE = 0x1
@@ -342,6 +342,79 @@ class HFBS:
         out = np.zeros(self._shape(), np.float32)
         check(self._lib.dtsgb_hfbs_download(self._h, int(image_type), _ptr(out)))
         return out
+
+
+def _ptr_array(arrays):
+    n = len(arrays)
+    out = (ctypes.c_void_p * n)()
+    for i, a in enumerate(arrays):
+        out[i] = None if a is None else a.ctypes.data
+    return out
+
+
+class Batch:
+    """Many images of uneven size solved together (no reference counterpart:
+    the reference solves one image per object).  solve_dts / solve_hfbs run
+    the per-image semantics of DomainTransformSolver / HFBS on every
+    instance with single launches; the launch sequence is replayed from a
+    CUDA graph while the parameters stay the same."""
+
+    def __init__(self, sizes, flags: int = 0, use_graphs: bool = True):
+        self._lib = _lib.load()
+        self.sizes = [(int(w), int(h)) for w, h in sizes]
+        n = len(self.sizes)
+        ws = (ctypes.c_int * n)(*[w for w, _ in self.sizes])
+        hs = (ctypes.c_int * n)(*[h for _, h in self.sizes])
+        b = ctypes.c_void_p()
+        check(self._lib.dtsgb_batch_create(n, ws, hs, flags, ctypes.byref(b)))
+        self._h = b
+        check(self._lib.dtsgb_batch_use_graphs(b, int(use_graphs)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.dtsgb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        check(self._lib.dtsgb_batch_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
+
+    def upload(self, color_space: COLOR_SPACE, rgba, target, confidence=None) -> None:
+        rg = [_rgba(a, (h, w)) for a, (w, h) in zip(rgba, self.sizes)]
+        tg = [_f32(a, (h, w)) for a, (w, h) in zip(target, self.sizes)]
+        cf = None
+        if confidence is not None:
+            cf = [None if a is None else _f32(a, (h, w))
+                  for a, (w, h) in zip(confidence, self.sizes)]
+        self._keep = (rg, tg, cf)
+        check(self._lib.dtsgb_batch_upload(self._h, int(color_space), _ptr_array(rg),
+                                           _ptr_array(tg),
+                                           None if cf is None else _ptr_array(cf)))
+
+    def solve_dts(self, filter_params: DomainFilterParams,
+                  optimize_params: DomainOptimizeParams,
+                  overwrite_target_above_conf: float = -1) -> None:
+        check(self._lib.dtsgb_batch_solve_dts(self._h, ctypes.byref(filter_params._c()),
+                                              ctypes.byref(optimize_params._c()),
+                                              float(overwrite_target_above_conf)))
+
+    def solve_hfbs(self, grid_params: HFBSGridParams) -> None:
+        check(self._lib.dtsgb_batch_solve_hfbs(self._h, ctypes.byref(grid_params._c())))
+
+    def download(self, which: int):
+        """which: 0 = DTS result, 1 = HFBS result."""
+        outs = [np.empty((h, w), np.float32) for w, h in self.sizes]
+        check(self._lib.dtsgb_batch_download(self._h, int(which), _ptr_array(outs)))
+        return outs
 
 
 # ---- generic solve API, src/edge_aware_solver.h:13-90 (cv::Mat-free) -------

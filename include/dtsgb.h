@@ -224,6 +224,46 @@ DTSGB_API int dtsgb_hfbs_grid_dims(dtsgb_hfbs_t h, int* gx, int* gy, int* gl);
  * 3 splat_norm, 4 inv_diag_A, 5 blurred c, 6 initial z, 7 final z. */
 DTSGB_API int dtsgb_hfbs_debug_grid(dtsgb_hfbs_t h, int which, float* dst);
 
+/* ===========================================================================
+ * Batched solves (new; no reference counterpart): n independent instances of
+ * uneven size in one HBM arena, each solved with DTS and/or HFBS by single
+ * launches that cover every instance (the reference solves one image per
+ * object, src/edge_aware_solver.h:59-90).  A batch reuses the per-image
+ * semantics of the classes above: dtsgb_batch_solve_dts is
+ * ComputeColorSpaceDifferential + IntegrateColorDifferentials + Optimize on
+ * every instance, dtsgb_batch_solve_hfbs is HFBS::Optimize on every instance.
+ * ===========================================================================*/
+typedef struct dtsgb_batch_s* dtsgb_batch_t;
+
+DTSGB_API int dtsgb_batch_create(int n, const int* widths, const int* heights,
+                                 unsigned flags, dtsgb_batch_t* out);
+DTSGB_API int dtsgb_batch_destroy(dtsgb_batch_t b);
+DTSGB_API int dtsgb_batch_set_stream(dtsgb_batch_t b, void* cuda_stream);
+/* Capture each solve as a CUDA graph on first use and replay it while the
+ * parameters stay the same (default on). */
+DTSGB_API int dtsgb_batch_use_graphs(dtsgb_batch_t b, int enable);
+/* Host arrays of n pointers: rgba (W*H*4 bytes each), target and confidence
+ * (W*H floats each).  confidence may be NULL, or hold NULL entries: ones. */
+DTSGB_API int dtsgb_batch_upload(dtsgb_batch_t b, int color_space,
+                                 const void* const* rgba,
+                                 const float* const* target,
+                                 const float* const* confidence);
+DTSGB_API int dtsgb_batch_upload_device(dtsgb_batch_t b, int color_space,
+                                        const void* const* rgba,
+                                        const float* const* target,
+                                        const float* const* confidence);
+DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b,
+                                    const dtsgb_filter_params* filter,
+                                    const dtsgb_optimize_params* optimize,
+                                    float overwrite_target_above_conf);
+DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b,
+                                     const dtsgb_hfbs_params* params);
+/* which: 0 = DTS result, 1 = HFBS result; dst: n pointers (W*H floats). */
+DTSGB_API int dtsgb_batch_download(dtsgb_batch_t b, int which,
+                                   float* const* dst);
+DTSGB_API int dtsgb_batch_download_device(dtsgb_batch_t b, int which,
+                                          float* const* dst);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,8 +26,8 @@ def oracle_mod():
 @pytest.fixture(scope="session")
 def dts():
     """The product package (loads libdtsgb.so, building it if needed)."""
-    from domain_transform_solver_gb300 import build as B
-    B.build()
+    import __graft_entry__
+    __graft_entry__.build()
     import domain_transform_solver_gb300 as D
     return D
 

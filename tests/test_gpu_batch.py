@@ -1,0 +1,93 @@
+"""Batched solves of ragged instances: identical (bitwise) to solving each
+image through the class API, with and without CUDA-graph replay, and the
+BF16 storage form checked against the FP64 oracle."""
+import numpy as np
+import pytest
+
+import parity as P
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(97, 61), (256, 300), (33, 190), (411, 129), (64, 64), (1, 17)]
+
+
+def _instances(scale_sizes=SIZES):
+    from domain_transform_solver_gb300 import workloads as W
+    return [W.depth_sr_instance(400 + i, w, h, n_poly=8, sample_frac=0.05)
+            for i, (w, h) in enumerate(scale_sizes)]
+
+
+def _single_dts(D, inst, flags, filt, opt):
+    h, w = inst.target.shape
+    s = D.DomainTransformSolver(D.ImageDim(w, h), flags=flags)
+    s.ClearAll()
+    s.InitFrame(D.COLOR_SPACE.YCbCr, inst.rgba, inst.target, inst.confidence)
+    s.ComputeColorSpaceDifferential(D.DomainFilterParams(**filt))
+    s.IntegrateColorDifferentials()
+    s.Optimize(D.DomainOptimizeParams(**opt))
+    return s.Download(D.ImageType.OPTIMIZED_QUANTITY)
+
+
+def _single_hfbs(D, inst, params):
+    h, w = inst.target.shape
+    # max grid one larger than the grid on every axis, like a batch instance
+    s = D.HFBS(D.ImageDim(w, h), -(-w // 8) + 1, -(-h // 8) + 1, 17)
+    s.SetFilterParams(D.HFBSGridParams(**params))
+    s.ClearAll()
+    s.InitFrame(D.COLOR_SPACE.YCbCr, inst.rgba, inst.target, inst.confidence)
+    s.Optimize()
+    return s.Download(D.ImageType.OPTIMIZED_QUANTITY)
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_batch_matches_single_image_solves(gpu_ready, graphs):
+    D = gpu_ready
+    from domain_transform_solver_gb300 import workloads as W
+    insts = _instances()
+    b = D.Batch([(i.width, i.height) for i in insts], use_graphs=graphs)
+    b.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in insts], [i.target for i in insts],
+             [i.confidence for i in insts])
+    opt = dict(W.CFG0_OPT, num_iterations=5)
+    hp = dict(W.CFG1_HFBS, optim_iter_max=12)
+    for rep in range(2):  # second pass replays the captured graphs
+        b.solve_dts(D.DomainFilterParams(**W.CFG0_FILTER), D.DomainOptimizeParams(**opt))
+        b.solve_hfbs(D.HFBSGridParams(**hp))
+        dts_out = b.download(0)
+        hfbs_out = b.download(1)
+        for inst, v, hv in zip(insts, dts_out, hfbs_out):
+            assert np.array_equal(v, _single_dts(D, inst, 0, W.CFG0_FILTER, opt))
+            ref = _single_hfbs(D, inst, hp)
+            assert np.array_equal(np.isnan(hv), np.isnan(ref))
+            assert np.array_equal(hv[~np.isnan(hv)], ref[~np.isnan(ref)])
+
+
+def test_batch_bf16_storage_against_oracle(gpu_ready, oracle_mod):
+    D = gpu_ready
+    from domain_transform_solver_gb300 import workloads as W
+    insts = _instances([(150, 90), (70, 201)])
+    b = D.Batch([(i.width, i.height) for i in insts], flags=D.FLAG_BF16_STORAGE)
+    b.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in insts], [i.target for i in insts],
+             [i.confidence for i in insts])
+    opt = dict(W.CFG0_OPT, num_iterations=6)
+    b.solve_dts(D.DomainFilterParams(**W.CFG0_FILTER), D.DomainOptimizeParams(**opt))
+    outs = b.download(0)
+    for inst, v in zip(insts, outs):
+        ref = _single_dts(D, inst, D.FLAG_BF16_STORAGE, W.CFG0_FILTER, opt)
+        assert np.array_equal(v, ref)
+        t, c = P.bf16_round(inst.target), P.bf16_round(inst.confidence)
+        h, w = t.shape
+        s = D.DomainTransformSolver(D.ImageDim(w, h), flags=D.FLAG_BF16_STORAGE)
+        s.InitFrame(D.COLOR_SPACE.YCbCr, inst.rgba, inst.target, inst.confidence)
+        s.ComputeColorSpaceDifferential(D.DomainFilterParams(**W.CFG0_FILTER))
+        ov = {(a, 8.0): s.DebugBounds(a, 8.0) for a in (0, 1)}
+        v64, _ = oracle_mod.dts_solve(inst.rgba, t, c, 1, W.CFG0_FILTER, opt, overrides=ov)
+        assert np.abs(v - v64).max() <= P.TOL_REL * P.target_range(t)
+
+
+def test_batch_rejects_bad_arguments(gpu_ready):
+    D = gpu_ready
+    with pytest.raises(D.DtsgbError):
+        D.Batch([(0, 10)])
+    b = D.Batch([(16, 16)])
+    with pytest.raises(D.DtsgbError):
+        b.download(0)  # nothing solved yet
