@@ -1,23 +1,26 @@
 """Benchmark of the DTS / HFBS hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg0]
+                    [--workload cfg3|cfg0|cfg1]
 
-One JSON line on stdout (rank 0).  A step is one solve of the workload with
-its inputs already resident in HBM (the reference's timed window,
-src/edge_aware_solver.h:72-84: differential, integration and all iterations);
-`e2e` times the same solve through the public C ABI with host buffers,
-the upload and download included.  Under torchrun each rank solves its own
-replica (independent instances, no collective).
+One JSON line on stdout (rank 0).  A step is one pass of the workload's
+solves with inputs already resident in HBM: for DTS the reference's timed
+window (src/edge_aware_solver.h:72-84: differential, integration, all
+iterations), for HFBS the whole HFBS::Optimize.  `e2e` times the same step
+through the public C ABI with pinned host buffers, the upload and the
+download included.  Under torchrun every rank solves its own copy of the
+workload (independent instances, no collective): weak scaling.
 
 --impl reference times the reference algorithm's CPU restatement (the FP32
-oracle port, all host threads) on the same workload; the reference's CUDA
-build cannot be built on this toolchain.
+oracle port, all host threads) on a bounded sample of the same workload; the
+reference's own CUDA build cannot be built with this toolchain.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -29,10 +32,14 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "oracle"))
 
 METRIC = "DTS/HFBS solve Mpix/s at fixed iters, fwd+bwd Mpix/s, %HBM peak; RMSE vs FP64"
 FALLBACK_HBM_GBS = 6800.0
 L2_FLUSH_BYTES = 256 << 20
+KERNEL_NAMES = {0: "k_bounds", 1: "k_dts_iter", 2: "k_filter", 3: "k_splat",
+                4: "k_bistoch", 5: "k_solve (HFBS heavy-ball)", 6: "hfbs setup kernels",
+                7: "k_slice", 8: "k_to_float"}
 
 
 def peaks():
@@ -88,36 +95,144 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _pinned_copy(a: np.ndarray) -> np.ndarray:
+    import torch
+    t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+    out = t.numpy()
+    out[...] = a  # the array's base is the pinned tensor, which it keeps alive
+    return out
+
+
+def _pinned_empty(shape, dtype=np.float32) -> np.ndarray:
+    import torch
+    t = torch.empty(shape, dtype=getattr(torch, np.dtype(dtype).name), pin_memory=True)
+    return t.numpy()
+
+
+def _ptrs(arrays):
+    arr = (ctypes.c_void_p * len(arrays))()
+    for i, a in enumerate(arrays):
+        arr[i] = a.ctypes.data
+    return arr
+
+
 # ---- workloads ---------------------------------------------------------------
+class Cfg3:
+    """64 ragged instances (W~U[256,1920], H~U[256,1080]), each solved by DTS
+    (config-0 parameters, 10 iterations) and HFBS (config-1 parameters, luma
+    from YCbCr, 64 iterations), BF16 target/confidence storage, FP32 math,
+    one launch per kernel across all instances, CUDA-graph replay."""
+
+    name = "cfg3_batched_dts_hfbs_64_ragged_bf16"
+    dtype = "bf16 storage, f32 math"
+
+    def __init__(self, rank: int):
+        import domain_transform_solver_gb300 as D
+        from domain_transform_solver_gb300 import workloads as W
+        self.D, self.W = D, W
+        self.insts = W.batched_instances()
+        self.sizes = [(i.width, i.height) for i in self.insts]
+        self.pixels = sum(w * h for w, h in self.sizes)
+        self.iters = W.CFG0_OPT["num_iterations"]
+        self.hp = dict(W.CFG1_HFBS)
+        self.voxels = sum(math.ceil(np.float32(w) / np.float32(8.0)) *
+                          math.ceil(np.float32(h) / np.float32(8.0)) * 16
+                          for w, h in self.sizes)
+
+    def setup(self, stream_handle: int):
+        D, W = self.D, self.W
+        self.b = D.Batch(self.sizes, flags=D.FLAG_BF16_STORAGE)
+        self.b.set_stream(stream_handle)
+        self.b.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in self.insts],
+                      [i.target for i in self.insts], [i.confidence for i in self.insts])
+        self.fp = D.DomainFilterParams(**W.CFG0_FILTER)._c()
+        self.op = D.DomainOptimizeParams(**W.CFG0_OPT)._c()
+        self.hpc = D.HFBSGridParams(**self.hp)._c()
+        self.lib = self.b._lib
+        # pinned host buffers (kept alive by these lists)
+        self._rgba = [_pinned_copy(i.rgba) for i in self.insts]
+        self._t = [_pinned_copy(i.target) for i in self.insts]
+        self._c = [_pinned_copy(i.confidence) for i in self.insts]
+        self._o0 = [_pinned_empty((h, w)) for w, h in self.sizes]
+        self._o1 = [_pinned_empty((h, w)) for w, h in self.sizes]
+        self.h_rgba, self.h_t, self.h_c = _ptrs(self._rgba), _ptrs(self._t), _ptrs(self._c)
+        self.h_o0, self.h_o1 = _ptrs(self._o0), _ptrs(self._o1)
+
+    def step(self):
+        from domain_transform_solver_gb300._lib import check
+        check(self.lib.dtsgb_batch_solve_dts(self.b.handle, ctypes.byref(self.fp),
+                                             ctypes.byref(self.op), ctypes.c_float(-1.0)))
+        check(self.lib.dtsgb_batch_solve_hfbs(self.b.handle, ctypes.byref(self.hpc)))
+
+    def step_e2e(self):
+        from domain_transform_solver_gb300._lib import check
+        h = self.b.handle
+        check(self.lib.dtsgb_batch_upload(h, 1, self.h_rgba, self.h_t, self.h_c))
+        self.step()
+        check(self.lib.dtsgb_batch_download(h, 0, self.h_o0))
+        check(self.lib.dtsgb_batch_download(h, 1, self.h_o1))
+
+    def e2e_bytes(self):
+        return self.pixels * (4 + 4 + 4), self.pixels * 4 * 2
+
+    def algorithmic_bytes(self):
+        """Bytes each launch of a kernel must move at minimum, per kernel id."""
+        px, vx = self.pixels, self.voxels
+        return {
+            0: 8 * px,            # read guide, write packed bounds
+            1: 16 * px,           # read v f32, t bf16, c bf16, bounds; write v f32
+            3: 8 * px + 12 * vx,  # read guide, t, c; write b, sum c, count
+            4: 12 * vx,           # read n, count; write n
+            5: 28 * vx,           # read z, n, b, invA, h; write h, z
+            7: 8 * px,            # read guide, write result (grid reads cached)
+            8: 6 * px,            # read t bf16, write v f32
+        }
+
+    def cpu_sample(self, real="f32"):
+        """A bounded sample: the four smallest instances, DTS + HFBS each."""
+        import oracle as O
+        W = self.W
+        order = sorted(range(len(self.insts)), key=lambda i: self.sizes[i][0] * self.sizes[i][1])
+        px = 0
+        for i in order[:4]:
+            inst = self.insts[i]
+            O.dts_solve(inst.rgba, inst.target, inst.confidence, 1, W.CFG0_FILTER,
+                        W.CFG0_OPT, real=real)
+            O.hfbs_solve(inst.rgba, inst.target, inst.confidence, 1, self.hp,
+                         max_grid=(inst.width, inst.height, 64), real=real)
+            px += inst.width * inst.height
+        return px, "4 smallest of the 64 instances, DTS + HFBS each"
+
+
 class Cfg0:
     """DTS depth super-resolution 640x480, FP32, 10 iterations (config 0)."""
 
     name = "cfg0_dts_depth_superres_640x480"
+    dtype = "f32"
 
     def __init__(self, rank: int):
         import domain_transform_solver_gb300 as D
         from domain_transform_solver_gb300 import workloads as W
         self.D, self.W = D, W
         self.inst = W.depth_sr_instance(W.SEED_BASE)
-        self.w, self.h = self.inst.width, self.inst.height
-        self.pixels = self.w * self.h
+        self.pixels = self.inst.width * self.inst.height
         self.iters = W.CFG0_OPT["num_iterations"]
+        self.voxels = 0
 
     def setup(self, stream_handle: int):
         D, W = self.D, self.W
-        self.s = D.DomainTransformSolver(D.ImageDim(self.w, self.h))
+        w, h = self.inst.width, self.inst.height
+        self.s = D.DomainTransformSolver(D.ImageDim(w, h))
         self.s.SetStream(stream_handle)
         self.s.ClearAll()
         self.s.InitFrame(D.COLOR_SPACE.YCbCr, self.inst.rgba, self.inst.target,
                          self.inst.confidence)
         self.fp = D.DomainFilterParams(**W.CFG0_FILTER)
         self.op = D.DomainOptimizeParams(**W.CFG0_OPT)
-        import torch
-        self.h_rgba = torch.from_numpy(self.inst.rgba.copy()).pin_memory().numpy()
-        self.h_t = torch.from_numpy(self.inst.target.copy()).pin_memory().numpy()
-        self.h_c = torch.from_numpy(self.inst.confidence.copy()).pin_memory().numpy()
-        self.h_out = torch.empty((self.h, self.w), dtype=torch.float32,
-                                 pin_memory=True).numpy()
+        self.h_rgba = _pinned_copy(self.inst.rgba)
+        self.h_t = _pinned_copy(self.inst.target)
+        self.h_c = _pinned_copy(self.inst.confidence)
+        self.h_out = _pinned_empty((h, w))
 
     def step(self):
         self.s.ComputeColorSpaceDifferential(self.fp)
@@ -125,46 +240,100 @@ class Cfg0:
         self.s.Optimize(self.op)
 
     def step_e2e(self):
-        from domain_transform_solver_gb300 import _lib
-        lib = _lib.load()
-        h = self.s.handle
-        import ctypes
-        _lib.check(lib.dtsgb_dts_init_frame(h, 1, ctypes.c_void_p(self.h_rgba.ctypes.data),
-                                            ctypes.c_void_p(self.h_t.ctypes.data),
-                                            ctypes.c_void_p(self.h_c.ctypes.data)))
+        from domain_transform_solver_gb300._lib import check
+        lib, h = self.s._lib, self.s.handle
+        check(lib.dtsgb_dts_init_frame(h, 1, ctypes.c_void_p(self.h_rgba.ctypes.data),
+                                       ctypes.c_void_p(self.h_t.ctypes.data),
+                                       ctypes.c_void_p(self.h_c.ctypes.data)))
         self.step()
-        _lib.check(lib.dtsgb_dts_download(h, 5, ctypes.c_void_p(self.h_out.ctypes.data)))
+        check(lib.dtsgb_dts_download(h, 5, ctypes.c_void_p(self.h_out.ctypes.data)))
 
     def e2e_bytes(self):
-        return self.pixels * (4 + 4 + 4), self.pixels * 4
+        return self.pixels * 12, self.pixels * 4
 
-    # dominant kernel: the fused X+Y iteration; algorithmic bytes per pixel
-    # and launch: read v, t, c (FP32) and the packed window bounds, write v
-    dominant_id = 1
-    dominant_name = "k_dts_iter (fused X+Y DTS iteration)"
-    bytes_per_px = 20
+    def algorithmic_bytes(self):
+        return {0: 8 * self.pixels, 1: 20 * self.pixels, 8: 8 * self.pixels}
 
-    def dominant_units(self):
-        return self.pixels
-
-    def cpu_solve(self, real="f32"):
+    def cpu_sample(self, real="f32"):
         import oracle as O
         W = self.W
         O.dts_solve(self.inst.rgba, self.inst.target, self.inst.confidence, 1,
                     W.CFG0_FILTER, W.CFG0_OPT, real=real)
-        return self.pixels
+        return self.pixels, "one full solve"
 
 
-WORKLOADS = {"cfg0": Cfg0}
+class Cfg1:
+    """HFBS colorization 640x480, U and V channels, 64 iterations (config 1)."""
+
+    name = "cfg1_hfbs_colorization_640x480_uv"
+    dtype = "f32"
+
+    def __init__(self, rank: int):
+        import domain_transform_solver_gb300 as D
+        from domain_transform_solver_gb300 import workloads as W
+        self.D, self.W = D, W
+        self.u, self.v = W.colorization_instance()
+        self.pixels = 2 * self.u.width * self.u.height
+        self.iters = W.CFG1_HFBS["optim_iter_max"]
+        self.voxels = 2 * 80 * 60 * 16
+
+    def setup(self, stream_handle: int):
+        D, W = self.D, self.W
+        w, h = self.u.width, self.u.height
+        self.b = D.Batch([(w, h), (w, h)])
+        self.b.set_stream(stream_handle)
+        self.b.upload(D.COLOR_SPACE.RGB, [self.u.rgba, self.u.rgba],
+                      [self.u.target, self.v], [self.u.confidence, self.u.confidence])
+        self.hpc = D.HFBSGridParams(**W.CFG1_HFBS)._c()
+        self.lib = self.b._lib
+        self._pin = [_pinned_copy(self.u.rgba), _pinned_copy(self.u.target),
+                     _pinned_copy(self.v), _pinned_copy(self.u.confidence),
+                     _pinned_empty((h, w)), _pinned_empty((h, w))]
+        rg, tu, tv, cf, o0, o1 = self._pin
+        self.h_rgba = _ptrs([rg, rg])
+        self.h_t = _ptrs([tu, tv])
+        self.h_c = _ptrs([cf, cf])
+        self.h_o = _ptrs([o0, o1])
+
+    def step(self):
+        from domain_transform_solver_gb300._lib import check
+        check(self.lib.dtsgb_batch_solve_hfbs(self.b.handle, ctypes.byref(self.hpc)))
+
+    def step_e2e(self):
+        from domain_transform_solver_gb300._lib import check
+        h = self.b.handle
+        check(self.lib.dtsgb_batch_upload(h, 0, self.h_rgba, self.h_t, self.h_c))
+        self.step()
+        check(self.lib.dtsgb_batch_download(h, 1, self.h_o))
+
+    def e2e_bytes(self):
+        return self.pixels * 12, self.pixels * 4
+
+    def algorithmic_bytes(self):
+        px, vx = self.pixels, self.voxels
+        return {3: 12 * px + 12 * vx, 4: 12 * vx, 5: 28 * vx, 7: 8 * px}
+
+    def cpu_sample(self, real="f32"):
+        import oracle as O
+        W = self.W
+        for t in (self.u.target, self.v):
+            O.hfbs_solve(self.u.rgba, t, self.u.confidence, 0, W.CFG1_HFBS,
+                         max_grid=(96, 96, 32), real=real)
+        return self.pixels, "U and V solves"
+
+
+WORKLOADS = {"cfg3": Cfg3, "cfg0": Cfg0, "cfg1": Cfg1}
 
 
 # ---- arms ----------------------------------------------------------------------
-def dist_setup(n_gpus):
+def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
+        import torch
         import torch.distributed as dist
+        torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     return world, rank, local
 
@@ -185,39 +354,43 @@ def max_over_ranks(world, value):
     return float(t.item())
 
 
+def cores_used():
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
 def cpu_baseline(wl, budget_s=12.0, real="f32"):
-    sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
     O.build()
-    wl.cpu_solve(real)  # warm-up (page-in, thread pool)
+    wl.cpu_sample(real)  # warm-up (page-in, thread pool)
     px, t0, n = 0, time.perf_counter(), 0
+    desc = ""
     while True:
-        px += wl.cpu_solve(real)
+        p, desc = wl.cpu_sample(real)
+        px += p
         n += 1
         el = time.perf_counter() - t0
-        if el >= budget_s or n >= 200:
+        if el >= budget_s or n >= 500:
             break
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": px / el / 1e6, "unit": "Mpix/s", "cores": cores, "kind": "port",
-            "sample": f"{n} full solves of {wl.name} by the FP32 oracle port "
-                      f"(OpenMP, {cores} threads), {el:.1f} s"}
+    return {"value": px / el / 1e6, "unit": "Mpix/s", "cores": cores_used(), "kind": "port",
+            "sample": f"{n} x ({desc}) of {wl.name} by the FP32 oracle port "
+                      f"(OpenMP, {cores_used()} threads), {el:.1f} s"}
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return
     wl = WORKLOADS[args.workload](rank)
-    sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
     O.build()
+    desc = ""
     for _ in range(args.warmup):
-        wl.cpu_solve()
+        wl.cpu_sample()
     t0 = time.perf_counter()
     px = 0
     for _ in range(args.steps):
-        px += wl.cpu_solve()
+        p, desc = wl.cpu_sample()
+        px += p
     el = time.perf_counter() - t0
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     value = px / el / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpix/s",
@@ -225,13 +398,14 @@ def run_reference(args, world, rank):
         "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": wl.name, "pixels_per_step": wl.pixels,
-                   "iterations": wl.iters},
-        "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full solves of {wl.name}"},
+                   "iterations": wl.iters, "sample_per_step": desc},
+        "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": cores_used(),
+                         "kind": "port", "sample": f"{args.steps} x ({desc})"},
         "e2e": {"value": value, "unit": "Mpix/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-        "note": "reference CUDA build not buildable here (empty libcua/CUB "
-                "submodules, CUDA 8/9 era); CPU restatement of its algorithm timed",
+        "note": "the reference's CUDA build cannot be built with this toolchain (empty "
+                "libcua/CUB submodules, CUDA 8/9-era CUB API); its algorithm's CPU "
+                "restatement is timed on all host threads",
     }
     print(json.dumps(line), flush=True)
 
@@ -239,61 +413,79 @@ def run_reference(args, world, rank):
 def run_ours(args, world, rank, local):
     import torch
     torch.cuda.set_device(local)
-    import domain_transform_solver_gb300 as D
+    import domain_transform_solver_gb300 as D  # noqa: F401  (loads libdtsgb.so)
     from domain_transform_solver_gb300 import _lib
     lib = _lib.load()
     wl = WORKLOADS[args.workload](rank)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     wl.setup(stream.cuda_stream)
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    big = wl.pixels * 16 > 2 * (129 << 20)
+    flush = None if big else torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32,
+                                         device="cuda")
     try:
-        dev_id = torch.cuda.get_device_properties(local).uuid
-        dev_id = "GPU-" + str(dev_id) if not str(dev_id).startswith("GPU-") else str(dev_id)
+        uid = str(torch.cuda.get_device_properties(local).uuid)
+        dev_id = uid if uid.startswith("GPU-") else "GPU-" + uid
     except Exception:
         dev_id = str(local)
-    for _ in range(max(args.warmup, 1)):
-        wl.step()
-    torch.cuda.synchronize()
-    sampler = ClockSampler(dev_id)
     lib.dtsgb_profile_reset()
     lib.dtsgb_profile_enable(1)
+    for _ in range(max(args.warmup, 3)):
+        wl.step()
+    torch.cuda.synchronize()
+    lib.dtsgb_profile_reset()
+    sampler = ClockSampler(dev_id)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
     barrier(world)
     torch.cuda.synchronize()
     for k in range(args.steps):
-        flush.zero_()  # L2 flush between steps (outside the step's events)
+        if flush is not None:
+            flush.zero_()  # L2 flush between steps, outside the step's events
         ev[k][0].record(stream)
         wl.step()
         ev[k][1].record(stream)
     torch.cuda.synchronize()
     barrier(world)
-    lib.dtsgb_profile_enable(0)
     clocks = sampler.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = max_over_ranks(world, sum(step_ms))
     ms_per_step = total_ms / args.steps
     value = world * wl.pixels / (ms_per_step * 1e-3) / 1e6
 
-    # per-kernel launch statistics from the profiled timed region
-    import ctypes
-    launches_total = 0
+    # per-kernel launch durations inside the timed region (CUDA events recorded
+    # on the launching stream by the library; graph replays keep the events of
+    # the latest replay, i.e. the last step)
     per_kernel = {}
     for kid in range(9):
         n, t = ctypes.c_int(), ctypes.c_double()
         lib.dtsgb_profile_read(kid, ctypes.byref(n), ctypes.byref(t))
-        launches_total += n.value
-        per_kernel[kid] = (n.value, t.value)
+        if n.value:
+            per_kernel[kid] = (n.value, t.value)
+    lib.dtsgb_profile_enable(0)
     lib.dtsgb_profile_reset()
-    n_dom, t_dom = per_kernel[wl.dominant_id]
-    avg_dom_ms = t_dom / max(n_dom, 1)
+    graph_replayed = hasattr(wl, "b")
+    steps_seen = 1 if graph_replayed else args.steps
+    launches_per_step = sum(n for n, _ in per_kernel.values()) / steps_seen
+    algo = wl.algorithmic_bytes()
     peak, peak_kind = peaks()
-    achieved = wl.bytes_per_px * wl.dominant_units() / (avg_dom_ms * 1e-3) / 1e9
+    kernels = {}
+    for kid, (n, t) in per_kernel.items():
+        avg = t / n
+        rec = {"launches_per_step": n / steps_seen, "avg_launch_ms": avg,
+               "share_of_step": (t / steps_seen) / ms_per_step}
+        if kid in algo:
+            rec["achieved_gbs"] = algo[kid] / (avg * 1e-3) / 1e9
+            rec["frac_of_measured_hbm"] = rec["achieved_gbs"] / peak
+        kernels[KERNEL_NAMES[kid]] = rec
+    dom = max(per_kernel, key=lambda k: per_kernel[k][1])
+    n_dom, t_dom = per_kernel[dom]
+    avg_dom = t_dom / n_dom
+    achieved = algo[dom] / (avg_dom * 1e-3) / 1e9 if dom in algo else None
     traffic = None
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get(wl.name)
+        traffic = json.loads(tf.read_text()).get(wl.name, {}).get(KERNEL_NAMES[dom])
 
     # e2e through the C ABI with pinned host buffers
     for _ in range(2):
@@ -302,12 +494,13 @@ def run_ours(args, world, rank, local):
     barrier(world)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    e_steps = max(1, min(args.steps, 10))
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(e_steps):
         wl.step_e2e()
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = max_over_ranks(world, e0.elapsed_time(e1)) / args.steps
+    e2e_ms = max_over_ranks(world, e0.elapsed_time(e1)) / e_steps
     h2d, d2h = wl.e2e_bytes()
     e2e_value = world * wl.pixels / (e2e_ms * 1e-3) / 1e6
 
@@ -315,18 +508,22 @@ def run_ours(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded, shapes of the reference's datasets)",
+        "dtype": wl.dtype, "data": "synthetic (seeded, shapes of the reference's datasets)",
         "config": {"workload": wl.name, "pixels_per_step": wl.pixels,
-                   "iterations": wl.iters, "l2": "flushed between steps (256 MB write)",
-                   "parallelism": f"replicas x{world}"},
+                   "voxels_per_step": wl.voxels, "iterations": wl.iters,
+                   "l2": ("inputs larger than L2" if big
+                          else "flushed between steps (256 MB write)"),
+                   "parallelism": f"independent instances x{world} GPUs"},
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-        "roofline": {"bound": "hbm", "kernel": wl.dominant_name, "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": traffic,
-                     "avg_launch_ms": avg_dom_ms, "launches": n_dom,
-                     "algorithmic_bytes_per_launch": wl.bytes_per_px * wl.dominant_units()},
-        "gpu_launches": launches_total,
+        "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": achieved,
+                     "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic": traffic, "avg_launch_ms": avg_dom,
+                     "algorithmic_bytes_per_launch": algo.get(dom)},
+        "kernels": kernels,
+        "gpu_launches": int(round(launches_per_step * args.steps)),
         "clocks": clocks,
     }
     if rank == 0 and world == 1:
@@ -341,9 +538,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="cfg0")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="cfg3")
     args = ap.parse_args()
-    world, rank, local = dist_setup(args.gpus)
+    world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:

@@ -115,6 +115,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_hfbs_download": ([vp, i, vp], i),
         "dtsgb_hfbs_download_device": ([vp, i, vp], i),
         "dtsgb_hfbs_grid_dims": ([vp, P(i), P(i), P(i)], i),
+        "dtsgb_dts_synchronize": ([vp], i),
+        "dtsgb_hfbs_synchronize": ([vp], i),
         "dtsgb_hfbs_debug_grid": ([vp, i, vp], i),
         "dtsgb_profile_enable": ([i], i),
         "dtsgb_profile_reset": ([], i),

@@ -60,6 +60,7 @@ struct dtsgb_batch_s {
   Tile* d_tb = nullptr;
   Tile* d_ti = nullptr;
   int ntb = 0, nti = 0;
+  bool small = false;
   int dts_res = -1;
   bool hfbs_done = false;
   bool use_graphs = true;
@@ -251,7 +252,13 @@ DTSGB_API int dtsgb_batch_create(int n, const int* widths, const int* heights,
   b->st = (flags & DTSGB_FLAG_BF16_STORAGE) ? Storage::BF16 : Storage::F32;
   b->ref_y = (flags & DTSGB_FLAG_FIX_Y_LIMIT) ? 0 : 1;
   std::vector<Tile> tb, ti;
-  long long off = 0;
+  long long off = 0, tiles64 = 0;
+  for (int i = 0; i < n; ++i)
+    tiles64 += (long long)((widths[i] + kIterTW - 1) / kIterTW) *
+               ((heights[i] + kIterTH - 1) / kIterTH);
+  b->small = use_small_iter_tiles(tiles64);
+  const int itw = b->small ? kIterSmallTW : kIterTW;
+  const int ith = b->small ? kIterSmallTH : kIterTH;
   for (int i = 0; i < n; ++i) {
     Inst I{widths[i], heights[i], round_up(widths[i], 32), 0, off};
     b->inst.push_back(I);
@@ -260,8 +267,8 @@ DTSGB_API int dtsgb_batch_create(int n, const int* widths, const int* heights,
     b->max_h = std::max(b->max_h, I.h);
     for (int y = 0; y < I.h; y += kBoundsTH)
       for (int x = 0; x < I.w; x += kBoundsTW) tb.push_back(Tile{i, x, y, 0});
-    for (int y = 0; y < I.h; y += kIterTH)
-      for (int x = 0; x < I.w; x += kIterTW) ti.push_back(Tile{i, x, y, 0});
+    for (int y = 0; y < I.h; y += ith)
+      for (int x = 0; x < I.w; x += itw) ti.push_back(Tile{i, x, y, 0});
   }
   b->total = off;
   b->ntb = (int)tb.size();
@@ -363,7 +370,7 @@ DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b, const dtsgb_filter_params* 
   const int halo = (int)std::floor(p->sigma_z);
   const bool iterate = p->loss != DTSGB_L1 && p->num_iterations > 0;
   const DtsLaunch Lb{b->d_inst, b->d_tb, b->ntb, b->n};
-  const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n};
+  const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n, b->small};
   int res = 0;
   auto enqueue = [&]() -> int {
     int st = launch_init_var(Li, b->st, b->target, b->v[0], b->stream);

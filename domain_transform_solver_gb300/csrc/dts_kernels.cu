@@ -462,12 +462,11 @@ int launch_bounds(const DtsLaunch& L, const uchar4* guide, uint32_t* bounds,
   return DTSGB_OK;
 }
 
-template <typename TS, int MODE>
-static int launch_iter_t(const DtsLaunch& L, const float* vin, float* vout,
-                         const void* target, const void* conf,
-                         const uint32_t* bounds, float lambda, float step,
-                         float overwrite, int hx, int hy, cudaStream_t s) {
-  const int TW = kIterTW, TH = kIterTH;
+template <typename TS, int MODE, int TW, int TH>
+static int launch_iter_shape(const DtsLaunch& L, const float* vin, float* vout,
+                             const void* target, const void* conf,
+                             const uint32_t* bounds, float lambda, float step,
+                             float overwrite, int hx, int hy, cudaStream_t s) {
   const size_t smem = sizeof(float) * ((size_t)(TH + 2 * hy) * (TW + 2 * hx) +
                                        (size_t)(TH + 2 * hy) * TW);
   if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "sigma_z too large");
@@ -479,6 +478,18 @@ static int launch_iter_t(const DtsLaunch& L, const float* vin, float* vout,
       bounds, lambda, step, overwrite, hx, hy);
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
+}
+
+template <typename TS, int MODE>
+static int launch_iter_t(const DtsLaunch& L, const float* vin, float* vout,
+                         const void* target, const void* conf,
+                         const uint32_t* bounds, float lambda, float step,
+                         float overwrite, int hx, int hy, cudaStream_t s) {
+  if (L.small)
+    return launch_iter_shape<TS, MODE, kIterSmallTW, kIterSmallTH>(
+        L, vin, vout, target, conf, bounds, lambda, step, overwrite, hx, hy, s);
+  return launch_iter_shape<TS, MODE, kIterTW, kIterTH>(
+      L, vin, vout, target, conf, bounds, lambda, step, overwrite, hx, hy, s);
 }
 
 int launch_dts_iter(const DtsLaunch& L, Storage st, IterMode mode,
@@ -543,13 +554,12 @@ int launch_fill_storage(Storage st, void* dst, long long n, float value,
   return DTSGB_OK;
 }
 
-template <int NCH, bool CONF, typename TS>
-static int launch_filter_t(const DtsLaunch& L, const float* in0,
-                           const float* in1, float* out0, float* out1,
-                           const uint32_t* bounds, int hx, int hy,
-                           void* conf_out, float scale, int left_clear,
-                           cudaStream_t s) {
-  const int TW = kIterTW, TH = kIterTH;
+template <int NCH, bool CONF, typename TS, int TW, int TH>
+static int launch_filter_shape(const DtsLaunch& L, const float* in0,
+                               const float* in1, float* out0, float* out1,
+                               const uint32_t* bounds, int hx, int hy,
+                               void* conf_out, float scale, int left_clear,
+                               cudaStream_t s) {
   const size_t smem = NCH * sizeof(float) *
                       ((size_t)(TH + 2 * hy) * (TW + 2 * hx) + (size_t)(TH + 2 * hy) * TW);
   if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "filter sigma too large");
@@ -561,6 +571,19 @@ static int launch_filter_t(const DtsLaunch& L, const float* in0,
       scale, left_clear);
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
+}
+
+template <int NCH, bool CONF, typename TS>
+static int launch_filter_t(const DtsLaunch& L, const float* in0,
+                           const float* in1, float* out0, float* out1,
+                           const uint32_t* bounds, int hx, int hy,
+                           void* conf_out, float scale, int left_clear,
+                           cudaStream_t s) {
+  if (L.small)
+    return launch_filter_shape<NCH, CONF, TS, kIterSmallTW, kIterSmallTH>(
+        L, in0, in1, out0, out1, bounds, hx, hy, conf_out, scale, left_clear, s);
+  return launch_filter_shape<NCH, CONF, TS, kIterTW, kIterTH>(
+      L, in0, in1, out0, out1, bounds, hx, hy, conf_out, scale, left_clear, s);
 }
 
 int launch_filter_pass(const DtsLaunch& L, int nch, const float* in0,

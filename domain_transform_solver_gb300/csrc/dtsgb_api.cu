@@ -91,13 +91,19 @@ struct dtsgb_dts_s {
 
   size_t tsize() const { return st == Storage::F32 ? 4 : 2; }
   DtsLaunch launch_b() const { return DtsLaunch{d_inst, d_tb, ntb, 1}; }
-  DtsLaunch launch_i() const { return DtsLaunch{d_inst, d_ti, nti, 1}; }
+  bool small = false;
+  DtsLaunch launch_i() const { return DtsLaunch{d_inst, d_ti, nti, 1, small}; }
 };
 
 static int dts_layout(dtsgb_dts_t h) {
   h->h_inst = Inst{h->w, h->h, h->pitch, 0, 0};
   std::vector<Tile> tb = make_tiles(h->w, h->h, kBoundsTW, kBoundsTH);
-  std::vector<Tile> ti = make_tiles(h->w, h->h, kIterTW, kIterTH);
+  const long long t64 = (long long)((h->w + kIterTW - 1) / kIterTW) *
+                        ((h->h + kIterTH - 1) / kIterTH);
+  h->small = use_small_iter_tiles(t64);
+  std::vector<Tile> ti =
+      h->small ? make_tiles(h->w, h->h, kIterSmallTW, kIterSmallTH)
+               : make_tiles(h->w, h->h, kIterTW, kIterTH);
   h->ntb = (int)tb.size();
   h->nti = (int)ti.size();
   DTSGB_CUDA(cudaMemcpyAsync(h->d_inst, &h->h_inst, sizeof(Inst),
@@ -153,8 +159,8 @@ DTSGB_API int dtsgb_dts_create(int max_w, int max_h, unsigned flags,
   h->own_stream = true;
   const size_t ntiles_b = (size_t)((max_w + kBoundsTW - 1) / kBoundsTW) *
                           ((max_h + kBoundsTH - 1) / kBoundsTH);
-  const size_t ntiles_i = (size_t)((max_w + kIterTW - 1) / kIterTW) *
-                          ((max_h + kIterTH - 1) / kIterTH);
+  const size_t ntiles_i = (size_t)((max_w + kIterSmallTW - 1) / kIterSmallTW) *
+                          ((max_h + kIterSmallTH - 1) / kIterSmallTH);
   if (!st) st = dalloc(&h->guide, h->plane);
   if (!st) st = dalloc((char**)&h->target, h->plane * h->tsize());
   if (!st) st = dalloc((char**)&h->conf, h->plane * h->tsize());
@@ -194,6 +200,12 @@ DTSGB_API int dtsgb_dts_set_stream(dtsgb_dts_t h, void* stream) {
     DTSGB_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     h->own_stream = true;
   }
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_dts_synchronize(dtsgb_dts_t h) {
+  if (!h) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null handle");
+  DTSGB_CUDA(cudaStreamSynchronize(h->stream));
   return DTSGB_OK;
 }
 
@@ -652,6 +664,12 @@ DTSGB_API int dtsgb_hfbs_set_stream(dtsgb_hfbs_t h, void* stream) {
     DTSGB_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     h->own_stream = true;
   }
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_hfbs_synchronize(dtsgb_hfbs_t h) {
+  if (!h) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null handle");
+  DTSGB_CUDA(cudaStreamSynchronize(h->stream));
   return DTSGB_OK;
 }
 

@@ -133,11 +133,15 @@ struct DtsLaunch {
   const Tile* d_tiles;  // device tile table for the tile shape in use
   int n_tiles;
   int n_inst;
+  bool small = false;   // iteration tiles of kIterSmallTW x kIterSmallTH
 };
 
 // Tile shapes (compile-time in the kernels).
 constexpr int kBoundsTW = 32, kBoundsTH = 32;
 constexpr int kIterTW = 64, kIterTH = 64;
+// Images too small to give every SM a few 64x64 tiles use 32x32 tiles.
+constexpr int kIterSmallTW = 32, kIterSmallTH = 32;
+inline bool use_small_iter_tiles(long long tiles64) { return tiles64 < 4 * 152; }
 
 int launch_color_convert(const Inst* h_inst, const Inst* d_inst, int n_inst,
                          uchar4* guide, int color_space, cudaStream_t s);

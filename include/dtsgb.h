@@ -134,6 +134,8 @@ DTSGB_API int dtsgb_dts_create(int max_w, int max_h, unsigned flags,
 DTSGB_API int dtsgb_dts_destroy(dtsgb_dts_t h);
 /* (new) stream for all later work of this handle; NULL = own stream. */
 DTSGB_API int dtsgb_dts_set_stream(dtsgb_dts_t h, void* cuda_stream);
+/* (new) wait for all work queued on the handle's stream. */
+DTSGB_API int dtsgb_dts_synchronize(dtsgb_dts_t h);
 /* SetImageDim, src/domain_transform_filter.h:31 (invalid dims: error, the
  * previous dims stay, as the reference ignores them). */
 DTSGB_API int dtsgb_dts_set_image_dim(dtsgb_dts_t h, int width, int height);
@@ -194,6 +196,7 @@ DTSGB_API int dtsgb_hfbs_create(int max_w, int max_h, int max_grid_x,
                                 unsigned flags, dtsgb_hfbs_t* out);
 DTSGB_API int dtsgb_hfbs_destroy(dtsgb_hfbs_t h);
 DTSGB_API int dtsgb_hfbs_set_stream(dtsgb_hfbs_t h, void* cuda_stream);
+DTSGB_API int dtsgb_hfbs_synchronize(dtsgb_hfbs_t h);
 /* SetImageDim, hfbs.h:115. */
 DTSGB_API int dtsgb_hfbs_set_image_dim(dtsgb_hfbs_t h, int width, int height);
 /* InitFrame(color_space, color_image, target, confidence), hfbs.h:121. */

@@ -30,12 +30,13 @@ def _parity(D, O, rgba, t, c, cs, params, max_grid):
     assert s.GridDims() == o.grid_dims()
     # bin assignment is integer work: counts bit-exact
     assert np.array_equal(s.DebugGrid(0), o.grid("splat_sum").astype(np.float32))
-    for k, name in ((1, "splat_c"), (2, "b"), (3, "splat_norm"), (4, "inv_diag_A"),
-                    (7, "z_final")):
-        g, r = s.DebugGrid(k), o.grid(name)
-        scale = max(1.0, float(np.abs(r).max()))
-        assert np.abs(g - r).max() <= 1e-4 * scale, name
     rng_t = P.target_range(t)
+    # scales: sums by their magnitude, z (target units) by the target range
+    for k, name, scale in ((1, "splat_c", None), (2, "b", None), (3, "splat_norm", None),
+                           (4, "inv_diag_A", None), (7, "z_final", rng_t)):
+        g, r = s.DebugGrid(k), o.grid(name)
+        scale = scale or max(1.0, float(np.abs(r).max()))
+        assert np.abs(g - r).max() <= 1e-4 * scale, name
     fin = np.isfinite(ref)
     assert np.array_equal(np.isfinite(out), fin)
     err = np.abs(out[fin] - ref[fin])
