@@ -453,6 +453,8 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
   B.max_pixels = max_px;
   B.max_cells = max_cells;
   B.max_lines = max_lines;
+  B.max_rows = 0;
+  for (const HInst& H : hi) B.max_rows = std::max(B.max_rows, (long long)H.gy * H.gl);
   B.max_gl = gl;
   B.guide = b->guide;
   B.target = b->target;

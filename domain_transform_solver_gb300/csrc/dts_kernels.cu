@@ -148,6 +148,94 @@ __global__ void __launch_bounds__(kThreads)
 // target replaces v where c > overwrite before each half-step
 // (src/domain_transform_solver.cu:126-130, 160-164).
 // ---------------------------------------------------------------------------
+// Window sums along a line held in shared memory (element stride `stride`),
+// for consecutive window positions: a position's window [lo, hi] is reached
+// from the previous one by adding the entering and subtracting the leaving
+// elements; the first position of a run, a backward move or a long jump sums
+// directly.  Runs are kSeg positions long, which bounds the rounding drift of
+// the running sum to a few ulp of the window sum.
+constexpr int kSeg = 8;
+
+struct Slide {
+  float sum;
+  int lo, hi;
+};
+
+__device__ __forceinline__ float window_sum(const float* __restrict__ s,
+                                            int stride, int lo, int hi,
+                                            Slide& w, bool fresh) {
+  float acc;
+  if (fresh || lo < w.lo || hi < w.hi || (lo - w.lo) + (hi - w.hi) > 6) {
+    acc = 0.f;
+    for (int k = lo; k <= hi; ++k) acc += s[k * stride];
+  } else {
+    acc = w.sum;
+    for (int k = w.hi + 1; k <= hi; ++k) acc += s[k * stride];
+    for (int k = w.lo; k < lo; ++k) acc -= s[k * stride];
+  }
+  w.sum = acc;
+  w.lo = lo;
+  w.hi = hi;
+  return acc;
+}
+
+// Eight consecutive values starting at an 8-element-aligned address; `full`
+// means all eight are inside the row, otherwise only the first n are read.
+__device__ __forceinline__ void load8(const float* __restrict__ p, bool full,
+                                      int n, float (&o)[kSeg]) {
+  if (full) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(p));
+    const float4 b = __ldg(reinterpret_cast<const float4*>(p) + 1);
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+  } else {
+#pragma unroll
+    for (int j = 0; j < kSeg; ++j) o[j] = j < n ? __ldg(p + j) : 0.f;
+  }
+}
+__device__ __forceinline__ void load8(const __nv_bfloat16* __restrict__ p,
+                                      bool full, int n, float (&o)[kSeg]) {
+  if (full) {
+    const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
+    const uint32_t w[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      o[2 * j] = __uint_as_float(w[j] << 16);
+      o[2 * j + 1] = __uint_as_float(w[j] & 0xffff0000u);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < kSeg; ++j) o[j] = j < n ? __bfloat162float(p[j]) : 0.f;
+  }
+}
+__device__ __forceinline__ void load8(const uint32_t* __restrict__ p, bool full,
+                                      int n, uint32_t (&o)[kSeg]) {
+  if (full) {
+    const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
+    const uint4 b = __ldg(reinterpret_cast<const uint4*>(p) + 1);
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+  } else {
+#pragma unroll
+    for (int j = 0; j < kSeg; ++j) o[j] = j < n ? __ldg(p + j) : 0u;
+  }
+}
+
+// X half-step update of one pixel (src/domain_transform_solver.cuh:37-86).
+template <int MODE>
+__device__ __forceinline__ float x_update(float v, float B, float tv, float cv,
+                                          float nf, float lambda, float step) {
+  const float cn = __fdiv_rn(cv, nf);
+  const float d = v - tv;
+  float g;
+  if (MODE == 0) {
+    g = 2.f * cn * d;
+  } else {
+    g = __fdiv_rn(cn * d, __fsqrt_rn(__fmaf_rn(d, d, 1e-6f)));
+  }
+  return __fmaf_rn(step, -__fmaf_rn(lambda, v - B, 0.5f * g), v);
+}
+
 template <typename TS, int MODE, int TW, int TH>
 __global__ void __launch_bounds__(kThreads)
     k_dts_iter(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
@@ -155,14 +243,18 @@ __global__ void __launch_bounds__(kThreads)
                const TS* __restrict__ tgt, const TS* __restrict__ cnf,
                const uint32_t* __restrict__ bnd, float lambda, float step,
                float overwrite, int hx, int hy) {
+  static_assert(TW % kSeg == 0 && TH % kSeg == 0, "tile must hold whole runs");
   extern __shared__ float sm[];
   const Tile t = tiles[blockIdx.x];
   const Inst in = insts[t.inst];
   const int W = in.w, H = in.h, P = in.pitch;
   const long long off = in.off;
   const int SW = TW + 2 * hx, SR = TH + 2 * hy;
-  float* sv = sm;            // SR x SW previous iterate
-  float* sx = sm + SR * SW;  // SR x TW after the X half-step
+  // odd row strides: one row per lane is bank-conflict free
+  const int SWp = SW | 1;
+  constexpr int TXp = TW + 1;
+  float* sv = sm;             // SR x SWp previous iterate (tile + halo)
+  float* sx = sm + SR * SWp;  // SR x TXp after the X half-step
   const bool over = overwrite > 0.f && overwrite < 1.f;
   const int gx0 = t.x0 - hx, gy0 = t.y0 - hy;
   for (int i = threadIdx.x; i < SR * SW; i += blockDim.x) {
@@ -174,53 +266,62 @@ __global__ void __launch_bounds__(kThreads)
       v = __ldg(vin + p);
       if (over && load_f(cnf + p) > overwrite) v = load_f(tgt + p);
     }
-    sv[i] = v;
+    sv[r * SWp + c] = v;
   }
   __syncthreads();
-  const float slam = step * lambda;
-  for (int i = threadIdx.x; i < SR * TW; i += blockDim.x) {
-    const int r = i / TW, c = i - r * TW;
-    const int x = t.x0 + c, y = gy0 + r;
-    float out = 0.f;
-    if (x < W && y >= 0 && y < H) {
-      const long long p = off + (long long)y * P + x;
-      const uint32_t b = __ldg(bnd + p);
-      // radii clamped to the staged halo: a window never reads outside it
-      const int dl = min((int)(b & 0xff), hx + 1), du = min((int)((b >> 8) & 0xff), hx);
-      const float* row = sv + r * SW + (c + hx);
-      float s = 0.f;
-      for (int k = 1 - dl; k <= du; ++k) s += row[k];
-      const float nf = (float)(dl + du);
-      const float B = __fdiv_rn(s, nf);
-      const float v = row[0];
-      const float tv = load_f(tgt + p), cv = load_f(cnf + p);
-      const float cn = __fdiv_rn(cv, nf);
-      const float d = v - tv;
-      float g;
-      if (MODE == 0) {
-        g = 2.f * cn * d;
-      } else {
-        g = __fdiv_rn(cn * d, __fsqrt_rn(__fmaf_rn(d, d, 1e-6f)));
+  // X half-step: one run of kSeg pixels of one row per item; consecutive
+  // lanes take consecutive rows.
+  constexpr int NSX = TW / kSeg;
+  for (int k = threadIdx.x; k < SR * NSX; k += blockDim.x) {
+    const int r = k % SR, sg = k / SR;
+    const int y = gy0 + r;
+    const int xs = t.x0 + sg * kSeg;
+    if (y < 0 || y >= H || xs >= W) continue;
+    const int n = min(kSeg, W - xs);
+    const bool full = n == kSeg;
+    const long long p = off + (long long)y * P + xs;
+    uint32_t b[kSeg];
+    float tv[kSeg], cv[kSeg];
+    load8(bnd + p, full, n, b);
+    load8(tgt + p, full, n, tv);
+    load8(cnf + p, full, n, cv);
+    const float* row = sv + r * SWp + hx + sg * kSeg;  // row[j] = v(xs + j)
+    float* out = sx + r * TXp + sg * kSeg;
+    Slide w{0.f, 0, -1};
+#pragma unroll
+    for (int j = 0; j < kSeg; ++j) {
+      if (j < n) {
+        // radii clamped to the staged halo: a window never reads outside it
+        const int dl = min((int)(b[j] & 0xff), hx + 1);
+        const int du = min((int)((b[j] >> 8) & 0xff), hx);
+        const float s = window_sum(row, 1, j + 1 - dl, j + du, w, j == 0);
+        const float nf = (float)(dl + du);
+        float o = x_update<MODE>(row[j], __fdiv_rn(s, nf), tv[j], cv[j], nf, lambda, step);
+        if (over && cv[j] > overwrite) o = tv[j];
+        out[j] = o;
       }
-      out = __fmaf_rn(step, -__fmaf_rn(lambda, v - B, 0.5f * g), v);
-      if (over && cv > overwrite) out = tv;
     }
-    sx[i] = out;
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
-    const int r = i / TW, c = i - r * TW;
-    const int x = t.x0 + c, y = t.y0 + r;
-    if (x >= W || y >= H) continue;
-    const long long p = off + (long long)y * P + x;
-    const uint32_t b = __ldg(bnd + p);
-    const int dl = min((int)((b >> 16) & 0xff), hy + 1), du = min((int)(b >> 24), hy);
-    const float* col = sx + (r + hy) * TW + c;
-    float s = 0.f;
-    for (int k = 1 - dl; k <= du; ++k) s += col[k * TW];
-    const float B = __fdiv_rn(s, (float)(dl + du));
-    const float v = col[0];
-    vout[p] = __fmaf_rn(-slam, v - B, v);
+  // Y half-step: one run of kSeg pixels of one column per item; consecutive
+  // lanes take consecutive columns (coalesced bounds loads and stores).
+  const float slam = step * lambda;
+  constexpr int NSY = TH / kSeg;
+  for (int k = threadIdx.x; k < TW * NSY; k += blockDim.x) {
+    const int c = k % TW, sg = k / TW;
+    const int x = t.x0 + c, ys = t.y0 + sg * kSeg;
+    if (x >= W || ys >= H) continue;
+    const int n = min(kSeg, H - ys);
+    const float* col = sx + (hy + sg * kSeg) * TXp + c;  // col[j*TXp] = vx(ys + j)
+    Slide w{0.f, 0, -1};
+    long long p = off + (long long)ys * P + x;
+    for (int j = 0; j < n; ++j, p += P) {
+      const uint32_t b = __ldg(bnd + p);
+      const int dl = min((int)((b >> 16) & 0xff), hy + 1), du = min((int)(b >> 24), hy);
+      const float s = window_sum(col, TXp, j + 1 - dl, j + du, w, j == 0);
+      const float v = col[j * TXp];
+      vout[p] = __fmaf_rn(-slam, v - __fdiv_rn(s, (float)(dl + du)), v);
+    }
   }
 }
 
@@ -467,8 +568,8 @@ static int launch_iter_shape(const DtsLaunch& L, const float* vin, float* vout,
                              const void* target, const void* conf,
                              const uint32_t* bounds, float lambda, float step,
                              float overwrite, int hx, int hy, cudaStream_t s) {
-  const size_t smem = sizeof(float) * ((size_t)(TH + 2 * hy) * (TW + 2 * hx) +
-                                       (size_t)(TH + 2 * hy) * TW);
+  const size_t smem = sizeof(float) * ((size_t)(TH + 2 * hy) * ((TW + 2 * hx) | 1) +
+                                       (size_t)(TH + 2 * hy) * (TW + 1));
   if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "sigma_z too large");
   int st = set_smem(k_dts_iter<TS, MODE, TW, TH>, smem);
   if (st) return st;

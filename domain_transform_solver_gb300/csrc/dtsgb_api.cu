@@ -790,6 +790,7 @@ DTSGB_API int dtsgb_hfbs_optimize(dtsgb_hfbs_t h) {
   B.max_voxels = (long long)I.gx * I.gy * I.gl;
   B.max_pixels = (long long)I.w * I.h;
   B.max_cells = (long long)I.gx * I.gy;
+  B.max_rows = (long long)I.gy * I.gl;
   B.max_lines = std::max({(long long)I.gy * I.gl, (long long)I.gx * I.gl,
                           (long long)I.gx * I.gy});
   B.max_gl = I.gl;

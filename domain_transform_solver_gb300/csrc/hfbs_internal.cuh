@@ -33,6 +33,7 @@ struct HfbsBatch {
   const HInst* d_inst;
   int n_inst;
   long long max_voxels, max_pixels, max_cells, max_lines;
+  long long max_rows;  // max over instances of gy * gl (grid rows along x)
   int max_gl;
   const uchar4* guide;
   const void* target;  // storage type st

@@ -102,27 +102,31 @@ __global__ void k_bistoch(const HInst* __restrict__ insts,
                           const float* __restrict__ count, float pad) {
   const HInst I = insts[blockIdx.y];
   const int gx = I.gx, gy = I.gy, gl = I.gl;
-  const long long n = (long long)gx * gy * gl;
   const float px = I.cov_x ? pad : 0.f, py = I.cov_y ? pad : 0.f,
               pz = I.cov_l ? pad : 0.f;
   const float* s = src + I.grid_off;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(i % gx);
-    const long long t = i / gx;
-    const int y = (int)(t % gy), z = (int)(t / gy);
-    const long long sy = gx, sz = (long long)gx * gy;
-    const float v = s[i];
-    float nb = x > 0 ? s[i - 1] : 0.f;
-    nb += x + 1 < gx ? s[i + 1] : px;
-    nb += y > 0 ? s[i - sy] : 0.f;
-    nb += y + 1 < gy ? s[i + sy] : py;
-    nb += z > 0 ? s[i - sz] : 0.f;
-    nb += z + 1 < gl ? s[i + sz] : pz;
-    const float blurred = 2.f * v + nb;
-    const float cnt = count[I.grid_off + i];
-    dst[I.grid_off + i] =
-        __fsqrt_rn(__fdiv_rn(v * (cnt + 0.00001f), blurred + 0.00001f));
+  const float* cn = count + I.grid_off;
+  float* d = dst + I.grid_off;
+  const int sy = gx, sz = gx * gy;
+  // one warp per grid row (fixed y, l); lanes stride along x
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < gy * gl;
+       row += nwarps) {
+    const int z = row / gy, y = row - z * gy;
+    const int base = row * gx;
+    for (int x = lane; x < gx; x += 32) {
+      const int i = base + x;
+      const float v = s[i];
+      float nb = x > 0 ? s[i - 1] : 0.f;
+      nb += x + 1 < gx ? s[i + 1] : px;
+      nb += y > 0 ? s[i - sy] : 0.f;
+      nb += y + 1 < gy ? s[i + sy] : py;
+      nb += z > 0 ? s[i - sz] : 0.f;
+      nb += z + 1 < gl ? s[i + sz] : pz;
+      const float blurred = 2.f * v + nb;
+      d[i] = __fsqrt_rn(__fdiv_rn(v * (cn[i] + 0.00001f), blurred + 0.00001f));
+    }
   }
 }
 
@@ -144,9 +148,73 @@ __global__ void k_inv_diag(const HInst* __restrict__ insts,
   }
 }
 
+// a15 along x (contiguous lines): one warp per line.  The forward recursion
+// F(i) = s(i) + beta*F(i-1) and the backward one S(i) = s(i) + beta*S(i+1)
+// are decayed scans over 32-element chunks (Hillis-Steele with beta^o weights,
+// carry scaled by beta^(lane+1) between chunks); d(i) = F(i) + beta*S(i+1).
+__global__ void k_laplace_x(const HInst* __restrict__ insts,
+                            const float* __restrict__ s0, float* __restrict__ d0,
+                            const float* __restrict__ s1, float* __restrict__ d1,
+                            float beta) {
+  const HInst I = insts[blockIdx.y];
+  const int gx = I.gx, nlines = I.gy * I.gl;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  float bo[5];  // beta^1, beta^2, beta^4, beta^8, beta^16
+  bo[0] = beta;
+#pragma unroll
+  for (int k = 1; k < 5; ++k) bo[k] = bo[k - 1] * bo[k - 1];
+  float blane = 1.f;  // beta^(lane+1)
+  for (int k = 0; k <= lane; ++k) blane *= beta;
+  float brev = 1.f;  // beta^(32-lane)
+  for (int k = lane; k < 32; ++k) brev *= beta;
+  for (int line = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; line < nlines;
+       line += nwarps) {
+    const long long base = I.grid_off + (long long)line * gx;
+    for (int f = 0; f < 2; ++f) {
+      const float* s = (f ? s1 : s0) + base;
+      float* d = (f ? d1 : d0) + base;
+      // forward: F
+      float carry = 0.f;
+      for (int x0 = 0; x0 < gx; x0 += 32) {
+        const int x = x0 + lane;
+        float r = x < gx ? s[x] : 0.f;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          const float t = __shfl_up_sync(0xffffffffu, r, 1 << k);
+          if (lane >= (1 << k)) r = __fmaf_rn(bo[k], t, r);
+        }
+        r = __fmaf_rn(blane, carry, r);
+        if (x < gx) d[x] = r;
+        carry = __shfl_sync(0xffffffffu, r, 31);
+      }
+      // backward: S over reversed chunks, add beta * S(i+1)
+      carry = 0.f;  // S of the first element after the chunk
+      const int last0 = ((gx - 1) / 32) * 32;
+      for (int x0 = last0; x0 >= 0; x0 -= 32) {
+        const int x = x0 + lane;
+        float r = x < gx ? s[x] : 0.f;  // suffix scan runs from lane 31 down
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          const float t = __shfl_down_sync(0xffffffffu, r, 1 << k);
+          if (lane + (1 << k) < 32) r = __fmaf_rn(bo[k], t, r);
+        }
+        // lanes past the end hold zeros, so the suffix needs no masking;
+        // add the carried S of the next chunk, decayed by beta^(32-lane)
+        r = __fmaf_rn(brev, carry, r);
+        float next = __shfl_down_sync(0xffffffffu, r, 1);  // S(i+1)
+        if (lane == 31) next = carry;
+        if (x < gx) d[x] = __fmaf_rn(beta, next, d[x]);
+        carry = __shfl_sync(0xffffffffu, r, 0);
+      }
+    }
+  }
+}
+
 // a15: Laplace sweep along one axis for two fields at once (src/hfbs.cu:
 // 355-427): d(i) = sum_j beta^|i-j| s(j), forward then backward recursion,
-// one thread per grid line.
+// one thread per grid line (used along y and l, where consecutive threads
+// take consecutive x and the accesses coalesce).
 __global__ void k_laplace(const HInst* __restrict__ insts, int axis,
                           const float* __restrict__ s0, float* __restrict__ d0,
                           const float* __restrict__ s1, float* __restrict__ d1,
@@ -213,30 +281,39 @@ __global__ void k_solve(const HInst* __restrict__ insts,
                         float alpha, float beta) {
   const HInst I = insts[blockIdx.y];
   const int gx = I.gx, gy = I.gy, gl = I.gl;
-  const long long n = (long long)gx * gy * gl;
   const float* z = zs + I.grid_off;
   const float* nn = norm + I.grid_off;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(i % gx);
-    const long long t = i / gx;
-    const int y = (int)(t % gy), zz = (int)(t / gy);
-    const long long sy = gx, sz = (long long)gx * gy;
-    float d = 0.f;
-    if (x > 0) d += z[i - 1] * nn[i - 1];
-    if (x + 1 < gx) d += z[i + 1] * nn[i + 1];
-    if (y > 0) d += z[i - sy] * nn[i - sy];
-    if (y + 1 < gy) d += z[i + sy] * nn[i + sy];
-    if (zz > 0) d += z[i - sz] * nn[i - sz];
-    if (zz + 1 < gl) d += z[i + sz] * nn[i + sz];
-    const long long g = I.grid_off + i;
-    const float q = (b[g] + lambda * nn[i] * d) * invA[g];
-    const float zc = z[i];
-    const float grad = zc - q;
-    const float gc = fabsf(grad) > 1.345f ? copysignf(1.f, grad) : grad;
-    const float hn = __fmaf_rn(beta, h[g], gc);
-    h[g] = hn;
-    zd[g] = zc - alpha * hn;
+  const float* bb = b + I.grid_off;
+  const float* ia = invA + I.grid_off;
+  float* hh = h + I.grid_off;
+  float* zo = zd + I.grid_off;
+  const int sy = gx, sz = gx * gy;
+  // one warp per grid row (fixed y, l); lanes stride along x
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < gy * gl;
+       row += nwarps) {
+    const int zz = row / gy, y = row - zz * gy;
+    const int base = row * gx;
+    for (int x = lane; x < gx; x += 32) {
+      const int i = base + x;
+      float d = 0.f;
+      if (x > 0) d += z[i - 1] * nn[i - 1];
+      if (x + 1 < gx) d += z[i + 1] * nn[i + 1];
+      if (y > 0) d += z[i - sy] * nn[i - sy];
+      if (y + 1 < gy) d += z[i + sy] * nn[i + sy];
+      if (zz > 0) d += z[i - sz] * nn[i - sz];
+      if (zz + 1 < gl) d += z[i + sz] * nn[i + sz];
+      const float q = (bb[i] + lambda * nn[i] * d) * ia[i];
+      const float zc = z[i];
+      const float grad = zc - q;
+      // |grad| > 1.345 with the double threshold of the reference: the
+      // smallest float above 1.345 (double) is 1.345f
+      const float gc = fabsf(grad) >= 1.345f ? copysignf(1.f, grad) : grad;
+      const float hn = __fmaf_rn(beta, hh[i], gc);
+      hh[i] = hn;
+      zo[i] = zc - alpha * hn;
+    }
   }
 }
 
@@ -302,6 +379,8 @@ int blocks_for(long long n) {
 int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   const int ni = B.n_inst;
   const dim3 gv(blocks_for(B.max_voxels), ni);
+  // row kernels: one warp per grid row, 8 warps per block
+  const dim3 gr((unsigned)std::min<long long>((B.max_rows + 7) / 8, 4096), ni);
   const dim3 gp(blocks_for(B.max_pixels), ni);
   const dim3 gc((B.max_cells + 63) / 64, ni);
   const size_t splat_smem = sizeof(float) * 3 * (size_t)B.max_gl * 64;
@@ -332,7 +411,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   float* dst = B.n1;
   for (int it = 0; it < p.bistoch_iter_max; ++it) {
     prof_begin(s, DTSGB_K_HFBS_BISTOCH);
-    k_bistoch<<<gv, kT, 0, s>>>(B.d_inst, src, dst, B.count,
+    k_bistoch<<<gr, kT, 0, s>>>(B.d_inst, src, dst, B.count,
                                 (it % 2 == 0) ? 1.f : 0.f);
     prof_end(s, DTSGB_K_HFBS_BISTOCH);
     float* t = src;
@@ -346,8 +425,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
                                p.lambda);
   // Laplace blur of (c, b): X -> Y -> Z.
   const dim3 gl_lines(blocks_for(B.max_lines), ni);
-  k_laplace<<<gl_lines, kT, 0, s>>>(B.d_inst, 0, B.csum, B.t0, B.b, B.t1,
-                                    p.neg_exp_beta);
+  k_laplace_x<<<gr, kT, 0, s>>>(B.d_inst, B.csum, B.t0, B.b, B.t1, p.neg_exp_beta);
   k_laplace<<<gl_lines, kT, 0, s>>>(B.d_inst, 1, B.t0, B.t2, B.t1, spare,
                                     p.neg_exp_beta);
   k_laplace<<<gl_lines, kT, 0, s>>>(B.d_inst, 2, B.t2, B.t0, spare, B.t1,
@@ -367,7 +445,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   float* zd = B.z1;
   for (int it = 0; it < p.optim_iter_max; ++it) {
     prof_begin(s, DTSGB_K_HFBS_SOLVE);
-    k_solve<<<gv, kT, 0, s>>>(B.d_inst, zs, zd, B.h, norm, B.b, B.invA, p.lambda,
+    k_solve<<<gr, kT, 0, s>>>(B.d_inst, zs, zd, B.h, norm, B.b, B.invA, p.lambda,
                               p.alpha, p.beta);
     prof_end(s, DTSGB_K_HFBS_SOLVE);
     float* t = zs;
