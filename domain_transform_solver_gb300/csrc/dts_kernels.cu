@@ -148,34 +148,19 @@ __global__ void __launch_bounds__(kThreads)
 // target replaces v where c > overwrite before each half-step
 // (src/domain_transform_solver.cu:126-130, 160-164).
 // ---------------------------------------------------------------------------
-// Window sums along a line held in shared memory (element stride `stride`),
-// for consecutive window positions: a position's window [lo, hi] is reached
-// from the previous one by adding the entering and subtracting the leaving
-// elements; the first position of a run, a backward move or a long jump sums
-// directly.  Runs are kSeg positions long, which bounds the rounding drift of
-// the running sum to a few ulp of the window sum.
+// Window sums are direct sums over the window, first element to last, never
+// a difference of running or prefix sums: a subtraction leaves an error of
+// about one ulp of the larger sum, and the Charbonnier gradient
+// x/sqrt(x^2+1e-6) magnifies errors in a near-zero residual about 1000-fold
+// (a one-pixel window must give back the pixel exactly).  Each thread
+// handles runs of kSeg consecutive pixels of a row so that the per-pixel
+// inputs come in as 16-byte vector loads.
 constexpr int kSeg = 8;
 
-struct Slide {
-  float sum;
-  int lo, hi;
-};
-
 __device__ __forceinline__ float window_sum(const float* __restrict__ s,
-                                            int stride, int lo, int hi,
-                                            Slide& w, bool fresh) {
-  float acc;
-  if (fresh || lo < w.lo || hi < w.hi || (lo - w.lo) + (hi - w.hi) > 6) {
-    acc = 0.f;
-    for (int k = lo; k <= hi; ++k) acc += s[k * stride];
-  } else {
-    acc = w.sum;
-    for (int k = w.hi + 1; k <= hi; ++k) acc += s[k * stride];
-    for (int k = w.lo; k < lo; ++k) acc -= s[k * stride];
-  }
-  w.sum = acc;
-  w.lo = lo;
-  w.hi = hi;
+                                            int stride, int lo, int hi) {
+  float acc = 0.f;
+  for (int k = lo; k <= hi; ++k) acc += s[k * stride];
   return acc;
 }
 
@@ -221,11 +206,12 @@ __device__ __forceinline__ void load8(const uint32_t* __restrict__ p, bool full,
   }
 }
 
-// X half-step update of one pixel (src/domain_transform_solver.cuh:37-86).
+// X half-step update of one pixel (src/domain_transform_solver.cuh:37-86);
+// rn = 1/n correctly rounded.
 template <int MODE>
 __device__ __forceinline__ float x_update(float v, float B, float tv, float cv,
-                                          float nf, float lambda, float step) {
-  const float cn = __fdiv_rn(cv, nf);
+                                          float rn, float lambda, float step) {
+  const float cn = cv * rn;
   const float d = v - tv;
   float g;
   if (MODE == 0) {
@@ -244,11 +230,11 @@ __global__ void __launch_bounds__(kThreads)
                const uint32_t* __restrict__ bnd, float lambda, float step,
                float overwrite, int hx, int hy) {
   static_assert(TW % kSeg == 0 && TH % kSeg == 0, "tile must hold whole runs");
+  static_assert(TW % 32 == 0, "tile width must be whole warps");
   extern __shared__ float sm[];
   const Tile t = tiles[blockIdx.x];
   const Inst in = insts[t.inst];
   const int W = in.w, H = in.h, P = in.pitch;
-  const long long off = in.off;
   const int SW = TW + 2 * hx, SR = TH + 2 * hy;
   // odd row strides: one row per lane is bank-conflict free
   const int SWp = SW | 1;
@@ -257,70 +243,85 @@ __global__ void __launch_bounds__(kThreads)
   float* sx = sm + SR * SWp;  // SR x TXp after the X half-step
   const bool over = overwrite > 0.f && overwrite < 1.f;
   const int gx0 = t.x0 - hx, gy0 = t.y0 - hy;
-  for (int i = threadIdx.x; i < SR * SW; i += blockDim.x) {
-    const int r = i / SW, c = i - r * SW;
-    const int x = gx0 + c, y = gy0 + r;
-    float v = 0.f;
-    if (x >= 0 && x < W && y >= 0 && y < H) {
-      const long long p = off + (long long)y * P + x;
-      v = __ldg(vin + p);
-      if (over && load_f(cnf + p) > overwrite) v = load_f(tgt + p);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = kThreads / 32;
+  const float* vin_i = vin + in.off;
+  const TS* tgt_i = tgt + in.off;
+  const TS* cnf_i = cnf + in.off;
+  const uint32_t* bnd_i = bnd + in.off;
+  // stage the iterate: one warp per row, lanes along x (coalesced)
+  for (int r = warp; r < SR; r += NW) {
+    const int y = gy0 + r;
+    const bool yok = y >= 0 && y < H;
+    const float* src = vin_i + (long long)y * P;
+    for (int c = lane; c < SW; c += 32) {
+      const int x = gx0 + c;
+      float v = 0.f;
+      if (yok && x >= 0 && x < W) {
+        v = __ldg(src + x);
+        if (over && load_f(cnf_i + (long long)y * P + x) > overwrite)
+          v = load_f(tgt_i + (long long)y * P + x);
+      }
+      sv[r * SWp + c] = v;
     }
-    sv[r * SWp + c] = v;
   }
   __syncthreads();
-  // X half-step: one run of kSeg pixels of one row per item; consecutive
-  // lanes take consecutive rows.
+  // X half-step: a run of kSeg pixels of one row per lane; the lanes of a
+  // warp take 32 consecutive rows of the same run.
   constexpr int NSX = TW / kSeg;
-  for (int k = threadIdx.x; k < SR * NSX; k += blockDim.x) {
-    const int r = k % SR, sg = k / SR;
+  const int row_blocks = (SR + 31) >> 5;
+  for (int item = warp; item < row_blocks * NSX; item += NW) {
+    const int sg = item % NSX;  // constant divisor
+    const int r = (item / NSX) * 32 + lane;
     const int y = gy0 + r;
     const int xs = t.x0 + sg * kSeg;
-    if (y < 0 || y >= H || xs >= W) continue;
+    if (r >= SR || y < 0 || y >= H || xs >= W) continue;
     const int n = min(kSeg, W - xs);
     const bool full = n == kSeg;
-    const long long p = off + (long long)y * P + xs;
+    const long long p = (long long)y * P + xs;
     uint32_t b[kSeg];
     float tv[kSeg], cv[kSeg];
-    load8(bnd + p, full, n, b);
-    load8(tgt + p, full, n, tv);
-    load8(cnf + p, full, n, cv);
+    load8(bnd_i + p, full, n, b);
+    load8(tgt_i + p, full, n, tv);
+    load8(cnf_i + p, full, n, cv);
     const float* row = sv + r * SWp + hx + sg * kSeg;  // row[j] = v(xs + j)
     float* out = sx + r * TXp + sg * kSeg;
-    Slide w{0.f, 0, -1};
 #pragma unroll
     for (int j = 0; j < kSeg; ++j) {
       if (j < n) {
         // radii clamped to the staged halo: a window never reads outside it
         const int dl = min((int)(b[j] & 0xff), hx + 1);
         const int du = min((int)((b[j] >> 8) & 0xff), hx);
-        const float s = window_sum(row, 1, j + 1 - dl, j + du, w, j == 0);
-        const float nf = (float)(dl + du);
-        float o = x_update<MODE>(row[j], __fdiv_rn(s, nf), tv[j], cv[j], nf, lambda, step);
+        const float s = window_sum(row, 1, j + 1 - dl, j + du);
+        const float rn = __frcp_rn((float)(dl + du));
+        float o = x_update<MODE>(row[j], s * rn, tv[j], cv[j], rn, lambda, step);
         if (over && cv[j] > overwrite) o = tv[j];
         out[j] = o;
       }
     }
   }
   __syncthreads();
-  // Y half-step: one run of kSeg pixels of one column per item; consecutive
-  // lanes take consecutive columns (coalesced bounds loads and stores).
+  // Y half-step: a run of kSeg rows of one column per lane; the lanes of a
+  // warp take 32 consecutive columns (coalesced bounds loads and stores).
   const float slam = step * lambda;
   constexpr int NSY = TH / kSeg;
-  for (int k = threadIdx.x; k < TW * NSY; k += blockDim.x) {
-    const int c = k % TW, sg = k / TW;
+  constexpr int CB = TW / 32;
+  float* vout_i = vout + in.off;
+  for (int item = warp; item < CB * NSY; item += NW) {
+    const int c = (item % CB) * 32 + lane;  // constant divisor
+    const int sg = item / CB;
     const int x = t.x0 + c, ys = t.y0 + sg * kSeg;
     if (x >= W || ys >= H) continue;
     const int n = min(kSeg, H - ys);
     const float* col = sx + (hy + sg * kSeg) * TXp + c;  // col[j*TXp] = vx(ys + j)
-    Slide w{0.f, 0, -1};
-    long long p = off + (long long)ys * P + x;
-    for (int j = 0; j < n; ++j, p += P) {
-      const uint32_t b = __ldg(bnd + p);
+    const uint32_t* bp = bnd_i + (long long)ys * P + x;
+    float* op = vout_i + (long long)ys * P + x;
+    for (int j = 0; j < n; ++j) {
+      const uint32_t b = __ldg(bp + j * P);
       const int dl = min((int)((b >> 16) & 0xff), hy + 1), du = min((int)(b >> 24), hy);
-      const float s = window_sum(col, TXp, j + 1 - dl, j + du, w, j == 0);
+      const float s = window_sum(col, TXp, j + 1 - dl, j + du);
       const float v = col[j * TXp];
-      vout[p] = __fmaf_rn(-slam, v - __fdiv_rn(s, (float)(dl + du)), v);
+      op[j * P] = __fmaf_rn(-slam, v - s * __frcp_rn((float)(dl + du)), v);
     }
   }
 }

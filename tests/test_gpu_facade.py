@@ -13,11 +13,28 @@ pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parents[1]
 
 
-def test_cpp_facade_matches_python(gpu_ready, tmp_path):
+def test_cpp_facade_matches_python(gpu_ready, oracle_mod, tmp_path):
     D = gpu_ready
+    import parity as P
     from domain_transform_solver_gb300 import workloads as W
     inst = W.depth_sr_instance(77, 200, 120, n_poly=10, stride=4)
     h, w = inst.target.shape
+    # the calls through the Python mirror, checked against the FP64 oracle
+    s = D.DomainTransformSolver(D.ImageDim(w, h))
+    s.SetImageDim(D.ImageDim(w, h))
+    s.ClearAll()
+    s.InitFrame(D.COLOR_SPACE.YCbCr, inst.rgba, inst.target, inst.confidence)
+    fp = dict(sigma_x=8.0, sigma_y=8.0, sigma_r=0.1)
+    op = dict(num_iterations=10, loss=1, lambda_=0.99, sigma_z=8.0, step_size=0.99)
+    s.ComputeColorSpaceDifferential(D.DomainFilterParams(**fp))
+    s.IntegrateColorDifferentials()
+    s.Optimize(D.DomainOptimizeParams(**op))
+    py_dts = s.Download(D.ImageType.OPTIMIZED_QUANTITY)
+    ov = {(a, 8.0): s.DebugBounds(a, 8.0) for a in (0, 1)}
+    ref, _ = oracle_mod.dts_solve(inst.rgba, inst.target, inst.confidence, 1, fp, op,
+                                  overrides=ov)
+    assert np.abs(py_dts - ref).max() <= P.TOL_REL * P.target_range(inst.target)
+    # the same calls from C++ through the facade header
     inst.rgba.tofile(tmp_path / "rgba.bin")
     inst.target.tofile(tmp_path / "target.bin")
     inst.confidence.tofile(tmp_path / "conf.bin")
@@ -30,17 +47,8 @@ def test_cpp_facade_matches_python(gpu_ready, tmp_path):
     r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert "facade ok" in r.stdout
-    # the same calls through the Python mirror
-    s = D.DomainTransformSolver(D.ImageDim(w, h))
-    s.SetImageDim(D.ImageDim(w, h))
-    s.ClearAll()
-    s.InitFrame(D.COLOR_SPACE.YCbCr, inst.rgba, inst.target, inst.confidence)
-    s.ComputeColorSpaceDifferential(D.DomainFilterParams(8, 8, 0.1))
-    s.IntegrateColorDifferentials()
-    s.Optimize(D.DomainOptimizeParams(num_iterations=10, loss=D.RobustLoss.L2,
-                                      lambda_=0.99, sigma_z=8, step_size=0.99))
     dts = np.fromfile(tmp_path / "dts.bin", np.float32).reshape(h, w)
-    assert np.array_equal(dts, s.Download(D.ImageType.OPTIMIZED_QUANTITY))
+    assert np.array_equal(dts, py_dts)
     color = np.fromfile(tmp_path / "color.bin", np.uint8).reshape(h, w, 4)
     assert np.array_equal(color, s.Download(D.ImageType.COLOR_IMAGE))
     f = D.DomainTransformFilter(D.ImageDim(w, h))
