@@ -208,9 +208,10 @@ __device__ __forceinline__ void load8(const uint32_t* __restrict__ p, bool full,
 
 // X half-step update of one pixel (src/domain_transform_solver.cuh:37-86);
 // rn = 1/n correctly rounded.
-template <int MODE>
+template <int MODE, bool STEREO = false>
 __device__ __forceinline__ float x_update(float v, float B, float tv, float cv,
-                                          float rn, float lambda, float step) {
+                                          float rn, float lambda, float step,
+                                          float extra = 0.f) {
   const float cn = cv * rn;
   const float d = v - tv;
   float g;
@@ -219,16 +220,39 @@ __device__ __forceinline__ float x_update(float v, float B, float tv, float cv,
   } else {
     g = __fdiv_rn(cn * d, __fsqrt_rn(__fmaf_rn(d, d, 1e-6f)));
   }
+  if (STEREO) g += extra;
   return __fmaf_rn(step, -__fmaf_rn(lambda, v - B, 0.5f * g), v);
 }
 
-template <typename TS, int MODE, int TW, int TH>
+// PhotometricL2LossTerm::operator() (src/domain_transform_loss_term.cuh:
+// 20-39) at pixel (x, y) of an image with row pitch P, for disparity d:
+//   lambda_p * 2 * SAD4(left(x), right(xi)) / 255
+//     * ((dH_right(xi)^2 - 1) * alpha),   xi = (int)(offset + x - d),
+// zero when offset + x - d falls outside [0, W).  dH_right is the right
+// image's dHdx, evaluated here from the right guide.
+__device__ __forceinline__ float photometric(const StereoArgs& sa, long long row,
+                                             int x, int W, float d) {
+  const float xr = (sa.offset + (float)x) - d;
+  if (!(xr >= 0.f && xr < (float)W)) return 0.f;
+  const int xi = (int)xr;
+  const uchar4 a = sa.left[row + x], b = sa.right[row + xi];
+  const float sad = ((float)abs((int)a.x - (int)b.x) + (float)abs((int)a.y - (int)b.y) +
+                     (float)abs((int)a.z - (int)b.z) + (float)abs((int)a.w - (int)b.w)) *
+                    (float)0.00392156863;
+  float gr = 0.f;
+  if (sa.ratio >= 0.f)
+    gr = edge_weight(b, xi > 0 ? sa.right[row + xi - 1] : make_uchar4(0, 0, 0, 0),
+                     sa.ratio);
+  return sa.lam_p * 2.f * sad * (__fmaf_rn(gr, gr, -1.f) * sa.alpha);
+}
+
+template <typename TS, int MODE, int TW, int TH, bool STEREO = false>
 __global__ void __launch_bounds__(kThreads)
     k_dts_iter(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
                const float* __restrict__ vin, float* __restrict__ vout,
                const TS* __restrict__ tgt, const TS* __restrict__ cnf,
                const uint32_t* __restrict__ bnd, float lambda, float step,
-               float overwrite, int hx, int hy) {
+               float overwrite, int hx, int hy, StereoArgs sa) {
   static_assert(TW % kSeg == 0 && TH % kSeg == 0, "tile must hold whole runs");
   static_assert(TW % 32 == 0, "tile width must be whole warps");
   extern __shared__ float sm[];
@@ -294,7 +318,11 @@ __global__ void __launch_bounds__(kThreads)
         const int du = min((int)((b[j] >> 8) & 0xff), hx);
         const float s = window_sum(row, 1, j + 1 - dl, j + du);
         const float rn = __frcp_rn((float)(dl + du));
-        float o = x_update<MODE>(row[j], s * rn, tv[j], cv[j], rn, lambda, step);
+        float extra = 0.f;
+        if (STEREO)
+          extra = photometric(sa, in.off + (long long)y * P, xs + j, W, row[j]);
+        float o = x_update<MODE, STEREO>(row[j], s * rn, tv[j], cv[j], rn, lambda,
+                                         step, extra);
         if (over && cv[j] > overwrite) o = tv[j];
         out[j] = o;
       }
@@ -564,53 +592,71 @@ int launch_bounds(const DtsLaunch& L, const uchar4* guide, uint32_t* bounds,
   return DTSGB_OK;
 }
 
-template <typename TS, int MODE, int TW, int TH>
+template <typename TS, int MODE, int TW, int TH, bool STEREO>
 static int launch_iter_shape(const DtsLaunch& L, const float* vin, float* vout,
                              const void* target, const void* conf,
                              const uint32_t* bounds, float lambda, float step,
-                             float overwrite, int hx, int hy, cudaStream_t s) {
+                             float overwrite, int hx, int hy, cudaStream_t s,
+                             const StereoArgs& sa) {
   const size_t smem = sizeof(float) * ((size_t)(TH + 2 * hy) * ((TW + 2 * hx) | 1) +
                                        (size_t)(TH + 2 * hy) * (TW + 1));
   if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "sigma_z too large");
-  int st = set_smem(k_dts_iter<TS, MODE, TW, TH>, smem);
+  int st = set_smem(k_dts_iter<TS, MODE, TW, TH, STEREO>, smem);
   if (st) return st;
   ProfScope ps(s, DTSGB_K_DTS_ITER);
-  k_dts_iter<TS, MODE, TW, TH><<<L.n_tiles, kThreads, smem, s>>>(
+  k_dts_iter<TS, MODE, TW, TH, STEREO><<<L.n_tiles, kThreads, smem, s>>>(
       L.d_inst, L.d_tiles, vin, vout, (const TS*)target, (const TS*)conf,
-      bounds, lambda, step, overwrite, hx, hy);
+      bounds, lambda, step, overwrite, hx, hy, sa);
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
 }
 
-template <typename TS, int MODE>
+template <typename TS, int MODE, bool STEREO>
 static int launch_iter_t(const DtsLaunch& L, const float* vin, float* vout,
                          const void* target, const void* conf,
                          const uint32_t* bounds, float lambda, float step,
-                         float overwrite, int hx, int hy, cudaStream_t s) {
+                         float overwrite, int hx, int hy, cudaStream_t s,
+                         const StereoArgs& sa) {
   if (L.small)
-    return launch_iter_shape<TS, MODE, kIterSmallTW, kIterSmallTH>(
-        L, vin, vout, target, conf, bounds, lambda, step, overwrite, hx, hy, s);
-  return launch_iter_shape<TS, MODE, kIterTW, kIterTH>(
-      L, vin, vout, target, conf, bounds, lambda, step, overwrite, hx, hy, s);
+    return launch_iter_shape<TS, MODE, kIterSmallTW, kIterSmallTH, STEREO>(
+        L, vin, vout, target, conf, bounds, lambda, step, overwrite, hx, hy, s, sa);
+  return launch_iter_shape<TS, MODE, kIterTW, kIterTH, STEREO>(
+      L, vin, vout, target, conf, bounds, lambda, step, overwrite, hx, hy, s, sa);
+}
+
+template <typename TS, bool STEREO>
+static int launch_iter_mode(const DtsLaunch& L, IterMode mode, const float* vin,
+                            float* vout, const void* target, const void* conf,
+                            const uint32_t* bounds, float lambda, float step,
+                            float overwrite, int hx, int hy, cudaStream_t s,
+                            const StereoArgs& sa) {
+  if (mode == IterMode::L2)
+    return launch_iter_t<TS, 0, STEREO>(L, vin, vout, target, conf, bounds, lambda,
+                                        step, overwrite, hx, hy, s, sa);
+  return launch_iter_t<TS, 1, STEREO>(L, vin, vout, target, conf, bounds, lambda,
+                                      step, overwrite, hx, hy, s, sa);
 }
 
 int launch_dts_iter(const DtsLaunch& L, Storage st, IterMode mode,
                     const float* vin, float* vout, const void* target,
                     const void* conf, const uint32_t* bounds, float lambda,
                     float step, float overwrite, int hx, int hy,
-                    cudaStream_t s) {
+                    cudaStream_t s, const StereoArgs* stereo) {
+  const StereoArgs none{nullptr, nullptr, 0.f, 0.f, 0.f, -1.f};
   if (st == Storage::F32) {
-    if (mode == IterMode::L2)
-      return launch_iter_t<float, 0>(L, vin, vout, target, conf, bounds, lambda,
-                                     step, overwrite, hx, hy, s);
-    return launch_iter_t<float, 1>(L, vin, vout, target, conf, bounds, lambda,
-                                   step, overwrite, hx, hy, s);
+    if (stereo)
+      return launch_iter_mode<float, true>(L, mode, vin, vout, target, conf, bounds,
+                                           lambda, step, overwrite, hx, hy, s, *stereo);
+    return launch_iter_mode<float, false>(L, mode, vin, vout, target, conf, bounds,
+                                          lambda, step, overwrite, hx, hy, s, none);
   }
-  if (mode == IterMode::L2)
-    return launch_iter_t<__nv_bfloat16, 0>(L, vin, vout, target, conf, bounds,
-                                           lambda, step, overwrite, hx, hy, s);
-  return launch_iter_t<__nv_bfloat16, 1>(L, vin, vout, target, conf, bounds,
-                                         lambda, step, overwrite, hx, hy, s);
+  if (stereo)
+    return launch_iter_mode<__nv_bfloat16, true>(L, mode, vin, vout, target, conf,
+                                                 bounds, lambda, step, overwrite, hx,
+                                                 hy, s, *stereo);
+  return launch_iter_mode<__nv_bfloat16, false>(L, mode, vin, vout, target, conf,
+                                                bounds, lambda, step, overwrite, hx,
+                                                hy, s, none);
 }
 
 int launch_target_to_float(const DtsLaunch& L, Storage st, const void* src,

@@ -85,6 +85,14 @@ struct dtsgb_dts_s {
 
   bool diff_valid = false;
   float ratio_x = 0.f, ratio_y = 0.f;
+  // the solver's filter_params_ (set only by ComputeColorSpaceDifferential)
+  bool solver_fp_valid = false;
+  float solver_sx = 0.f, solver_sr = 0.f;
+  // DomainTransformStereo: right guide (converted), centre offset and the
+  // sigma ratio of its dHdx (-1: ProcessRightFrame not called)
+  uchar4* right = nullptr;
+  float center_offset = 0.f;
+  float right_ratio = -1.f;
   bool bounds_valid = false;
   float b_sx = 0.f, b_sy = 0.f;
   int var_idx = -1;
@@ -118,6 +126,7 @@ static int dts_layout(dtsgb_dts_t h) {
 }
 
 static void dts_free(dtsgb_dts_t h) {
+  dfree(h->right);
   dfree(h->guide);
   dfree(h->target);
   dfree(h->conf);
@@ -162,6 +171,7 @@ DTSGB_API int dtsgb_dts_create(int max_w, int max_h, unsigned flags,
   const size_t ntiles_i = (size_t)((max_w + kIterSmallTW - 1) / kIterSmallTW) *
                           ((max_h + kIterSmallTH - 1) / kIterSmallTH);
   if (!st) st = dalloc(&h->guide, h->plane);
+  if (!st && (flags & DTSGB_FLAG_STEREO)) st = dalloc(&h->right, h->plane);
   if (!st) st = dalloc((char**)&h->target, h->plane * h->tsize());
   if (!st) st = dalloc((char**)&h->conf, h->plane * h->tsize());
   if (!st) st = dalloc(&h->bounds, h->plane);
@@ -292,6 +302,54 @@ DTSGB_API int dtsgb_dts_compute_differential(dtsgb_dts_t h,
   h->ratio_y = p->sigma_y / p->sigma_r;
   h->diff_valid = true;
   h->bounds_valid = false;
+  h->solver_fp_valid = true;
+  h->solver_sx = p->sigma_x;
+  h->solver_sr = p->sigma_r;
+  return DTSGB_OK;
+}
+
+static int dts_init_right(dtsgb_dts_t h, float offset, int cs, const void* rgba,
+                          cudaMemcpyKind kind) {
+  if (!h || !rgba) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  if (!h->right)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT,
+                "InitRightFrame needs a handle created with DTSGB_FLAG_STEREO");
+  if (cs < DTSGB_RGB || cs > DTSGB_YYY)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "invalid color space");
+  if (!std::isfinite(offset))
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "center offset must be finite");
+  const size_t wb = (size_t)h->w * 4;
+  DTSGB_CUDA(cudaMemcpy2DAsync(h->right, (size_t)h->pitch * 4, rgba, wb, wb, h->h,
+                               kind, h->stream));
+  int st = launch_color_convert_flat(h->right, (long long)h->pitch * h->h, cs,
+                                     h->stream);
+  if (st) return st;
+  h->center_offset = offset;
+  if (kind == cudaMemcpyHostToDevice) DTSGB_CUDA(cudaStreamSynchronize(h->stream));
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_dts_init_right_frame(dtsgb_dts_t h, float offset, int cs,
+                                         const void* rgba) {
+  return dts_init_right(h, offset, cs, rgba, cudaMemcpyHostToDevice);
+}
+
+DTSGB_API int dtsgb_dts_init_right_frame_device(dtsgb_dts_t h, float offset,
+                                                int cs, const void* rgba) {
+  return dts_init_right(h, offset, cs, rgba, cudaMemcpyDeviceToDevice);
+}
+
+DTSGB_API int dtsgb_dts_process_right_frame(dtsgb_dts_t h) {
+  if (!h) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null handle");
+  if (!h->right)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT,
+                "ProcessRightFrame needs a handle created with DTSGB_FLAG_STEREO");
+  if (!h->solver_fp_valid)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT,
+                "ProcessRightFrame uses the filter params of "
+                "ComputeColorSpaceDifferential: call that first");
+  // the right image's dHdx is evaluated from its guide when a pass needs it
+  h->right_ratio = h->solver_sx / h->solver_sr;
   return DTSGB_OK;
 }
 
@@ -340,11 +398,25 @@ DTSGB_API int dtsgb_dts_optimize(dtsgb_dts_t h, const dtsgb_optimize_params* p,
   if (st) return st;
   const int halo = (int)std::floor(p->sigma_z);
   const IterMode mode = p->loss == DTSGB_L2 ? IterMode::L2 : IterMode::CHARB;
+  // DomainTransformStereo::Optimize adds PhotometricL2LossTerm with
+  // alpha = (sigma_r / sigma_x)^2 of filter_params_, beta = -1
+  // (src/domain_transform_stereo.cu:77-88)
+  StereoArgs sa{};
+  const StereoArgs* sp = nullptr;
+  if (h->flags & DTSGB_FLAG_STEREO) {
+    if (!h->solver_fp_valid)
+      return fail(DTSGB_ERR_INVALID_ARGUMENT,
+                  "stereo Optimize needs ComputeColorSpaceDifferential first");
+    const float sxr = h->solver_sr / h->solver_sx;
+    sa = StereoArgs{h->guide, h->right, h->center_offset, p->photo_consis_lambda,
+                    sxr * sxr, h->right_ratio};
+    sp = &sa;
+  }
   int a = 0, b = 1;
   for (int it = 0; it < p->num_iterations; ++it) {
     st = launch_dts_iter(h->launch_i(), h->st, mode, h->v[a], h->v[b],
                          h->target, h->conf, h->bounds, p->lambda, p->step_size,
-                         overwrite, halo, halo, h->stream);
+                         overwrite, halo, halo, h->stream, sp);
     if (st) return st;
     std::swap(a, b);
   }

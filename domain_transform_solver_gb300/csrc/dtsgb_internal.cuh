@@ -81,7 +81,9 @@ inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 inline long long round_up_ll(long long v, long long m) { return (v + m - 1) / m * m; }
 inline bool finite_pos(float v) { return v == v && v > 0.f && v < 3.4e38f; }
 
-// Zero-initialised device allocation; returns a DTSGB_* status.
+// Zero-initialised device allocation; returns a DTSGB_* status.  The fill
+// runs on the legacy default stream, which the handles' non-blocking streams
+// do not wait for, so it is finished here before the buffer is handed out.
 template <typename T>
 int dalloc(T** p, size_t count) {
   *p = nullptr;
@@ -94,6 +96,7 @@ int dalloc(T** p, size_t count) {
                                           : cuda_fail(e, "cudaMalloc");
   }
   e = cudaMemset(*p, 0, count * sizeof(T));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
   return 0;
 }
@@ -154,11 +157,22 @@ int launch_bounds(const DtsLaunch& L, const uchar4* guide, uint32_t* bounds,
                   int ref_y_limit, cudaStream_t s);
 
 enum class IterMode : int { L2 = 0, CHARB = 1 };
+
+// DomainTransformStereo's photometric term (src/domain_transform_loss_term.cuh):
+// converted left / right guides (same layout as the iterate), centre
+// offset, photo_consis_lambda, alpha = (sigma_r/sigma_x)^2 and the sigma
+// ratio of the right image's dHdx (negative: dHdx never computed, reads 0).
+struct StereoArgs {
+  const uchar4* left;
+  const uchar4* right;
+  float offset, lam_p, alpha, ratio;
+};
+
 int launch_dts_iter(const DtsLaunch& L, Storage st, IterMode mode,
                     const float* vin, float* vout, const void* target,
                     const void* conf, const uint32_t* bounds, float lambda,
                     float step, float overwrite, int halo_x, int halo_y,
-                    cudaStream_t s);
+                    cudaStream_t s, const StereoArgs* stereo = nullptr);
 // v = target (as float), optionally overwritten nowhere: the initial iterate.
 int launch_init_var(const DtsLaunch& L, Storage st, const void* target,
                     float* v, cudaStream_t s);

@@ -35,12 +35,13 @@ __all__ = [
     "DomainFilterParamsVec1", "DomainOptimizeParams", "HFBSGridParams",
     "DomainTransformFilter", "DomainTransformSolver", "HFBS", "DtsOptions",
     "HfbsOptions", "Solve", "EdgeAwareOptimize", "DtsgbError",
-    "FLAG_BF16_STORAGE", "FLAG_FIX_Y_LIMIT", "Batch",
+    "FLAG_BF16_STORAGE", "FLAG_FIX_Y_LIMIT", "Batch", "DomainTransformStereo",
 ]
 
 FLAG_BF16_STORAGE = 0x1
 FLAG_FIX_Y_LIMIT = 0x2
 FLAG_FILTER_ONLY = 0x4
+FLAG_STEREO = 0x8
 
 
 @dataclass
@@ -261,6 +262,22 @@ class DomainTransformSolver(DomainTransformFilter):
                           left_side_clear_width: int) -> None:
         check(self._lib.dtsgb_dts_compute_confidence(
             self._h, ctypes.byref(conf_params._c()), int(left_side_clear_width)))
+
+
+class DomainTransformStereo(DomainTransformSolver):
+    """src/domain_transform_stereo.h:93-114: the solver plus a right image;
+    Optimize adds the photometric term of PhotometricL2LossTerm."""
+
+    _flags_base = FLAG_STEREO
+
+    def InitRightFrame(self, center_offset: float, color_space: COLOR_SPACE,
+                       color_image) -> None:
+        rgba = _rgba(color_image, self._shape())
+        check(self._lib.dtsgb_dts_init_right_frame(self._h, float(center_offset),
+                                                   int(color_space), _ptr(rgba)))
+
+    def ProcessRightFrame(self) -> None:
+        check(self._lib.dtsgb_dts_process_right_frame(self._h))
 
 
 class HFBS:

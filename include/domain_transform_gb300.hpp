@@ -201,6 +201,22 @@ class DomainTransformSolver : public DomainTransformFilter {
   DomainFilterParams filter_params_{};
 };
 
+// ---- src/domain_transform_stereo.h:93-114 ------------------------------------
+class DomainTransformStereo : public DomainTransformSolver {
+ public:
+  explicit DomainTransformStereo(const ImageDim& max_image_dims, unsigned flags = 0)
+      : DomainTransformSolver(max_image_dims, flags | DTSGB_FLAG_STEREO) {}
+  void InitRightFrame(const float center_offset, const COLOR_SPACE& color_space,
+                      void* color_image) {
+    detail::on_status(dtsgb_dts_init_right_frame(h_, center_offset,
+                                                 static_cast<int>(color_space),
+                                                 color_image));
+  }
+  // Always call this after ComputeColorSpaceDifferential().
+  void ProcessRightFrame() { detail::on_status(dtsgb_dts_process_right_frame(h_)); }
+  // Optimize (inherited) adds the photometric term on a stereo handle.
+};
+
 // ---- class HFBS, src/hfbs.h:99-150 -------------------------------------------
 class HFBS {
  public:

@@ -107,6 +107,13 @@ struct ora_dts {
   int ref_y_limit, contract;
   uint8_t* color;
   REAL *dH, *dV, *ctH, *ctV, *var, *target, *conf;
+  /* the solver's own filter params (filter_params_, set only by its public
+   * ComputeColorSpaceDifferential, src/domain_transform_solver.cu:89-93) */
+  float fp_sx, fp_sy, fp_sr;
+  /* DomainTransformStereo: right image, its dHdx, centre offset */
+  uint8_t* right_color;
+  REAL* right_dH;
+  float center_offset;
   int n_ovr;
   int ovr_axis[ORA_MAX_OVR];
   float ovr_sigma[ORA_MAX_OVR];
@@ -130,6 +137,8 @@ EXPORT ora_dts* ora_dts_create(int max_w, int max_h) {
   s->var = ora_alloc_real(n);
   s->target = ora_alloc_real(n);
   s->conf = ora_alloc_real(n);
+  s->right_color = (uint8_t*)calloc(n * 4, 1);
+  s->right_dH = ora_alloc_real(n);
   return s;
 }
 
@@ -152,6 +161,8 @@ EXPORT void ora_dts_destroy(ora_dts* s) {
   free(s->var);
   free(s->target);
   free(s->conf);
+  free(s->right_color);
+  free(s->right_dH);
   free(s);
 }
 
@@ -218,21 +229,55 @@ static REAL ora_edge(const uint8_t* a, const uint8_t* b, float ratio) {
   return R_SQRT(R_FMA(t, (REAL)ratio, (REAL)1));
 }
 
-EXPORT void ora_dts_differential(ora_dts* s, float sigma_x, float sigma_y,
-                                 float sigma_r) {
-  const float rx = sigma_x / sigma_r, ry = sigma_y / sigma_r;
-  const int W = s->w, H = s->h;
+static void ora_edges(const uint8_t* color, int W, int H, float rx, float ry,
+                      REAL* dH, REAL* dV) {
   static const uint8_t zero4[4] = {0, 0, 0, 0};
 #pragma omp parallel for schedule(static)
   for (int y = 0; y < H; ++y) {
     for (int x = 0; x < W; ++x) {
-      const uint8_t* cur = s->color + 4 * ((size_t)y * W + x);
+      const uint8_t* cur = color + 4 * ((size_t)y * W + x);
       const uint8_t* left = x > 0 ? cur - 4 : zero4;
       const uint8_t* up = y > 0 ? cur - 4 * (size_t)W : zero4;
-      s->dH[(size_t)y * W + x] = ora_edge(cur, left, rx);
-      s->dV[(size_t)y * W + x] = ora_edge(cur, up, ry);
+      dH[(size_t)y * W + x] = ora_edge(cur, left, rx);
+      dV[(size_t)y * W + x] = ora_edge(cur, up, ry);
     }
   }
+}
+
+/* DomainTransformFilter::ComputeColorSpaceDifferential: the DT of the
+ * current guide for these sigmas (Filter calls this base version, which does
+ * not touch the solver's filter_params_). */
+static void dts_diff(ora_dts* s, float sigma_x, float sigma_y, float sigma_r) {
+  ora_edges(s->color, s->w, s->h, sigma_x / sigma_r, sigma_y / sigma_r, s->dH,
+            s->dV);
+}
+
+/* DomainTransformSolver::ComputeColorSpaceDifferential
+ * (src/domain_transform_solver.cu:89-93): records filter_params_ too. */
+EXPORT void ora_dts_differential(ora_dts* s, float sigma_x, float sigma_y,
+                                 float sigma_r) {
+  s->fp_sx = sigma_x;
+  s->fp_sy = sigma_y;
+  s->fp_sr = sigma_r;
+  dts_diff(s, sigma_x, sigma_y, sigma_r);
+}
+
+/* DomainTransformStereo::InitRightFrame / ProcessRightFrame
+ * (src/domain_transform_stereo.cu:17-27): the right image in the same colour
+ * space, and its dHdx for the solver's filter_params_. */
+EXPORT void ora_dts_init_right_frame(ora_dts* s, float center_offset,
+                                     int color_space, const uint8_t* rgba) {
+  s->center_offset = center_offset;
+  ora_color_convert(color_space, s->contract, rgba, s->right_color,
+                    (int64_t)s->w * s->h);
+}
+
+EXPORT void ora_dts_process_right_frame(ora_dts* s) {
+  const size_t n = (size_t)s->w * s->h;
+  REAL* dv = ora_alloc_real(n);
+  ora_edges(s->right_color, s->w, s->h, s->fp_sx / s->fp_sr, s->fp_sy / s->fp_sr,
+            s->right_dH, dv);
+  free(dv);
 }
 
 /* a3. IntegrateColorDifferentials -- src/domain_transform_filter.cu:85-90,
@@ -417,7 +462,7 @@ static void ora_box_pass(const ora_dts* s, int axis, const REAL* in, REAL* out,
  * 3*2^(N-i-1)/sqrt(4^N-1) (computed in double, stored as float). */
 static void ora_filter_buffers(ora_dts* s, float sx, float sy, float sr,
                                const REAL* in, REAL* out, int num_iter) {
-  ora_dts_differential(s, sx, sy, sr);
+  dts_diff(s, sx, sy, sr);
   ora_dts_integrate(s);
   const size_t n = (size_t)s->w * s->h;
   REAL* a = ora_alloc_real(n);
@@ -498,10 +543,52 @@ EXPORT void ora_dts_compute_confidence(ora_dts* s, float sx, float sy, float sr,
  * overwrite in (0,1) the target is copied over v where c > overwrite before
  * each half-step (CopyVariableFlagGreaterThanThresh, common_kernels.cuh:36-50).
  */
+static void dts_optimize(ora_dts* s, int num_iterations, int loss,
+                         float lambda, float sigma_z, float step,
+                         float overwrite, int stereo, float photo_lambda);
+
 EXPORT void ora_dts_optimize(ora_dts* s, int num_iterations, int loss,
                              float lambda, float sigma_z, float step,
                              float overwrite) {
+  dts_optimize(s, num_iterations, loss, lambda, sigma_z, step, overwrite, 0, 0.f);
+}
+
+/* DomainTransformStereo::Optimize (src/domain_transform_stereo.cu:44-158):
+ * Optimize with PhotometricL2LossTerm (src/domain_transform_loss_term.cuh:
+ * 20-39) added to the data gradient of the X half-step:
+ *   xr = center_offset + x - v;  if 0 <= xr < W:
+ *   g += lambda_p * 2 * SAD4(left(x,y), right((int)xr, y)) / 255
+ *        * ((dH_right((int)xr, y)^2 - 1) * (sigma_r / sigma_x)^2)
+ * with the solver's filter_params_ sigmas. */
+EXPORT void ora_dts_optimize_stereo(ora_dts* s, int num_iterations, int loss,
+                                    float lambda, float sigma_z, float step,
+                                    float photo_lambda, float overwrite) {
+  dts_optimize(s, num_iterations, loss, lambda, sigma_z, step, overwrite, 1,
+               photo_lambda);
+}
+
+static const float kInv255 = (float)0.00392156863; /* common_kernels.cuh:9 */
+
+static REAL photometric(const ora_dts* s, int x, int y, REAL d, REAL alpha,
+                        REAL lam_p) {
+  const int W = s->w;
+  const REAL xr = (REAL)s->center_offset + (REAL)x - d;
+  if (!(xr >= 0 && xr < (REAL)W)) return 0;
+  const int xi = (int)xr;
+  const uint8_t* a = s->color + 4 * ((size_t)y * W + x);
+  const uint8_t* b = s->right_color + 4 * ((size_t)y * W + xi);
+  int sad = 0;
+  for (int k = 0; k < 4; ++k) sad += abs((int)a[k] - (int)b[k]);
+  const REAL gr = s->right_dH[(size_t)y * W + xi];
+  return lam_p * 2 * ((REAL)sad * (REAL)kInv255) * ((gr * gr - 1) * alpha);
+}
+
+static void dts_optimize(ora_dts* s, int num_iterations, int loss,
+                         float lambda, float sigma_z, float step,
+                         float overwrite, int stereo, float photo_lambda) {
   const int W = s->w, H = s->h;
+  const float sxr = s->fp_sr / s->fp_sx;  /* "sigma_x_div_sigma_r", stereo.cu:80 */
+  const REAL alpha = (REAL)(sxr * sxr);
   const size_t n = (size_t)W * H;
   REAL* v = ora_alloc_real(n);
   REAL* S = ora_alloc_real(n);
@@ -536,6 +623,7 @@ EXPORT void ora_dts_optimize(ora_dts* s, int num_iterations, int loss,
           g = 2 * cn * d;
         else
           g = cn * d / R_SQRT(d * d + (REAL)0.000001);
+        if (stereo) g += photometric(s, x, y, v[k], alpha, (REAL)photo_lambda);
         const REAL stepv = -(lam * (v[k] - B) + (REAL)0.5 * g);
         vx[k] = v[k] + st * stepv;
       }

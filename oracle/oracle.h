@@ -70,6 +70,13 @@ void ora_dts_compute_confidence(ora_dts* s, float sigma_x, float sigma_y,
                                 float sigma_r, float sigma0, int left_clear);
 void ora_dts_optimize(ora_dts* s, int num_iterations, int loss, float lambda,
                       float sigma_z, float step_size, float overwrite);
+/* DomainTransformStereo (src/domain_transform_stereo.h:93-114). */
+void ora_dts_init_right_frame(ora_dts* s, float center_offset, int color_space,
+                              const uint8_t* rgba);
+void ora_dts_process_right_frame(ora_dts* s);
+void ora_dts_optimize_stereo(ora_dts* s, int num_iterations, int loss,
+                             float lambda, float sigma_z, float step_size,
+                             float photo_lambda, float overwrite);
 /* Download: COLOR_IMAGE -> uint8 RGBA, everything else -> REAL. */
 void ora_dts_download(const ora_dts* s, int image_type, void* dst);
 /* Window bounds of the current domain transform for one sigma.

@@ -59,6 +59,9 @@ def lib(real: str = "f64") -> ctypes.CDLL:
             "ora_dts_filter": ([vp, f, f, f, vp, vp, i], None),
             "ora_dts_compute_confidence": ([vp, f, f, f, f, i], None),
             "ora_dts_optimize": ([vp, i, i, f, f, f, f], None),
+            "ora_dts_init_right_frame": ([vp, f, i, vp], None),
+            "ora_dts_process_right_frame": ([vp], None),
+            "ora_dts_optimize_stereo": ([vp, i, i, f, f, f, f, f], None),
             "ora_dts_download": ([vp, i, vp], None),
             "ora_dts_bounds": ([vp, i, f, vp, vp, vp], None),
             "ora_dts_add_bounds_override": ([vp, i, f, vp, vp], None),
@@ -154,6 +157,18 @@ class OracleDTS:
     def optimize(self, num_iterations, loss, lam, sigma_z, step, overwrite=-1.0):
         self.L.ora_dts_optimize(self.h, num_iterations, int(loss), lam, sigma_z,
                                 step, overwrite)
+
+    def init_right_frame(self, center_offset, cs, rgba):
+        rgba = np.ascontiguousarray(rgba, np.uint8)
+        self.L.ora_dts_init_right_frame(self.h, center_offset, int(cs), _p(rgba))
+
+    def process_right_frame(self):
+        self.L.ora_dts_process_right_frame(self.h)
+
+    def optimize_stereo(self, num_iterations, loss, lam, sigma_z, step, photo_lambda,
+                        overwrite=-1.0):
+        self.L.ora_dts_optimize_stereo(self.h, num_iterations, int(loss), lam, sigma_z,
+                                       step, photo_lambda, overwrite)
 
     def download(self, image_type):
         if image_type == 0:

@@ -98,11 +98,35 @@ def box(v: np.ndarray, L, U, axis: int):
     return out
 
 
-def dts_solve(guide, t, c, filt, opt, overwrite=-1.0, ref_y_limit=True):
+def photometric(guide, right, right_dH, v, offset, photo, filt):
+    """PhotometricL2LossTerm::operator() for every pixel
+    (src/domain_transform_loss_term.cuh:20-39)."""
+    H, W = v.shape
+    sxr = np.float32(np.float32(filt["sigma_r"]) / np.float32(filt["sigma_x"]))
+    alpha = float(np.float32(sxr * sxr))
+    inv255 = float(np.float32(0.00392156863))
+    out = np.zeros((H, W))
+    for y in range(H):
+        for x in range(W):
+            xr = float(np.float32(offset)) + x - v[y, x]
+            if 0 <= xr < W:
+                xi = int(xr)
+                sad = int(np.abs(guide[y, x].astype(int) - right[y, xi].astype(int)).sum())
+                g = right_dH[y, xi]
+                out[y, x] = float(np.float32(photo)) * 2 * (sad * inv255) * ((g * g - 1) * alpha)
+    return out
+
+
+def dts_solve(guide, t, c, filt, opt, overwrite=-1.0, ref_y_limit=True, stereo=None):
     """ComputeColorSpaceDifferential -> Integrate -> Optimize on a converted
-    guide (H, W, 4)."""
+    guide (H, W, 4).  stereo = (converted right guide, centre offset,
+    photo_consis_lambda) adds DomainTransformStereo's photometric term."""
     H, W = t.shape
     dH, dV = differentials(guide, filt["sigma_x"], filt["sigma_y"], filt["sigma_r"])
+    right_dH = None
+    if stereo is not None:
+        right_dH, _ = differentials(stereo[0], filt["sigma_x"], filt["sigma_y"],
+                                    filt["sigma_r"])
     ctH, ctV = np.cumsum(dH, 1), np.cumsum(dV, 0)
     sz = float(np.float32(opt["sigma_z"]))
     Lx, Ux = all_bounds(ctH, 0, sz, W)
@@ -124,6 +148,8 @@ def dts_solve(guide, t, c, filt, opt, overwrite=-1.0, ref_y_limit=True):
             g = 2 * cn * d
         else:
             g = cn * d / np.sqrt(d * d + 1e-6)
+        if stereo is not None:
+            g = g + photometric(guide, stereo[0], right_dH, v, stereo[1], stereo[2], filt)
         v = v + st * (-(lam * (v - B) + 0.5 * g))
         if over:
             v = np.where(c > overwrite, t, v)

@@ -251,3 +251,37 @@ def test_f32_baseline_close_to_f64(oracle_mod):
     v32, _ = oracle_mod.dts_solve(inst.rgba, inst.target, inst.confidence, 1, filt, kw,
                                   real="f32")
     assert np.sqrt(np.mean((v64 - v32) ** 2)) < 1e-3 * np.ptp(inst.target)
+
+
+# ---- DomainTransformStereo: photometric term --------------------------------
+@pytest.mark.parametrize("loss", [1, 2])
+def test_oracle_stereo_matches_numpy(oracle_mod, loss):
+    W_, H_ = 40, 18
+    rng = np.random.default_rng(31 + loss)
+    left = rng.integers(0, 256, (H_, W_, 4)).astype(np.uint8)
+    right = np.roll(left, -3, axis=1)
+    right[..., :3] = np.clip(right[..., :3].astype(int) + rng.integers(-4, 5, right[..., :3].shape),
+                             0, 255).astype(np.uint8)
+    # disparities near half-integers so (int)(offset + x - d) is far from a tie
+    t = (rng.integers(1, 8, (H_, W_)) + 0.5 + rng.uniform(-0.1, 0.1, (H_, W_))).astype(np.float32)
+    c = (rng.random((H_, W_)) < 0.5).astype(np.float32)
+    filt = dict(sigma_x=8.0, sigma_y=8.0, sigma_r=0.2)
+    opt = dict(num_iterations=3, loss=loss, lambda_=0.99, sigma_z=6.0, step_size=0.9)
+    o = oracle_mod.OracleDTS(W_, H_)
+    o.init_frame(1, left, t, c)
+    o.init_right_frame(2.0, 1, right)
+    o.differential(8.0, 8.0, 0.2)
+    o.integrate()
+    o.process_right_frame()
+    o.optimize_stereo(3, loss, 0.99, 6.0, 0.9, 0.01)
+    v = o.download(5)
+    ref = R.dts_solve(o.download(0), t, c, filt, opt,
+                      stereo=(oracle_mod.color_convert(1, right), 2.0, 0.01))
+    assert np.allclose(v, ref, rtol=0, atol=1e-9)
+    # the term is active: without it the result differs
+    o2 = oracle_mod.OracleDTS(W_, H_)
+    o2.init_frame(1, left, t, c)
+    o2.differential(8.0, 8.0, 0.2)
+    o2.integrate()
+    o2.optimize(3, loss, 0.99, 6.0, 0.9)
+    assert np.abs(o2.download(5) - v).max() > 1e-3
