@@ -62,8 +62,11 @@ enum { DTSGB_L1 = 0, DTSGB_L2 = 1, DTSGB_CHARBONNIER = 2 };
 /* Search the Y-pass window up to the image height instead of reproducing the
  * reference's width limit (src/domain_transform_filter.cuh:22). */
 #define DTSGB_FLAG_FIX_Y_LIMIT 0x2u
-/* HFBS only: keep the filter-only (DomainTransformFilter) download set. */
+/* Keep the filter-only (DomainTransformFilter) download set. */
 #define DTSGB_FLAG_FILTER_ONLY 0x4u
+/* DomainTransformStereo (src/domain_transform_stereo.h:93-114): the handle
+ * holds a right image and Optimize adds the photometric term. */
+#define DTSGB_FLAG_STEREO 0x8u
 
 /* ---- parameter structs, field order of the reference ----------------------*/
 /* DomainFilterParams = DomainFilterParamsVec<0>,
@@ -176,6 +179,17 @@ DTSGB_API int dtsgb_dts_download_device(dtsgb_dts_t h, int image_type,
                                         void* image);
 /* ClearAll, filter.h:49 / solver.h:78. */
 DTSGB_API int dtsgb_dts_clear_all(dtsgb_dts_t h);
+/* DomainTransformStereo::InitRightFrame(center_offset, color_space, image),
+ * src/domain_transform_stereo.h:98 (handle created with DTSGB_FLAG_STEREO). */
+DTSGB_API int dtsgb_dts_init_right_frame(dtsgb_dts_t h, float center_offset,
+                                         int color_space, const void* rgba);
+DTSGB_API int dtsgb_dts_init_right_frame_device(dtsgb_dts_t h,
+                                                float center_offset,
+                                                int color_space,
+                                                const void* rgba);
+/* DomainTransformStereo::ProcessRightFrame, stereo.h:102: the right image's
+ * domain transform for the solver's current filter params. */
+DTSGB_API int dtsgb_dts_process_right_frame(dtsgb_dts_t h);
 /* (new, tests) window bounds the kernels use for one sigma on the current
  * domain transform; axis 0 = X, 1 = Y.  l, u: host W*H int32 each; the
  * window is the index range (l, u] along the axis. */
