@@ -131,6 +131,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_batch_solve_hfbs": ([vp, P(HfbsParams)], i),
         "dtsgb_batch_download": ([vp, i, pvp], i),
         "dtsgb_batch_download_device": ([vp, i, pvp], i),
+        "dtsgb_dts_solve_noalloc": ([i, i, i, vp, vp, vp, P(FilterParams),
+                                     P(OptimizeParams), f, vp, vp], i),
         "dtsgb_dts_init_right_frame": ([vp, f, i, vp], i),
         "dtsgb_dts_init_right_frame_device": ([vp, f, i, vp], i),
         "dtsgb_dts_process_right_frame": ([vp], i),

@@ -242,6 +242,38 @@ DTSGB_API int dtsgb_hfbs_grid_dims(dtsgb_hfbs_t h, int* gx, int* gy, int* gl);
 DTSGB_API int dtsgb_hfbs_debug_grid(dtsgb_hfbs_t h, int which, float* dst);
 
 /* ===========================================================================
+ * Allocation-free DTS solve (no counterpart in the reference).
+ *
+ * For callers that cannot call cudaMalloc: code that runs inside a CUDA-graph
+ * capture owned by another framework, real-time pipelines that forbid device
+ * allocation after start-up, or hosts whose own allocator must own every
+ * device allocation.  One call is ComputeColorSpaceDifferential +
+ * IntegrateColorDifferentials + Optimize of DomainTransformSolver on device
+ * buffers the caller owns: rgba (W*H*4 bytes, RGBA, dense rows), target and
+ * confidence (W*H floats; confidence may be NULL = all ones) and output (W*H
+ * floats, must not alias an input), all enqueued on cuda_stream.
+ *
+ * The solve's scratch (8 bytes per pixel: window bounds and one iterate) is a
+ * static device array of DTSGB_NOALLOC_MAX_PIXELS pixels (8 MiB) inside the
+ * library, which every GPU that loads the library holds until the process
+ * exits.  Larger images return DTSGB_ERR_UNSUPPORTED.  The first call on a
+ * device looks the array up with cudaGetSymbolAddress, so make it before any
+ * stream capture.  All calls on a device share the array and it keeps the
+ * previous call's contents; nothing in it needs to start at zero, since a
+ * call writes every element it reads before reading it.  Calls that overlap
+ * on the GPU race on the array and must be serialised by the caller.  The call allocates nothing: no cudaMalloc,
+ * cudaFree, stream creation or allocating library routine.
+ * ===========================================================================*/
+#define DTSGB_NOALLOC_MAX_PIXELS (1LL << 20)
+DTSGB_API int dtsgb_dts_solve_noalloc(int width, int height, int color_space,
+                                      const void* rgba, const float* target,
+                                      const float* confidence,
+                                      const dtsgb_filter_params* filter,
+                                      const dtsgb_optimize_params* optimize,
+                                      float overwrite_target_above_conf,
+                                      float* output, void* cuda_stream);
+
+/* ===========================================================================
  * Batched solves (new; no reference counterpart): n independent instances of
  * uneven size in one HBM arena, each solved with DTS and/or HFBS by single
  * launches that cover every instance (the reference solves one image per
