@@ -654,6 +654,108 @@ static void dts_optimize(ora_dts* s, int num_iterations, int loss,
   free(S);
 }
 
+/* Adjoint of Optimize (no reference counterpart: the reference has no
+ * gradients).  With the windows fixed, one iteration is
+ *   X: v1 = v - s*(lambda*(v - Bx v) + 0.5*g(v)),  0.5*g = (c/n)(v-t)  (L2)
+ *                                            or 0.5*(c/n)(v-t)/sqrt((v-t)^2+e)
+ *   Y: v2 = v1 - s*lambda*(v1 - By v1)
+ * where B averages over the pixel's window.  Given dL/dv_N (gout), this
+ * accumulates dL/dt and dL/dc over all iterations (v_0 = t).  The forward
+ * iterates are recomputed and kept (test-size images only). */
+static void box_transpose(const ora_dts* s, int axis, const REAL* gin,
+                          const int32_t* l, const int32_t* u, REAL* gout) {
+  /* gout(q) = sum over p with q in (l_p, u_p] of gin(p) / (u_p - l_p) */
+  const int W = s->w, H = s->h;
+  const size_t n = (size_t)W * H;
+  for (size_t k = 0; k < n; ++k) gout[k] = 0;
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const size_t p = (size_t)y * W + x;
+      const REAL a = gin[p] / (REAL)(u[p] - l[p]);
+      for (int q = l[p] + 1; q <= u[p]; ++q) {
+        const size_t k = axis == 0 ? (size_t)y * W + q : (size_t)q * W + x;
+        gout[k] += a;
+      }
+    }
+}
+
+EXPORT int ora_dts_backward(ora_dts* s, int num_iterations, int loss,
+                            float lambda, float sigma_z, float step,
+                            const REAL* grad_out, REAL* grad_t, REAL* grad_c) {
+  if (loss != ORA_L2 && loss != ORA_CHARBONNIER) return -1;
+  const int W = s->w, H = s->h;
+  const size_t n = (size_t)W * H;
+  int32_t *lx, *ux, *ly, *uy;
+  ora_pass_bounds(s, 0, sigma_z, &lx, &ux);
+  ora_pass_bounds(s, 1, sigma_z, &ly, &uy);
+  const REAL lam = lambda, st = step, eps = (REAL)0.000001;
+  /* forward, keeping the X-step input of every iteration */
+  REAL* vs = ora_alloc_real(n * (size_t)(num_iterations + 1));
+  REAL* S = ora_alloc_real(n);
+  REAL* tmp = ora_alloc_real(n);
+  memcpy(vs, s->target, n * sizeof(REAL));
+  for (int it = 0; it < num_iterations; ++it) {
+    const REAL* v = vs + n * it;
+    REAL* vn = vs + n * (it + 1);
+    ora_row_prefix(v, S, W, H);
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        const size_t k = (size_t)y * W + x;
+        const REAL B = ora_window_mean(S + (size_t)y * W, 1, lx[k], ux[k]);
+        const REAL cn = s->conf[k] / (REAL)(ux[k] - lx[k]);
+        const REAL d = v[k] - s->target[k];
+        const REAL hg = loss == ORA_L2 ? cn * d : (REAL)0.5 * cn * d / R_SQRT(d * d + eps);
+        tmp[k] = v[k] - st * (lam * (v[k] - B) + hg);
+      }
+    ora_col_prefix(tmp, S, W, H);
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        const size_t k = (size_t)y * W + x;
+        const REAL B = ora_window_mean(S + x, (size_t)W, ly[k], uy[k]);
+        vn[k] = tmp[k] - st * lam * (tmp[k] - B);
+      }
+  }
+  REAL* g = ora_alloc_real(n);
+  REAL* g1 = ora_alloc_real(n);
+  memcpy(g, grad_out, n * sizeof(REAL));
+  for (size_t k = 0; k < n; ++k) grad_t[k] = grad_c[k] = 0;
+  for (int it = num_iterations - 1; it >= 0; --it) {
+    const REAL* v = vs + n * it;
+    /* Y^T */
+    box_transpose(s, 1, g, ly, uy, tmp);
+    for (size_t k = 0; k < n; ++k) g1[k] = (1 - st * lam) * g[k] + st * lam * tmp[k];
+    /* X^T */
+    box_transpose(s, 0, g1, lx, ux, tmp);
+    for (size_t k = 0; k < n; ++k) {
+      const REAL nk = (REAL)(ux[k] - lx[k]);
+      const REAL d = v[k] - s->target[k];
+      REAL dh_dv, dh_dc;  /* derivatives of 0.5*g */
+      if (loss == ORA_L2) {
+        dh_dv = s->conf[k] / nk;
+        dh_dc = d / nk;
+      } else {
+        const REAL r = R_SQRT(d * d + eps);
+        dh_dv = (REAL)0.5 * (s->conf[k] / nk) * eps / (r * r * r);
+        dh_dc = (REAL)0.5 * d / (nk * r);
+      }
+      grad_t[k] += st * dh_dv * g1[k];
+      grad_c[k] += -st * dh_dc * g1[k];
+      g[k] = (1 - st * lam - st * dh_dv) * g1[k] + st * lam * tmp[k];
+    }
+  }
+  for (size_t k = 0; k < n; ++k) grad_t[k] += g[k];
+  free(vs);
+  free(S);
+  free(tmp);
+  free(g);
+  free(g1);
+  free(lx);
+  free(ux);
+  free(ly);
+  free(uy);
+  return 0;
+}
+
 /* Download -- src/domain_transform_filter.cu:51-74 and
  * src/domain_transform_solver.cu:63-87. */
 EXPORT void ora_dts_download(const ora_dts* s, int type, void* dst) {

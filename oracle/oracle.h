@@ -77,6 +77,12 @@ void ora_dts_process_right_frame(ora_dts* s);
 void ora_dts_optimize_stereo(ora_dts* s, int num_iterations, int loss,
                              float lambda, float sigma_z, float step_size,
                              float photo_lambda, float overwrite);
+/* Adjoint of Optimize with the windows fixed: dL/dt and dL/dc for an
+ * upstream gradient dL/dv of the result (L2 or Charbonnier; returns -1 for
+ * other losses). */
+int ora_dts_backward(ora_dts* s, int num_iterations, int loss, float lambda,
+                     float sigma_z, float step_size, const REAL* grad_out,
+                     REAL* grad_t, REAL* grad_c);
 /* Download: COLOR_IMAGE -> uint8 RGBA, everything else -> REAL. */
 void ora_dts_download(const ora_dts* s, int image_type, void* dst);
 /* Window bounds of the current domain transform for one sigma.

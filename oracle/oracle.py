@@ -62,6 +62,7 @@ def lib(real: str = "f64") -> ctypes.CDLL:
             "ora_dts_init_right_frame": ([vp, f, i, vp], None),
             "ora_dts_process_right_frame": ([vp], None),
             "ora_dts_optimize_stereo": ([vp, i, i, f, f, f, f, f], None),
+            "ora_dts_backward": ([vp, i, i, f, f, f, vp, vp, vp], i),
             "ora_dts_download": ([vp, i, vp], None),
             "ora_dts_bounds": ([vp, i, f, vp, vp, vp], None),
             "ora_dts_add_bounds_override": ([vp, i, f, vp, vp], None),
@@ -169,6 +170,16 @@ class OracleDTS:
                         overwrite=-1.0):
         self.L.ora_dts_optimize_stereo(self.h, num_iterations, int(loss), lam, sigma_z,
                                        step, photo_lambda, overwrite)
+
+    def backward(self, num_iterations, loss, lam, sigma_z, step, grad_out):
+        g = np.ascontiguousarray(grad_out, self.dt)
+        gt = np.empty((self.hh, self.w), self.dt)
+        gc = np.empty((self.hh, self.w), self.dt)
+        st = self.L.ora_dts_backward(self.h, num_iterations, int(loss), lam, sigma_z, step,
+                                     _p(g), _p(gt), _p(gc))
+        if st != 0:
+            raise ValueError("unsupported loss for the adjoint")
+        return gt, gc
 
     def download(self, image_type):
         if image_type == 0:

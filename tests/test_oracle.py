@@ -285,3 +285,44 @@ def test_oracle_stereo_matches_numpy(oracle_mod, loss):
     o2.integrate()
     o2.optimize(3, loss, 0.99, 6.0, 0.9)
     assert np.abs(o2.download(5) - v).max() > 1e-3
+
+
+# ---- adjoint of the fixed-iteration solve ------------------------------------
+@pytest.mark.parametrize("loss", [1, 2])
+def test_oracle_adjoint_matches_central_differences(oracle_mod, loss):
+    """dL/dt and dL/dc of L = <gout, v_N> against FP64 central differences of
+    the forward solve with the same (fixed) windows."""
+    W_, H_ = 24, 16
+    rng = np.random.default_rng(5 + loss)
+    g = rng.integers(0, 256, (H_, W_, 4)).astype(np.uint8)
+    t = rng.uniform(0, 5, (H_, W_)).astype(np.float32)
+    c = rng.uniform(0.1, 1.0, (H_, W_)).astype(np.float32)
+    gout = rng.normal(0, 1, (H_, W_))
+    filt = dict(sigma_x=8.0, sigma_y=8.0, sigma_r=0.2)
+    iters, lam, sz, step = 4, 0.9, 5.0, 0.8
+    o = oracle_mod.OracleDTS(W_, H_)
+    o.init_frame(1, g, t, c)
+    o.differential(8.0, 8.0, 0.2)
+    o.integrate()
+    gt, gc = o.backward(iters, loss, lam, sz, step, gout)
+
+    def L(tt, cc):
+        o2 = oracle_mod.OracleDTS(W_, H_)
+        o2.init_frame(1, g, tt, cc)
+        o2.differential(8.0, 8.0, 0.2)
+        o2.integrate()
+        o2.optimize(iters, loss, lam, sz, step)
+        return float((o2.download(5) * gout).sum())
+
+    # the forward takes float32 inputs: perturb by exactly representable steps
+    picks = rng.choice(W_ * H_, 12, replace=False)
+    for k in picks:
+        y, x = divmod(int(k), W_)
+        for arr, grad in ((t, gt), (c, gc)):
+            h = np.float32(2.0 ** -8)
+            a = arr.copy(); a[y, x] += h
+            b = arr.copy(); b[y, x] -= h
+            args_p = (a, c) if arr is t else (t, a)
+            args_m = (b, c) if arr is t else (t, b)
+            fd = (L(*args_p) - L(*args_m)) / (2 * float(h))
+            assert abs(fd - grad[y, x]) <= 2e-3 * max(1.0, abs(fd)), (k, fd, grad[y, x])
