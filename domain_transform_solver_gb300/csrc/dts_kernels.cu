@@ -8,9 +8,12 @@
 // floor(sigma)+1 pixels from its centre.  Every pass is therefore a
 // bounded-radius stencil over a tile plus halo held in shared memory: no
 // global prefix sums, no transposes, no long-row cancellation.
+#include <algorithm>
+
 #include "../../include/dtsgb.h"
 #include "color.cuh"
 #include "dtsgb_internal.cuh"
+#include "fixed_point.cuh"
 
 namespace dtsgb {
 
@@ -135,12 +138,11 @@ __global__ void __launch_bounds__(kThreads)
 
 // ---------------------------------------------------------------------------
 // One solver iteration (a6/a7): the X half-step followed by the Y half-step
-// in one kernel.  A CTA owns a TWxTH output tile and stages the previous
-// iterate over the tile plus a halo of floor(sigma) on all sides.  The X
-// half-step is evaluated for the tile columns over the tile rows plus the
-// vertical halo (those rows feed the Y windows), kept in shared memory, and
-// the Y half-step writes the tile.  HBM traffic per pixel and iteration:
-// read v, t, c, bounds; write v.
+// in one kernel (k_dts_iter_prefix below).  A CTA owns a TWxTH output tile;
+// the X half-step is evaluated for the tile columns over the tile rows plus
+// a vertical halo of floor(sigma) (those rows feed the Y windows), kept in
+// shared memory, and the Y half-step writes the tile.  HBM traffic per pixel
+// and iteration: read v, t, c, bounds; write v.
 //   X: v' = v - s*(lambda*(v - B_x) + 0.5*g),
 //      g = 2*(c/n)*(v - t) (L2) or (c/n)*(v-t)/sqrt((v-t)^2 + 1e-6)
 //   Y: v' = v - s*lambda*(v - B_y)
@@ -148,63 +150,6 @@ __global__ void __launch_bounds__(kThreads)
 // target replaces v where c > overwrite before each half-step
 // (src/domain_transform_solver.cu:126-130, 160-164).
 // ---------------------------------------------------------------------------
-// Window sums are direct sums over the window, first element to last, never
-// a difference of running or prefix sums: a subtraction leaves an error of
-// about one ulp of the larger sum, and the Charbonnier gradient
-// x/sqrt(x^2+1e-6) magnifies errors in a near-zero residual about 1000-fold
-// (a one-pixel window must give back the pixel exactly).  Each thread
-// handles runs of kSeg consecutive pixels of a row so that the per-pixel
-// inputs come in as 16-byte vector loads.
-constexpr int kSeg = 8;
-
-__device__ __forceinline__ float window_sum(const float* __restrict__ s,
-                                            int stride, int lo, int hi) {
-  float acc = 0.f;
-  for (int k = lo; k <= hi; ++k) acc += s[k * stride];
-  return acc;
-}
-
-// Eight consecutive values starting at an 8-element-aligned address; `full`
-// means all eight are inside the row, otherwise only the first n are read.
-__device__ __forceinline__ void load8(const float* __restrict__ p, bool full,
-                                      int n, float (&o)[kSeg]) {
-  if (full) {
-    const float4 a = __ldg(reinterpret_cast<const float4*>(p));
-    const float4 b = __ldg(reinterpret_cast<const float4*>(p) + 1);
-    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
-    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
-  } else {
-#pragma unroll
-    for (int j = 0; j < kSeg; ++j) o[j] = j < n ? __ldg(p + j) : 0.f;
-  }
-}
-__device__ __forceinline__ void load8(const __nv_bfloat16* __restrict__ p,
-                                      bool full, int n, float (&o)[kSeg]) {
-  if (full) {
-    const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
-    const uint32_t w[4] = {a.x, a.y, a.z, a.w};
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      o[2 * j] = __uint_as_float(w[j] << 16);
-      o[2 * j + 1] = __uint_as_float(w[j] & 0xffff0000u);
-    }
-  } else {
-#pragma unroll
-    for (int j = 0; j < kSeg; ++j) o[j] = j < n ? __bfloat162float(p[j]) : 0.f;
-  }
-}
-__device__ __forceinline__ void load8(const uint32_t* __restrict__ p, bool full,
-                                      int n, uint32_t (&o)[kSeg]) {
-  if (full) {
-    const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
-    const uint4 b = __ldg(reinterpret_cast<const uint4*>(p) + 1);
-    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
-    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
-  } else {
-#pragma unroll
-    for (int j = 0; j < kSeg; ++j) o[j] = j < n ? __ldg(p + j) : 0u;
-  }
-}
 
 // X half-step update of one pixel (src/domain_transform_solver.cuh:37-86);
 // rn = 1/n correctly rounded.
@@ -246,111 +191,193 @@ __device__ __forceinline__ float photometric(const StereoArgs& sa, long long row
   return sa.lam_p * 2.f * sad * (__fmaf_rn(gr, gr, -1.f) * sa.alpha);
 }
 
-template <typename TS, int MODE, int TW, int TH, bool STEREO = false>
-__global__ void __launch_bounds__(kThreads)
-    k_dts_iter(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
-               const float* __restrict__ vin, float* __restrict__ vout,
-               const TS* __restrict__ tgt, const TS* __restrict__ cnf,
-               const uint32_t* __restrict__ bnd, float lambda, float step,
-               float overwrite, int hx, int hy, StereoArgs sa) {
-  static_assert(TW % kSeg == 0 && TH % kSeg == 0, "tile must hold whole runs");
-  static_assert(TW % 32 == 0, "tile width must be whole warps");
-  extern __shared__ float sm[];
+// ---------------------------------------------------------------------------
+// Fused X+Y iteration with window sums from fixed-point prefix sums
+// (fixed_point.cuh): a window sum is P[p+du] - P[p-dl] of a wrapping 32-bit
+// integer prefix, exact for the converted values; the scale comes from the
+// largest magnitude in the row (X) or among the tile's X results (Y).
+//
+// X half-step: one warp per row of the tile plus the vertical halo; each
+// lane scans four consecutive values, a warp shuffle scan joins the lanes,
+// and the row's prefix sits in a per-warp shared buffer.  A warp issues the
+// global loads of its next row before working on the current one.  Y
+// half-step: the X results stay in shared memory; each thread scans a
+// segment of one column, segment offsets are added in a second pass, and
+// the tile's output rows are written coalesced.  Reciprocals 1/n come from
+// a per-block table of correctly rounded values.
+// ---------------------------------------------------------------------------
+template <int TW, int TH, int NT>
+struct PrefixIterSmem {
+  // bytes of shared memory for halos hx, hy
+  static size_t bytes(int hx, int hy) {
+    const size_t SR = TH + 2 * hy, SWX = TW + 2 * hx + 1;
+    const size_t py = std::max((SR + 1) * TW, (size_t)(NT / 32) * SWX) * 4;
+    const size_t seg = (size_t)(NT / TW) * TW * 4;
+    const size_t sx = SR * (TW + 1) * 4;
+    const size_t sby = (size_t)TH * TW * 2;
+    const size_t rt = (size_t)(2 * std::max(hx, hy) + 2) * 4;
+    return py + seg + sx + sby + rt + 16;
+  }
+};
+
+template <typename TS, int MODE, int TW, int TH, int NT, bool STEREO = false>
+__global__ void __launch_bounds__(NT, 1024 / NT)
+    k_dts_iter_prefix(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
+                      const float* __restrict__ vin, float* __restrict__ vout,
+                      const TS* __restrict__ tgt, const TS* __restrict__ cnf,
+                      const uint32_t* __restrict__ bnd, float lambda, float step,
+                      float overwrite, int hx, int hy, StereoArgs sa) {
+  static_assert(TW % 32 == 0 && NT % TW == 0, "tile width: whole warps");
+  constexpr int NW = NT / 32, NSEG = NT / TW, TWp = TW + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
   const Tile t = tiles[blockIdx.x];
   const Inst in = insts[t.inst];
   const int W = in.w, H = in.h, P = in.pitch;
-  const int SW = TW + 2 * hx, SR = TH + 2 * hy;
-  // odd row strides: one row per lane is bank-conflict free
-  const int SWp = SW | 1;
-  constexpr int TXp = TW + 1;
-  float* sv = sm;             // SR x SWp previous iterate (tile + halo)
-  float* sx = sm + SR * SWp;  // SR x TXp after the X half-step
+  const int SR = TH + 2 * hy, SWX = TW + 2 * hx + 1, RY = SR + 1;
+  const int pyn = max(RY * TW, NW * SWX);
+  unsigned* Py = reinterpret_cast<unsigned*>(smraw);  // RY x TW (Y phase)
+  unsigned* Xb = Py;                                  // NW x SWX (X phase)
+  unsigned* segtot = Py + pyn;                        // NSEG x TW
+  float* sx = reinterpret_cast<float*>(segtot + NSEG * TW);   // SR x TWp
+  uint16_t* sby = reinterpret_cast<uint16_t*>(sx + SR * TWp);  // TH x TW
+  float* rtab = reinterpret_cast<float*>(sby + TH * TW);
+  const int nrt = 2 * max(hx, hy) + 2;
+  unsigned* smax = reinterpret_cast<unsigned*>(rtab + nrt);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < nrt; i += NT) rtab[i] = i ? __frcp_rn((float)i) : 0.f;
+  if (tid == 0) *smax = 0u;
+  __syncthreads();
   const bool over = overwrite > 0.f && overwrite < 1.f;
-  const int gx0 = t.x0 - hx, gy0 = t.y0 - hy;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int NW = kThreads / 32;
-  const float* vin_i = vin + in.off;
-  const TS* tgt_i = tgt + in.off;
-  const TS* cnf_i = cnf + in.off;
-  const uint32_t* bnd_i = bnd + in.off;
-  // stage the iterate: one warp per row, lanes along x (coalesced)
-  for (int r = warp; r < SR; r += NW) {
+  const int gx0 = t.x0 - hx - 1;  // image x of X prefix entry 0 (a zero entry)
+  const int gy0 = t.y0 - hy;      // image y of sx row 0
+  const int lgx = ceil_log2(2 * hx + 1), lgy = ceil_log2(2 * hy + 1);
+  // ---- X half-step ----------------------------------------------------------
+  constexpr int CPL = TW / 32;  // tile columns per lane
+  struct RowIn {
+    float v4[4];  // prefix entries 4*lane .. 4*lane+3
+    uint32_t b[CPL];  // tile columns lane + 32k
+    float tv[CPL], cv[CPL], vc[CPL];
+  };
+  auto load_v = [&](bool yok, long long row, int cc) -> float {  // prefix entry cc
+    const int x = gx0 + cc;
+    if (cc < 1 || cc >= SWX || !yok || (unsigned)x >= (unsigned)W) return 0.f;
+    float v = __ldg(vin + row + x);
+    if (over && load_f(cnf + row + x) > overwrite) v = load_f(tgt + row + x);
+    return v;
+  };
+  auto fetch = [&](int r, RowIn& R) {
     const int y = gy0 + r;
-    const bool yok = y >= 0 && y < H;
-    const float* src = vin_i + (long long)y * P;
-    for (int c = lane; c < SW; c += 32) {
-      const int x = gx0 + c;
-      float v = 0.f;
-      if (yok && x >= 0 && x < W) {
-        v = __ldg(src + x);
-        if (over && load_f(cnf_i + (long long)y * P + x) > overwrite)
-          v = load_f(tgt_i + (long long)y * P + x);
-      }
-      sv[r * SWp + c] = v;
-    }
-  }
-  __syncthreads();
-  // X half-step: a run of kSeg pixels of one row per lane; the lanes of a
-  // warp take 32 consecutive rows of the same run.
-  constexpr int NSX = TW / kSeg;
-  const int row_blocks = (SR + 31) >> 5;
-  for (int item = warp; item < row_blocks * NSX; item += NW) {
-    const int sg = item % NSX;  // constant divisor
-    const int r = (item / NSX) * 32 + lane;
-    const int y = gy0 + r;
-    const int xs = t.x0 + sg * kSeg;
-    if (r >= SR || y < 0 || y >= H || xs >= W) continue;
-    const int n = min(kSeg, W - xs);
-    const bool full = n == kSeg;
-    const long long p = (long long)y * P + xs;
-    uint32_t b[kSeg];
-    float tv[kSeg], cv[kSeg];
-    load8(bnd_i + p, full, n, b);
-    load8(tgt_i + p, full, n, tv);
-    load8(cnf_i + p, full, n, cv);
-    const float* row = sv + r * SWp + hx + sg * kSeg;  // row[j] = v(xs + j)
-    float* out = sx + r * TXp + sg * kSeg;
+    const bool yok = (unsigned)y < (unsigned)H;
+    const long long row = in.off + (long long)y * P;
 #pragma unroll
-    for (int j = 0; j < kSeg; ++j) {
-      if (j < n) {
-        // radii clamped to the staged halo: a window never reads outside it
-        const int dl = min((int)(b[j] & 0xff), hx + 1);
-        const int du = min((int)((b[j] >> 8) & 0xff), hx);
-        const float s = window_sum(row, 1, j + 1 - dl, j + du);
-        const float rn = __frcp_rn((float)(dl + du));
-        float extra = 0.f;
-        if (STEREO)
-          extra = photometric(sa, in.off + (long long)y * P, xs + j, W, row[j]);
-        float o = x_update<MODE, STEREO>(row[j], s * rn, tv[j], cv[j], rn, lambda,
-                                         step, extra);
-        if (over && cv[j] > overwrite) o = tv[j];
-        out[j] = o;
+    for (int j = 0; j < 4; ++j) R.v4[j] = load_v(yok, row, 4 * lane + j);
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) {
+      const int x = t.x0 + lane + 32 * k;
+      R.b[k] = 0u;
+      R.tv[k] = R.cv[k] = R.vc[k] = 0.f;
+      if (yok && x < W) {
+        const long long p = row + x;
+        R.b[k] = __ldg(bnd + p);
+        R.tv[k] = load_f(tgt + p);
+        R.cv[k] = load_f(cnf + p);
+        R.vc[k] = __ldg(vin + p);
       }
     }
-  }
-  __syncthreads();
-  // Y half-step: a run of kSeg rows of one column per lane; the lanes of a
-  // warp take 32 consecutive columns (coalesced bounds loads and stores).
-  const float slam = step * lambda;
-  constexpr int NSY = TH / kSeg;
-  constexpr int CB = TW / 32;
-  float* vout_i = vout + in.off;
-  for (int item = warp; item < CB * NSY; item += NW) {
-    const int c = (item % CB) * 32 + lane;  // constant divisor
-    const int sg = item / CB;
-    const int x = t.x0 + c, ys = t.y0 + sg * kSeg;
-    if (x >= W || ys >= H) continue;
-    const int n = min(kSeg, H - ys);
-    const float* col = sx + (hy + sg * kSeg) * TXp + c;  // col[j*TXp] = vx(ys + j)
-    const uint32_t* bp = bnd_i + (long long)ys * P + x;
-    float* op = vout_i + (long long)ys * P + x;
-    for (int j = 0; j < n; ++j) {
-      const uint32_t b = __ldg(bp + j * P);
-      const int dl = min((int)((b >> 16) & 0xff), hy + 1), du = min((int)(b >> 24), hy);
-      const float s = window_sum(col, TXp, j + 1 - dl, j + du);
-      const float v = col[j * TXp];
-      op[j * P] = __fmaf_rn(-slam, v - s * __frcp_rn((float)(dl + du)), v);
+  };
+  float mloc = 0.f;
+  unsigned* xb = Xb + warp * SWX;
+  RowIn cur, nxt;
+  if (warp < SR) fetch(warp, cur);
+  for (int r = warp; r < SR; r += NW) {
+    if (r + NW < SR) fetch(r + NW, nxt);
+    const int y = gy0 + r;
+    const bool yok = (unsigned)y < (unsigned)H;
+    const long long row = in.off + (long long)y * P;
+    float m = fmaxf(fmaxf(fabsf(cur.v4[0]), fabsf(cur.v4[1])),
+                    fmaxf(fabsf(cur.v4[2]), fabsf(cur.v4[3])));
+    for (int base = 128; base < SWX; base += 128)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) m = fmaxf(m, fabsf(load_v(yok, row, base + 4 * lane + j)));
+    const int F = fx_shift(warp_max_nonneg(m), lgx);
+    const float sF = pow2f(F), isF = pow2f(-F);
+    unsigned carry = 0;
+    for (int base = 0; base < SWX; base += 128) {
+      unsigned s4[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float v = base == 0 ? cur.v4[j] : load_v(yok, row, base + 4 * lane + j);
+        s4[j] = fx_from(v, sF) + (j ? s4[j - 1] : 0u);
+      }
+      const unsigned incl = warp_incl_scan(s4[3], lane);
+      const unsigned off = carry + incl - s4[3];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int cc = base + 4 * lane + j;
+        if (cc < SWX) xb[cc] = off + s4[j];
+      }
+      carry += __shfl_sync(0xffffffffu, incl, 31);
     }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) {
+      const int c = lane + 32 * k;
+      const int x = t.x0 + c;
+      float o = 0.f;
+      if (yok && x < W) {
+        const uint32_t b = cur.b[k];
+        const float tv = cur.tv[k], cv = cur.cv[k];
+        float v = cur.vc[k];
+        if (over && cv > overwrite) v = tv;
+        const int dl = min((int)(b & 0xff), hx + 1);
+        const int du = min((int)((b >> 8) & 0xff), hx);
+        const float rn = rtab[dl + du];
+        const int i = c + hx + 1;
+        const float B = fx_window(xb[i + du], xb[i - dl], rn * isF);
+        float extra = 0.f;
+        if (STEREO) extra = photometric(sa, row, x, W, v);
+        o = x_update<MODE, STEREO>(v, B, tv, cv, rn, lambda, step, extra);
+        if (over && cv > overwrite) o = tv;
+        if (r >= hy && r < hy + TH) sby[(r - hy) * TW + c] = (uint16_t)(b >> 16);
+      }
+      sx[r * TWp + c] = o;
+      mloc = fmaxf(mloc, fabsf(o));
+    }
+    __syncwarp();  // the warp's prefix buffer is rewritten for its next row
+    cur = nxt;
+  }
+  mloc = warp_max_nonneg(mloc);
+  if (lane == 0) atomicMax(smax, __float_as_uint(mloc));
+  __syncthreads();
+  // ---- Y half-step ----------------------------------------------------------
+  const int Fy = fx_shift(__uint_as_float(*smax), lgy);
+  const float sFy = pow2f(Fy), isFy = pow2f(-Fy);
+  const int c = tid % TW, sgi = tid / TW;
+  const int seg = (RY + NSEG - 1) / NSEG;
+  const int k0 = min(sgi * seg, RY), k1 = min(k0 + seg, RY);
+  unsigned acc = 0;
+  for (int k = k0; k < k1; ++k) {
+    if (k > 0) acc += fx_from(sx[(k - 1) * TWp + c], sFy);
+    Py[k * TW + c] = acc;
+  }
+  segtot[sgi * TW + c] = acc;
+  __syncthreads();
+  unsigned off = 0;
+  for (int s2 = 0; s2 < sgi; ++s2) off += segtot[s2 * TW + c];
+  for (int k = k0; k < k1; ++k) Py[k * TW + c] += off;
+  __syncthreads();
+  const float slam = step * lambda;
+  const int x = t.x0 + c;
+  for (int j = sgi; j < TH; j += NSEG) {
+    const int y = t.y0 + j;
+    if (y >= H || x >= W) continue;
+    const uint32_t b = sby[j * TW + c];
+    const int dl = min((int)(b & 0xff), hy + 1), du = min((int)(b >> 8), hy);
+    const int k = j + hy + 1;
+    const float B = fx_window(Py[(k + du) * TW + c], Py[(k - dl) * TW + c],
+                              rtab[dl + du] * isFy);
+    const float v = sx[(j + hy) * TWp + c];
+    vout[in.off + (long long)y * P + x] = __fmaf_rn(-slam, v - B, v);
   }
 }
 
@@ -598,13 +625,13 @@ static int launch_iter_shape(const DtsLaunch& L, const float* vin, float* vout,
                              const uint32_t* bounds, float lambda, float step,
                              float overwrite, int hx, int hy, cudaStream_t s,
                              const StereoArgs& sa) {
-  const size_t smem = sizeof(float) * ((size_t)(TH + 2 * hy) * ((TW + 2 * hx) | 1) +
-                                       (size_t)(TH + 2 * hy) * (TW + 1));
+  constexpr int NT = TW >= 64 ? 512 : 256;
+  const size_t smem = PrefixIterSmem<TW, TH, NT>::bytes(hx, hy);
   if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "sigma_z too large");
-  int st = set_smem(k_dts_iter<TS, MODE, TW, TH, STEREO>, smem);
+  int st = set_smem(k_dts_iter_prefix<TS, MODE, TW, TH, NT, STEREO>, smem);
   if (st) return st;
   ProfScope ps(s, DTSGB_K_DTS_ITER);
-  k_dts_iter<TS, MODE, TW, TH, STEREO><<<L.n_tiles, kThreads, smem, s>>>(
+  k_dts_iter_prefix<TS, MODE, TW, TH, NT, STEREO><<<L.n_tiles, NT, smem, s>>>(
       L.d_inst, L.d_tiles, vin, vout, (const TS*)target, (const TS*)conf,
       bounds, lambda, step, overwrite, hx, hy, sa);
   DTSGB_CUDA(cudaGetLastError());
