@@ -1,7 +1,7 @@
 """Benchmark of the DTS / HFBS hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg3|cfg0|cfg1]
+                    [--workload cfg3|cfg0|cfg1|cfg4]
 
 One JSON line on stdout (rank 0).  A step is one pass of the workload's
 solves with inputs already resident in HBM: for DTS the reference's timed
@@ -39,7 +39,7 @@ FALLBACK_HBM_GBS = 6800.0
 L2_FLUSH_BYTES = 256 << 20
 KERNEL_NAMES = {0: "k_bounds", 1: "k_dts_iter", 2: "k_filter", 3: "k_splat",
                 4: "k_bistoch", 5: "k_solve (HFBS heavy-ball)", 6: "hfbs setup kernels",
-                7: "k_slice", 8: "k_to_float"}
+                7: "k_slice", 8: "k_to_float", 9: "k_dts_adjoint"}
 
 
 def peaks():
@@ -322,7 +322,113 @@ class Cfg1:
         return self.pixels, "U and V solves"
 
 
-WORKLOADS = {"cfg3": Cfg3, "cfg0": Cfg0, "cfg1": Cfg1}
+class Cfg4:
+    """Differentiable DTS: 16 x 1024x768 config-0-style instances, FP32,
+    L2, 10 iterations, forward with checkpoints every ceil(sqrt(10)) = 4
+    iterations plus the adjoint (dL/dtarget, dL/dconfidence) for an N(0,1)
+    upstream gradient.  One step = forward + backward; the guide's window
+    bounds are held fixed (piecewise constant in the guide)."""
+
+    name = "cfg4_dts_fwd_bwd_16x1024x768_f32"
+    dtype = "f32"
+
+    def __init__(self, rank: int):
+        import domain_transform_solver_gb300 as D
+        from domain_transform_solver_gb300 import workloads as W
+        self.D, self.W = D, W
+        self.insts, self.grads = W.grad_instances()
+        self.sizes = [(i.width, i.height) for i in self.insts]
+        self.pixels = sum(w * h for w, h in self.sizes)
+        self.iters = W.CFG0_OPT["num_iterations"]
+        self.voxels = 0
+
+    def setup(self, stream_handle: int):
+        import torch
+        D, W = self.D, self.W
+        self.b = D.Batch(self.sizes)
+        self.b.set_stream(stream_handle)
+        self.b.enable_grad(True, 0)
+        self.b.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in self.insts],
+                      [i.target for i in self.insts], [i.confidence for i in self.insts])
+        self.fp = D.DomainFilterParams(**W.CFG0_FILTER)._c()
+        self.op = D.DomainOptimizeParams(**W.CFG0_OPT)._c()
+        self.lib = self.b._lib
+        dev = torch.device("cuda")
+        # upstream gradients resident in HBM; gradient outputs in HBM
+        self.d_g = torch.from_numpy(np.stack(self.grads)).to(dev)
+        self.d_gt = torch.empty_like(self.d_g)
+        self.d_gc = torch.empty_like(self.d_g)
+        n = len(self.sizes)
+        self.p_g = (ctypes.c_void_p * n)(*[self.d_g[i].data_ptr() for i in range(n)])
+        self.p_gt = (ctypes.c_void_p * n)(*[self.d_gt[i].data_ptr() for i in range(n)])
+        self.p_gc = (ctypes.c_void_p * n)(*[self.d_gc[i].data_ptr() for i in range(n)])
+        self._rgba = [_pinned_copy(i.rgba) for i in self.insts]
+        self._t = [_pinned_copy(i.target) for i in self.insts]
+        self._c = [_pinned_copy(i.confidence) for i in self.insts]
+        self._g = [_pinned_copy(g) for g in self.grads]
+        self._v = [_pinned_empty((h, w)) for w, h in self.sizes]
+        self._ogt = [_pinned_empty((h, w)) for w, h in self.sizes]
+        self._ogc = [_pinned_empty((h, w)) for w, h in self.sizes]
+        self.h_rgba, self.h_t, self.h_c = _ptrs(self._rgba), _ptrs(self._t), _ptrs(self._c)
+        self.h_g, self.h_v = _ptrs(self._g), _ptrs(self._v)
+        self.h_gt, self.h_gc = _ptrs(self._ogt), _ptrs(self._ogc)
+        # the plain forward (no checkpoints) of the same batch, for the ratio
+        self.fwd = D.Batch(self.sizes)
+        self.fwd.set_stream(stream_handle)
+        self.fwd.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in self.insts],
+                        [i.target for i in self.insts], [i.confidence for i in self.insts])
+
+    def step(self):
+        from domain_transform_solver_gb300._lib import check
+        check(self.lib.dtsgb_batch_solve_dts(self.b.handle, ctypes.byref(self.fp),
+                                             ctypes.byref(self.op), ctypes.c_float(-1.0)))
+        check(self.lib.dtsgb_batch_dts_backward_device(self.b.handle, self.p_g, self.p_gt,
+                                                       self.p_gc))
+
+    def forward_only(self):
+        from domain_transform_solver_gb300._lib import check
+        check(self.lib.dtsgb_batch_solve_dts(self.fwd.handle, ctypes.byref(self.fp),
+                                             ctypes.byref(self.op), ctypes.c_float(-1.0)))
+
+    def step_e2e(self):
+        from domain_transform_solver_gb300._lib import check
+        h = self.b.handle
+        check(self.lib.dtsgb_batch_upload(h, 1, self.h_rgba, self.h_t, self.h_c))
+        check(self.lib.dtsgb_batch_solve_dts(h, ctypes.byref(self.fp), ctypes.byref(self.op),
+                                             ctypes.c_float(-1.0)))
+        check(self.lib.dtsgb_batch_download(h, 0, self.h_v))
+        check(self.lib.dtsgb_batch_dts_backward(h, self.h_g, self.h_gt, self.h_gc))
+
+    def e2e_bytes(self):
+        # rgba, target, confidence, upstream gradient in; v, dL/dt, dL/dc out
+        return self.pixels * 16, self.pixels * 12
+
+    def algorithmic_bytes(self):
+        px = self.pixels
+        return {
+            0: 8 * px,   # read guide, write packed bounds
+            1: 20 * px,  # read v, t, c, bounds; write v (f32)
+            8: 8 * px,   # read t, write v
+            9: 40 * px,  # read g, v_k, t, c, bounds; read+write dL/dt, dL/dc; write g
+        }
+
+    def cpu_sample(self, real="f32"):
+        """A bounded sample: one instance, forward + adjoint by the FP32 port."""
+        import oracle as O
+        W = self.W
+        inst, g = self.insts[0], self.grads[0]
+        o = O.OracleDTS(inst.width, inst.height, real=real)
+        o.init_frame(1, inst.rgba, inst.target, inst.confidence)
+        o.differential(W.CFG0_FILTER["sigma_x"], W.CFG0_FILTER["sigma_y"],
+                       W.CFG0_FILTER["sigma_r"])
+        o.integrate()
+        op = W.CFG0_OPT
+        o.backward(op["num_iterations"], op["loss"], op["lambda_"], op["sigma_z"],
+                   op["step_size"], g)
+        return inst.width * inst.height, "1 of the 16 instances, forward + adjoint"
+
+
+WORKLOADS = {"cfg3": Cfg3, "cfg0": Cfg0, "cfg1": Cfg1, "cfg4": Cfg4}
 
 
 # ---- arms ----------------------------------------------------------------------
@@ -457,7 +563,7 @@ def run_ours(args, world, rank, local):
     # on the launching stream by the library; graph replays keep the events of
     # the latest replay, i.e. the last step)
     per_kernel = {}
-    for kid in range(9):
+    for kid in range(len(KERNEL_NAMES)):
         n, t = ctypes.c_int(), ctypes.c_double()
         lib.dtsgb_profile_read(kid, ctypes.byref(n), ctypes.byref(t))
         if n.value:
@@ -504,6 +610,24 @@ def run_ours(args, world, rank, local):
     h2d, d2h = wl.e2e_bytes()
     e2e_value = world * wl.pixels / (e2e_ms * 1e-3) / 1e6
 
+    fwd_ratio = None
+    if hasattr(wl, "forward_only"):
+        for _ in range(3):
+            wl.forward_only()
+        torch.cuda.synchronize()
+        f_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                for _ in range(args.steps)]
+        for k in range(args.steps):
+            if flush is not None:
+                flush.zero_()
+            f_ev[k][0].record(stream)
+            wl.forward_only()
+            f_ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        fwd_ms = max_over_ranks(world, sum(a.elapsed_time(b) for a, b in f_ev)) / args.steps
+        fwd_ratio = {"forward_ms": fwd_ms, "fwd_bwd_ms": ms_per_step,
+                     "fwd_bwd_over_forward": ms_per_step / fwd_ms}
+
     line = {
         "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
@@ -526,6 +650,8 @@ def run_ours(args, world, rank, local):
         "gpu_launches": int(round(launches_per_step * args.steps)),
         "clocks": clocks,
     }
+    if fwd_ratio:
+        line["fwd_bwd"] = fwd_ratio
     if rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline(wl)
     if rank == 0:

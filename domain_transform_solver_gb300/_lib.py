@@ -131,6 +131,14 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_batch_solve_hfbs": ([vp, P(HfbsParams)], i),
         "dtsgb_batch_download": ([vp, i, pvp], i),
         "dtsgb_batch_download_device": ([vp, i, pvp], i),
+        "dtsgb_batch_set_tuning": ([vp, i, ll], i),
+        "dtsgb_batch_get_tuning": ([vp, i, P(ll)], i),
+        "dtsgb_batch_autotune": ([vp, P(FilterParams), P(OptimizeParams), f,
+                                  P(HfbsParams), i], i),
+        "dtsgb_batch_enable_grad": ([vp, i, i], i),
+        "dtsgb_batch_grad_info": ([vp, P(i), P(i)], i),
+        "dtsgb_batch_dts_backward": ([vp, pvp, pvp, pvp], i),
+        "dtsgb_batch_dts_backward_device": ([vp, pvp, pvp, pvp], i),
         "dtsgb_dts_solve_noalloc": ([i, i, i, vp, vp, vp, P(FilterParams),
                                      P(OptimizeParams), f, vp, vp], i),
         "dtsgb_dts_init_right_frame": ([vp, f, i, vp], i),

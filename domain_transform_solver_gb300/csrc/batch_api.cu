@@ -58,9 +58,12 @@ struct dtsgb_batch_s {
   float* scratch = nullptr;
   Inst* d_inst = nullptr;
   Tile* d_tb = nullptr;
-  Tile* d_ti = nullptr;
-  int ntb = 0, nti = 0;
+  Tile* d_ti = nullptr;     // iteration tiles of the shape in use
+  Tile* d_ti_big = nullptr;  // kIterTW x kIterTH tiles
+  Tile* d_ti_small = nullptr;  // kIterSmallTW x kIterSmallTH tiles
+  int ntb = 0, nti = 0, nti_big = 0, nti_small = 0;
   bool small = false;
+  long long hfbs_group_voxels = 0;  // L2-resident HFBS group budget (0: off)
   int dts_res = -1;
   bool hfbs_done = false;
   bool use_graphs = true;
@@ -71,6 +74,15 @@ struct dtsgb_batch_s {
   long long gcap = 0;
   float* ovf = nullptr;
   long long ocap = 0;
+  // gradients of the DTS solve
+  bool grad = false;
+  int grad_seg_req = 0;          // 0: ceil(sqrt(N))
+  int grad_seg = 1;              // segment length of the planes below
+  int grad_n = -1;               // iterations the adjoint replays (-1: none kept)
+  std::vector<float*> gplanes;   // checkpoints, segment planes, 2 adjoint, dt, dc
+  dtsgb_optimize_params gopt{};  // parameters of the solve the planes belong to
+  float ghalo = 0.f;
+  Graph g_bwd;
 
   size_t tsize() const { return st == Storage::F32 ? 4 : 2; }
 };
@@ -86,9 +98,22 @@ void drop_graph(dtsgb_batch_t b, Graph& g) {
   g.key.clear();
 }
 
+void free_grad_planes(dtsgb_batch_t b) {
+  for (auto& p : b->gplanes) dfree(p);
+  b->gplanes.clear();
+}
+
+void select_tiles(dtsgb_batch_t b, bool small) {
+  b->small = small;
+  b->d_ti = small ? b->d_ti_small : b->d_ti_big;
+  b->nti = small ? b->nti_small : b->nti_big;
+}
+
 void batch_free(dtsgb_batch_t b) {
   drop_graph(b, b->g_dts);
   drop_graph(b, b->g_hfbs);
+  drop_graph(b, b->g_bwd);
+  free_grad_planes(b);
   dfree(b->guide);
   dfree(b->target);
   dfree(b->conf);
@@ -99,13 +124,55 @@ void batch_free(dtsgb_batch_t b) {
   dfree(b->scratch);
   dfree(b->d_inst);
   dfree(b->d_tb);
-  dfree(b->d_ti);
+  dfree(b->d_ti_big);
+  dfree(b->d_ti_small);
+  b->d_ti = nullptr;
   dfree(b->d_hinst);
   for (auto& p : b->hg) dfree(p);
   dfree(b->ovf);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
   b->stream = nullptr;
 }
+
+// Planes for the adjoint of an N-iteration solve with segment length seg:
+// ceil(N/seg) - 1 checkpoints, seg recompute planes, two adjoint planes and
+// the two gradient planes.  Reallocation drops the graphs that captured the
+// old pointers.
+int ensure_grad_planes(dtsgb_batch_t b, int n_iter, int seg) {
+  const int nseg = (n_iter + seg - 1) / seg;
+  const size_t need = (size_t)std::max(nseg - 1, 0) + seg + 4;
+  if (b->gplanes.size() == need && b->grad_seg == seg) return DTSGB_OK;
+  DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+  drop_graph(b, b->g_dts);
+  drop_graph(b, b->g_bwd);
+  free_grad_planes(b);
+  b->grad_seg = seg;
+  for (size_t k = 0; k < need; ++k) {
+    float* p = nullptr;
+    int st = dalloc(&p, (size_t)b->total);
+    if (st) {
+      free_grad_planes(b);
+      return st;
+    }
+    b->gplanes.push_back(p);
+  }
+  return DTSGB_OK;
+}
+
+DtsGrad grad_view(dtsgb_batch_t b, int n_iter) {
+  const int seg = b->grad_seg;
+  const int ncp = std::max((n_iter + seg - 1) / seg - 1, 0);
+  float* const* P = b->gplanes.data();
+  DtsGrad G;
+  G.seg = seg;
+  G.cp = P;
+  G.segbuf = P + ncp;
+  G.g[0] = P[ncp + seg];
+  G.g[1] = P[ncp + seg + 1];
+  return G;
+}
+float* grad_plane_t(dtsgb_batch_t b) { return b->gplanes[b->gplanes.size() - 2]; }
+float* grad_plane_c(dtsgb_batch_t b) { return b->gplanes[b->gplanes.size() - 1]; }
 
 // Run `enqueue` directly, or through the solve's CUDA graph (captured on the
 // first call with this key, replayed afterwards).
@@ -208,6 +275,7 @@ int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
                                       b->total, b->stream)))
     return st;
   b->dts_res = -1;
+  b->grad_n = -1;
   b->hfbs_done = false;
   if (kind == cudaMemcpyHostToDevice) DTSGB_CUDA(cudaStreamSynchronize(b->stream));
   return DTSGB_OK;
@@ -236,6 +304,35 @@ int ensure_hfbs_buffers(dtsgb_batch_t b, long long voxels, long long planes) {
 
 }  // namespace
 
+namespace {
+// Mean device time of `reps` runs of `run` on the batch stream (after one
+// untimed run, which also captures the graph).
+template <typename F>
+int time_runs(dtsgb_batch_t b, int reps, F run, float* ms) {
+  int st = run();
+  if (st) return st;
+  cudaEvent_t e0, e1;
+  DTSGB_CUDA(cudaEventCreate(&e0));
+  cudaError_t e = cudaEventCreate(&e1);
+  if (e != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return cuda_fail(e, "cudaEventCreate");
+  }
+  e = cudaEventRecord(e0, b->stream);
+  for (int r = 0; r < reps && !st && e == cudaSuccess; ++r) st = run();
+  if (!st && e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+  if (!st && e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float t = 0.f;
+  if (!st && e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  if (e != cudaSuccess) return cuda_fail(e, "autotune timing");
+  *ms = t / reps;
+  return DTSGB_OK;
+}
+}  // namespace
+
 extern "C" {
 
 DTSGB_API int dtsgb_batch_create(int n, const int* widths, const int* heights,
@@ -251,14 +348,12 @@ DTSGB_API int dtsgb_batch_create(int n, const int* widths, const int* heights,
   b->flags = flags;
   b->st = (flags & DTSGB_FLAG_BF16_STORAGE) ? Storage::BF16 : Storage::F32;
   b->ref_y = (flags & DTSGB_FLAG_FIX_Y_LIMIT) ? 0 : 1;
-  std::vector<Tile> tb, ti;
+  std::vector<Tile> tb, ti, ts;
   long long off = 0, tiles64 = 0;
   for (int i = 0; i < n; ++i)
     tiles64 += (long long)((widths[i] + kIterTW - 1) / kIterTW) *
                ((heights[i] + kIterTH - 1) / kIterTH);
   b->small = use_small_iter_tiles(tiles64);
-  const int itw = b->small ? kIterSmallTW : kIterTW;
-  const int ith = b->small ? kIterSmallTH : kIterTH;
   for (int i = 0; i < n; ++i) {
     Inst I{widths[i], heights[i], round_up(widths[i], 32), 0, off};
     b->inst.push_back(I);
@@ -267,12 +362,15 @@ DTSGB_API int dtsgb_batch_create(int n, const int* widths, const int* heights,
     b->max_h = std::max(b->max_h, I.h);
     for (int y = 0; y < I.h; y += kBoundsTH)
       for (int x = 0; x < I.w; x += kBoundsTW) tb.push_back(Tile{i, x, y, 0});
-    for (int y = 0; y < I.h; y += ith)
-      for (int x = 0; x < I.w; x += itw) ti.push_back(Tile{i, x, y, 0});
+    for (int y = 0; y < I.h; y += kIterTH)
+      for (int x = 0; x < I.w; x += kIterTW) ti.push_back(Tile{i, x, y, 0});
+    for (int y = 0; y < I.h; y += kIterSmallTH)
+      for (int x = 0; x < I.w; x += kIterSmallTW) ts.push_back(Tile{i, x, y, 0});
   }
   b->total = off;
   b->ntb = (int)tb.size();
-  b->nti = (int)ti.size();
+  b->nti_big = (int)ti.size();
+  b->nti_small = (int)ts.size();
   int st = DTSGB_OK;
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -291,16 +389,22 @@ DTSGB_API int dtsgb_batch_create(int n, const int* widths, const int* heights,
   if (!st && b->st == Storage::BF16) st = dalloc(&b->scratch, T);
   if (!st) st = dalloc(&b->d_inst, (size_t)n);
   if (!st) st = dalloc(&b->d_tb, tb.size());
-  if (!st) st = dalloc(&b->d_ti, ti.size());
+  if (!st) st = dalloc(&b->d_ti_big, ti.size());
+  if (!st) st = dalloc(&b->d_ti_small, ts.size());
   if (!st) st = dalloc(&b->d_hinst, (size_t)n);
   if (!st) {
     e = cudaMemcpy(b->d_inst, b->inst.data(), n * sizeof(Inst), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
       e = cudaMemcpy(b->d_tb, tb.data(), tb.size() * sizeof(Tile), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
-      e = cudaMemcpy(b->d_ti, ti.data(), ti.size() * sizeof(Tile), cudaMemcpyHostToDevice);
+      e = cudaMemcpy(b->d_ti_big, ti.data(), ti.size() * sizeof(Tile),
+                     cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_ti_small, ts.data(), ts.size() * sizeof(Tile),
+                     cudaMemcpyHostToDevice);
     if (e != cudaSuccess) st = cuda_fail(e, "batch tables");
   }
+  select_tiles(b, b->small);
   if (st) {
     batch_free(b);
     delete b;
@@ -371,8 +475,30 @@ DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b, const dtsgb_filter_params* 
   const bool iterate = p->loss != DTSGB_L1 && p->num_iterations > 0;
   const DtsLaunch Lb{b->d_inst, b->d_tb, b->ntb, b->n};
   const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n, b->small};
+  const bool over = overwrite > 0.f && overwrite < 1.f;
+  const int n_kept = iterate ? p->num_iterations : 0;
+  b->grad_n = -1;
+  if (b->grad) {
+    if (iterate && over)
+      return fail(DTSGB_ERR_UNSUPPORTED,
+                  "gradients are not available with the confidence overwrite");
+    const int seg = b->grad_seg_req > 0 ? b->grad_seg_req
+                                        : dts_checkpoint_segment(std::max(n_kept, 1));
+    int st = ensure_grad_planes(b, n_kept, seg);
+    if (st) return st;
+  }
   int res = 0;
   auto enqueue = [&]() -> int {
+    if (b->grad && iterate) {
+      const IterMode mode = p->loss == DTSGB_L2 ? IterMode::L2 : IterMode::CHARB;
+      int st = launch_bounds(Lb, b->guide, b->bounds, rx, ry, p->sigma_z, p->sigma_z,
+                             b->ref_y, b->stream);
+      if (st) return st;
+      return dts_forward_checkpointed(Li, b->st, mode, grad_view(b, n_kept), b->target,
+                                      b->conf, b->bounds, p->lambda, p->step_size, halo,
+                                      p->num_iterations, b->v[0], b->v[1], &res,
+                                      b->stream);
+    }
     int st = launch_init_var(Li, b->st, b->target, b->v[0], b->stream);
     if (st || !iterate) return st;
     st = launch_bounds(Lb, b->guide, b->bounds, rx, ry, p->sigma_z, p->sigma_z,
@@ -389,15 +515,111 @@ DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b, const dtsgb_filter_params* 
     }
     return DTSGB_OK;
   };
-  res = iterate ? (p->num_iterations % 2) : 0;
+  res = iterate ? (b->grad ? dts_checkpointed_result_index(p->num_iterations, b->grad_seg)
+                           : p->num_iterations % 2)
+                : 0;
   std::vector<char> key;
   key_append(key, *f);
   key_append(key, *p);
   key_append(key, overwrite);
+  key_append(key, b->grad);
+  key_append(key, b->grad_seg);
+  key_append(key, b->small);
   int st = run_graph(b, b->g_dts, key, enqueue);
   if (st) return st;
   b->dts_res = res;
+  if (b->grad) {
+    b->grad_n = n_kept;
+    b->gopt = *p;
+    b->ghalo = (float)halo;
+  }
   return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_batch_enable_grad(dtsgb_batch_t b, int enable, int segment) {
+  if (!b) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null handle");
+  if (segment < 0) return fail(DTSGB_ERR_INVALID_ARGUMENT, "segment < 0");
+  if (b->grad != (enable != 0) || b->grad_seg_req != segment) {
+    DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+    drop_graph(b, b->g_dts);
+    drop_graph(b, b->g_bwd);
+  }
+  b->grad = enable != 0;
+  b->grad_seg_req = segment;
+  b->grad_n = -1;
+  if (!b->grad) free_grad_planes(b);
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_batch_grad_info(dtsgb_batch_t b, int* segment, int* planes) {
+  if (!b || !segment || !planes) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  *segment = b->grad_n >= 0 ? b->grad_seg : 0;
+  *planes = (int)b->gplanes.size();
+  return DTSGB_OK;
+}
+
+static int batch_backward(dtsgb_batch_t b, const float* const* grad_out,
+                          float* const* grad_t, float* const* grad_c,
+                          cudaMemcpyKind up, cudaMemcpyKind down) {
+  if (!b || !grad_out) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  if (b->grad_n < 0)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT,
+                "no DTS solve with gradients enabled since the last upload");
+  for (int i = 0; i < b->n; ++i)
+    if (!grad_out[i]) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null gradient pointer");
+  const int n_iter = b->grad_n;
+  DtsGrad G = grad_view(b, n_iter);
+  for (int i = 0; i < b->n; ++i) {
+    const Inst& I = b->inst[i];
+    const size_t wb = (size_t)I.w * 4;
+    DTSGB_CUDA(cudaMemcpy2DAsync(G.g[0] + I.off, (size_t)I.pitch * 4, grad_out[i], wb, wb,
+                                 I.h, up, b->stream));
+  }
+  const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n, b->small};
+  const dtsgb_optimize_params p = b->gopt;
+  const int halo = (int)b->ghalo;
+  auto enqueue = [&]() -> int {
+    const IterMode mode = p.loss == DTSGB_L2 ? IterMode::L2 : IterMode::CHARB;
+    return dts_backward(Li, b->d_inst, b->n, b->total, b->st, mode, G, b->target, b->conf,
+                        b->bounds, p.lambda, p.step_size, halo, n_iter, grad_plane_t(b),
+                        grad_plane_c(b), b->stream);
+  };
+  std::vector<char> key;
+  key_append(key, p);
+  key_append(key, n_iter);
+  key_append(key, b->grad_seg);
+  key_append(key, b->small);
+  int st = run_graph(b, b->g_bwd, key, enqueue);
+  if (st) return st;
+  for (int k = 0; k < 2; ++k) {
+    float* const* dst = k == 0 ? grad_t : grad_c;
+    const float* src = k == 0 ? grad_plane_t(b) : grad_plane_c(b);
+    if (!dst) continue;
+    for (int i = 0; i < b->n; ++i) {
+      if (!dst[i]) continue;
+      const Inst& I = b->inst[i];
+      const size_t wb = (size_t)I.w * 4;
+      DTSGB_CUDA(cudaMemcpy2DAsync(dst[i], wb, src + I.off, (size_t)I.pitch * 4, wb, I.h,
+                                   down, b->stream));
+    }
+  }
+  if (down == cudaMemcpyDeviceToHost) DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_batch_dts_backward(dtsgb_batch_t b, const float* const* grad_out,
+                                       float* const* grad_target,
+                                       float* const* grad_confidence) {
+  return batch_backward(b, grad_out, grad_target, grad_confidence, cudaMemcpyHostToDevice,
+                        cudaMemcpyDeviceToHost);
+}
+
+DTSGB_API int dtsgb_batch_dts_backward_device(dtsgb_batch_t b,
+                                              const float* const* grad_out,
+                                              float* const* grad_target,
+                                              float* const* grad_confidence) {
+  return batch_backward(b, grad_out, grad_target, grad_confidence,
+                        cudaMemcpyDeviceToDevice, cudaMemcpyDeviceToDevice);
 }
 
 DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p) {
@@ -475,13 +697,95 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
   B.t2 = b->hg[HG_T2];
   B.ovf = b->ovf;
   B.keep_debug = false;
+  B.h_inst = b->hinst.data();
+  B.group_voxels = b->hfbs_group_voxels;
   HParams hp{p->sigma_x, p->sigma_y, p->sigma_l, p->lambda, p->alpha, p->beta,
              p->bistoch_iter_max, p->optim_iter_max, p->neg_exp_beta};
   std::vector<char> key;
   key_append(key, hp);
+  key_append(key, b->hfbs_group_voxels);
   st = run_graph(b, b->g_hfbs, key, [&]() { return hfbs_enqueue_solve(B, hp, b->stream); });
   if (st) return st;
   b->hfbs_done = true;
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_batch_set_tuning(dtsgb_batch_t b, int knob, long long value) {
+  if (!b) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null handle");
+  if (knob == DTSGB_TUNE_DTS_TILE) {
+    if (value != kIterTW && value != kIterSmallTW)
+      return fail(DTSGB_ERR_INVALID_ARGUMENT, "DTS tile must be 64 or 32");
+    const bool small = value == kIterSmallTW;
+    if (small != b->small) {
+      select_tiles(b, small);
+      b->grad_n = -1;  // checkpoints were computed with the other tile shape
+    }
+    return DTSGB_OK;
+  }
+  if (knob == DTSGB_TUNE_HFBS_GROUP_VOXELS) {
+    if (value < 0) return fail(DTSGB_ERR_INVALID_ARGUMENT, "group budget < 0");
+    b->hfbs_group_voxels = value;
+    return DTSGB_OK;
+  }
+  return fail(DTSGB_ERR_INVALID_ARGUMENT, "unknown tuning knob");
+}
+
+DTSGB_API int dtsgb_batch_get_tuning(dtsgb_batch_t b, int knob, long long* value) {
+  if (!b || !value) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  if (knob == DTSGB_TUNE_DTS_TILE) {
+    *value = b->small ? kIterSmallTW : kIterTW;
+    return DTSGB_OK;
+  }
+  if (knob == DTSGB_TUNE_HFBS_GROUP_VOXELS) {
+    *value = b->hfbs_group_voxels;
+    return DTSGB_OK;
+  }
+  return fail(DTSGB_ERR_INVALID_ARGUMENT, "unknown tuning knob");
+}
+
+
+DTSGB_API int dtsgb_batch_autotune(dtsgb_batch_t b, const dtsgb_filter_params* f,
+                                   const dtsgb_optimize_params* p, float overwrite,
+                                   const dtsgb_hfbs_params* hp, int reps) {
+  if (!b) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null handle");
+  if ((f == nullptr) != (p == nullptr))
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "filter and optimize params go together");
+  if (reps < 1) reps = 3;
+  int st;
+  if (f) {
+    float best = 3.4e38f;
+    long long best_tile = kIterTW;
+    for (long long tile : {(long long)kIterTW, (long long)kIterSmallTW}) {
+      if ((st = dtsgb_batch_set_tuning(b, DTSGB_TUNE_DTS_TILE, tile))) return st;
+      float ms = 0.f;
+      st = time_runs(b, reps, [&]() { return dtsgb_batch_solve_dts(b, f, p, overwrite); },
+                     &ms);
+      if (st == DTSGB_ERR_UNSUPPORTED) continue;  // halo too large for this shape
+      if (st) return st;
+      if (ms < best) {
+        best = ms;
+        best_tile = tile;
+      }
+    }
+    if ((st = dtsgb_batch_set_tuning(b, DTSGB_TUNE_DTS_TILE, best_tile))) return st;
+    if ((st = dtsgb_batch_solve_dts(b, f, p, overwrite))) return st;
+  }
+  if (hp) {
+    float best = 3.4e38f;
+    long long best_g = 0;
+    for (long long g : {0LL, 1000000LL, 2000000LL, 4000000LL, 8000000LL}) {
+      if ((st = dtsgb_batch_set_tuning(b, DTSGB_TUNE_HFBS_GROUP_VOXELS, g))) return st;
+      float ms = 0.f;
+      if ((st = time_runs(b, reps, [&]() { return dtsgb_batch_solve_hfbs(b, hp); }, &ms)))
+        return st;
+      if (ms < best) {
+        best = ms;
+        best_g = g;
+      }
+    }
+    if ((st = dtsgb_batch_set_tuning(b, DTSGB_TUNE_HFBS_GROUP_VOXELS, best_g))) return st;
+    if ((st = dtsgb_batch_solve_hfbs(b, hp))) return st;
+  }
   return DTSGB_OK;
 }
 

@@ -204,4 +204,34 @@ int launch_row_prefix(const Inst* h_inst, const Inst* d_inst, int n_inst,
 int launch_unpack_bounds(const DtsLaunch& L, const uint32_t* bounds, int axis,
                          int32_t* l, int32_t* u, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// Adjoint of the fixed-window solve (dts_adjoint.cu).
+// ---------------------------------------------------------------------------
+struct DtsGrad {
+  int seg;               // iterations per checkpoint segment (>= 1)
+  float* const* cp;      // checkpoints v_seg, v_2seg, ...: ceil(N/seg) - 1 planes
+  float* const* segbuf;  // seg planes for the recomputed iterates of a segment
+  float* g[2];           // adjoint ping-pong; g[0] holds dL/dv_N on entry
+};
+// ceil(sqrt(num_iterations)): the segment length that minimises the planes
+// held, ceil(N/seg) - 1 + seg.
+int dts_checkpoint_segment(int num_iterations);
+// The forward solve (init + num_iterations fused iterations, no overwrite),
+// writing v_seg, v_2seg, ... into G.cp; the result ends in v0 or v1
+// (*result_idx).
+int dts_forward_checkpointed(const DtsLaunch& L, Storage st, IterMode mode,
+                             const DtsGrad& G, const void* target, const void* conf,
+                             const uint32_t* bounds, float lambda, float step, int halo,
+                             int num_iterations, float* v0, float* v1, int* result_idx,
+                             cudaStream_t s);
+// Which of v0 / v1 holds the result of dts_forward_checkpointed.
+int dts_checkpointed_result_index(int num_iterations, int seg);
+// dL/dt and dL/dc (planes of the instance layout, overwritten) for the
+// upstream gradient in G.g[0]; G.g[0] and G.g[1] are clobbered.
+int dts_backward(const DtsLaunch& L, const Inst* d_inst, int n_inst, long long plane,
+                 Storage st, IterMode mode, const DtsGrad& G, const void* target,
+                 const void* conf, const uint32_t* bounds, float lambda, float step,
+                 int halo, int num_iterations, float* grad_t, float* grad_c,
+                 cudaStream_t s);
+
 }  // namespace dtsgb

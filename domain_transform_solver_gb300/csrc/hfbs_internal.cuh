@@ -32,6 +32,10 @@ struct HParams {
 struct HfbsBatch {
   const HInst* d_inst;
   int n_inst;
+  // host copy of the instance table and the voxel budget of an L2-resident
+  // group (0: all instances together); see hfbs_enqueue_solve
+  const HInst* h_inst = nullptr;
+  long long group_voxels = 0;
   long long max_voxels, max_pixels, max_cells, max_lines;
   long long max_rows;  // max over instances of gy * gl (grid rows along x)
   int max_gl;

@@ -11,6 +11,9 @@
 // The splat is atomic-free and deterministic: one thread per spatial cell
 // walks the cell's pixels in row-major order and bins them into per-thread
 // luma histograms held in shared memory.
+#include <algorithm>
+#include <vector>
+
 #include "../../include/dtsgb.h"
 #include "dtsgb_internal.cuh"
 #include "hfbs_internal.cuh"
@@ -115,17 +118,35 @@ __global__ void k_bistoch(const HInst* __restrict__ insts,
        row += nwarps) {
     const int z = row / gy, y = row - z * gy;
     const int base = row * gx;
-    for (int x = lane; x < gx; x += 32) {
-      const int i = base + x;
-      const float v = s[i];
-      float nb = x > 0 ? s[i - 1] : 0.f;
-      nb += x + 1 < gx ? s[i + 1] : px;
-      nb += y > 0 ? s[i - sy] : 0.f;
-      nb += y + 1 < gy ? s[i + sy] : py;
-      nb += z > 0 ? s[i - sz] : 0.f;
-      nb += z + 1 < gl ? s[i + sz] : pz;
-      const float blurred = 2.f * v + nb;
-      d[i] = __fsqrt_rn(__fdiv_rn(v * (cn[i] + 0.00001f), blurred + 0.00001f));
+    // four x positions per lane per pass: all their loads are issued before
+    // any result is computed
+    for (int x0 = lane; x0 < gx; x0 += 128) {
+      float v[4], nb[4], cc[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int x = x0 + 32 * j;
+        v[j] = nb[j] = cc[j] = 0.f;
+        if (x < gx) {
+          const int i = base + x;
+          v[j] = s[i];
+          float a = x > 0 ? s[i - 1] : 0.f;
+          a += x + 1 < gx ? s[i + 1] : px;
+          a += y > 0 ? s[i - sy] : 0.f;
+          a += y + 1 < gy ? s[i + sy] : py;
+          a += z > 0 ? s[i - sz] : 0.f;
+          a += z + 1 < gl ? s[i + sz] : pz;
+          nb[j] = a;
+          cc[j] = cn[i];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int x = x0 + 32 * j;
+        if (x >= gx) break;
+        const float blurred = 2.f * v[j] + nb[j];
+        d[base + x] =
+            __fsqrt_rn(__fdiv_rn(v[j] * (cc[j] + 0.00001f), blurred + 0.00001f));
+      }
     }
   }
 }
@@ -295,24 +316,45 @@ __global__ void k_solve(const HInst* __restrict__ insts,
        row += nwarps) {
     const int zz = row / gy, y = row - zz * gy;
     const int base = row * gx;
-    for (int x = lane; x < gx; x += 32) {
-      const int i = base + x;
-      float d = 0.f;
-      if (x > 0) d += z[i - 1] * nn[i - 1];
-      if (x + 1 < gx) d += z[i + 1] * nn[i + 1];
-      if (y > 0) d += z[i - sy] * nn[i - sy];
-      if (y + 1 < gy) d += z[i + sy] * nn[i + sy];
-      if (zz > 0) d += z[i - sz] * nn[i - sz];
-      if (zz + 1 < gl) d += z[i + sz] * nn[i + sz];
-      const float q = (bb[i] + lambda * nn[i] * d) * ia[i];
-      const float zc = z[i];
-      const float grad = zc - q;
-      // |grad| > 1.345 with the double threshold of the reference: the
-      // smallest float above 1.345 (double) is 1.345f
-      const float gc = fabsf(grad) >= 1.345f ? copysignf(1.f, grad) : grad;
-      const float hn = __fmaf_rn(beta, hh[i], gc);
-      hh[i] = hn;
-      zo[i] = zc - alpha * hn;
+    // four x positions per lane per pass: all their loads are issued before
+    // any result is computed
+    for (int x0 = lane; x0 < gx; x0 += 128) {
+      float d[4], zc[4], nc[4], bc[4], ic[4], hc[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int x = x0 + 32 * j;
+        d[j] = zc[j] = nc[j] = bc[j] = ic[j] = hc[j] = 0.f;
+        if (x < gx) {
+          const int i = base + x;
+          float a = 0.f;
+          if (x > 0) a += z[i - 1] * nn[i - 1];
+          if (x + 1 < gx) a += z[i + 1] * nn[i + 1];
+          if (y > 0) a += z[i - sy] * nn[i - sy];
+          if (y + 1 < gy) a += z[i + sy] * nn[i + sy];
+          if (zz > 0) a += z[i - sz] * nn[i - sz];
+          if (zz + 1 < gl) a += z[i + sz] * nn[i + sz];
+          d[j] = a;
+          zc[j] = z[i];
+          nc[j] = nn[i];
+          bc[j] = bb[i];
+          ic[j] = ia[i];
+          hc[j] = hh[i];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int x = x0 + 32 * j;
+        if (x >= gx) break;
+        const int i = base + x;
+        const float q = (bc[j] + lambda * nc[j] * d[j]) * ic[j];
+        const float grad = zc[j] - q;
+        // |grad| > 1.345 with the double threshold of the reference: the
+        // smallest float above 1.345 (double) is 1.345f
+        const float gc = fabsf(grad) >= 1.345f ? copysignf(1.f, grad) : grad;
+        const float hn = __fmaf_rn(beta, hc[j], gc);
+        hh[i] = hn;
+        zo[i] = zc[j] - alpha * hn;
+      }
     }
   }
 }
@@ -407,16 +449,49 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   // bistochastization ping-pong: even iterations read the buffer filled with
   // ones, whose covered pad faces hold 1
   k_fill_ones<<<gv, kT, 0, s>>>(B.d_inst, B.n0);
+  // The iterative stages (bistochastization, heavy-ball) touch only their own
+  // instance's grid, so they run group by group: all iterations of a group
+  // of consecutive instances whose grids fit in L2 before the next group,
+  // which then streams from L2 instead of HBM after its first iteration.
+  struct Group {
+    int first, count;
+    long long rows;
+  };
+  std::vector<Group> groups;
+  if (B.h_inst && B.group_voxels > 0) {
+    Group g{0, 0, 0};
+    long long vox = 0;
+    for (int i = 0; i < ni; ++i) {
+      const HInst& H = B.h_inst[i];
+      const long long v = (long long)H.gx * H.gy * H.gl;
+      if (g.count > 0 && vox + v > B.group_voxels) {
+        groups.push_back(g);
+        g = Group{i, 0, 0};
+        vox = 0;
+      }
+      ++g.count;
+      vox += v;
+      g.rows = std::max(g.rows, (long long)H.gy * H.gl);
+    }
+    groups.push_back(g);
+  } else {
+    groups.push_back(Group{0, ni, B.max_rows});
+  }
+  auto row_grid = [](const Group& g) {
+    return dim3((unsigned)std::min<long long>((g.rows + 7) / 8, 4096), g.count);
+  };
   float* src = B.n0;
   float* dst = B.n1;
-  for (int it = 0; it < p.bistoch_iter_max; ++it) {
-    prof_begin(s, DTSGB_K_HFBS_BISTOCH);
-    k_bistoch<<<gr, kT, 0, s>>>(B.d_inst, src, dst, B.count,
-                                (it % 2 == 0) ? 1.f : 0.f);
-    prof_end(s, DTSGB_K_HFBS_BISTOCH);
-    float* t = src;
-    src = dst;
-    dst = t;
+  for (const Group& g : groups) {
+    src = B.n0;
+    dst = B.n1;
+    for (int it = 0; it < p.bistoch_iter_max; ++it) {
+      prof_begin(s, DTSGB_K_HFBS_BISTOCH);
+      k_bistoch<<<row_grid(g), kT, 0, s>>>(B.d_inst + g.first, src, dst, B.count,
+                                           (it % 2 == 0) ? 1.f : 0.f);
+      prof_end(s, DTSGB_K_HFBS_BISTOCH);
+      std::swap(src, dst);
+    }
   }
   float* norm = src;
   float* spare = dst;
@@ -443,14 +518,16 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   }
   float* zs = B.z0;
   float* zd = B.z1;
-  for (int it = 0; it < p.optim_iter_max; ++it) {
-    prof_begin(s, DTSGB_K_HFBS_SOLVE);
-    k_solve<<<gr, kT, 0, s>>>(B.d_inst, zs, zd, B.h, norm, B.b, B.invA, p.lambda,
-                              p.alpha, p.beta);
-    prof_end(s, DTSGB_K_HFBS_SOLVE);
-    float* t = zs;
-    zs = zd;
-    zd = t;
+  for (const Group& g : groups) {
+    zs = B.z0;
+    zd = B.z1;
+    for (int it = 0; it < p.optim_iter_max; ++it) {
+      prof_begin(s, DTSGB_K_HFBS_SOLVE);
+      k_solve<<<row_grid(g), kT, 0, s>>>(B.d_inst + g.first, zs, zd, B.h, norm, B.b,
+                                         B.invA, p.lambda, p.alpha, p.beta);
+      prof_end(s, DTSGB_K_HFBS_SOLVE);
+      std::swap(zs, zd);
+    }
   }
   if (B.keep_debug)
     DTSGB_CUDA(cudaMemcpyAsync(B.dbg_z_final, zs, B.grid_bytes,

@@ -35,13 +35,16 @@ __all__ = [
     "DomainFilterParamsVec1", "DomainOptimizeParams", "HFBSGridParams",
     "DomainTransformFilter", "DomainTransformSolver", "HFBS", "DtsOptions",
     "HfbsOptions", "Solve", "EdgeAwareOptimize", "DtsgbError",
-    "FLAG_BF16_STORAGE", "FLAG_FIX_Y_LIMIT", "Batch", "DomainTransformStereo",
+    "FLAG_BF16_STORAGE", "FLAG_FIX_Y_LIMIT", "TUNE_DTS_TILE", "TUNE_HFBS_GROUP_VOXELS",
+    "Batch", "DomainTransformStereo",
 ]
 
 FLAG_BF16_STORAGE = 0x1
 FLAG_FIX_Y_LIMIT = 0x2
 FLAG_FILTER_ONLY = 0x4
 FLAG_STEREO = 0x8
+TUNE_DTS_TILE = 0
+TUNE_HFBS_GROUP_VOXELS = 1
 
 
 @dataclass
@@ -369,6 +372,15 @@ def _ptr_array(arrays):
     return out
 
 
+def _vp_array(ptrs):
+    """ctypes array of device addresses (ints; None or 0 = skip)."""
+    n = len(ptrs)
+    out = (ctypes.c_void_p * n)()
+    for i, p in enumerate(ptrs):
+        out[i] = None if not p else int(p)
+    return out
+
+
 class Batch:
     """Many images of uneven size solved together (no reference counterpart:
     the reference solves one image per object).  solve_dts / solve_hfbs run
@@ -432,6 +444,66 @@ class Batch:
         outs = [np.empty((h, w), np.float32) for w, h in self.sizes]
         check(self._lib.dtsgb_batch_download(self._h, int(which), _ptr_array(outs)))
         return outs
+
+    # ---- device pointers (integers), e.g. from torch tensors ----------------
+    def upload_device(self, color_space: COLOR_SPACE, rgba_ptrs, target_ptrs,
+                      confidence_ptrs=None) -> None:
+        conf = None if confidence_ptrs is None else _vp_array(confidence_ptrs)
+        check(self._lib.dtsgb_batch_upload_device(self._h, int(color_space),
+                                                  _vp_array(rgba_ptrs),
+                                                  _vp_array(target_ptrs), conf))
+
+    def download_device(self, which: int, dst_ptrs) -> None:
+        check(self._lib.dtsgb_batch_download_device(self._h, int(which),
+                                                    _vp_array(dst_ptrs)))
+
+    # ---- tuning (no reference counterpart) ----------------------------------
+    def set_tuning(self, knob: int, value: int) -> None:
+        check(self._lib.dtsgb_batch_set_tuning(self._h, int(knob), int(value)))
+
+    def get_tuning(self, knob: int) -> int:
+        v = ctypes.c_longlong()
+        check(self._lib.dtsgb_batch_get_tuning(self._h, int(knob), ctypes.byref(v)))
+        return v.value
+
+    def autotune(self, filter_params=None, optimize_params=None, grid_params=None,
+                 overwrite_target_above_conf: float = -1, reps: int = 3) -> None:
+        """Time each tile shape / HFBS group budget on the uploaded batch and
+        keep the fastest."""
+        f = None if filter_params is None else ctypes.byref(filter_params._c())
+        o = None if optimize_params is None else ctypes.byref(optimize_params._c())
+        g = None if grid_params is None else ctypes.byref(grid_params._c())
+        check(self._lib.dtsgb_batch_autotune(self._h, f, o,
+                                             float(overwrite_target_above_conf), g,
+                                             int(reps)))
+
+    # ---- gradients of the DTS solve (no reference counterpart) --------------
+    def enable_grad(self, enable: bool = True, segment: int = 0) -> None:
+        """Keep checkpoints in solve_dts every `segment` iterations
+        (0 = ceil(sqrt(N))) so that backward() can run."""
+        check(self._lib.dtsgb_batch_enable_grad(self._h, int(enable), int(segment)))
+
+    def grad_info(self):
+        """(segment length, planes held) of the last solve."""
+        seg, planes = ctypes.c_int(), ctypes.c_int()
+        check(self._lib.dtsgb_batch_grad_info(self._h, ctypes.byref(seg),
+                                              ctypes.byref(planes)))
+        return seg.value, planes.value
+
+    def backward(self, grad_out):
+        """dL/dtarget, dL/dconfidence (lists of HxW float32) for the upstream
+        gradients dL/dv of the last solve_dts results."""
+        go = [_f32(a, (h, w)) for a, (w, h) in zip(grad_out, self.sizes)]
+        gt = [np.empty((h, w), np.float32) for w, h in self.sizes]
+        gc = [np.empty((h, w), np.float32) for w, h in self.sizes]
+        check(self._lib.dtsgb_batch_dts_backward(self._h, _ptr_array(go), _ptr_array(gt),
+                                                 _ptr_array(gc)))
+        return gt, gc
+
+    def backward_device(self, grad_out_ptrs, grad_target_ptrs, grad_conf_ptrs=None) -> None:
+        gc = None if grad_conf_ptrs is None else _vp_array(grad_conf_ptrs)
+        check(self._lib.dtsgb_batch_dts_backward_device(self._h, _vp_array(grad_out_ptrs),
+                                                        _vp_array(grad_target_ptrs), gc))
 
 
 # ---- generic solve API, src/edge_aware_solver.h:13-90 (cv::Mat-free) -------

@@ -182,6 +182,15 @@ def batched_instances(seed: int = SEED_BASE + 3, n: int = 64, scale: float = 1.0
     return out
 
 
+def grad_instances(seed: int = SEED_BASE + 4, n: int = 16, w: int = 1024, h: int = 768):
+    """cfg 4: n cfg-0-style instances of w x h (samples every 8 px) and one
+    N(0,1) upstream gradient dL/dv per instance."""
+    insts = [depth_sr_instance(seed * 1000 + i, w, h) for i in range(n)]
+    rng = np.random.default_rng(seed)
+    grads = [rng.standard_normal((h, w)).astype(np.float32) for _ in range(n)]
+    return insts, grads
+
+
 # ---- solver parameters of each configuration -------------------------------
 CFG0_FILTER = dict(sigma_x=8.0, sigma_y=8.0, sigma_r=0.1)
 CFG0_OPT = dict(num_iterations=10, loss=1, lambda_=0.99, sigma_z=8.0, step_size=0.99)

@@ -117,7 +117,8 @@ enum {
   DTSGB_K_HFBS_OTHER = 6,
   DTSGB_K_HFBS_SLICE = 7,
   DTSGB_K_DTS_OTHER = 8, /* iterate init, conversions                 */
-  DTSGB_K_COUNT = 9
+  DTSGB_K_DTS_ADJOINT = 9, /* adjoint of one fused iteration          */
+  DTSGB_K_COUNT = 10
 };
 DTSGB_API int dtsgb_profile_enable(int enable);
 DTSGB_API int dtsgb_profile_reset(void);
@@ -312,6 +313,53 @@ DTSGB_API int dtsgb_batch_download(dtsgb_batch_t b, int which,
                                    float* const* dst);
 DTSGB_API int dtsgb_batch_download_device(dtsgb_batch_t b, int which,
                                           float* const* dst);
+
+/* ---- Tuning (new).  DTSGB_TUNE_DTS_TILE: side of the square tiles of the
+ * fused DTS iteration and its adjoint, 64 or 32 (default: 32 when the batch
+ * has fewer than 4 x 152 tiles of 64 x 64).  DTSGB_TUNE_HFBS_GROUP_VOXELS:
+ * the HFBS iterations run over groups of consecutive instances holding at
+ * most this many grid voxels, all iterations of one group before the next,
+ * so that a group's grids can stay in L2 (0, the default: all instances at
+ * once).  Neither changes results beyond the last bits of the DTS iterate
+ * (HFBS: bitwise identical). */
+#define DTSGB_TUNE_DTS_TILE 0
+#define DTSGB_TUNE_HFBS_GROUP_VOXELS 1
+DTSGB_API int dtsgb_batch_set_tuning(dtsgb_batch_t b, int knob, long long value);
+DTSGB_API int dtsgb_batch_get_tuning(dtsgb_batch_t b, int knob, long long* value);
+/* Times the uploaded batch's solves under each tile shape (filter and
+ * optimize given) and HFBS group budget (hfbs given; 0, 1M, 2M, 4M, 8M
+ * voxels), reps runs each on the batch's stream, keeps the fastest setting
+ * of each knob and leaves the results of one solve with it. */
+DTSGB_API int dtsgb_batch_autotune(dtsgb_batch_t b, const dtsgb_filter_params* filter,
+                                   const dtsgb_optimize_params* optimize,
+                                   float overwrite_target_above_conf,
+                                   const dtsgb_hfbs_params* hfbs, int reps);
+
+/* ---- Gradients of the batched DTS solve (new; the reference has no
+ * gradients).  With gradients enabled, dtsgb_batch_solve_dts also keeps the
+ * iterate v_k every `segment` iterations (0 = ceil(sqrt(num_iterations))),
+ * and dtsgb_batch_dts_backward maps an upstream gradient dL/dv of each DTS
+ * result to dL/dtarget and dL/dconfidence of the same solve.  The window
+ * bounds found from the guide are held fixed: they are piecewise constant in
+ * the guide, so the solve's derivative with respect to the guide's edge
+ * weights is zero almost everywhere.  The iterates between checkpoints are
+ * recomputed, so the solve holds ceil(N/segment) - 1 + segment + 4 planes of
+ * W*H floats per instance, not N.  L2 and Charbonnier; L1 and zero iterations
+ * return the target, so dL/dtarget = dL/dv.  A solve with the confidence
+ * overwrite in (0,1) returns DTSGB_ERR_UNSUPPORTED while gradients are on.
+ * For BF16 storage the derivative is taken at the BF16-rounded target and
+ * confidence.  grad_target / grad_confidence (n pointers, W*H floats) may be
+ * NULL or hold NULL entries to skip an output. */
+DTSGB_API int dtsgb_batch_enable_grad(dtsgb_batch_t b, int enable, int segment);
+/* segment length and planes held by the last solve (0, 0 before any). */
+DTSGB_API int dtsgb_batch_grad_info(dtsgb_batch_t b, int* segment, int* planes);
+DTSGB_API int dtsgb_batch_dts_backward(dtsgb_batch_t b, const float* const* grad_out,
+                                       float* const* grad_target,
+                                       float* const* grad_confidence);
+DTSGB_API int dtsgb_batch_dts_backward_device(dtsgb_batch_t b,
+                                              const float* const* grad_out,
+                                              float* const* grad_target,
+                                              float* const* grad_confidence);
 
 #ifdef __cplusplus
 }

@@ -212,6 +212,16 @@ EXPORT void ora_dts_init_frame(ora_dts* s, int color_space, const uint8_t* rgba,
   }
 }
 
+/* Target and confidence at the oracle's own precision (NULL keeps a plane);
+ * used by finite-difference checks, whose perturbations a float would round
+ * away. */
+EXPORT void ora_dts_set_target_conf(ora_dts* s, const REAL* target,
+                                    const REAL* confidence) {
+  const int64_t n = (int64_t)s->w * s->h;
+  if (target) memcpy(s->target, target, (size_t)n * sizeof(REAL));
+  if (confidence) memcpy(s->conf, confidence, (size_t)n * sizeof(REAL));
+}
+
 /* a2. dHdx / dVdy -- src/domain_transform_common_kernels.cuh:71-116 and
  * ComputeColorSpaceDifferential, src/domain_transform_filter.cu:92-110.
  * The backward neighbour of column 0 / row 0 is read through a surface with
@@ -668,12 +678,16 @@ static void box_transpose(const ora_dts* s, int axis, const REAL* gin,
   const int W = s->w, H = s->h;
   const size_t n = (size_t)W * H;
   for (size_t k = 0; k < n; ++k) gout[k] = 0;
-  for (int y = 0; y < H; ++y)
-    for (int x = 0; x < W; ++x) {
-      const size_t p = (size_t)y * W + x;
+  /* windows stay inside their row (axis 0) or column (axis 1): one thread
+   * per row / column, each scattering in a fixed order */
+  const int lines = axis == 0 ? H : W, len = axis == 0 ? W : H;
+#pragma omp parallel for schedule(static)
+  for (int li = 0; li < lines; ++li)
+    for (int j = 0; j < len; ++j) {
+      const size_t p = axis == 0 ? (size_t)li * W + j : (size_t)j * W + li;
       const REAL a = gin[p] / (REAL)(u[p] - l[p]);
       for (int q = l[p] + 1; q <= u[p]; ++q) {
-        const size_t k = axis == 0 ? (size_t)y * W + q : (size_t)q * W + x;
+        const size_t k = axis == 0 ? (size_t)li * W + q : (size_t)q * W + li;
         gout[k] += a;
       }
     }
@@ -698,6 +712,7 @@ EXPORT int ora_dts_backward(ora_dts* s, int num_iterations, int loss,
     const REAL* v = vs + n * it;
     REAL* vn = vs + n * (it + 1);
     ora_row_prefix(v, S, W, H);
+#pragma omp parallel for schedule(static)
     for (int y = 0; y < H; ++y)
       for (int x = 0; x < W; ++x) {
         const size_t k = (size_t)y * W + x;
@@ -708,6 +723,7 @@ EXPORT int ora_dts_backward(ora_dts* s, int num_iterations, int loss,
         tmp[k] = v[k] - st * (lam * (v[k] - B) + hg);
       }
     ora_col_prefix(tmp, S, W, H);
+#pragma omp parallel for schedule(static)
     for (int y = 0; y < H; ++y)
       for (int x = 0; x < W; ++x) {
         const size_t k = (size_t)y * W + x;
@@ -723,9 +739,11 @@ EXPORT int ora_dts_backward(ora_dts* s, int num_iterations, int loss,
     const REAL* v = vs + n * it;
     /* Y^T */
     box_transpose(s, 1, g, ly, uy, tmp);
+#pragma omp parallel for schedule(static)
     for (size_t k = 0; k < n; ++k) g1[k] = (1 - st * lam) * g[k] + st * lam * tmp[k];
     /* X^T */
     box_transpose(s, 0, g1, lx, ux, tmp);
+#pragma omp parallel for schedule(static)
     for (size_t k = 0; k < n; ++k) {
       const REAL nk = (REAL)(ux[k] - lx[k]);
       const REAL d = v[k] - s->target[k];

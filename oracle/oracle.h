@@ -9,7 +9,7 @@
  * PARITY UNPINNED: the reference ships no golden vectors and cannot be built
  * or run here (empty libcua/CUB submodules, no OpenCV/GTest, CUDA 8/9 era).
  * The restatement is anchored on the reference's source (file:line cited per
- * function) plus known-answer tests in tests/test_oracle_kat.py, and on one
+ * function) plus known-answer tests in tests/test_oracle.py, and on one
  * GPU-side pin: the colour-conversion expression compiled by nvcc.
  *
  * The same source is compiled twice:
@@ -61,6 +61,9 @@ int ora_dts_set_image_dim(ora_dts* s, int w, int h);
 void ora_dts_clear_all(ora_dts* s);
 void ora_dts_init_frame(ora_dts* s, int color_space, const uint8_t* rgba,
                         const float* target, const float* confidence);
+/* target / confidence at REAL precision (NULL keeps a plane) */
+void ora_dts_set_target_conf(ora_dts* s, const REAL* target,
+                             const REAL* confidence);
 void ora_dts_differential(ora_dts* s, float sigma_x, float sigma_y,
                           float sigma_r);
 void ora_dts_integrate(ora_dts* s);

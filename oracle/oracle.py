@@ -54,6 +54,7 @@ def lib(real: str = "f64") -> ctypes.CDLL:
             "ora_dts_set_image_dim": ([vp, i, i], i),
             "ora_dts_clear_all": ([vp], None),
             "ora_dts_init_frame": ([vp, i, vp, vp, vp], None),
+            "ora_dts_set_target_conf": ([vp, vp, vp], None),
             "ora_dts_differential": ([vp, f, f, f], None),
             "ora_dts_integrate": ([vp], None),
             "ora_dts_filter": ([vp, f, f, f, vp, vp, i], None),
@@ -139,6 +140,12 @@ class OracleDTS:
         t = None if target is None else np.ascontiguousarray(target, np.float32)
         c = None if conf is None else np.ascontiguousarray(conf, np.float32)
         self.L.ora_dts_init_frame(self.h, int(cs), _p(rgba), _p(t), _p(c))
+
+    def set_target_conf(self, target=None, conf=None):
+        """target / confidence at the oracle's precision (FP64 for "f64")."""
+        t = None if target is None else np.ascontiguousarray(target, self.dt)
+        c = None if conf is None else np.ascontiguousarray(conf, self.dt)
+        self.L.ora_dts_set_target_conf(self.h, _p(t), _p(c))
 
     def differential(self, sx, sy, sr):
         self.L.ora_dts_differential(self.h, sx, sy, sr)

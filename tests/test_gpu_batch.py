@@ -91,3 +91,39 @@ def test_batch_rejects_bad_arguments(gpu_ready):
     b = D.Batch([(16, 16)])
     with pytest.raises(D.DtsgbError):
         b.download(0)  # nothing solved yet
+
+
+def test_tuning_knobs_and_autotune(gpu_ready):
+    """HFBS grouping changes only the launch order: bitwise-identical grids.
+    The DTS tile shape changes the fixed-point scales of the window sums:
+    results agree to FP32 rounding.  The autotuner keeps a valid setting."""
+    import ctypes
+    D = gpu_ready
+    from domain_transform_solver_gb300 import workloads as W
+    insts = _instances()
+    b = D.Batch([(i.width, i.height) for i in insts])
+    b.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in insts], [i.target for i in insts],
+             [i.confidence for i in insts])
+    fp = D.DomainFilterParams(**W.CFG0_FILTER)
+    op = D.DomainOptimizeParams(**dict(W.CFG0_OPT, num_iterations=4))
+    hp = D.HFBSGridParams(**dict(W.CFG1_HFBS, optim_iter_max=8))
+    outs = {}
+    for tile in (64, 32):
+        for group in (0, 30000):
+            b.set_tuning(D.TUNE_DTS_TILE, tile)
+            b.set_tuning(D.TUNE_HFBS_GROUP_VOXELS, group)
+            assert b.get_tuning(D.TUNE_DTS_TILE) == tile
+            b.solve_dts(fp, op)
+            b.solve_hfbs(hp)
+            outs[(tile, group)] = (b.download(0), b.download(1))
+    ref_d, ref_h = outs[(64, 0)]
+    for (tile, group), (d, h) in outs.items():
+        for a, r in zip(h, ref_h):
+            assert np.array_equal(a, r, equal_nan=True)
+        for a, r, inst in zip(d, ref_d, insts):
+            assert np.abs(a - r).max() <= 1e-6 * max(P.target_range(inst.target), 1.0)
+    b.autotune(fp, op, hp, reps=1)
+    assert b.get_tuning(D.TUNE_DTS_TILE) in (64, 32)
+    assert b.get_tuning(D.TUNE_HFBS_GROUP_VOXELS) in (0, 1000000, 2000000, 4000000, 8000000)
+    for a, r in zip(b.download(1), ref_h):
+        assert np.array_equal(a, r, equal_nan=True)
