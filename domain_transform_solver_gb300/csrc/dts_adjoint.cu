@@ -73,6 +73,15 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   float* rtab = reinterpret_cast<float*>(smraw + L.rt);
   unsigned* smax = reinterpret_cast<unsigned*>(smraw + L.mx);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // per-instance bases: every offset below is a 32-bit pixel index
+  const float* gin_i = gin + in.off;
+  float* gout_i = gout + in.off;
+  const float* vk_i = vk + in.off;
+  const TS* tgt_i = tgt + in.off;
+  const TS* cnf_i = cnf + in.off;
+  const uint32_t* bnd_i = bnd + in.off;
+  float* gt_i = grad_t + in.off;
+  float* gc_i = grad_c + in.off;
   const int nrt = 2 * max(hx, hy) + 2;
   for (int i = tid; i < nrt; i += NT) rtab[i] = i ? __frcp_rn((float)i) : 0.f;
   for (int i = tid; i < (TH + 1) * SWc; i += NT) D[i] = 0u;
@@ -83,36 +92,32 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   const int lgx = ceil_log2(2 * hx + 1), lgy = ceil_log2(2 * hy + 1);
   // ---- Y^T: a2 = g2 / n_y over the tile + halo --------------------------------
   float m = 0.f;
-  const int nitems = SR * SWc;
-  for (int i0 = tid; i0 < nitems; i0 += 4 * NT) {
-    // four items' loads in flight before any is used
-    uint32_t bb[4];
-    float gg[4];
+  // one warp per row, lanes along the row (no index divisions), two rows of
+  // loads in flight
+  constexpr int NWp = NT / 32;
+  for (int r0 = warp; r0 < SR; r0 += 2 * NWp) {
+    for (int c0 = lane; c0 < SWc; c0 += 32) {
+      uint32_t bb[2];
+      float gg[2];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int i = i0 + j * NT;
-      bb[j] = 0u;
-      gg[j] = 0.f;
-      if (i < nitems) {
-        const int r = i / SWc, c = i - r * SWc;
-        const int x = gx0 + c, y = gy0 + r;
-        if ((unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H) {
-          const long long p = in.off + (long long)y * P + x;
-          bb[j] = __ldg(bnd + p);
-          gg[j] = __ldg(gin + p);
-        }
+      for (int u = 0; u < 2; ++u) {
+        const int r = r0 + u * NWp, x = gx0 + c0, y = gy0 + r;
+        const bool ok = r < SR && (unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H;
+        const int p = y * P + x;
+        bb[u] = ok ? __ldg(bnd_i + p) : 0u;
+        gg[u] = ok ? __ldg(gin_i + p) : 0.f;
       }
-    }
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int i = i0 + j * NT;
-      if (i >= nitems) break;
-      const uint16_t b16 = (uint16_t)(bb[j] >> 16);
-      const int n = min((int)(b16 & 0xff), hy + 1) + min((int)(b16 >> 8), hy);
-      const float a = b16 ? gg[j] * rtab[n] : 0.f;
-      S2[i] = a;
-      By[i] = b16;
-      m = fmaxf(m, fabsf(a));
+      for (int u = 0; u < 2; ++u) {
+        const int r = r0 + u * NWp;
+        if (r >= SR) break;
+        const uint16_t b16 = (uint16_t)(bb[u] >> 16);
+        const int n = min((int)(b16 & 0xff), hy + 1) + min((int)(b16 >> 8), hy);
+        const float a = b16 ? gg[u] * rtab[n] : 0.f;
+        S2[r * SWc + c0] = a;
+        By[r * SWc + c0] = b16;
+        m = fmaxf(m, fabsf(a));
+      }
     }
   }
   m = warp_max_nonneg(m);
@@ -121,16 +126,18 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   {
     const int F = fx_shift(__uint_as_float(*smax), lgy);
     const float sF = pow2f(F);
-    for (int i = tid; i < SR * SWc; i += NT) {
-      const uint16_t b16 = By[i];
-      if (!b16) continue;  // outside the image (a window always holds its pixel)
-      const int r = i / SWc, c = i - r * SWc;
-      const int dl = min((int)(b16 & 0xff), hy + 1), du = min((int)(b16 >> 8), hy);
-      const int lo = max(r - hy - dl + 1, 0), hi = min(r - hy + du, TH - 1);
-      if (lo > hi) continue;
-      const unsigned A = fx_from(S2[i], sF);
-      atomicAdd(D + lo * SWc + c, A);
-      atomicAdd(D + (hi + 1) * SWc + c, 0u - A);
+    for (int r = warp; r < SR; r += NWp) {
+      for (int c = lane; c < SWc; c += 32) {
+        const int i = r * SWc + c;
+        const uint16_t b16 = By[i];
+        if (!b16) continue;  // outside the image (a window always holds its pixel)
+        const int dl = min((int)(b16 & 0xff), hy + 1), du = min((int)(b16 >> 8), hy);
+        const int lo = max(r - hy - dl + 1, 0), hi = min(r - hy + du, TH - 1);
+        if (lo > hi) continue;
+        const unsigned A = fx_from(S2[i], sF);
+        atomicAdd(D + lo * SWc + c, A);
+        atomicAdd(D + (hi + 1) * SWc + c, 0u - A);
+      }
     }
     __syncthreads();
     // column prefix over the tile rows, in segments
@@ -159,8 +166,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int y = t.y0 + k + j;
-          gv[j] = (k + j < k1 && xok && y < H) ? __ldg(gin + in.off + (long long)y * P + x)
-                                               : 0.f;
+          gv[j] = (k + j < k1 && xok && y < H) ? __ldg(gin_i + y * P + x) : 0.f;
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -187,24 +193,22 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
     float v[CPL], tv[CPL], cv[CPL], gt[CPL], gc[CPL];  // tile columns lane + 32k
   };
   auto fetch = [&](int rr, RowAdj& R) {
-    const long long row = in.off + (long long)(t.y0 + rr) * P;
+    const int row = (t.y0 + rr) * P;
 #pragma unroll
     for (int j = 0; j < BPL; ++j) {
       const int c = lane + 32 * j, x = gx0 + c;
-      R.bh[j] = (c < SWc && (unsigned)x < (unsigned)W) ? __ldg(bnd + row + x) : 0u;
+      R.bh[j] = (c < SWc && (unsigned)x < (unsigned)W) ? __ldg(bnd_i + row + x) : 0u;
     }
 #pragma unroll
     for (int k = 0; k < CPL; ++k) {
       const int x = t.x0 + lane + 32 * k;
-      R.v[k] = R.tv[k] = R.cv[k] = R.gt[k] = R.gc[k] = 0.f;
-      if (x < W) {
-        const long long p = row + x;
-        R.v[k] = __ldg(vk + p);
-        R.tv[k] = load_f(tgt + p);
-        R.cv[k] = load_f(cnf + p);
-        R.gt[k] = grad_t[p];
-        R.gc[k] = grad_c[p];
-      }
+      const bool ok = x < W;
+      const int p = row + x;
+      R.v[k] = ok ? __ldg(vk_i + p) : 0.f;
+      R.tv[k] = ok ? load_f(tgt_i + p) : 0.f;
+      R.cv[k] = ok ? load_f(cnf_i + p) : 0.f;
+      R.gt[k] = ok ? gt_i[p] : 0.f;
+      R.gc[k] = ok ? gc_i[p] : 0.f;
     }
   };
   const int rows = min(TH, H - t.y0);
@@ -213,7 +217,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   if (warp < rows) fetch(warp, cur);
   for (int rr = warp; rr < rows; rr += NW) {
     if (rr + NW < rows) fetch(rr + NW, nxt);
-    const long long row = in.off + (long long)(t.y0 + rr) * P;
+    const int row = (t.y0 + rr) * P;
     const float* g1r = S2 + rr * SWc;
     // visit(b, c) for the window columns c of this lane: the first BPL from
     // the prefetched registers, any further ones (halos above 32) reloaded
@@ -225,7 +229,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
       }
       for (int c = lane + 32 * BPL; c < SWc; c += 32) {
         const int x = gx0 + c;
-        if ((unsigned)x < (unsigned)W) visit(__ldg(bnd + row + x), c);
+        if ((unsigned)x < (unsigned)W) visit(__ldg(bnd_i + row + x), c);
       }
     };
     for (int k = lane; k <= TW; k += 32) xb[k] = 0u;
@@ -255,10 +259,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
       carry = __shfl_sync(0xffffffffu, incl, 31);
       const int x = t.x0 + cc;
       if (x >= W) continue;
-      const long long p = row + x;
+      const int p = row + x;
       const float bt = fx_window(incl, 0u, isF);
       const float g1 = g1r[hx + cc];
-      const uint32_t b = __ldg(bnd + p);
+      const uint32_t b = __ldg(bnd_i + p);
       const float rn = rtab[min((int)(b & 0xff), hx + 1) + min((int)((b >> 8) & 0xff), hx)];
       const float v = cur.v[k], tv = cur.tv[k], cv = cur.cv[k];
       const float d = v - tv;
@@ -271,9 +275,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
         dh_dv = __fdiv_rn(0.5f * (cv * rn) * 1e-6f, rt * rt * rt);
         dh_dc = __fdiv_rn(0.5f * d * rn, rt);
       }
-      gout[p] = __fmaf_rn(1.f - slam - step * dh_dv, g1, slam * bt);
-      grad_t[p] = cur.gt[k] + step * dh_dv * g1;
-      grad_c[p] = cur.gc[k] - step * dh_dc * g1;
+      gout_i[p] = __fmaf_rn(1.f - slam - step * dh_dv, g1, slam * bt);
+      gt_i[p] = cur.gt[k] + step * dh_dv * g1;
+      gc_i[p] = cur.gc[k] - step * dh_dc * g1;
     }
     __syncwarp();  // the warp's buffer is cleared for its next row
     cur = nxt;

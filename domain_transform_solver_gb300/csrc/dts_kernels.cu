@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kThreads)
 
 // ---------------------------------------------------------------------------
 // One solver iteration (a6/a7): the X half-step followed by the Y half-step
-// in one kernel (k_dts_iter_prefix below).  A CTA owns a TWxTH output tile;
+// in one kernel (k_dts_iter_tile below).  A CTA owns a TWxTH output tile;
 // the X half-step is evaluated for the tile columns over the tile rows plus
 // a vertical halo of floor(sigma) (those rows feed the Y windows), kept in
 // shared memory, and the Y half-step writes the tile.  HBM traffic per pixel
@@ -194,163 +194,257 @@ __device__ __forceinline__ float photometric(const StereoArgs& sa, long long row
 // ---------------------------------------------------------------------------
 // Fused X+Y iteration with window sums from fixed-point prefix sums
 // (fixed_point.cuh): a window sum is P[p+du] - P[p-dl] of a wrapping 32-bit
-// integer prefix, exact for the converted values; the scale comes from the
-// largest magnitude in the row (X) or among the tile's X results (Y).
+// integer prefix, exact for the converted values.
 //
-// X half-step: one warp per row of the tile plus the vertical halo; each
-// lane scans four consecutive values, a warp shuffle scan joins the lanes,
-// and the row's prefix sits in a per-warp shared buffer.  A warp issues the
-// global loads of its next row before working on the current one.  Y
-// half-step: the X results stay in shared memory; each thread scans a
-// segment of one column, segment offsets are added in a second pass, and
-// the tile's output rows are written coalesced.  Reciprocals 1/n come from
-// a per-block table of correctly rounded values.
+// Phases of one CTA (TW x TH tile, halos hx, hy; SR = TH + 2hy rows):
+//  1. stage the iterate over SR rows x (TW + 2hx + 1) prefix entries
+//     (entry 0 is a zero left of every window) into shared memory, with
+//     coalesced loads, and reduce its largest magnitude (the X scale);
+//  2. convert in place and scan: one thread per 16-entry segment of a row,
+//     then segment offsets are added;
+//  3. X half-step for the tile columns over all SR rows (one thread per
+//     pixel, independent loads of bounds, target, confidence, iterate),
+//     results kept in shared memory with their largest magnitude (the Y
+//     scale);
+//  4. Y prefix per column in segments, offsets added;
+//  5. Y half-step for the tile, written coalesced.
+// Reciprocals 1/n come from a per-block table of correctly rounded values.
 // ---------------------------------------------------------------------------
+constexpr int kXSeg = 16;  // prefix entries per thread in the X scan
+
 template <int TW, int TH, int NT>
-struct PrefixIterSmem {
-  // bytes of shared memory for halos hx, hy
-  static size_t bytes(int hx, int hy) {
-    const size_t SR = TH + 2 * hy, SWX = TW + 2 * hx + 1;
-    const size_t py = std::max((SR + 1) * TW, (size_t)(NT / 32) * SWX) * 4;
-    const size_t seg = (size_t)(NT / TW) * TW * 4;
-    const size_t sx = SR * (TW + 1) * 4;
-    const size_t sby = (size_t)TH * TW * 2;
-    const size_t rt = (size_t)(2 * std::max(hx, hy) + 2) * 4;
-    return py + seg + sx + sby + rt + 16;
+struct TileIterSmem {
+  int swxp, nsx, pyn, xs_off, sx_off, sby_off, segy_off, rt_off, mx_off, total;
+  __host__ __device__ TileIterSmem(int hx, int hy) {
+    const int SR = TH + 2 * hy, SWX = TW + 2 * hx + 1;
+    swxp = (SWX + 3) & ~3;
+    nsx = (swxp + kXSeg - 1) / kXSeg;
+    pyn = max(SR * swxp, (SR + 1) * TW);  // X prefix, later the Y prefix
+    xs_off = pyn * 4;                                   // X segment totals
+    sx_off = xs_off + SR * nsx * 4;                     // SR x (TW+1) f32
+    sby_off = sx_off + SR * (TW + 1) * 4;               // SR x TW u16
+    segy_off = (sby_off + SR * TW * 2 + 3) & ~3;        // NT/TW x TW u32
+    rt_off = segy_off + (NT / TW) * TW * 4;             // reciprocal table
+    mx_off = rt_off + (2 * max(hx, hy) + 2) * 4;
+    total = mx_off + 16;
   }
 };
 
+// v = t where c > overwrite, in place (DomainTransformSolver::Optimize's
+// overwrite before the X half-step, src/domain_transform_solver.cu:126-130).
+template <typename TS>
+__global__ void k_overwrite(const Inst* __restrict__ insts, float* __restrict__ v,
+                            const TS* __restrict__ tgt, const TS* __restrict__ cnf,
+                            float overwrite) {
+  const Inst in = insts[blockIdx.y];
+  const long long n = (long long)in.pitch * in.h;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    if (load_f(cnf + in.off + i) > overwrite) v[in.off + i] = load_f(tgt + in.off + i);
+}
+
 template <typename TS, int MODE, int TW, int TH, int NT, bool STEREO = false>
 __global__ void __launch_bounds__(NT, 1024 / NT)
-    k_dts_iter_prefix(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
-                      const float* __restrict__ vin, float* __restrict__ vout,
-                      const TS* __restrict__ tgt, const TS* __restrict__ cnf,
-                      const uint32_t* __restrict__ bnd, float lambda, float step,
-                      float overwrite, int hx, int hy, StereoArgs sa) {
+    k_dts_iter_tile(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
+                    const float* __restrict__ vin, float* __restrict__ vout,
+                    const TS* __restrict__ tgt, const TS* __restrict__ cnf,
+                    const uint32_t* __restrict__ bnd, float lambda, float step,
+                    float overwrite, int hx, int hy, StereoArgs sa, TileIterSmem<TW, TH, NT> L) {
   static_assert(TW % 32 == 0 && NT % TW == 0, "tile width: whole warps");
-  constexpr int NW = NT / 32, NSEG = NT / TW, TWp = TW + 1;
+  constexpr int NSEG = NT / TW, TWp = TW + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   const Tile t = tiles[blockIdx.x];
   const Inst in = insts[t.inst];
   const int W = in.w, H = in.h, P = in.pitch;
+  // per-instance bases: every offset below is a 32-bit pixel index
+  const float* vin_i = vin + in.off;
+  float* vout_i = vout + in.off;
+  const TS* tgt_i = tgt + in.off;
+  const TS* cnf_i = cnf + in.off;
+  const uint32_t* bnd_i = bnd + in.off;
   const int SR = TH + 2 * hy, SWX = TW + 2 * hx + 1, RY = SR + 1;
-  const int pyn = max(RY * TW, NW * SWX);
-  unsigned* Py = reinterpret_cast<unsigned*>(smraw);  // RY x TW (Y phase)
-  unsigned* Xb = Py;                                  // NW x SWX (X phase)
-  unsigned* segtot = Py + pyn;                        // NSEG x TW
-  float* sx = reinterpret_cast<float*>(segtot + NSEG * TW);   // SR x TWp
-  uint16_t* sby = reinterpret_cast<uint16_t*>(sx + SR * TWp);  // TH x TW
-  float* rtab = reinterpret_cast<float*>(sby + TH * TW);
+  const int SWXp = L.swxp, NSX = L.nsx;
+  unsigned* XP = reinterpret_cast<unsigned*>(smraw);           // SR x SWXp
+  unsigned* Py = XP;                                           // RY x TW (phase 4)
+  unsigned* segx = reinterpret_cast<unsigned*>(smraw + L.xs_off);  // SR x NSX
+  float* sx = reinterpret_cast<float*>(smraw + L.sx_off);      // SR x TWp
+  uint16_t* sby = reinterpret_cast<uint16_t*>(smraw + L.sby_off);  // SR x TW
+  unsigned* segy = reinterpret_cast<unsigned*>(smraw + L.segy_off);
+  float* rtab = reinterpret_cast<float*>(smraw + L.rt_off);
+  unsigned* smax = reinterpret_cast<unsigned*>(smraw + L.mx_off);  // [0] X, [1] Y
+  const int tid = threadIdx.x, lane = tid & 31;
   const int nrt = 2 * max(hx, hy) + 2;
-  unsigned* smax = reinterpret_cast<unsigned*>(rtab + nrt);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int i = tid; i < nrt; i += NT) rtab[i] = i ? __frcp_rn((float)i) : 0.f;
-  if (tid == 0) *smax = 0u;
+  if (tid < 2) smax[tid] = 0u;
   __syncthreads();
-  const bool over = overwrite > 0.f && overwrite < 1.f;
+  const bool over = overwrite > 0.f && overwrite < 1.f;  // v itself is already
+                                                          // overwritten
   const int gx0 = t.x0 - hx - 1;  // image x of X prefix entry 0 (a zero entry)
-  const int gy0 = t.y0 - hy;      // image y of sx row 0
+  const int gy0 = t.y0 - hy;      // image y of row 0
   const int lgx = ceil_log2(2 * hx + 1), lgy = ceil_log2(2 * hy + 1);
-  // ---- X half-step ----------------------------------------------------------
-  constexpr int CPL = TW / 32;  // tile columns per lane
-  struct RowIn {
-    float v4[4];  // prefix entries 4*lane .. 4*lane+3
-    uint32_t b[CPL];  // tile columns lane + 32k
-    float tv[CPL], cv[CPL], vc[CPL];
+  // ---- 3'. the X half-step's per-pixel loads, issued early -----------------------
+  // Thread (c, r0) handles tile column c of rows r0, r0 + RS, ...; two rows per
+  // pass.  The first pass's loads are issued before the staging so that their
+  // latency overlaps phases 1-2; each later pass is loaded while the previous
+  // one is computed.
+  constexpr int RS = NT / TW;  // rows per pass step
+  const int c3 = tid % TW, r03 = tid / TW;
+  const int x3 = t.x0 + c3;
+  const bool xok3 = x3 < W;
+  struct Pass {
+    uint32_t b[2];
+    float tv[2], cv[2], vv[2];
   };
-  auto load_v = [&](bool yok, long long row, int cc) -> float {  // prefix entry cc
-    const int x = gx0 + cc;
-    if (cc < 1 || cc >= SWX || !yok || (unsigned)x >= (unsigned)W) return 0.f;
-    float v = __ldg(vin + row + x);
-    if (over && load_f(cnf + row + x) > overwrite) v = load_f(tgt + row + x);
-    return v;
-  };
-  auto fetch = [&](int r, RowIn& R) {
-    const int y = gy0 + r;
-    const bool yok = (unsigned)y < (unsigned)H;
-    const long long row = in.off + (long long)y * P;
+  auto fetch = [&](int r0, Pass& Q) {
 #pragma unroll
-    for (int j = 0; j < 4; ++j) R.v4[j] = load_v(yok, row, 4 * lane + j);
-#pragma unroll
-    for (int k = 0; k < CPL; ++k) {
-      const int x = t.x0 + lane + 32 * k;
-      R.b[k] = 0u;
-      R.tv[k] = R.cv[k] = R.vc[k] = 0.f;
-      if (yok && x < W) {
-        const long long p = row + x;
-        R.b[k] = __ldg(bnd + p);
-        R.tv[k] = load_f(tgt + p);
-        R.cv[k] = load_f(cnf + p);
-        R.vc[k] = __ldg(vin + p);
-      }
+    for (int u = 0; u < 2; ++u) {
+      const int r = r0 + u * RS, y = gy0 + r;
+      const bool ok = r < SR && xok3 && (unsigned)y < (unsigned)H;
+      const int p = y * P + x3;
+      Q.b[u] = ok ? __ldg(bnd_i + p) : 0u;
+      Q.tv[u] = ok ? load_f(tgt_i + p) : 0.f;
+      Q.cv[u] = ok ? load_f(cnf_i + p) : 0.f;
+      Q.vv[u] = ok ? __ldg(vin_i + p) : 0.f;
     }
   };
-  float mloc = 0.f;
-  unsigned* xb = Xb + warp * SWX;
-  RowIn cur, nxt;
-  if (warp < SR) fetch(warp, cur);
-  for (int r = warp; r < SR; r += NW) {
-    if (r + NW < SR) fetch(r + NW, nxt);
-    const int y = gy0 + r;
-    const bool yok = (unsigned)y < (unsigned)H;
-    const long long row = in.off + (long long)y * P;
-    float m = fmaxf(fmaxf(fabsf(cur.v4[0]), fabsf(cur.v4[1])),
-                    fmaxf(fabsf(cur.v4[2]), fabsf(cur.v4[3])));
-    for (int base = 128; base < SWX; base += 128)
+  Pass QA, QB;
+  fetch(r03, QA);
+  // ---- 1. stage the iterate: one warp per row, three rows in flight -----------
+  float m = 0.f;
+  {
+    const int warp = tid >> 5;
+    constexpr int NW = NT / 32;
+    for (int r0 = warp; r0 < SR; r0 += 2 * NW) {
+      float vals[2][3];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) m = fmaxf(m, fabsf(load_v(yok, row, base + 4 * lane + j)));
-    const int F = fx_shift(warp_max_nonneg(m), lgx);
-    const float sF = pow2f(F), isF = pow2f(-F);
-    unsigned carry = 0;
-    for (int base = 0; base < SWX; base += 128) {
-      unsigned s4[4];
+      for (int u = 0; u < 2; ++u) {
+        const int r = r0 + u * NW, y = gy0 + r;
+        const bool yok = r < SR && (unsigned)y < (unsigned)H;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float v = base == 0 ? cur.v4[j] : load_v(yok, row, base + 4 * lane + j);
-        s4[j] = fx_from(v, sF) + (j ? s4[j - 1] : 0u);
+        for (int k = 0; k < 3; ++k) {
+          const int cc = lane + 32 * k, x = gx0 + cc;
+          vals[u][k] = (yok && cc >= 1 && cc < SWX && (unsigned)x < (unsigned)W)
+                           ? __ldg(vin_i + y * P + x)
+                           : 0.f;
+        }
       }
-      const unsigned incl = warp_incl_scan(s4[3], lane);
-      const unsigned off = carry + incl - s4[3];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int cc = base + 4 * lane + j;
-        if (cc < SWX) xb[cc] = off + s4[j];
+      for (int u = 0; u < 2; ++u) {
+        const int r = r0 + u * NW;
+        if (r >= SR) break;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const int cc = lane + 32 * k;
+          if (cc < SWXp) XP[r * SWXp + cc] = __float_as_uint(vals[u][k]);
+          m = fmaxf(m, fabsf(vals[u][k]));
+        }
+        // rows wider than 96 entries (halos above 15)
+        for (int cc = lane + 96; cc < SWXp; cc += 32) {
+          const int x = gx0 + cc, y = gy0 + r;
+          const float v = (cc < SWX && (unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H)
+                              ? __ldg(vin_i + y * P + x)
+                              : 0.f;
+          XP[r * SWXp + cc] = __float_as_uint(v);
+          m = fmaxf(m, fabsf(v));
+        }
       }
-      carry += __shfl_sync(0xffffffffu, incl, 31);
     }
-    __syncwarp();
-#pragma unroll
-    for (int k = 0; k < CPL; ++k) {
-      const int c = lane + 32 * k;
-      const int x = t.x0 + c;
-      float o = 0.f;
-      if (yok && x < W) {
-        const uint32_t b = cur.b[k];
-        const float tv = cur.tv[k], cv = cur.cv[k];
-        float v = cur.vc[k];
-        if (over && cv > overwrite) v = tv;
-        const int dl = min((int)(b & 0xff), hx + 1);
-        const int du = min((int)((b >> 8) & 0xff), hx);
-        const float rn = rtab[dl + du];
-        const int i = c + hx + 1;
-        const float B = fx_window(xb[i + du], xb[i - dl], rn * isF);
-        float extra = 0.f;
-        if (STEREO) extra = photometric(sa, row, x, W, v);
-        o = x_update<MODE, STEREO>(v, B, tv, cv, rn, lambda, step, extra);
-        if (over && cv > overwrite) o = tv;
-        if (r >= hy && r < hy + TH) sby[(r - hy) * TW + c] = (uint16_t)(b >> 16);
-      }
-      sx[r * TWp + c] = o;
-      mloc = fmaxf(mloc, fabsf(o));
-    }
-    __syncwarp();  // the warp's prefix buffer is rewritten for its next row
-    cur = nxt;
   }
-  mloc = warp_max_nonneg(mloc);
-  if (lane == 0) atomicMax(smax, __float_as_uint(mloc));
+  m = warp_max_nonneg(m);
+  if (lane == 0) atomicMax(&smax[0], __float_as_uint(m));
   __syncthreads();
-  // ---- Y half-step ----------------------------------------------------------
-  const int Fy = fx_shift(__uint_as_float(*smax), lgy);
+  // ---- 2. X prefix: scan 16-entry segments, then add segment offsets ----------
+  {
+    const int F = fx_shift(__uint_as_float(smax[0]), lgx);
+    const float sF = pow2f(F);
+    for (int i = tid; i < SR * NSX; i += NT) {
+      const int sg = i / SR, r = i - sg * SR;  // lanes on rows: conflict-free
+      unsigned* e = XP + r * SWXp + sg * kXSeg;
+      const int n = min(kXSeg, SWXp - sg * kXSeg);
+      unsigned acc = 0u;
+      if (n == kXSeg) {
+#pragma unroll
+        for (int q = 0; q < kXSeg; q += 4) {
+          uint4 w = *reinterpret_cast<uint4*>(e + q);
+          acc += fx_from(__uint_as_float(w.x), sF); w.x = acc;
+          acc += fx_from(__uint_as_float(w.y), sF); w.y = acc;
+          acc += fx_from(__uint_as_float(w.z), sF); w.z = acc;
+          acc += fx_from(__uint_as_float(w.w), sF); w.w = acc;
+          *reinterpret_cast<uint4*>(e + q) = w;
+        }
+      } else {
+        for (int q = 0; q < n; ++q) {
+          acc += fx_from(__uint_as_float(e[q]), sF);
+          e[q] = acc;
+        }
+      }
+      segx[r * NSX + sg] = acc;
+    }
+    __syncthreads();
+    for (int i = tid; i < SR * NSX; i += NT) {
+      const int sg = i / SR, r = i - sg * SR;  // lanes on rows: conflict-free
+      if (sg == 0) continue;
+      unsigned off = 0u;
+      for (int s2 = 0; s2 < sg; ++s2) off += segx[r * NSX + s2];
+      unsigned* e = XP + r * SWXp + sg * kXSeg;
+      const int n = min(kXSeg, SWXp - sg * kXSeg);
+      if (n == kXSeg) {
+#pragma unroll
+        for (int q = 0; q < kXSeg; q += 4) {
+          uint4 w = *reinterpret_cast<uint4*>(e + q);
+          w.x += off; w.y += off; w.z += off; w.w += off;
+          *reinterpret_cast<uint4*>(e + q) = w;
+        }
+      } else {
+        for (int q = 0; q < n; ++q) e[q] += off;
+      }
+    }
+    __syncthreads();
+  }
+  // ---- 3. X half-step for the tile columns over all rows -----------------------
+  {
+    const int F = fx_shift(__uint_as_float(smax[0]), lgx);
+    const float isF = pow2f(-F);
+    float mloc = 0.f;
+    auto compute = [&](int r0, const Pass& Q) {
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int r = r0 + u * RS;
+        if (r >= SR) break;
+        float o = 0.f;
+        const uint32_t b = Q.b[u];
+        if (b) {  // inside the image (a window always holds its own pixel)
+          const int dl = min((int)(b & 0xff), hx + 1);
+          const int du = min((int)((b >> 8) & 0xff), hx);
+          const float rn = rtab[dl + du];
+          const unsigned* e = XP + r * SWXp + c3 + hx + 1;
+          const float B = fx_window(e[du], e[-dl], rn * isF);
+          float extra = 0.f;
+          if (STEREO) extra = photometric(sa, in.off + (gy0 + r) * P, x3, W, Q.vv[u]);
+          o = x_update<MODE, STEREO>(Q.vv[u], B, Q.tv[u], Q.cv[u], rn, lambda, step, extra);
+          if (over && Q.cv[u] > overwrite) o = Q.tv[u];
+        }
+        sx[r * TWp + c3] = o;
+        sby[r * TW + c3] = (uint16_t)(b >> 16);
+        mloc = fmaxf(mloc, fabsf(o));
+      }
+    };
+    int r0 = r03;
+    while (r0 < SR) {
+      if (r0 + 2 * RS < SR) fetch(r0 + 2 * RS, QB);
+      compute(r0, QA);
+      r0 += 2 * RS;
+      if (r0 >= SR) break;
+      if (r0 + 2 * RS < SR) fetch(r0 + 2 * RS, QA);
+      compute(r0, QB);
+      r0 += 2 * RS;
+    }
+    mloc = warp_max_nonneg(mloc);
+    if (lane == 0) atomicMax(&smax[1], __float_as_uint(mloc));
+  }
+  __syncthreads();
+  // ---- 4. Y prefix per column in segments ---------------------------------------
+  const int Fy = fx_shift(__uint_as_float(smax[1]), lgy);
   const float sFy = pow2f(Fy), isFy = pow2f(-Fy);
   const int c = tid % TW, sgi = tid / TW;
   const int seg = (RY + NSEG - 1) / NSEG;
@@ -360,24 +454,25 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
     if (k > 0) acc += fx_from(sx[(k - 1) * TWp + c], sFy);
     Py[k * TW + c] = acc;
   }
-  segtot[sgi * TW + c] = acc;
+  segy[sgi * TW + c] = acc;
   __syncthreads();
   unsigned off = 0;
-  for (int s2 = 0; s2 < sgi; ++s2) off += segtot[s2 * TW + c];
+  for (int s2 = 0; s2 < sgi; ++s2) off += segy[s2 * TW + c];
   for (int k = k0; k < k1; ++k) Py[k * TW + c] += off;
   __syncthreads();
+  // ---- 5. Y half-step, written coalesced ----------------------------------------
   const float slam = step * lambda;
   const int x = t.x0 + c;
-  for (int j = sgi; j < TH; j += NSEG) {
-    const int y = t.y0 + j;
-    if (y >= H || x >= W) continue;
-    const uint32_t b = sby[j * TW + c];
+  if (x >= W) return;
+  const int jmax = min(TH, H - t.y0);
+  for (int j = sgi; j < jmax; j += NSEG) {
+    const uint32_t b = sby[(j + hy) * TW + c];
     const int dl = min((int)(b & 0xff), hy + 1), du = min((int)(b >> 8), hy);
     const int k = j + hy + 1;
-    const float B = fx_window(Py[(k + du) * TW + c], Py[(k - dl) * TW + c],
-                              rtab[dl + du] * isFy);
+    const float Bv = fx_window(Py[(k + du) * TW + c], Py[(k - dl) * TW + c],
+                               rtab[dl + du] * isFy);
     const float v = sx[(j + hy) * TWp + c];
-    vout[in.off + (long long)y * P + x] = __fmaf_rn(-slam, v - B, v);
+    vout_i[(t.y0 + j) * P + x] = __fmaf_rn(-slam, v - Bv, v);
   }
 }
 
@@ -626,14 +721,21 @@ static int launch_iter_shape(const DtsLaunch& L, const float* vin, float* vout,
                              float overwrite, int hx, int hy, cudaStream_t s,
                              const StereoArgs& sa) {
   constexpr int NT = TW >= 64 ? 512 : 256;
-  const size_t smem = PrefixIterSmem<TW, TH, NT>::bytes(hx, hy);
+  const TileIterSmem<TW, TH, NT> lay(hx, hy);
+  const size_t smem = (size_t)lay.total;
   if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "sigma_z too large");
-  int st = set_smem(k_dts_iter_prefix<TS, MODE, TW, TH, NT, STEREO>, smem);
+  if (overwrite > 0.f && overwrite < 1.f) {
+    // the input iterate is overwritten in place, as the reference does
+    k_overwrite<TS><<<dim3(64, L.n_inst), kThreads, 0, s>>>(
+        L.d_inst, const_cast<float*>(vin), (const TS*)target, (const TS*)conf, overwrite);
+    DTSGB_CUDA(cudaGetLastError());
+  }
+  int st = set_smem(k_dts_iter_tile<TS, MODE, TW, TH, NT, STEREO>, smem);
   if (st) return st;
   ProfScope ps(s, DTSGB_K_DTS_ITER);
-  k_dts_iter_prefix<TS, MODE, TW, TH, NT, STEREO><<<L.n_tiles, NT, smem, s>>>(
+  k_dts_iter_tile<TS, MODE, TW, TH, NT, STEREO><<<L.n_tiles, NT, smem, s>>>(
       L.d_inst, L.d_tiles, vin, vout, (const TS*)target, (const TS*)conf,
-      bounds, lambda, step, overwrite, hx, hy, sa);
+      bounds, lambda, step, overwrite, hx, hy, sa, lay);
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
 }

@@ -858,6 +858,7 @@ DTSGB_API int dtsgb_hfbs_optimize(dtsgb_hfbs_t h) {
                              cudaMemcpyHostToDevice, h->stream));
   HfbsBatch B{};
   B.d_inst = h->d_inst;
+  B.h_inst = &I;
   B.n_inst = 1;
   B.max_voxels = (long long)I.gx * I.gy * I.gl;
   B.max_pixels = (long long)I.w * I.h;

@@ -111,48 +111,53 @@ __global__ void k_bistoch(const HInst* __restrict__ insts,
   const float* cn = count + I.grid_off;
   float* d = dst + I.grid_off;
   const int sy = gx, sz = gx * gy;
-  // one warp per grid row (fixed y, l); lanes stride along x
-  const int lane = threadIdx.x & 31;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < gy * gl;
-       row += nwarps) {
-    const int z = row / gy, y = row - z * gy;
-    const int base = row * gx;
-    // four x positions per lane per pass: all their loads are issued before
-    // any result is computed
-    for (int x0 = lane; x0 < gx; x0 += 128) {
-      float v[4], nb[4], cc[4];
+  // one thread per (x, y) column, marching along l: the l-neighbours come
+  // from registers, and the loads of level l+1 are issued before level l is
+  // computed
+  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < sz;
+       col += gridDim.x * blockDim.x) {
+    const int y = col / gx, x = col - y * gx;
+    const bool xm = x > 0, xp = x + 1 < gx, ym = y > 0, yp = y + 1 < gy;
+    auto nb4 = [&](int i, float (&o)[5]) {  // x-1, x+1, y-1, y+1, count
+      o[0] = xm ? s[i - 1] : 0.f;
+      o[1] = xp ? s[i + 1] : px;
+      o[2] = ym ? s[i - sy] : 0.f;
+      o[3] = yp ? s[i + sy] : py;
+      o[4] = cn[i];
+    };
+    float vprev = 0.f, vcur = s[col];
+    float cur[5], nxt[5];
+    nb4(col, cur);
+    for (int l = 0; l < gl; ++l) {
+      const int i = l * sz + col;
+      const bool more = l + 1 < gl;
+      const float vnext = more ? s[i + sz] : pz;
+      if (more) nb4(i + sz, nxt);
+      float a = cur[0];
+      a += cur[1];
+      a += cur[2];
+      a += cur[3];
+      a += l > 0 ? vprev : 0.f;
+      a += vnext;
+      const float blurred = 2.f * vcur + a;
+      d[i] = __fsqrt_rn(__fdiv_rn(vcur * (cur[4] + 0.00001f), blurred + 0.00001f));
+      vprev = vcur;
+      vcur = vnext;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int x = x0 + 32 * j;
-        v[j] = nb[j] = cc[j] = 0.f;
-        if (x < gx) {
-          const int i = base + x;
-          v[j] = s[i];
-          float a = x > 0 ? s[i - 1] : 0.f;
-          a += x + 1 < gx ? s[i + 1] : px;
-          a += y > 0 ? s[i - sy] : 0.f;
-          a += y + 1 < gy ? s[i + sy] : py;
-          a += z > 0 ? s[i - sz] : 0.f;
-          a += z + 1 < gl ? s[i + sz] : pz;
-          nb[j] = a;
-          cc[j] = cn[i];
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int x = x0 + 32 * j;
-        if (x >= gx) break;
-        const float blurred = 2.f * v[j] + nb[j];
-        d[base + x] =
-            __fsqrt_rn(__fdiv_rn(v[j] * (cc[j] + 0.00001f), blurred + 0.00001f));
-      }
+      for (int k = 0; k < 5; ++k) cur[k] = nxt[k];
     }
   }
 }
 
 // a14: CalcInvDiagA (src/hfbs.cu:159-195):
-// invA = 1 / max(1e-3, lambda*(count - 2 n^2) + sum c).
+// invA = 1 / max(1e-3, lambda*(count - 2 n^2) + sum c), evaluated by the
+// reference in double and stored as float.  For a float d, rounding 1/d to
+// double and then to float gives the correctly rounded float reciprocal (a
+// product of a 24-bit and a 25-bit significand cannot come within 2^-53 of 1
+// without equalling it, so 1/d never lands within a double ulp of a float
+// midpoint), so the FP64 division is replaced by __frcp_rn.  d >= 1e-3f is
+// the float form of (double)d > 1e-3, and 1/1e-3 rounds to 1000 (NaN too,
+// as fmax returns the other operand).
 __global__ void k_inv_diag(const HInst* __restrict__ insts,
                            const float* __restrict__ count,
                            const float* __restrict__ csum,
@@ -165,7 +170,7 @@ __global__ void k_inv_diag(const HInst* __restrict__ insts,
     const long long g = I.grid_off + i;
     const float nv = norm[g];
     const float diag = lambda * (count[g] - 2.f * nv * nv) + csum[g];
-    invA[g] = (float)(1.0 / fmax(1e-3, (double)diag));
+    invA[g] = diag >= 1e-3f ? __frcp_rn(diag) : 1000.f;
   }
 }
 
@@ -316,12 +321,12 @@ __global__ void k_solve(const HInst* __restrict__ insts,
        row += nwarps) {
     const int zz = row / gy, y = row - zz * gy;
     const int base = row * gx;
-    // four x positions per lane per pass: all their loads are issued before
-    // any result is computed
-    for (int x0 = lane; x0 < gx; x0 += 128) {
-      float d[4], zc[4], nc[4], bc[4], ic[4], hc[4];
+    // two x positions per lane per pass: their 34 loads are issued before
+    // either result is computed
+    for (int x0 = lane; x0 < gx; x0 += 64) {
+      float d[2], zc[2], nc[2], bc[2], ic[2], hc[2];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < 2; ++j) {
         const int x = x0 + 32 * j;
         d[j] = zc[j] = nc[j] = bc[j] = ic[j] = hc[j] = 0.f;
         if (x < gx) {
@@ -342,7 +347,7 @@ __global__ void k_solve(const HInst* __restrict__ insts,
         }
       }
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < 2; ++j) {
         const int x = x0 + 32 * j;
         if (x >= gx) break;
         const int i = base + x;
@@ -359,8 +364,60 @@ __global__ void k_solve(const HInst* __restrict__ insts,
   }
 }
 
+__device__ __forceinline__ float slice_pixel(const HInst& I, const float* __restrict__ count,
+                                             const float* __restrict__ ovf,
+                                             const float* __restrict__ z, const HParams& p,
+                                             int x, int y, unsigned char luma) {
+  const float fx = (float)x * 1.0f / p.sigma_x;
+  const float fy = (float)y * 1.0f / p.sigma_y;
+  const float fz = (float)luma * 1.0f / p.sigma_l;
+  const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
+  const float wx = fx - x0, wy = fy - y0, wz = fz - z0;
+  // the eight corners' loads are all issued before the weighting
+  float cnt[2][2][2], zv[2][2][2];
+#pragma unroll
+  for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 2; ++dx) {
+        const int ix = (int)x0 + dx, iy = (int)y0 + dy, iz = (int)z0 + dz;
+        float c = 0.f, v = 0.f;
+        if (ix < I.gx && iy < I.gy && iz < I.gl) {
+          const long long g = gidx(I, ix, iy, iz);
+          c = count[g];
+          v = z[g];
+        } else if (ix < I.gx && iy < I.gy && iz == I.gl) {
+          c = ovf[I.plane_off + (long long)iy * I.gx + ix];
+        }
+        cnt[dz][dy][dx] = c;
+        zv[dz][dy][dx] = v;
+      }
+  float num[2][2], den[2][2];
+#pragma unroll
+  for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy) {
+      float ns = 0.f, ds = 0.f;
+#pragma unroll
+      for (int dx = 0; dx < 2; ++dx) {
+        const float w = dx ? wx : 1.f - wx;
+        ns += cnt[dz][dy][dx] * zv[dz][dy][dx] * w;
+        ds += cnt[dz][dy][dx] * w;
+      }
+      num[dz][dy] = ns;
+      den[dz][dy] = ds;
+    }
+  const float c0 = num[0][0] * (1.f - wy) + num[0][1] * wy;
+  const float c1 = num[1][0] * (1.f - wy) + num[1][1] * wy;
+  const float c0m = den[0][0] * (1.f - wy) + den[0][1] * wy;
+  const float c1m = den[1][0] * (1.f - wy) + den[1][1] * wy;
+  return __fdiv_rn(c0 * (1.f - wz) + c1 * wz, c0m * (1.f - wz) + c1m * wz);
+}
+
 // a17: SliceSolution<true> (src/hfbs.cu:246-330): count-weighted trilinear
-// interpolation of z at (x/sx, y/sy, L/sl).
+// interpolation of z at (x/sx, y/sy, L/sl).  One warp per image row, lanes
+// along x, two pixels per lane per pass.
 __global__ void k_slice(const HInst* __restrict__ insts,
                         const uchar4* __restrict__ guide,
                         const float* __restrict__ count,
@@ -368,45 +425,23 @@ __global__ void k_slice(const HInst* __restrict__ insts,
                         const float* __restrict__ z, float* __restrict__ out,
                         HParams p) {
   const HInst I = insts[blockIdx.y];
-  const long long npx = (long long)I.w * I.h;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int y = (int)(i / I.w), x = (int)(i - (long long)y * I.w);
-    const long long pp = I.pix_off + (long long)y * I.pitch + x;
-    const float fx = (float)x * 1.0f / p.sigma_x;
-    const float fy = (float)y * 1.0f / p.sigma_y;
-    const float fz = (float)guide[pp].x * 1.0f / p.sigma_l;
-    const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
-    const float wx = fx - x0, wy = fy - y0, wz = fz - z0;
-    float num[2][2], den[2][2];
-#pragma unroll
-    for (int dz = 0; dz < 2; ++dz)
-#pragma unroll
-      for (int dy = 0; dy < 2; ++dy) {
-        float ns = 0.f, ds = 0.f;
-#pragma unroll
-        for (int dx = 0; dx < 2; ++dx) {
-          const int ix = (int)x0 + dx, iy = (int)y0 + dy, iz = (int)z0 + dz;
-          float cnt = 0.f, zv = 0.f;
-          if (ix < I.gx && iy < I.gy && iz < I.gl) {
-            const long long g = gidx(I, ix, iy, iz);
-            cnt = count[g];
-            zv = z[g];
-          } else if (ix < I.gx && iy < I.gy && iz == I.gl) {
-            cnt = ovf[I.plane_off + (long long)iy * I.gx + ix];
-          }
-          const float w = dx ? wx : 1.f - wx;
-          ns += cnt * zv * w;
-          ds += cnt * w;
-        }
-        num[dz][dy] = ns;
-        den[dz][dy] = ds;
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  const uchar4* g = guide + I.pix_off;
+  float* o = out + I.pix_off;
+  for (int y = blockIdx.x * wpb + (threadIdx.x >> 5); y < I.h; y += gridDim.x * wpb) {
+    const int row = y * I.pitch;
+    for (int x0 = lane; x0 < I.w; x0 += 64) {
+      const int x1 = x0 + 32;
+      const unsigned char l0 = g[row + x0].x;
+      const unsigned char l1 = x1 < I.w ? g[row + x1].x : 0;
+      const float r0 = slice_pixel(I, count, ovf, z, p, x0, y, l0);
+      if (x1 < I.w) {
+        const float r1 = slice_pixel(I, count, ovf, z, p, x1, y, l1);
+        o[row + x1] = r1;
       }
-    const float c0 = num[0][0] * (1.f - wy) + num[0][1] * wy;
-    const float c1 = num[1][0] * (1.f - wy) + num[1][1] * wy;
-    const float c0m = den[0][0] * (1.f - wy) + den[0][1] * wy;
-    const float c1m = den[1][0] * (1.f - wy) + den[1][1] * wy;
-    out[pp] = __fdiv_rn(c0 * (1.f - wz) + c1 * wz, c0m * (1.f - wz) + c1m * wz);
+      o[row + x0] = r0;
+    }
   }
 }
 
@@ -423,7 +458,11 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   const dim3 gv(blocks_for(B.max_voxels), ni);
   // row kernels: one warp per grid row, 8 warps per block
   const dim3 gr((unsigned)std::min<long long>((B.max_rows + 7) / 8, 4096), ni);
-  const dim3 gp(blocks_for(B.max_pixels), ni);
+  // slice: one warp per image row, 8 rows per block
+  long long max_h = 1;
+  for (int i = 0; B.h_inst && i < ni; ++i) max_h = std::max<long long>(max_h, B.h_inst[i].h);
+  if (!B.h_inst) max_h = (B.max_pixels + 31) / 32;
+  const dim3 gp((unsigned)std::min<long long>((max_h + 7) / 8, 4096), ni);
   const dim3 gc((B.max_cells + 63) / 64, ni);
   const size_t splat_smem = sizeof(float) * 3 * (size_t)B.max_gl * 64;
   prof_begin(s, DTSGB_K_HFBS_SPLAT);
@@ -455,7 +494,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   // which then streams from L2 instead of HBM after its first iteration.
   struct Group {
     int first, count;
-    long long rows;
+    long long cols;  // max over the group of gx * gy
   };
   std::vector<Group> groups;
   if (B.h_inst && B.group_voxels > 0) {
@@ -471,14 +510,15 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
       }
       ++g.count;
       vox += v;
-      g.rows = std::max(g.rows, (long long)H.gy * H.gl);
+      g.cols = std::max(g.cols, (long long)H.gx * H.gy);
     }
     groups.push_back(g);
   } else {
-    groups.push_back(Group{0, ni, B.max_rows});
+    groups.push_back(Group{0, ni, B.max_cells});
   }
-  auto row_grid = [](const Group& g) {
-    return dim3((unsigned)std::min<long long>((g.rows + 7) / 8, 4096), g.count);
+  // column kernels (bistochastization, heavy-ball): one thread per (x, y)
+  auto col_grid = [](const Group& g) {
+    return dim3((unsigned)std::min<long long>((g.cols + kT - 1) / kT, 4096), g.count);
   };
   float* src = B.n0;
   float* dst = B.n1;
@@ -487,7 +527,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
     dst = B.n1;
     for (int it = 0; it < p.bistoch_iter_max; ++it) {
       prof_begin(s, DTSGB_K_HFBS_BISTOCH);
-      k_bistoch<<<row_grid(g), kT, 0, s>>>(B.d_inst + g.first, src, dst, B.count,
+      k_bistoch<<<col_grid(g), kT, 0, s>>>(B.d_inst + g.first, src, dst, B.count,
                                            (it % 2 == 0) ? 1.f : 0.f);
       prof_end(s, DTSGB_K_HFBS_BISTOCH);
       std::swap(src, dst);
@@ -521,10 +561,16 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   for (const Group& g : groups) {
     zs = B.z0;
     zd = B.z1;
+    long long rows = 0;  // one warp per grid row (y, l) of the group's largest grid
+    for (int i = 0; i < g.count; ++i)
+      rows = B.h_inst ? std::max(rows, (long long)B.h_inst[g.first + i].gy *
+                                           B.h_inst[g.first + i].gl)
+                      : B.max_rows;
+    const dim3 gr_g((unsigned)std::min<long long>((rows + 7) / 8, 4096), g.count);
     for (int it = 0; it < p.optim_iter_max; ++it) {
       prof_begin(s, DTSGB_K_HFBS_SOLVE);
-      k_solve<<<row_grid(g), kT, 0, s>>>(B.d_inst + g.first, zs, zd, B.h, norm, B.b,
-                                         B.invA, p.lambda, p.alpha, p.beta);
+      k_solve<<<gr_g, kT, 0, s>>>(B.d_inst + g.first, zs, zd, B.h, norm, B.b, B.invA,
+                                  p.lambda, p.alpha, p.beta);
       prof_end(s, DTSGB_K_HFBS_SOLVE);
       std::swap(zs, zd);
     }
