@@ -126,11 +126,15 @@ class Cfg3:
     name = "cfg3_batched_dts_hfbs_64_ragged_bf16"
     dtype = "bf16 storage, f32 math"
 
-    def __init__(self, rank: int):
+    def __init__(self, rank: int, scale: float = 1.0):
         import domain_transform_solver_gb300 as D
         from domain_transform_solver_gb300 import workloads as W
         self.D, self.W = D, W
-        self.insts = W.batched_instances()
+        # scale < 1 shrinks every instance (profiling captures of a smaller
+        # case); the reported workload is scale 1
+        self.insts = W.batched_instances(scale=scale)
+        if scale != 1.0:
+            self.name = f"{self.name}_scale{scale:g}"
         self.sizes = [(i.width, i.height) for i in self.insts]
         self.pixels = sum(w * h for w, h in self.sizes)
         self.iters = W.CFG0_OPT["num_iterations"]
@@ -142,6 +146,9 @@ class Cfg3:
     def setup(self, stream_handle: int):
         D, W = self.D, self.W
         self.b = D.Batch(self.sizes, flags=D.FLAG_BF16_STORAGE)
+        # every step solves the same inputs: keeping the guide-derived windows
+        # and HFBS normalisation across steps would skip work, so it is off
+        self.b.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)
         self.b.set_stream(stream_handle)
         self.b.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in self.insts],
                       [i.target for i in self.insts], [i.confidence for i in self.insts])
@@ -324,9 +331,10 @@ class Cfg1:
 
 class Cfg4:
     """Differentiable DTS: 16 x 1024x768 config-0-style instances, FP32,
-    L2, 10 iterations, forward with checkpoints every ceil(sqrt(10)) = 4
-    iterations plus the adjoint (dL/dtarget, dL/dconfidence) for an N(0,1)
-    upstream gradient.  One step = forward + backward; the guide's window
+    L2, 10 iterations, forward with checkpoints (the automatic segment
+    length: 2 for 10 iterations, 10 planes held instead of 10 + 4 iterates)
+    plus the adjoint (dL/dtarget, dL/dconfidence) for an N(0,1) upstream
+    gradient.  One step = forward + backward; the guide's window
     bounds are held fixed (piecewise constant in the guide)."""
 
     name = "cfg4_dts_fwd_bwd_16x1024x768_f32"
@@ -346,6 +354,7 @@ class Cfg4:
         import torch
         D, W = self.D, self.W
         self.b = D.Batch(self.sizes)
+        self.b.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)  # full work every step
         self.b.set_stream(stream_handle)
         self.b.enable_grad(True, 0)
         self.b.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in self.insts],
@@ -374,6 +383,7 @@ class Cfg4:
         self.h_gt, self.h_gc = _ptrs(self._ogt), _ptrs(self._ogc)
         # the plain forward (no checkpoints) of the same batch, for the ratio
         self.fwd = D.Batch(self.sizes)
+        self.fwd.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)
         self.fwd.set_stream(stream_handle)
         self.fwd.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in self.insts],
                         [i.target for i in self.insts], [i.confidence for i in self.insts])
@@ -432,6 +442,12 @@ WORKLOADS = {"cfg3": Cfg3, "cfg0": Cfg0, "cfg1": Cfg1, "cfg4": Cfg4}
 
 
 # ---- arms ----------------------------------------------------------------------
+def make_workload(args, rank):
+    if args.workload == "cfg3":
+        return Cfg3(rank, scale=args.scale)
+    return WORKLOADS[args.workload](rank)
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -485,7 +501,7 @@ def cpu_baseline(wl, budget_s=12.0, real="f32"):
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    wl = WORKLOADS[args.workload](rank)
+    wl = make_workload(args, rank)
     import oracle as O
     O.build()
     desc = ""
@@ -522,7 +538,7 @@ def run_ours(args, world, rank, local):
     import domain_transform_solver_gb300 as D  # noqa: F401  (loads libdtsgb.so)
     from domain_transform_solver_gb300 import _lib
     lib = _lib.load()
-    wl = WORKLOADS[args.workload](rank)
+    wl = make_workload(args, rank)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     wl.setup(stream.cuda_stream)
@@ -637,7 +653,8 @@ def run_ours(args, world, rank, local):
                    "voxels_per_step": wl.voxels, "iterations": wl.iters,
                    "l2": ("inputs larger than L2" if big
                           else "flushed between steps (256 MB write)"),
-                   "parallelism": f"independent instances x{world} GPUs"},
+                   "parallelism": f"independent instances x{world} GPUs",
+                   "guide_state_reuse": "off (every step recomputes all of it)"},
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": achieved,
@@ -665,6 +682,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="cfg3")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="cfg3 only: shrink every instance (smaller profiling case)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

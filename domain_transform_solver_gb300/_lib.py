@@ -127,6 +127,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_batch_use_graphs": ([vp, i], i),
         "dtsgb_batch_upload": ([vp, i, pvp, pvp, pvp], i),
         "dtsgb_batch_upload_device": ([vp, i, pvp, pvp, pvp], i),
+        "dtsgb_batch_upload_targets": ([vp, pvp, pvp], i),
+        "dtsgb_batch_upload_targets_device": ([vp, pvp, pvp], i),
         "dtsgb_batch_solve_dts": ([vp, P(FilterParams), P(OptimizeParams), f], i),
         "dtsgb_batch_solve_hfbs": ([vp, P(HfbsParams)], i),
         "dtsgb_batch_download": ([vp, i, pvp], i),
@@ -136,6 +138,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_batch_autotune": ([vp, P(FilterParams), P(OptimizeParams), f,
                                   P(HfbsParams), i], i),
         "dtsgb_batch_enable_grad": ([vp, i, i], i),
+        "dtsgb_png_unfilter": ([vp, i, i, i, vp], i),
         "dtsgb_batch_grad_info": ([vp, P(i), P(i)], i),
         "dtsgb_batch_dts_backward": ([vp, pvp, pvp, pvp], i),
         "dtsgb_batch_dts_backward_device": ([vp, pvp, pvp, pvp], i),

@@ -64,6 +64,21 @@ struct dtsgb_batch_s {
   int ntb = 0, nti = 0, nti_big = 0, nti_small = 0;
   bool small = false;
   long long hfbs_group_voxels = 0;  // L2-resident HFBS group budget (0: off)
+  // Guide-derived state kept across solves while the guide is unchanged
+  // (video frames that change only the target): the DTS window bounds and
+  // the HFBS bistochastized normalisation.
+  unsigned long long guide_gen = 0;  // bumped by every guide upload
+  bool reuse = true;
+  struct BoundsKey {
+    unsigned long long gen;
+    float rx, ry, sz;
+    int ref_y;
+  } bkey{~0ull, 0.f, 0.f, 0.f, 0};
+  struct NormKey {
+    unsigned long long gen;
+    float sx, sy, sl;
+    int bistoch;
+  } nkey{~0ull, 0.f, 0.f, 0.f, 0};
   int dts_res = -1;
   bool hfbs_done = false;
   bool use_graphs = true;
@@ -76,7 +91,7 @@ struct dtsgb_batch_s {
   long long ocap = 0;
   // gradients of the DTS solve
   bool grad = false;
-  int grad_seg_req = 0;          // 0: ceil(sqrt(N))
+  int grad_seg_req = 0;          // 0: dts_checkpoint_segment(N)
   int grad_seg = 1;              // segment length of the planes below
   int grad_n = -1;               // iterations the adjoint replays (-1: none kept)
   std::vector<float*> gplanes;   // checkpoints, segment planes, 2 adjoint, dt, dc
@@ -227,25 +242,9 @@ int upload_plane(dtsgb_batch_t b, int i, const float* src, void* dst,
   return DTSGB_OK;
 }
 
-int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
-                 const float* const* target, const float* const* conf,
-                 cudaMemcpyKind kind) {
-  if (!b || !rgba || !target) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
-  if (cs < DTSGB_RGB || cs > DTSGB_YYY)
-    return fail(DTSGB_ERR_INVALID_ARGUMENT, "invalid color space");
-  for (int i = 0; i < b->n; ++i)
-    if (!rgba[i] || !target[i])
-      return fail(DTSGB_ERR_INVALID_ARGUMENT, "null image pointer");
+int batch_upload_targets(dtsgb_batch_t b, const float* const* target,
+                         const float* const* conf, cudaMemcpyKind kind) {
   int st;
-  for (int i = 0; i < b->n; ++i) {
-    const Inst& I = b->inst[i];
-    const size_t wb = (size_t)I.w * 4;
-    DTSGB_CUDA(cudaMemcpy2DAsync(b->guide + I.off, (size_t)I.pitch * 4, rgba[i], wb,
-                                 wb, I.h, kind, b->stream));
-  }
-  st = launch_color_convert_flat(b->guide, b->total, cs, b->stream);
-  if (st) return st;
-  // target
   for (int i = 0; i < b->n; ++i)
     if ((st = upload_plane(b, i, target[i], b->target, kind))) return st;
   if (b->st == Storage::BF16 &&
@@ -253,11 +252,9 @@ int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
                                       b->total, b->stream)))
     return st;
   // confidence (missing -> ones)
-  bool any_conf = false;
   for (int i = 0; i < b->n; ++i) {
     const Inst& I = b->inst[i];
     if (conf && conf[i]) {
-      any_conf = true;
       if ((st = upload_plane(b, i, conf[i], b->conf, kind))) return st;
     } else if (b->st == Storage::F32) {
       if ((st = launch_fill_storage(Storage::F32, (float*)b->conf + I.off,
@@ -269,7 +266,6 @@ int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
         return st;
     }
   }
-  (void)any_conf;
   if (b->st == Storage::BF16 &&
       (st = launch_storage_from_float(nullptr, 0, b->st, b->scratch, b->conf,
                                       b->total, b->stream)))
@@ -281,10 +277,32 @@ int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
   return DTSGB_OK;
 }
 
+int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
+                 const float* const* target, const float* const* conf,
+                 cudaMemcpyKind kind) {
+  if (!b || !rgba || !target) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  if (cs < DTSGB_RGB || cs > DTSGB_YYY)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "invalid color space");
+  for (int i = 0; i < b->n; ++i)
+    if (!rgba[i] || !target[i])
+      return fail(DTSGB_ERR_INVALID_ARGUMENT, "null image pointer");
+  for (int i = 0; i < b->n; ++i) {
+    const Inst& I = b->inst[i];
+    const size_t wb = (size_t)I.w * 4;
+    DTSGB_CUDA(cudaMemcpy2DAsync(b->guide + I.off, (size_t)I.pitch * 4, rgba[i], wb,
+                                 wb, I.h, kind, b->stream));
+  }
+  int st = launch_color_convert_flat(b->guide, b->total, cs, b->stream);
+  if (st) return st;
+  ++b->guide_gen;
+  return batch_upload_targets(b, target, conf, kind);
+}
+
 int ensure_hfbs_buffers(dtsgb_batch_t b, long long voxels, long long planes) {
   if (voxels > b->gcap) {
     for (auto& p : b->hg) dfree(p);
     b->gcap = 0;
+    b->nkey.gen = ~0ull;  // the normalisation is gone with the old planes
     for (int k = 0; k < HG_NUM; ++k) {
       int st = dalloc(&b->hg[k], (size_t)voxels);
       if (st) return st;
@@ -451,6 +469,23 @@ DTSGB_API int dtsgb_batch_upload(dtsgb_batch_t b, int cs, const void* const* rgb
   return batch_upload(b, cs, rgba, target, conf, cudaMemcpyHostToDevice);
 }
 
+DTSGB_API int dtsgb_batch_upload_targets(dtsgb_batch_t b, const float* const* target,
+                                         const float* const* conf) {
+  if (!b || !target) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  for (int i = 0; i < b->n; ++i)
+    if (!target[i]) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null image pointer");
+  return batch_upload_targets(b, target, conf, cudaMemcpyHostToDevice);
+}
+
+DTSGB_API int dtsgb_batch_upload_targets_device(dtsgb_batch_t b,
+                                                const float* const* target,
+                                                const float* const* conf) {
+  if (!b || !target) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  for (int i = 0; i < b->n; ++i)
+    if (!target[i]) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null image pointer");
+  return batch_upload_targets(b, target, conf, cudaMemcpyDeviceToDevice);
+}
+
 DTSGB_API int dtsgb_batch_upload_device(dtsgb_batch_t b, int cs,
                                         const void* const* rgba,
                                         const float* const* target,
@@ -474,7 +509,8 @@ DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b, const dtsgb_filter_params* 
   const int halo = (int)std::floor(p->sigma_z);
   const bool iterate = p->loss != DTSGB_L1 && p->num_iterations > 0;
   const DtsLaunch Lb{b->d_inst, b->d_tb, b->ntb, b->n};
-  const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n, b->small};
+  const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n, b->small, b->d_ti_small,
+                     b->nti_small};
   const bool over = overwrite > 0.f && overwrite < 1.f;
   const int n_kept = iterate ? p->num_iterations : 0;
   b->grad_n = -1;
@@ -488,11 +524,17 @@ DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b, const dtsgb_filter_params* 
     if (st) return st;
   }
   int res = 0;
+  const dtsgb_batch_s::BoundsKey bk{b->guide_gen, rx, ry, p->sigma_z, b->ref_y};
+  const bool keep_bounds = b->reuse && std::memcmp(&bk, &b->bkey, sizeof bk) == 0;
+  auto bounds = [&]() -> int {
+    if (keep_bounds) return DTSGB_OK;  // same guide and sigmas: windows unchanged
+    return launch_bounds(Lb, b->guide, b->bounds, rx, ry, p->sigma_z, p->sigma_z,
+                         b->ref_y, b->stream);
+  };
   auto enqueue = [&]() -> int {
     if (b->grad && iterate) {
       const IterMode mode = p->loss == DTSGB_L2 ? IterMode::L2 : IterMode::CHARB;
-      int st = launch_bounds(Lb, b->guide, b->bounds, rx, ry, p->sigma_z, p->sigma_z,
-                             b->ref_y, b->stream);
+      int st = bounds();
       if (st) return st;
       return dts_forward_checkpointed(Li, b->st, mode, grad_view(b, n_kept), b->target,
                                       b->conf, b->bounds, p->lambda, p->step_size, halo,
@@ -501,8 +543,7 @@ DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b, const dtsgb_filter_params* 
     }
     int st = launch_init_var(Li, b->st, b->target, b->v[0], b->stream);
     if (st || !iterate) return st;
-    st = launch_bounds(Lb, b->guide, b->bounds, rx, ry, p->sigma_z, p->sigma_z,
-                       b->ref_y, b->stream);
+    st = bounds();
     if (st) return st;
     const IterMode mode = p->loss == DTSGB_L2 ? IterMode::L2 : IterMode::CHARB;
     int a = 0;
@@ -525,8 +566,13 @@ DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b, const dtsgb_filter_params* 
   key_append(key, b->grad);
   key_append(key, b->grad_seg);
   key_append(key, b->small);
+  key_append(key, keep_bounds);
   int st = run_graph(b, b->g_dts, key, enqueue);
-  if (st) return st;
+  if (st) {
+    b->bkey.gen = ~0ull;
+    return st;
+  }
+  if (iterate) b->bkey = bk;
   b->dts_res = res;
   if (b->grad) {
     b->grad_n = n_kept;
@@ -575,7 +621,8 @@ static int batch_backward(dtsgb_batch_t b, const float* const* grad_out,
     DTSGB_CUDA(cudaMemcpy2DAsync(G.g[0] + I.off, (size_t)I.pitch * 4, grad_out[i], wb, wb,
                                  I.h, up, b->stream));
   }
-  const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n, b->small};
+  const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n, b->small, b->d_ti_small,
+                     b->nti_small};
   const dtsgb_optimize_params p = b->gopt;
   const int halo = (int)b->ghalo;
   auto enqueue = [&]() -> int {
@@ -699,13 +746,22 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
   B.keep_debug = false;
   B.h_inst = b->hinst.data();
   B.group_voxels = b->hfbs_group_voxels;
+  // the bistochastized normalisation depends only on the guide's bins
+  const dtsgb_batch_s::NormKey nk{b->guide_gen, p->sigma_x, p->sigma_y, p->sigma_l,
+                                  p->bistoch_iter_max};
+  B.reuse_norm = b->reuse && same_tables && std::memcmp(&nk, &b->nkey, sizeof nk) == 0;
   HParams hp{p->sigma_x, p->sigma_y, p->sigma_l, p->lambda, p->alpha, p->beta,
              p->bistoch_iter_max, p->optim_iter_max, p->neg_exp_beta};
   std::vector<char> key;
   key_append(key, hp);
   key_append(key, b->hfbs_group_voxels);
+  key_append(key, B.reuse_norm);
   st = run_graph(b, b->g_hfbs, key, [&]() { return hfbs_enqueue_solve(B, hp, b->stream); });
-  if (st) return st;
+  if (st) {
+    b->nkey.gen = ~0ull;
+    return st;
+  }
+  b->nkey = nk;
   b->hfbs_done = true;
   return DTSGB_OK;
 }
@@ -727,6 +783,10 @@ DTSGB_API int dtsgb_batch_set_tuning(dtsgb_batch_t b, int knob, long long value)
     b->hfbs_group_voxels = value;
     return DTSGB_OK;
   }
+  if (knob == DTSGB_TUNE_REUSE_GUIDE_STATE) {
+    b->reuse = value != 0;
+    return DTSGB_OK;
+  }
   return fail(DTSGB_ERR_INVALID_ARGUMENT, "unknown tuning knob");
 }
 
@@ -738,6 +798,10 @@ DTSGB_API int dtsgb_batch_get_tuning(dtsgb_batch_t b, int knob, long long* value
   }
   if (knob == DTSGB_TUNE_HFBS_GROUP_VOXELS) {
     *value = b->hfbs_group_voxels;
+    return DTSGB_OK;
+  }
+  if (knob == DTSGB_TUNE_REUSE_GUIDE_STATE) {
+    *value = b->reuse ? 1 : 0;
     return DTSGB_OK;
   }
   return fail(DTSGB_ERR_INVALID_ARGUMENT, "unknown tuning knob");

@@ -319,6 +319,9 @@ int launch_adj_t(const DtsLaunch& L, const float* gin, float* gout, const float*
   if (L.small)
     return launch_adj_shape<TS, MODE, kIterSmallTW, kIterSmallTH>(
         L, gin, gout, vk, t, c, bounds, gt, gc, lambda, step, hx, hy, s);
+  if (L.d_tiles_small && AdjSmem<kIterTW, kIterTH, 512>(hx, hy).total > 227 * 1024)
+    return launch_adj_shape<TS, MODE, kIterSmallTW, kIterSmallTH>(
+        L.as_small(), gin, gout, vk, t, c, bounds, gt, gc, lambda, step, hx, hy, s);
   return launch_adj_shape<TS, MODE, kIterTW, kIterTH>(L, gin, gout, vk, t, c, bounds, gt,
                                                       gc, lambda, step, hx, hy, s);
 }
@@ -345,9 +348,19 @@ int launch_adjoint(const DtsLaunch& L, Storage st, IterMode mode, const float* g
 }  // namespace
 
 int dts_checkpoint_segment(int num_iterations) {
-  int k = 1;
-  while (k * k < num_iterations) ++k;
-  return k;
+  // fewest planes held (ceil(N/K) - 1 + K), and among those the fewest
+  // recomputed iterations (N - ceil(N/K)): the smallest such K
+  const int n = std::max(num_iterations, 1);
+  int best = 1;
+  long long best_planes = -1;
+  for (int k = 1; k <= n; ++k) {
+    const long long planes = (n + k - 1) / k - 1 + k;
+    if (best_planes < 0 || planes < best_planes) {
+      best_planes = planes;
+      best = k;
+    }
+  }
+  return best;
 }
 
 // Destination of the iterate v_next of an N-iteration forward from v_cur:

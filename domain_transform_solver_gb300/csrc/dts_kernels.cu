@@ -68,24 +68,27 @@ __global__ void __launch_bounds__(kThreads)
   float* sH = sm;            // TH x DW
   float* sV = sm + TH * DW;  // DR x TW
   const uchar4 zero = make_uchar4(0, 0, 0, 0);
-  for (int i = threadIdx.x; i < TH * DW; i += blockDim.x) {
-    const int r = i / DW, c = i - r * DW;
-    const int x = t.x0 - rx + 1 + c, y = t.y0 + r;
-    float w = 0.f;
-    if (x >= 0 && x < W && y < H) {
-      const uchar4 cur = g[(long long)y * P + x];
-      const uchar4 prev = x > 0 ? g[(long long)y * P + x - 1] : zero;
-      w = ratio_x < 0.f ? 0.f : edge_weight(cur, prev, ratio_x);
+  // dH: one warp per tile row, lanes along the row (no index divisions)
+  for (int r = threadIdx.x >> 5; r < TH; r += blockDim.x >> 5) {
+    const int y = t.y0 + r;
+    for (int c = threadIdx.x & 31; c < DW; c += 32) {
+      const int x = t.x0 - rx + 1 + c;
+      float w = 0.f;
+      if (x >= 0 && x < W && y < H) {
+        const uchar4 cur = g[y * P + x];
+        const uchar4 prev = x > 0 ? g[y * P + x - 1] : zero;
+        w = ratio_x < 0.f ? 0.f : edge_weight(cur, prev, ratio_x);
+      }
+      sH[r * DW + c] = w;
     }
-    sH[i] = w;
   }
   for (int i = threadIdx.x; i < DR * TW; i += blockDim.x) {
     const int r = i / TW, c = i - r * TW;
     const int x = t.x0 + c, y = t.y0 - ry + 1 + r;
     float w = 0.f;
     if (x < W && y >= 0 && y < H) {
-      const uchar4 cur = g[(long long)y * P + x];
-      const uchar4 prev = y > 0 ? g[(long long)(y - 1) * P + x] : zero;
+      const uchar4 cur = g[y * P + x];
+      const uchar4 prev = y > 0 ? g[(y - 1) * P + x] : zero;
       w = ratio_y < 0.f ? 0.f : edge_weight(cur, prev, ratio_y);
     }
     sV[i] = w;
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(kThreads)
         break;
       }
     }
-    bo[(long long)y * P + x] = pack_bounds(dlx, dux, dly, duy);
+    bo[y * P + x] = pack_bounds(dlx, dux, dly, duy);
   }
 }
 
@@ -477,6 +480,197 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
 }
 
 // ---------------------------------------------------------------------------
+// The same iteration for large halos (k_dts_iter_rows): shared memory grows
+// linearly with the halo instead of with its square, so every sigma_z below
+// 254 fits the 32 x 32 tiles.  Window sums from fixed-point prefix sums
+// (fixed_point.cuh) as in k_dts_iter_tile; the X scale comes from the
+// largest magnitude in the row (X) or among the tile's X results (Y).
+//
+// X half-step: one warp per row of the tile plus the vertical halo; each
+// lane scans four consecutive values, a warp shuffle scan joins the lanes,
+// and the row's prefix sits in a per-warp shared buffer.  A warp issues the
+// global loads of its next row before working on the current one.  Y
+// half-step: the X results stay in shared memory; each thread scans a
+// segment of one column, segment offsets are added in a second pass, and
+// the tile's output rows are written coalesced.  Reciprocals 1/n come from
+// a per-block table of correctly rounded values.
+// ---------------------------------------------------------------------------
+template <int TW, int TH, int NT>
+struct PrefixIterSmem {
+  // bytes of shared memory for halos hx, hy
+  static size_t bytes(int hx, int hy) {
+    const size_t SR = TH + 2 * hy, SWX = TW + 2 * hx + 1;
+    const size_t py = std::max((SR + 1) * TW, (size_t)(NT / 32) * SWX) * 4;
+    const size_t seg = (size_t)(NT / TW) * TW * 4;
+    const size_t sx = SR * (TW + 1) * 4;
+    const size_t sby = (size_t)TH * TW * 2;
+    const size_t rt = (size_t)(2 * std::max(hx, hy) + 2) * 4;
+    return py + seg + sx + sby + rt + 16;
+  }
+};
+
+template <typename TS, int MODE, int TW, int TH, int NT, bool STEREO = false>
+__global__ void __launch_bounds__(NT, 1024 / NT)
+    k_dts_iter_rows(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
+                      const float* __restrict__ vin, float* __restrict__ vout,
+                      const TS* __restrict__ tgt, const TS* __restrict__ cnf,
+                      const uint32_t* __restrict__ bnd, float lambda, float step,
+                      float overwrite, int hx, int hy, StereoArgs sa) {
+  static_assert(TW % 32 == 0 && NT % TW == 0, "tile width: whole warps");
+  constexpr int NW = NT / 32, NSEG = NT / TW, TWp = TW + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const Tile t = tiles[blockIdx.x];
+  const Inst in = insts[t.inst];
+  const int W = in.w, H = in.h, P = in.pitch;
+  const int SR = TH + 2 * hy, SWX = TW + 2 * hx + 1, RY = SR + 1;
+  const int pyn = max(RY * TW, NW * SWX);
+  unsigned* Py = reinterpret_cast<unsigned*>(smraw);  // RY x TW (Y phase)
+  unsigned* Xb = Py;                                  // NW x SWX (X phase)
+  unsigned* segtot = Py + pyn;                        // NSEG x TW
+  float* sx = reinterpret_cast<float*>(segtot + NSEG * TW);   // SR x TWp
+  uint16_t* sby = reinterpret_cast<uint16_t*>(sx + SR * TWp);  // TH x TW
+  float* rtab = reinterpret_cast<float*>(sby + TH * TW);
+  const int nrt = 2 * max(hx, hy) + 2;
+  unsigned* smax = reinterpret_cast<unsigned*>(rtab + nrt);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < nrt; i += NT) rtab[i] = i ? __frcp_rn((float)i) : 0.f;
+  if (tid == 0) *smax = 0u;
+  __syncthreads();
+  const bool over = overwrite > 0.f && overwrite < 1.f;
+  const int gx0 = t.x0 - hx - 1;  // image x of X prefix entry 0 (a zero entry)
+  const int gy0 = t.y0 - hy;      // image y of sx row 0
+  const int lgx = ceil_log2(2 * hx + 1), lgy = ceil_log2(2 * hy + 1);
+  // ---- X half-step ----------------------------------------------------------
+  constexpr int CPL = TW / 32;  // tile columns per lane
+  struct RowIn {
+    float v4[4];  // prefix entries 4*lane .. 4*lane+3
+    uint32_t b[CPL];  // tile columns lane + 32k
+    float tv[CPL], cv[CPL], vc[CPL];
+  };
+  auto load_v = [&](bool yok, long long row, int cc) -> float {  // prefix entry cc
+    const int x = gx0 + cc;
+    if (cc < 1 || cc >= SWX || !yok || (unsigned)x >= (unsigned)W) return 0.f;
+    float v = __ldg(vin + row + x);
+    if (over && load_f(cnf + row + x) > overwrite) v = load_f(tgt + row + x);
+    return v;
+  };
+  auto fetch = [&](int r, RowIn& R) {
+    const int y = gy0 + r;
+    const bool yok = (unsigned)y < (unsigned)H;
+    const long long row = in.off + (long long)y * P;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) R.v4[j] = load_v(yok, row, 4 * lane + j);
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) {
+      const int x = t.x0 + lane + 32 * k;
+      R.b[k] = 0u;
+      R.tv[k] = R.cv[k] = R.vc[k] = 0.f;
+      if (yok && x < W) {
+        const long long p = row + x;
+        R.b[k] = __ldg(bnd + p);
+        R.tv[k] = load_f(tgt + p);
+        R.cv[k] = load_f(cnf + p);
+        R.vc[k] = __ldg(vin + p);
+      }
+    }
+  };
+  float mloc = 0.f;
+  unsigned* xb = Xb + warp * SWX;
+  RowIn cur, nxt;
+  if (warp < SR) fetch(warp, cur);
+  for (int r = warp; r < SR; r += NW) {
+    if (r + NW < SR) fetch(r + NW, nxt);
+    const int y = gy0 + r;
+    const bool yok = (unsigned)y < (unsigned)H;
+    const long long row = in.off + (long long)y * P;
+    float m = fmaxf(fmaxf(fabsf(cur.v4[0]), fabsf(cur.v4[1])),
+                    fmaxf(fabsf(cur.v4[2]), fabsf(cur.v4[3])));
+    for (int base = 128; base < SWX; base += 128)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) m = fmaxf(m, fabsf(load_v(yok, row, base + 4 * lane + j)));
+    const int F = fx_shift(warp_max_nonneg(m), lgx);
+    const float sF = pow2f(F), isF = pow2f(-F);
+    unsigned carry = 0;
+    for (int base = 0; base < SWX; base += 128) {
+      unsigned s4[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float v = base == 0 ? cur.v4[j] : load_v(yok, row, base + 4 * lane + j);
+        s4[j] = fx_from(v, sF) + (j ? s4[j - 1] : 0u);
+      }
+      const unsigned incl = warp_incl_scan(s4[3], lane);
+      const unsigned off = carry + incl - s4[3];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int cc = base + 4 * lane + j;
+        if (cc < SWX) xb[cc] = off + s4[j];
+      }
+      carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) {
+      const int c = lane + 32 * k;
+      const int x = t.x0 + c;
+      float o = 0.f;
+      if (yok && x < W) {
+        const uint32_t b = cur.b[k];
+        const float tv = cur.tv[k], cv = cur.cv[k];
+        float v = cur.vc[k];
+        if (over && cv > overwrite) v = tv;
+        const int dl = min((int)(b & 0xff), hx + 1);
+        const int du = min((int)((b >> 8) & 0xff), hx);
+        const float rn = rtab[dl + du];
+        const int i = c + hx + 1;
+        const float B = fx_window(xb[i + du], xb[i - dl], rn * isF);
+        float extra = 0.f;
+        if (STEREO) extra = photometric(sa, row, x, W, v);
+        o = x_update<MODE, STEREO>(v, B, tv, cv, rn, lambda, step, extra);
+        if (over && cv > overwrite) o = tv;
+        if (r >= hy && r < hy + TH) sby[(r - hy) * TW + c] = (uint16_t)(b >> 16);
+      }
+      sx[r * TWp + c] = o;
+      mloc = fmaxf(mloc, fabsf(o));
+    }
+    __syncwarp();  // the warp's prefix buffer is rewritten for its next row
+    cur = nxt;
+  }
+  mloc = warp_max_nonneg(mloc);
+  if (lane == 0) atomicMax(smax, __float_as_uint(mloc));
+  __syncthreads();
+  // ---- Y half-step ----------------------------------------------------------
+  const int Fy = fx_shift(__uint_as_float(*smax), lgy);
+  const float sFy = pow2f(Fy), isFy = pow2f(-Fy);
+  const int c = tid % TW, sgi = tid / TW;
+  const int seg = (RY + NSEG - 1) / NSEG;
+  const int k0 = min(sgi * seg, RY), k1 = min(k0 + seg, RY);
+  unsigned acc = 0;
+  for (int k = k0; k < k1; ++k) {
+    if (k > 0) acc += fx_from(sx[(k - 1) * TWp + c], sFy);
+    Py[k * TW + c] = acc;
+  }
+  segtot[sgi * TW + c] = acc;
+  __syncthreads();
+  unsigned off = 0;
+  for (int s2 = 0; s2 < sgi; ++s2) off += segtot[s2 * TW + c];
+  for (int k = k0; k < k1; ++k) Py[k * TW + c] += off;
+  __syncthreads();
+  const float slam = step * lambda;
+  const int x = t.x0 + c;
+  for (int j = sgi; j < TH; j += NSEG) {
+    const int y = t.y0 + j;
+    if (y >= H || x >= W) continue;
+    const uint32_t b = sby[j * TW + c];
+    const int dl = min((int)(b & 0xff), hy + 1), du = min((int)(b >> 8), hy);
+    const int k = j + hy + 1;
+    const float B = fx_window(Py[(k + du) * TW + c], Py[(k - dl) * TW + c],
+                              rtab[dl + du] * isFy);
+    const float v = sx[(j + hy) * TWp + c];
+    vout[in.off + (long long)y * P + x] = __fmaf_rn(-slam, v - B, v);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Filter pass (a5): X box mean then Y box mean over NCH channels sharing the
 // windows (src/domain_transform_filter.cuh:30-71).  With CONF the Y result
 // is not stored; instead the confidence epilogue of
@@ -723,12 +917,24 @@ static int launch_iter_shape(const DtsLaunch& L, const float* vin, float* vout,
   constexpr int NT = TW >= 64 ? 512 : 256;
   const TileIterSmem<TW, TH, NT> lay(hx, hy);
   const size_t smem = (size_t)lay.total;
-  if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "sigma_z too large");
+  const size_t smem_rows = PrefixIterSmem<TW, TH, NT>::bytes(hx, hy);
+  if (smem > kMaxSmem && smem_rows > kMaxSmem)
+    return fail(DTSGB_ERR_UNSUPPORTED, "sigma_z too large");
   if (overwrite > 0.f && overwrite < 1.f) {
     // the input iterate is overwritten in place, as the reference does
     k_overwrite<TS><<<dim3(64, L.n_inst), kThreads, 0, s>>>(
         L.d_inst, const_cast<float*>(vin), (const TS*)target, (const TS*)conf, overwrite);
     DTSGB_CUDA(cudaGetLastError());
+  }
+  if (smem > kMaxSmem) {  // halo too large for the tile-staged kernel
+    int st = set_smem(k_dts_iter_rows<TS, MODE, TW, TH, NT, STEREO>, smem_rows);
+    if (st) return st;
+    ProfScope ps(s, DTSGB_K_DTS_ITER);
+    k_dts_iter_rows<TS, MODE, TW, TH, NT, STEREO><<<L.n_tiles, NT, smem_rows, s>>>(
+        L.d_inst, L.d_tiles, vin, vout, (const TS*)target, (const TS*)conf,
+        bounds, lambda, step, overwrite, hx, hy, sa);
+    DTSGB_CUDA(cudaGetLastError());
+    return DTSGB_OK;
   }
   int st = set_smem(k_dts_iter_tile<TS, MODE, TW, TH, NT, STEREO>, smem);
   if (st) return st;
@@ -749,6 +955,12 @@ static int launch_iter_t(const DtsLaunch& L, const float* vin, float* vout,
   if (L.small)
     return launch_iter_shape<TS, MODE, kIterSmallTW, kIterSmallTH, STEREO>(
         L, vin, vout, target, conf, bounds, lambda, step, overwrite, hx, hy, s, sa);
+  if (L.d_tiles_small &&
+      (size_t)TileIterSmem<kIterTW, kIterTH, 512>(hx, hy).total > kMaxSmem &&
+      PrefixIterSmem<kIterTW, kIterTH, 512>::bytes(hx, hy) > kMaxSmem)
+    return launch_iter_shape<TS, MODE, kIterSmallTW, kIterSmallTH, STEREO>(
+        L.as_small(), vin, vout, target, conf, bounds, lambda, step, overwrite, hx, hy,
+        s, sa);
   return launch_iter_shape<TS, MODE, kIterTW, kIterTH, STEREO>(
       L, vin, vout, target, conf, bounds, lambda, step, overwrite, hx, hy, s, sa);
 }
@@ -859,6 +1071,11 @@ static int launch_filter_t(const DtsLaunch& L, const float* in0,
   if (L.small)
     return launch_filter_shape<NCH, CONF, TS, kIterSmallTW, kIterSmallTH>(
         L, in0, in1, out0, out1, bounds, hx, hy, conf_out, scale, left_clear, s);
+  if (L.d_tiles_small &&
+      NCH * sizeof(float) * ((size_t)(kIterTH + 2 * hy) * (kIterTW + 2 * hx) +
+                             (size_t)(kIterTH + 2 * hy) * kIterTW) > kMaxSmem)
+    return launch_filter_shape<NCH, CONF, TS, kIterSmallTW, kIterSmallTH>(
+        L.as_small(), in0, in1, out0, out1, bounds, hx, hy, conf_out, scale, left_clear, s);
   return launch_filter_shape<NCH, CONF, TS, kIterTW, kIterTH>(
       L, in0, in1, out0, out1, bounds, hx, hy, conf_out, scale, left_clear, s);
 }

@@ -81,7 +81,8 @@ struct dtsgb_dts_s {
   Inst* d_inst = nullptr;
   Tile* d_tb = nullptr;  // bounds tiles
   Tile* d_ti = nullptr;  // iteration tiles
-  int ntb = 0, nti = 0;
+  Tile* d_ti_small = nullptr;  // small iteration tiles when d_ti holds big ones
+  int ntb = 0, nti = 0, nti_small = 0;
 
   bool diff_valid = false;
   float ratio_x = 0.f, ratio_y = 0.f;
@@ -100,7 +101,9 @@ struct dtsgb_dts_s {
   size_t tsize() const { return st == Storage::F32 ? 4 : 2; }
   DtsLaunch launch_b() const { return DtsLaunch{d_inst, d_tb, ntb, 1}; }
   bool small = false;
-  DtsLaunch launch_i() const { return DtsLaunch{d_inst, d_ti, nti, 1, small}; }
+  DtsLaunch launch_i() const {
+    return DtsLaunch{d_inst, d_ti, nti, 1, small, small ? nullptr : d_ti_small, nti_small};
+  }
 };
 
 static int dts_layout(dtsgb_dts_t h) {
@@ -114,6 +117,14 @@ static int dts_layout(dtsgb_dts_t h) {
                : make_tiles(h->w, h->h, kIterTW, kIterTH);
   h->ntb = (int)tb.size();
   h->nti = (int)ti.size();
+  if (!h->small) {
+    // small tiles too, for halos that do not fit the big tiles' shared memory
+    std::vector<Tile> ts = make_tiles(h->w, h->h, kIterSmallTW, kIterSmallTH);
+    h->nti_small = (int)ts.size();
+    DTSGB_CUDA(cudaMemcpyAsync(h->d_ti_small, ts.data(), ts.size() * sizeof(Tile),
+                               cudaMemcpyHostToDevice, h->stream));
+    DTSGB_CUDA(cudaStreamSynchronize(h->stream));
+  }
   DTSGB_CUDA(cudaMemcpyAsync(h->d_inst, &h->h_inst, sizeof(Inst),
                              cudaMemcpyHostToDevice, h->stream));
   DTSGB_CUDA(cudaMemcpyAsync(h->d_tb, tb.data(), tb.size() * sizeof(Tile),
@@ -136,6 +147,7 @@ static void dts_free(dtsgb_dts_t h) {
   dfree(h->d_inst);
   dfree(h->d_tb);
   dfree(h->d_ti);
+  dfree(h->d_ti_small);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   h->stream = nullptr;
 }
@@ -180,6 +192,7 @@ DTSGB_API int dtsgb_dts_create(int max_w, int max_h, unsigned flags,
   if (!st) st = dalloc(&h->d_inst, 1);
   if (!st) st = dalloc(&h->d_tb, ntiles_b);
   if (!st) st = dalloc(&h->d_ti, ntiles_i);
+  if (!st) st = dalloc(&h->d_ti_small, ntiles_i);
   if (!st) st = dts_layout(h);
   if (st) {
     if (st == DTSGB_ERR_CUDA && g_last_error.find("memory") != std::string::npos)

@@ -137,6 +137,18 @@ struct DtsLaunch {
   int n_tiles;
   int n_inst;
   bool small = false;   // iteration tiles of kIterSmallTW x kIterSmallTH
+  // kIterSmallTW x kIterSmallTH tiles, used when a halo is too large for the
+  // shared memory of the big tiles (null: none)
+  const Tile* d_tiles_small = nullptr;
+  int n_tiles_small = 0;
+  // the same launch on the small tiles
+  DtsLaunch as_small() const {
+    DtsLaunch s = *this;
+    s.d_tiles = d_tiles_small;
+    s.n_tiles = n_tiles_small;
+    s.small = true;
+    return s;
+  }
 };
 
 // Tile shapes (compile-time in the kernels).
@@ -213,8 +225,9 @@ struct DtsGrad {
   float* const* segbuf;  // seg planes for the recomputed iterates of a segment
   float* g[2];           // adjoint ping-pong; g[0] holds dL/dv_N on entry
 };
-// ceil(sqrt(num_iterations)): the segment length that minimises the planes
-// held, ceil(N/seg) - 1 + seg.
+// The segment length that minimises the planes held, ceil(N/seg) - 1 + seg
+// (near sqrt(N)), taking the smallest such length, which recomputes the
+// fewest iterations.
 int dts_checkpoint_segment(int num_iterations);
 // The forward solve (init + num_iterations fused iterations, no overwrite),
 // writing v_seg, v_2seg, ... into G.cp; the result ends in v0 or v1

@@ -36,6 +36,9 @@ struct HfbsBatch {
   // group (0: all instances together); see hfbs_enqueue_solve
   const HInst* h_inst = nullptr;
   long long group_voxels = 0;
+  // the bistochastized normalisation in n0 / n1 (by the parity of
+  // bistoch_iter_max) is that of the same guide and grid: skip recomputing it
+  bool reuse_norm = false;
   long long max_voxels, max_pixels, max_cells, max_lines;
   long long max_rows;  // max over instances of gy * gl (grid rows along x)
   int max_gl;

@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(64)
             float* __restrict__ count, float* __restrict__ csum,
             float* __restrict__ b, float* __restrict__ ovf, HParams p) {
   extern __shared__ float sh[];
+  __shared__ int lbin[256];  // luma bin of each 8-bit luma value
   const HInst I = insts[blockIdx.y];
   const int ncell = I.gx * I.gy;
   const int cell = blockIdx.x * blockDim.x + threadIdx.x;
@@ -57,6 +58,9 @@ __global__ void __launch_bounds__(64)
   float* hist = sh;
   const int T = blockDim.x;
   if (blockIdx.x * blockDim.x >= ncell) return;
+  for (int l = threadIdx.x; l < 256; l += T)
+    lbin[l] = (int)floorf((float)l * 1.0f / p.sigma_l);
+  __syncthreads();
   for (int k = 0; k < 3 * gl; ++k) hist[k * T + threadIdx.x] = 0.f;
   float ovf_cnt = 0.f;
   if (cell < ncell) {
@@ -67,7 +71,7 @@ __global__ void __launch_bounds__(64)
       const long long row = I.pix_off + (long long)y * I.pitch;
       for (int x = xs; x < xe; ++x) {
         const uchar4 g = guide[row + x];
-        const int bl = (int)floorf((float)g.x * 1.0f / p.sigma_l);
+        const int bl = lbin[g.x];
         const float c = load_f(cnf + row + x);
         const float ct = c * load_f(tgt + row + x);
         if (bl < gl) {
@@ -364,13 +368,14 @@ __global__ void k_solve(const HInst* __restrict__ insts,
   }
 }
 
+constexpr int kSliceXTable = 2048;
+
 __device__ __forceinline__ float slice_pixel(const HInst& I, const float* __restrict__ count,
                                              const float* __restrict__ ovf,
                                              const float* __restrict__ z, const HParams& p,
-                                             int x, int y, unsigned char luma) {
-  const float fx = (float)x * 1.0f / p.sigma_x;
-  const float fy = (float)y * 1.0f / p.sigma_y;
-  const float fz = (float)luma * 1.0f / p.sigma_l;
+                                             int x, float fy, float fz, const float* fxt) {
+  // x * 1.0f / sigma_x from the block's table where it covers x
+  const float fx = x < kSliceXTable ? fxt[x] : (float)x * 1.0f / p.sigma_x;
   const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
   const float wx = fx - x0, wy = fy - y0, wz = fz - z0;
   // the eight corners' loads are all issued before the weighting
@@ -424,20 +429,29 @@ __global__ void k_slice(const HInst* __restrict__ insts,
                         const float* __restrict__ ovf,
                         const float* __restrict__ z, float* __restrict__ out,
                         HParams p) {
+  // the reference's x/sx and L/sl (correctly rounded divisions) are the same
+  // for every row: computed once per block into tables
+  __shared__ float fxt[kSliceXTable];
+  __shared__ float fzt[256];
   const HInst I = insts[blockIdx.y];
+  for (int i = threadIdx.x; i < min(I.w, kSliceXTable); i += blockDim.x)
+    fxt[i] = (float)i * 1.0f / p.sigma_x;
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) fzt[i] = (float)i * 1.0f / p.sigma_l;
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
   const uchar4* g = guide + I.pix_off;
   float* o = out + I.pix_off;
   for (int y = blockIdx.x * wpb + (threadIdx.x >> 5); y < I.h; y += gridDim.x * wpb) {
     const int row = y * I.pitch;
+    const float fy = (float)y * 1.0f / p.sigma_y;
     for (int x0 = lane; x0 < I.w; x0 += 64) {
       const int x1 = x0 + 32;
-      const unsigned char l0 = g[row + x0].x;
-      const unsigned char l1 = x1 < I.w ? g[row + x1].x : 0;
-      const float r0 = slice_pixel(I, count, ovf, z, p, x0, y, l0);
+      const float z0 = fzt[g[row + x0].x];
+      const float z1 = x1 < I.w ? fzt[g[row + x1].x] : 0.f;
+      const float r0 = slice_pixel(I, count, ovf, z, p, x0, fy, z0, fxt);
       if (x1 < I.w) {
-        const float r1 = slice_pixel(I, count, ovf, z, p, x1, y, l1);
+        const float r1 = slice_pixel(I, count, ovf, z, p, x1, fy, z1, fxt);
         o[row + x1] = r1;
       }
       o[row + x0] = r0;
@@ -467,7 +481,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   const size_t splat_smem = sizeof(float) * 3 * (size_t)B.max_gl * 64;
   prof_begin(s, DTSGB_K_HFBS_SPLAT);
   if (B.st == Storage::F32) {
-    if (splat_smem > 48 * 1024)
+    if (splat_smem + sizeof(int) * 256 > 48 * 1024)  // plus the static luma table
       DTSGB_CUDA(cudaFuncSetAttribute(k_splat<float>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)splat_smem));
@@ -475,7 +489,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
         B.d_inst, B.guide, (const float*)B.target, (const float*)B.conf, B.count,
         B.csum, B.b, B.ovf, p);
   } else {
-    if (splat_smem > 48 * 1024)
+    if (splat_smem + sizeof(int) * 256 > 48 * 1024)  // plus the static luma table
       DTSGB_CUDA(cudaFuncSetAttribute(k_splat<__nv_bfloat16>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)splat_smem));
@@ -487,7 +501,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   prof_end(s, DTSGB_K_HFBS_SPLAT);
   // bistochastization ping-pong: even iterations read the buffer filled with
   // ones, whose covered pad faces hold 1
-  k_fill_ones<<<gv, kT, 0, s>>>(B.d_inst, B.n0);
+  if (!B.reuse_norm) k_fill_ones<<<gv, kT, 0, s>>>(B.d_inst, B.n0);
   // The iterative stages (bistochastization, heavy-ball) touch only their own
   // instance's grid, so they run group by group: all iterations of a group
   // of consecutive instances whose grids fit in L2 before the next group,
@@ -525,6 +539,10 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   for (const Group& g : groups) {
     src = B.n0;
     dst = B.n1;
+    if (B.reuse_norm) {
+      if (p.bistoch_iter_max % 2) std::swap(src, dst);
+      continue;
+    }
     for (int it = 0; it < p.bistoch_iter_max; ++it) {
       prof_begin(s, DTSGB_K_HFBS_BISTOCH);
       k_bistoch<<<col_grid(g), kT, 0, s>>>(B.d_inst + g.first, src, dst, B.count,

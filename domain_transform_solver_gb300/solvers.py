@@ -36,6 +36,7 @@ __all__ = [
     "DomainTransformFilter", "DomainTransformSolver", "HFBS", "DtsOptions",
     "HfbsOptions", "Solve", "EdgeAwareOptimize", "DtsgbError",
     "FLAG_BF16_STORAGE", "FLAG_FIX_Y_LIMIT", "TUNE_DTS_TILE", "TUNE_HFBS_GROUP_VOXELS",
+    "TUNE_REUSE_GUIDE_STATE",
     "Batch", "DomainTransformStereo",
 ]
 
@@ -45,6 +46,7 @@ FLAG_FILTER_ONLY = 0x4
 FLAG_STEREO = 0x8
 TUNE_DTS_TILE = 0
 TUNE_HFBS_GROUP_VOXELS = 1
+TUNE_REUSE_GUIDE_STATE = 2
 
 
 @dataclass
@@ -429,6 +431,18 @@ class Batch:
                                            _ptr_array(tg),
                                            None if cf is None else _ptr_array(cf)))
 
+    def upload_targets(self, target, confidence=None) -> None:
+        """New target / confidence for the same guides (video frames): the
+        guide-derived window bounds and HFBS normalisation are kept."""
+        tg = [_f32(a, (h, w)) for a, (w, h) in zip(target, self.sizes)]
+        cf = None
+        if confidence is not None:
+            cf = [None if a is None else _f32(a, (h, w))
+                  for a, (w, h) in zip(confidence, self.sizes)]
+        self._keep_t = (tg, cf)
+        check(self._lib.dtsgb_batch_upload_targets(self._h, _ptr_array(tg),
+                                                   None if cf is None else _ptr_array(cf)))
+
     def solve_dts(self, filter_params: DomainFilterParams,
                   optimize_params: DomainOptimizeParams,
                   overwrite_target_above_conf: float = -1) -> None:
@@ -480,7 +494,7 @@ class Batch:
     # ---- gradients of the DTS solve (no reference counterpart) --------------
     def enable_grad(self, enable: bool = True, segment: int = 0) -> None:
         """Keep checkpoints in solve_dts every `segment` iterations
-        (0 = ceil(sqrt(N))) so that backward() can run."""
+        (0 = automatic, near sqrt(N)) so that backward() can run."""
         check(self._lib.dtsgb_batch_enable_grad(self._h, int(enable), int(segment)))
 
     def grad_info(self):

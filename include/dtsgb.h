@@ -302,6 +302,13 @@ DTSGB_API int dtsgb_batch_upload_device(dtsgb_batch_t b, int color_space,
                                         const void* const* rgba,
                                         const float* const* target,
                                         const float* const* confidence);
+/* Replace target and confidence only; the guide (and the state derived
+ * from it) is kept.  n host / device pointers as in dtsgb_batch_upload. */
+DTSGB_API int dtsgb_batch_upload_targets(dtsgb_batch_t b, const float* const* target,
+                                         const float* const* confidence);
+DTSGB_API int dtsgb_batch_upload_targets_device(dtsgb_batch_t b,
+                                                const float* const* target,
+                                                const float* const* confidence);
 DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b,
                                     const dtsgb_filter_params* filter,
                                     const dtsgb_optimize_params* optimize,
@@ -324,6 +331,12 @@ DTSGB_API int dtsgb_batch_download_device(dtsgb_batch_t b, int which,
  * (HFBS: bitwise identical). */
 #define DTSGB_TUNE_DTS_TILE 0
 #define DTSGB_TUNE_HFBS_GROUP_VOXELS 1
+/* DTSGB_TUNE_REUSE_GUIDE_STATE (default 1): while the guide is unchanged
+ * (dtsgb_batch_upload_targets between solves, as for video frames whose
+ * target changes), a DTS solve with the same sigmas keeps the window bounds
+ * and an HFBS solve with the same grid keeps the bistochastized
+ * normalisation instead of recomputing them; results are identical. */
+#define DTSGB_TUNE_REUSE_GUIDE_STATE 2
 DTSGB_API int dtsgb_batch_set_tuning(dtsgb_batch_t b, int knob, long long value);
 DTSGB_API int dtsgb_batch_get_tuning(dtsgb_batch_t b, int knob, long long* value);
 /* Times the uploaded batch's solves under each tile shape (filter and
@@ -337,7 +350,9 @@ DTSGB_API int dtsgb_batch_autotune(dtsgb_batch_t b, const dtsgb_filter_params* f
 
 /* ---- Gradients of the batched DTS solve (new; the reference has no
  * gradients).  With gradients enabled, dtsgb_batch_solve_dts also keeps the
- * iterate v_k every `segment` iterations (0 = ceil(sqrt(num_iterations))),
+ * iterate v_k every `segment` iterations (0 = automatic: the length that
+ * holds the fewest planes, near sqrt(num_iterations), and of those the
+ * shortest),
  * and dtsgb_batch_dts_backward maps an upstream gradient dL/dv of each DTS
  * result to dL/dtarget and dL/dconfidence of the same solve.  The window
  * bounds found from the guide are held fixed: they are piecewise constant in
@@ -348,7 +363,9 @@ DTSGB_API int dtsgb_batch_autotune(dtsgb_batch_t b, const dtsgb_filter_params* f
  * return the target, so dL/dtarget = dL/dv.  A solve with the confidence
  * overwrite in (0,1) returns DTSGB_ERR_UNSUPPORTED while gradients are on.
  * For BF16 storage the derivative is taken at the BF16-rounded target and
- * confidence.  grad_target / grad_confidence (n pointers, W*H floats) may be
+ * confidence.  The adjoint's tile holds sigma_z below 80 (larger values
+ * return DTSGB_ERR_UNSUPPORTED from the backward; the forward takes any
+ * sigma_z below 254).  grad_target / grad_confidence (n pointers, W*H floats) may be
  * NULL or hold NULL entries to skip an output. */
 DTSGB_API int dtsgb_batch_enable_grad(dtsgb_batch_t b, int enable, int segment);
 /* segment length and planes held by the last solve (0, 0 before any). */
@@ -360,6 +377,13 @@ DTSGB_API int dtsgb_batch_dts_backward_device(dtsgb_batch_t b,
                                               const float* const* grad_out,
                                               float* const* grad_target,
                                               float* const* grad_confidence);
+
+/* ---- Host-side image helper (no counterpart: the reference's drivers decode
+ * PNG with OpenCV).  Undoes the PNG row filters (types 0-4) of `height` rows
+ * of `stride` bytes, each preceded by its filter byte in `raw`, with `bpp`
+ * bytes per pixel; writes height * stride bytes to `out`. */
+DTSGB_API int dtsgb_png_unfilter(const unsigned char* raw, int height, int stride,
+                                 int bpp, unsigned char* out);
 
 #ifdef __cplusplus
 }

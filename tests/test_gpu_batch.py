@@ -127,3 +127,81 @@ def test_tuning_knobs_and_autotune(gpu_ready):
     assert b.get_tuning(D.TUNE_HFBS_GROUP_VOXELS) in (0, 1000000, 2000000, 4000000, 8000000)
     for a, r in zip(b.download(1), ref_h):
         assert np.array_equal(a, r, equal_nan=True)
+
+
+def test_video_frames_reuse_guide_state(gpu_ready):
+    """Frames that change only the target (upload_targets) keep the window
+    bounds and the HFBS normalisation: results equal a fresh batch's bitwise,
+    and a changed sigma or a new guide recomputes them."""
+    D = gpu_ready
+    from domain_transform_solver_gb300 import workloads as W
+    insts = _instances(SIZES[:4])
+    sizes = [(i.width, i.height) for i in insts]
+    rng = np.random.default_rng(5)
+    frames = [[(i.target * (1.0 + 0.1 * k) + rng.normal(0, 0.01, i.target.shape))
+               .astype(np.float32) for i in insts] for k in range(3)]
+    fp = D.DomainFilterParams(**W.CFG0_FILTER)
+    hp = D.HFBSGridParams(**dict(W.CFG1_HFBS, optim_iter_max=8))
+    b = D.Batch(sizes)
+    b.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in insts], frames[0],
+             [i.confidence for i in insts])
+    for k, frame in enumerate(frames):
+        sz = 8.0 if k < 2 else 6.0  # the last frame changes sigma_z
+        op = D.DomainOptimizeParams(**dict(W.CFG0_OPT, num_iterations=4, sigma_z=sz))
+        if k:
+            b.upload_targets(frame, [i.confidence for i in insts])
+        b.solve_dts(fp, op)
+        b.solve_hfbs(hp)
+        fresh = D.Batch(sizes, use_graphs=False)
+        fresh.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)
+        fresh.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in insts], frame,
+                     [i.confidence for i in insts])
+        fresh.solve_dts(fp, op)
+        fresh.solve_hfbs(hp)
+        for a, r in zip(b.download(0), fresh.download(0)):
+            assert np.array_equal(a, r)
+        for a, r in zip(b.download(1), fresh.download(1)):
+            assert np.array_equal(a, r, equal_nan=True)
+    # a new guide invalidates the kept state
+    rgba2 = [np.ascontiguousarray(i.rgba[::-1]) for i in insts]
+    b.upload(D.COLOR_SPACE.YCbCr, rgba2, frames[0], [i.confidence for i in insts])
+    op = D.DomainOptimizeParams(**dict(W.CFG0_OPT, num_iterations=4))
+    b.solve_dts(fp, op)
+    fresh = D.Batch(sizes)
+    fresh.upload(D.COLOR_SPACE.YCbCr, rgba2, frames[0], [i.confidence for i in insts])
+    fresh.solve_dts(fp, op)
+    for a, r in zip(b.download(0), fresh.download(0)):
+        assert np.array_equal(a, r)
+
+
+def test_large_halos(gpu_ready):
+    """sigma_z = 100 exceeds the tile-staged kernel's shared memory on 64 x 64
+    tiles (the large-halo kernel runs instead); sigma_z = 200 exceeds both
+    kernels there and runs on 32 x 32 tiles.  Class API and batch agree
+    bitwise on the same tiles; the tile shapes agree to FP32 rounding."""
+    D = gpu_ready
+    from domain_transform_solver_gb300 import workloads as W
+    inst = W.depth_sr_instance(77, 2560, 1024, n_poly=12, sample_frac=0.05)
+    fp = D.DomainFilterParams(**W.CFG0_FILTER)
+    rng_t = float(inst.target.max() - inst.target.min())
+    for sz in (100.0, 200.0):
+        op = D.DomainOptimizeParams(**dict(W.CFG0_OPT, num_iterations=2, sigma_z=sz))
+        s = D.DomainTransformSolver(D.ImageDim(2560, 1024))
+        s.InitFrame(D.COLOR_SPACE.YCbCr, inst.rgba, inst.target, inst.confidence)
+        s.ComputeColorSpaceDifferential(fp)
+        s.IntegrateColorDifferentials()
+        s.Optimize(op)
+        v = s.Download(D.ImageType.OPTIMIZED_QUANTITY)
+        assert np.isfinite(v).all()
+        outs = {}
+        for tile in (64, 32):
+            b = D.Batch([(2560, 1024)])
+            assert b.get_tuning(D.TUNE_DTS_TILE) == 64
+            b.set_tuning(D.TUNE_DTS_TILE, tile)
+            b.upload(D.COLOR_SPACE.YCbCr, [inst.rgba], [inst.target], [inst.confidence])
+            b.solve_dts(fp, op)
+            outs[tile] = b.download(0)[0]
+        assert np.array_equal(v, outs[64])
+        assert np.abs(outs[64] - outs[32]).max() <= 1e-6 * rng_t
+        if sz == 200.0:
+            assert np.array_equal(outs[64], outs[32])
