@@ -153,10 +153,13 @@ struct DtsLaunch {
 
 // Tile shapes (compile-time in the kernels).
 constexpr int kBoundsTW = 32, kBoundsTH = 32;
-constexpr int kIterTW = 64, kIterTH = 64;
-// Images too small to give every SM a few 64x64 tiles use 32x32 tiles.
+constexpr int kIterTW = 64, kIterTH = 128;
+// Work too small to give every SM a few 64x64-pixel blocks (under about
+// 2.5 Mpx in all) uses 32x32 tiles.  tiles_big counts kIterTW x kIterTH tiles.
 constexpr int kIterSmallTW = 32, kIterSmallTH = 32;
-inline bool use_small_iter_tiles(long long tiles64) { return tiles64 < 4 * 152; }
+inline bool use_small_iter_tiles(long long tiles_big) {
+  return tiles_big * kIterTW * kIterTH < 4LL * 152 * 64 * 64;
+}
 
 int launch_color_convert(const Inst* h_inst, const Inst* d_inst, int n_inst,
                          uchar4* guide, int color_space, cudaStream_t s);

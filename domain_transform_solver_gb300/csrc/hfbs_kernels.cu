@@ -368,6 +368,120 @@ __global__ void k_solve(const HInst* __restrict__ insts,
   }
 }
 
+// a16, K steps per pass (temporal blocking).  A CTA loads a 24 x 24 block of
+// (x, y) columns, a 16 x 16 tile plus a K = 4 column halo, with all l levels;
+// each thread keeps the z, h and n of its column in registers (b and invA
+// in shared memory) and the z * n products of a step go through shared
+// memory to the x and y neighbours.  Step k updates the columns at least k
+// inside the block, whose neighbours the previous step updated, so after K
+// steps the tile is exact.  Outside the grid (and above level gl) z = n = 0,
+// so z * n there adds zero to a neighbour sum without bounds tests.  The
+// neighbour sum adds the six rounded products in the reference's order
+// (x-1, x+1, y-1, y+1, l-1, l+1).  HBM traffic is about a quarter of four
+// one-step passes: the halo comes from L2.  h ping-pongs between hs and hd
+// because a neighbouring CTA reads the old h of this tile's columns as its
+// halo.
+//
+// The block arrives by 4-byte cp.async copies (zero-filled outside the grid),
+// all in flight at once without holding registers; z, h and n are staged in
+// the space the z * n buffers use afterwards.  Every thread reads and writes
+// only its own column there, so the reuse needs no barrier.
+constexpr int kTBT = 16, kTBK = 4, kTBL = kTBT + 2 * kTBK;
+constexpr int kTBMaxGL = 16;
+constexpr int kTBThreads = kTBL * kTBL;  // one thread per (x, y) column
+constexpr int kTBPlane = kTBMaxGL * kTBThreads;  // floats per staged array
+// b, invA, then z, h, n staged (later z * n, double-buffered)
+constexpr size_t kTBSmem = sizeof(float) * 5 * kTBPlane;
+
+// True when column (xx, yy) of a temporally blocked block is updated at step
+// k: it lies at least k columns inside the block.
+__device__ __forceinline__ bool tb_active(int xx, int yy, int k) {
+  return xx >= k && xx < kTBL - k && yy >= k && yy < kTBL - k;
+}
+
+// 4-byte global -> shared copy; copies zero bytes (the destination is
+// zero-filled) when !valid, and src must then still be a mapped address.
+__device__ __forceinline__ void cp_async_f32(float* dst, const float* src, bool valid) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src),
+               "r"(valid ? 4 : 0)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(kTBThreads, 1)
+    k_solve_tb(const HInst* __restrict__ insts, const float* __restrict__ zs,
+               float* __restrict__ zd, const float* __restrict__ hs, float* __restrict__ hd,
+               const float* __restrict__ norm, const float* __restrict__ b,
+               const float* __restrict__ invA, float lambda, float alpha, float beta,
+               int steps) {
+  extern __shared__ float tb_s[];
+  float* Bs = tb_s;
+  float* As = Bs + kTBPlane;
+  float* R = As + kTBPlane;  // z, h, n staging; then z * n [2]
+  const HInst I = insts[blockIdx.y];
+  const int gx = I.gx, gy = I.gy, gl = I.gl;  // gl <= kTBMaxGL (host checks)
+  const int tiles_x = (gx + kTBT - 1) / kTBT;
+  if ((int)blockIdx.x >= tiles_x * ((gy + kTBT - 1) / kTBT)) return;
+  const int ty = blockIdx.x / tiles_x, tx = blockIdx.x - ty * tiles_x;
+  const int c = threadIdx.x, yy = c / kTBL, xx = c - yy * kTBL;
+  const int x = tx * kTBT - kTBK + xx, y = ty * kTBT - kTBK + yy;
+  const bool in = x >= 0 && x < gx && y >= 0 && y < gy;
+  const int plane = gx * gy, col = in ? y * gx + x : 0;
+  const long long g0 = I.grid_off + col;
+#pragma unroll
+  for (int l = 0; l < kTBMaxGL; ++l) {
+    const bool v = in && l < gl;
+    const long long i = g0 + (v ? (long long)l * plane : 0);
+    cp_async_f32(R + l * kTBThreads + c, zs + i, v);
+    cp_async_f32(R + kTBPlane + l * kTBThreads + c, hs + i, v);
+    cp_async_f32(R + 2 * kTBPlane + l * kTBThreads + c, norm + i, v);
+    cp_async_f32(Bs + l * kTBThreads + c, b + i, v);
+    cp_async_f32(As + l * kTBThreads + c, invA + i, v);
+  }
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+  float z[kTBMaxGL], h[kTBMaxGL], n[kTBMaxGL];
+#pragma unroll
+  for (int l = 0; l < kTBMaxGL; ++l) {
+    z[l] = R[l * kTBThreads + c];
+    h[l] = R[kTBPlane + l * kTBThreads + c];
+    n[l] = R[2 * kTBPlane + l * kTBThreads + c];
+  }
+  for (int k = 1; k <= steps; ++k) {
+    float* P = R + (k & 1) * kTBPlane;
+#pragma unroll
+    for (int l = 0; l < kTBMaxGL; ++l) P[l * kTBThreads + c] = z[l] * n[l];
+    __syncthreads();
+    if (in && tb_active(xx, yy, k)) {
+      float below = 0.f, cur = z[0] * n[0];
+#pragma unroll
+      for (int l = 0; l < kTBMaxGL; ++l) {
+        const float above = l + 1 < kTBMaxGL ? z[l + 1] * n[l + 1] : 0.f;
+        const float* q = P + l * kTBThreads + c;
+        const float d = q[-1] + q[1] + q[-kTBL] + q[kTBL] + below + above;
+        const float qb = (Bs[l * kTBThreads + c] + lambda * n[l] * d) * As[l * kTBThreads + c];
+        const float grad = z[l] - qb;
+        // |grad| > 1.345 with the double threshold of the reference: the
+        // smallest float above 1.345 (double) is 1.345f
+        const float gc = fabsf(grad) >= 1.345f ? copysignf(1.f, grad) : grad;
+        h[l] = __fmaf_rn(beta, h[l], gc);
+        z[l] = z[l] - alpha * h[l];
+        below = cur;
+        cur = above;
+      }
+    }
+  }
+  if (in && xx >= kTBK && xx < kTBK + kTBT && yy >= kTBK && yy < kTBK + kTBT) {
+    float* zo = zd + g0;
+    float* ho = hd + g0;
+#pragma unroll
+    for (int l = 0; l < kTBMaxGL; ++l)
+      if (l < gl) {
+        zo[l * plane] = z[l];
+        ho[l * plane] = h[l];
+      }
+  }
+}
+
 constexpr int kSliceXTable = 2048;
 
 __device__ __forceinline__ float slice_pixel(const HInst& I, const float* __restrict__ count,
@@ -576,6 +690,38 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   }
   float* zs = B.z0;
   float* zd = B.z1;
+  if (B.max_gl <= kTBMaxGL && B.h_inst) {
+    // K heavy-ball steps per pass; h ping-pongs through the free blur
+    // temporary t2 (its final value is not needed)
+    static bool attr = false;
+    if (!attr) {
+      DTSGB_CUDA(cudaFuncSetAttribute(k_solve_tb, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kTBSmem));
+      attr = true;
+    }
+    for (const Group& g : groups) {
+      zs = B.z0;
+      zd = B.z1;
+      float* hs = B.h;
+      float* hd = B.t2;
+      long long tiles = 1;
+      for (int i = 0; i < g.count; ++i) {
+        const HInst& H = B.h_inst[g.first + i];
+        tiles = std::max(tiles, (long long)((H.gx + kTBT - 1) / kTBT) * ((H.gy + kTBT - 1) / kTBT));
+      }
+      const dim3 gt((unsigned)tiles, g.count);
+      for (int it = 0; it < p.optim_iter_max; it += kTBK) {
+        const int steps = std::min(kTBK, p.optim_iter_max - it);
+        prof_begin(s, DTSGB_K_HFBS_SOLVE);
+        k_solve_tb<<<gt, kTBThreads, kTBSmem, s>>>(B.d_inst + g.first, zs, zd, hs, hd, norm,
+                                                    B.b, B.invA, p.lambda, p.alpha, p.beta,
+                                                    steps);
+        prof_end(s, DTSGB_K_HFBS_SOLVE);
+        std::swap(zs, zd);
+        std::swap(hs, hd);
+      }
+    }
+  } else
   for (const Group& g : groups) {
     zs = B.z0;
     zd = B.z1;

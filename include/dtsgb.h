@@ -321,9 +321,10 @@ DTSGB_API int dtsgb_batch_download(dtsgb_batch_t b, int which,
 DTSGB_API int dtsgb_batch_download_device(dtsgb_batch_t b, int which,
                                           float* const* dst);
 
-/* ---- Tuning (new).  DTSGB_TUNE_DTS_TILE: side of the square tiles of the
- * fused DTS iteration and its adjoint, 64 or 32 (default: 32 when the batch
- * has fewer than 4 x 152 tiles of 64 x 64).  DTSGB_TUNE_HFBS_GROUP_VOXELS:
+/* ---- Tuning (new).  DTSGB_TUNE_DTS_TILE: tile width of the fused DTS
+ * iteration and its adjoint, 64 (64 x 128 tiles) or 32 (32 x 32 tiles;
+ * the default when the batch holds under 4 x 152 x 64 x 64 pixels).
+ * DTSGB_TUNE_HFBS_GROUP_VOXELS:
  * the HFBS iterations run over groups of consecutive instances holding at
  * most this many grid voxels, all iterations of one group before the next,
  * so that a group's grids can stay in L2 (0, the default: all instances at

@@ -175,7 +175,7 @@ def test_video_frames_reuse_guide_state(gpu_ready):
 
 
 def test_large_halos(gpu_ready):
-    """sigma_z = 100 exceeds the tile-staged kernel's shared memory on 64 x 64
+    """sigma_z = 100 exceeds the tile-staged kernel's shared memory on 64 x 128
     tiles (the large-halo kernel runs instead); sigma_z = 200 exceeds both
     kernels there and runs on 32 x 32 tiles.  Class API and batch agree
     bitwise on the same tiles; the tile shapes agree to FP32 rounding."""
