@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(kThreads)
 
 // ---------------------------------------------------------------------------
 // One solver iteration (a6/a7): the X half-step followed by the Y half-step
-// in one kernel (k_dts_iter_tile below).  A CTA owns a TWxTH output tile;
+// in one kernel (k_dts_iter_vec below).  A CTA owns a TWxTH output tile;
 // the X half-step is evaluated for the tile columns over the tile rows plus
 // a vertical halo of floor(sigma) (those rows feed the Y windows), kept in
 // shared memory, and the Y half-step writes the tile.  HBM traffic per pixel
@@ -194,45 +194,6 @@ __device__ __forceinline__ float photometric(const StereoArgs& sa, long long row
   return sa.lam_p * 2.f * sad * (__fmaf_rn(gr, gr, -1.f) * sa.alpha);
 }
 
-// ---------------------------------------------------------------------------
-// Fused X+Y iteration with window sums from fixed-point prefix sums
-// (fixed_point.cuh): a window sum is P[p+du] - P[p-dl] of a wrapping 32-bit
-// integer prefix, exact for the converted values.
-//
-// Phases of one CTA (TW x TH tile, halos hx, hy; SR = TH + 2hy rows):
-//  1. stage the iterate over SR rows x (TW + 2hx + 1) prefix entries
-//     (entry 0 is a zero left of every window) into shared memory, with
-//     coalesced loads, and reduce its largest magnitude (the X scale);
-//  2. convert in place and scan: one thread per 16-entry segment of a row,
-//     then segment offsets are added;
-//  3. X half-step for the tile columns over all SR rows (one thread per
-//     pixel, independent loads of bounds, target, confidence, iterate),
-//     results kept in shared memory with their largest magnitude (the Y
-//     scale);
-//  4. Y prefix per column in segments, offsets added;
-//  5. Y half-step for the tile, written coalesced.
-// Reciprocals 1/n come from a per-block table of correctly rounded values.
-// ---------------------------------------------------------------------------
-constexpr int kXSeg = 16;  // prefix entries per thread in the X scan
-
-template <int TW, int TH, int NT>
-struct TileIterSmem {
-  int swxp, nsx, pyn, xs_off, sx_off, sby_off, segy_off, rt_off, mx_off, total;
-  __host__ __device__ TileIterSmem(int hx, int hy) {
-    const int SR = TH + 2 * hy, SWX = TW + 2 * hx + 1;
-    swxp = (SWX + 3) & ~3;
-    nsx = (swxp + kXSeg - 1) / kXSeg;
-    pyn = max(SR * swxp, (SR + 1) * TW);  // X prefix, later the Y prefix
-    xs_off = pyn * 4;                                   // X segment totals
-    sx_off = xs_off + SR * nsx * 4;                     // SR x (TW+1) f32
-    sby_off = sx_off + SR * (TW + 1) * 4;               // SR x TW u16
-    segy_off = (sby_off + SR * TW * 2 + 3) & ~3;        // NT/TW x TW u32
-    rt_off = segy_off + (NT / TW) * TW * 4;             // reciprocal table
-    mx_off = rt_off + (2 * max(hx, hy) + 2) * 4;
-    total = mx_off + 16;
-  }
-};
-
 // v = t where c > overwrite, in place (DomainTransformSolver::Optimize's
 // overwrite before the X half-step, src/domain_transform_solver.cu:126-130).
 template <typename TS>
@@ -246,236 +207,349 @@ __global__ void k_overwrite(const Inst* __restrict__ insts, float* __restrict__ 
     if (load_f(cnf + in.off + i) > overwrite) v[in.off + i] = load_f(tgt + in.off + i);
 }
 
+// ---------------------------------------------------------------------------
+// The fused X+Y iteration with four adjacent pixels per thread
+// (k_dts_iter_vec): every global access is a 16-byte (f32) or 8-byte (bf16)
+// vector.  Tiles start at
+// multiples of 4 pixels and planes at multiples of 32 elements with a pitch
+// of a multiple of 32, so every group of four is aligned and lies inside
+// its row's pitch.  Phases of one CTA (TW x TH tile, halos hx, hy; SR = TH +
+// 2hy rows):
+//  1. stage the iterate over SR rows x SW columns, from HA >= hx + 1
+//     columns left of the tile (SW and HA multiples of 4), and reduce its
+//     largest magnitude (the X scale);
+//  2. the rows are converted to fixed point and scanned: a thread per
+//     16-entry segment, then the segment offsets are added;
+//  3. X half-step for the tile columns over all SR rows, four pixels per
+//     thread, the next group's loads in flight while one is computed;
+//     results and the Y bounds kept in shared memory with their largest
+//     magnitude (the Y scale);
+//  4. Y prefix: one warp per group of four columns, one lane per segment of
+//     rows, segment offsets from a warp scan;
+//  5. Y half-step for the tile, four pixels per thread, vector stores.
+// ---------------------------------------------------------------------------
+// i / d for 0 <= i < 2^16 and 2 <= d < 2^16 with m = ceil(2^32 / d): the
+// error term i * (m * d - 2^32) / (d * 2^32) stays below 1 / d.
+__host__ __forceinline__ unsigned fast_div_magic(unsigned d) {
+  return (unsigned)((0x100000000ull + d - 1) / d);
+}
+__device__ __forceinline__ int fast_div(int i, unsigned m) {
+  return (int)__umulhi((unsigned)i, m);
+}
+
+template <int TW, int TH, int NT>
+struct VecIterSmem {
+  int ha, sw, sws, sr, nsx, seg, sx_off, sby_off, rt_off, mx_off, total;
+  unsigned sw4_magic, sr_magic;  // fast_div_magic(sw / 4), fast_div_magic(sr)
+  __host__ VecIterSmem(int hx, int hy) {
+    constexpr int TQ = TW + 4;  // sx / Py row stride: 16 bytes mod 128
+    ha = (hx + 4) & ~3;
+    sw = ha + TW + ((hx + 3) & ~3);
+    // X row stride: an odd number of 16-byte chunks, so that 8 consecutive
+    // rows start in 8 different chunks of the banks
+    sws = ((sw >> 2) & 1) ? sw : sw + 4;
+    nsx = (sw + 15) / 16;  // 16-entry scan segments per row
+    sr = TH + 2 * hy;
+    // rows per lane in the Y scan; odd, so that the 32 lanes' rows spread
+    // over all banks
+    seg = ((sr + 1 + 31) / 32) | 1;
+    sx_off = max(sr * sws, (sr + 1) * TQ) * 4;  // X prefix, later the Y prefix
+    sby_off = sx_off + sr * TQ * 4;
+    rt_off = sby_off + sr * TW * 2;
+    mx_off = rt_off + ((2 * max(hx, hy) + 2) * 4 + 15) / 16 * 16;
+    total = mx_off + 16;
+    sw4_magic = fast_div_magic((unsigned)(sw >> 2));
+    sr_magic = fast_div_magic((unsigned)sr);
+  }
+};
+
+// Four consecutive storage values, kept packed until they are used.
+template <typename TS>
+struct Raw4;
+template <>
+struct Raw4<float> {
+  float4 v;
+  __device__ __forceinline__ void load(const float* p) {
+    v = __ldg(reinterpret_cast<const float4*>(p));
+  }
+  __device__ __forceinline__ void zero() { v = make_float4(0.f, 0.f, 0.f, 0.f); }
+  __device__ __forceinline__ float operator[](int k) const {
+    return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
+  }
+};
+template <>
+struct Raw4<__nv_bfloat16> {
+  uint2 v;
+  __device__ __forceinline__ void load(const __nv_bfloat16* p) {
+    v = __ldg(reinterpret_cast<const uint2*>(p));
+  }
+  __device__ __forceinline__ void zero() { v = make_uint2(0u, 0u); }
+  // bf16 -> f32 is exact: the 16 bits become the high half
+  __device__ __forceinline__ float operator[](int k) const {
+    const unsigned w = k < 2 ? v.x : v.y;
+    return __uint_as_float((k & 1) ? (w & 0xffff0000u) : (w << 16));
+  }
+};
+
+__device__ __forceinline__ float f4_get(const float4& v, int k) {
+  return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
+}
+__device__ __forceinline__ unsigned u4_get(const uint4& v, int k) {
+  return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
+}
+
 template <typename TS, int MODE, int TW, int TH, int NT, bool STEREO = false>
 __global__ void __launch_bounds__(NT, 1024 / NT)
-    k_dts_iter_tile(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
-                    const float* __restrict__ vin, float* __restrict__ vout,
-                    const TS* __restrict__ tgt, const TS* __restrict__ cnf,
-                    const uint32_t* __restrict__ bnd, float lambda, float step,
-                    float overwrite, int hx, int hy, StereoArgs sa, TileIterSmem<TW, TH, NT> L) {
-  static_assert(TW % 32 == 0 && NT % TW == 0, "tile width: whole warps");
-  constexpr int NSEG = NT / TW, TWp = TW + 1;
+    k_dts_iter_vec(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
+                   const float* __restrict__ vin, float* __restrict__ vout,
+                   const TS* __restrict__ tgt, const TS* __restrict__ cnf,
+                   const uint32_t* __restrict__ bnd, float lambda, float step,
+                   float overwrite, int hx, int hy, StereoArgs sa, VecIterSmem<TW, TH, NT> L) {
+  constexpr int QW = TW / 4, TQ = TW + 4, RPP = NT / QW, NW = NT / 32;
+  static_assert(TW % 32 == 0 && NT % TW == 0 && NW >= QW, "tile shape");
   extern __shared__ __align__(16) unsigned char smraw[];
   const Tile t = tiles[blockIdx.x];
   const Inst in = insts[t.inst];
   const int W = in.w, H = in.h, P = in.pitch;
-  // per-instance bases: every offset below is a 32-bit pixel index
   const float* vin_i = vin + in.off;
   float* vout_i = vout + in.off;
   const TS* tgt_i = tgt + in.off;
   const TS* cnf_i = cnf + in.off;
   const uint32_t* bnd_i = bnd + in.off;
-  const int SR = TH + 2 * hy, SWX = TW + 2 * hx + 1, RY = SR + 1;
-  const int SWXp = L.swxp, NSX = L.nsx;
-  unsigned* XP = reinterpret_cast<unsigned*>(smraw);           // SR x SWXp
-  unsigned* Py = XP;                                           // RY x TW (phase 4)
-  unsigned* segx = reinterpret_cast<unsigned*>(smraw + L.xs_off);  // SR x NSX
-  float* sx = reinterpret_cast<float*>(smraw + L.sx_off);      // SR x TWp
+  const int SR = L.sr, SW = L.sw, SWS = L.sws, HA = L.ha;
+  float* Xf = reinterpret_cast<float*>(smraw);          // SR x SWS: iterate, then
+  unsigned* XP = reinterpret_cast<unsigned*>(smraw);    // its X prefix
+  unsigned* Py = XP;                                    // (SR + 1) x TQ, phase 4
+  float* sx = reinterpret_cast<float*>(smraw + L.sx_off);          // SR x TQ
   uint16_t* sby = reinterpret_cast<uint16_t*>(smraw + L.sby_off);  // SR x TW
-  unsigned* segy = reinterpret_cast<unsigned*>(smraw + L.segy_off);
   float* rtab = reinterpret_cast<float*>(smraw + L.rt_off);
   unsigned* smax = reinterpret_cast<unsigned*>(smraw + L.mx_off);  // [0] X, [1] Y
-  const int tid = threadIdx.x, lane = tid & 31;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nrt = 2 * max(hx, hy) + 2;
   for (int i = tid; i < nrt; i += NT) rtab[i] = i ? __frcp_rn((float)i) : 0.f;
   if (tid < 2) smax[tid] = 0u;
-  __syncthreads();
   const bool over = overwrite > 0.f && overwrite < 1.f;  // v itself is already
                                                           // overwritten
-  const int gx0 = t.x0 - hx - 1;  // image x of X prefix entry 0 (a zero entry)
-  const int gy0 = t.y0 - hy;      // image y of row 0
+  const int xs = t.x0 - HA;   // image x of staged column 0
+  const int gy0 = t.y0 - hy;  // image y of row 0
   const int lgx = ceil_log2(2 * hx + 1), lgy = ceil_log2(2 * hy + 1);
-  // ---- 3'. the X half-step's per-pixel loads, issued early -----------------------
-  // Thread (c, r0) handles tile column c of rows r0, r0 + RS, ...; two rows per
-  // pass.  The first pass's loads are issued before the staging so that their
-  // latency overlaps phases 1-2; each later pass is loaded while the previous
-  // one is computed.
-  constexpr int RS = NT / TW;  // rows per pass step
-  const int c3 = tid % TW, r03 = tid / TW;
-  const int x3 = t.x0 + c3;
-  const bool xok3 = x3 < W;
-  struct Pass {
-    uint32_t b[2];
-    float tv[2], cv[2], vv[2];
+  // ---- 3'. the X half-step's loads for this thread's first group ------------
+  const int cq = tid % QW, r3 = tid / QW;  // group of columns x3 .. x3 + 3
+  const int x3 = t.x0 + 4 * cq;
+  struct Quad {
+    uint4 b;  // 0 outside the image
+    Raw4<TS> tv, cv;
+    float4 vv;
   };
-  auto fetch = [&](int r0, Pass& Q) {
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int r = r0 + u * RS, y = gy0 + r;
-      const bool ok = r < SR && xok3 && (unsigned)y < (unsigned)H;
+  auto fetch = [&](int r, Quad& Q) {
+    const int y = gy0 + r;
+    if (r < SR && x3 < W && (unsigned)y < (unsigned)H) {
       const int p = y * P + x3;
-      Q.b[u] = ok ? __ldg(bnd_i + p) : 0u;
-      Q.tv[u] = ok ? load_f(tgt_i + p) : 0.f;
-      Q.cv[u] = ok ? load_f(cnf_i + p) : 0.f;
-      Q.vv[u] = ok ? __ldg(vin_i + p) : 0.f;
+      Q.b = __ldg(reinterpret_cast<const uint4*>(bnd_i + p));
+      Q.tv.load(tgt_i + p);
+      Q.cv.load(cnf_i + p);
+      Q.vv = __ldg(reinterpret_cast<const float4*>(vin_i + p));
+      if (x3 + 4 > W) {  // columns past the width hold the pitch's padding
+        if (x3 + 1 >= W) Q.b.y = 0u;
+        if (x3 + 2 >= W) Q.b.z = 0u;
+        Q.b.w = 0u;
+      }
+    } else {
+      Q.b = make_uint4(0u, 0u, 0u, 0u);
+      Q.tv.zero();
+      Q.cv.zero();
+      Q.vv = make_float4(0.f, 0.f, 0.f, 0.f);
     }
   };
-  Pass QA, QB;
-  fetch(r03, QA);
-  // ---- 1. stage the iterate: one warp per row, three rows in flight -----------
+  Quad QA, QB;
+  fetch(r3, QA);
+  __syncthreads();  // smax initialised
+  // ---- 1. stage the iterate, four columns per item, four items in flight -------
   float m = 0.f;
   {
-    const int warp = tid >> 5;
-    constexpr int NW = NT / 32;
-    for (int r0 = warp; r0 < SR; r0 += 2 * NW) {
-      float vals[2][3];
+    constexpr int U = 4;
+    const int SW4 = SW >> 2, n = SR * SW4;
+    const unsigned mg = L.sw4_magic;
+    for (int i0 = tid; i0 < n; i0 += U * NT) {
+      float4 v[U];
+      int dst[U];
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int r = r0 + u * NW, y = gy0 + r;
-        const bool yok = r < SR && (unsigned)y < (unsigned)H;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const int cc = lane + 32 * k, x = gx0 + cc;
-          vals[u][k] = (yok && cc >= 1 && cc < SWX && (unsigned)x < (unsigned)W)
-                           ? __ldg(vin_i + y * P + x)
-                           : 0.f;
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * NT;
+        const int r = fast_div(i, mg), q = i - r * SW4;
+        const int y = gy0 + r, x = xs + 4 * q;
+        dst[u] = i < n ? r * SWS + 4 * q : -1;
+        v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < n && (unsigned)y < (unsigned)H && x >= 0 && x < W)
+          v[u] = __ldg(reinterpret_cast<const float4*>(vin_i + y * P + x));
+        if (x + 4 > W) {  // columns past the width hold the pitch's padding
+          if (x + 1 >= W) v[u].y = 0.f;
+          if (x + 2 >= W) v[u].z = 0.f;
+          v[u].w = 0.f;
         }
       }
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int r = r0 + u * NW;
-        if (r >= SR) break;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const int cc = lane + 32 * k;
-          if (cc < SWXp) XP[r * SWXp + cc] = __float_as_uint(vals[u][k]);
-          m = fmaxf(m, fabsf(vals[u][k]));
-        }
-        // rows wider than 96 entries (halos above 15)
-        for (int cc = lane + 96; cc < SWXp; cc += 32) {
-          const int x = gx0 + cc, y = gy0 + r;
-          const float v = (cc < SWX && (unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H)
-                              ? __ldg(vin_i + y * P + x)
-                              : 0.f;
-          XP[r * SWXp + cc] = __float_as_uint(v);
-          m = fmaxf(m, fabsf(v));
-        }
+      for (int u = 0; u < U; ++u) {
+        if (dst[u] >= 0) *reinterpret_cast<float4*>(Xf + dst[u]) = v[u];
+        m = fmaxf(m, fmaxf(fmaxf(fabsf(v[u].x), fabsf(v[u].y)),
+                           fmaxf(fabsf(v[u].z), fabsf(v[u].w))));
       }
     }
   }
   m = warp_max_nonneg(m);
   if (lane == 0) atomicMax(&smax[0], __float_as_uint(m));
   __syncthreads();
-  // ---- 2. X prefix: scan 16-entry segments, then add segment offsets ----------
+  // ---- 2. X prefix: a thread per 16-entry segment of a row, then offsets -------
   {
-    const int F = fx_shift(__uint_as_float(smax[0]), lgx);
-    const float sF = pow2f(F);
-    for (int i = tid; i < SR * NSX; i += NT) {
-      const int sg = i / SR, r = i - sg * SR;  // lanes on rows: conflict-free
-      unsigned* e = XP + r * SWXp + sg * kXSeg;
-      const int n = min(kXSeg, SWXp - sg * kXSeg);
+    const float sF = pow2f(fx_shift(__uint_as_float(smax[0]), lgx));
+    const int NSX = L.nsx, n = SR * NSX, SW4 = SW >> 2;
+    unsigned* segx = reinterpret_cast<unsigned*>(sx);  // SR x NSX totals (sx is free)
+    for (int i = tid; i < n; i += NT) {
+      const int sg = fast_div(i, L.sr_magic), r = i - sg * SR;  // lanes on rows
+      uint4* e = reinterpret_cast<uint4*>(XP + r * SWS) + 4 * sg;
+      const float4* f = reinterpret_cast<const float4*>(Xf + r * SWS) + 4 * sg;
+      const int nq = min(4, SW4 - 4 * sg);
       unsigned acc = 0u;
-      if (n == kXSeg) {
 #pragma unroll
-        for (int q = 0; q < kXSeg; q += 4) {
-          uint4 w = *reinterpret_cast<uint4*>(e + q);
-          acc += fx_from(__uint_as_float(w.x), sF); w.x = acc;
-          acc += fx_from(__uint_as_float(w.y), sF); w.y = acc;
-          acc += fx_from(__uint_as_float(w.z), sF); w.z = acc;
-          acc += fx_from(__uint_as_float(w.w), sF); w.w = acc;
-          *reinterpret_cast<uint4*>(e + q) = w;
-        }
-      } else {
-        for (int q = 0; q < n; ++q) {
-          acc += fx_from(__uint_as_float(e[q]), sF);
-          e[q] = acc;
+      for (int q = 0; q < 4; ++q) {
+        if (q < nq) {
+          const float4 v = f[q];
+          uint4 w;
+          w.x = acc += fx_from(v.x, sF);
+          w.y = acc += fx_from(v.y, sF);
+          w.z = acc += fx_from(v.z, sF);
+          w.w = acc += fx_from(v.w, sF);
+          e[q] = w;
         }
       }
       segx[r * NSX + sg] = acc;
     }
     __syncthreads();
-    for (int i = tid; i < SR * NSX; i += NT) {
-      const int sg = i / SR, r = i - sg * SR;  // lanes on rows: conflict-free
+    for (int i = tid; i < n; i += NT) {
+      const int sg = fast_div(i, L.sr_magic), r = i - sg * SR;
       if (sg == 0) continue;
       unsigned off = 0u;
       for (int s2 = 0; s2 < sg; ++s2) off += segx[r * NSX + s2];
-      unsigned* e = XP + r * SWXp + sg * kXSeg;
-      const int n = min(kXSeg, SWXp - sg * kXSeg);
-      if (n == kXSeg) {
+      uint4* e = reinterpret_cast<uint4*>(XP + r * SWS) + 4 * sg;
+      const int nq = min(4, SW4 - 4 * sg);
 #pragma unroll
-        for (int q = 0; q < kXSeg; q += 4) {
-          uint4 w = *reinterpret_cast<uint4*>(e + q);
-          w.x += off; w.y += off; w.z += off; w.w += off;
-          *reinterpret_cast<uint4*>(e + q) = w;
+      for (int q = 0; q < 4; ++q) {
+        if (q < nq) {
+          uint4 w = e[q];
+          w.x += off;
+          w.y += off;
+          w.z += off;
+          w.w += off;
+          e[q] = w;
         }
-      } else {
-        for (int q = 0; q < n; ++q) e[q] += off;
       }
     }
-    __syncthreads();
   }
+  __syncthreads();
   // ---- 3. X half-step for the tile columns over all rows -----------------------
   {
-    const int F = fx_shift(__uint_as_float(smax[0]), lgx);
-    const float isF = pow2f(-F);
+    const float isF = pow2f(-fx_shift(__uint_as_float(smax[0]), lgx));
     float mloc = 0.f;
-    auto compute = [&](int r0, const Pass& Q) {
+    auto compute = [&](int r, const Quad& Q) {
+      const unsigned* e0 = XP + r * SWS + HA + 4 * cq;  // e0[k]: prefix at x3 + k
+      float o[4];
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int r = r0 + u * RS;
-        if (r >= SR) break;
-        float o = 0.f;
-        const uint32_t b = Q.b[u];
+      for (int k = 0; k < 4; ++k) {
+        o[k] = 0.f;
+        const uint32_t b = u4_get(Q.b, k);
         if (b) {  // inside the image (a window always holds its own pixel)
           const int dl = min((int)(b & 0xff), hx + 1);
           const int du = min((int)((b >> 8) & 0xff), hx);
           const float rn = rtab[dl + du];
-          const unsigned* e = XP + r * SWXp + c3 + hx + 1;
-          const float B = fx_window(e[du], e[-dl], rn * isF);
+          const float B = fx_window(e0[k + du], e0[k - dl], rn * isF);
+          const float vv = f4_get(Q.vv, k), tv = Q.tv[k], cv = Q.cv[k];
           float extra = 0.f;
-          if (STEREO) extra = photometric(sa, in.off + (gy0 + r) * P, x3, W, Q.vv[u]);
-          o = x_update<MODE, STEREO>(Q.vv[u], B, Q.tv[u], Q.cv[u], rn, lambda, step, extra);
-          if (over && Q.cv[u] > overwrite) o = Q.tv[u];
+          if (STEREO)
+            extra = photometric(sa, in.off + (long long)(gy0 + r) * P, x3 + k, W, vv);
+          o[k] = x_update<MODE, STEREO>(vv, B, tv, cv, rn, lambda, step, extra);
+          if (over && cv > overwrite) o[k] = tv;
         }
-        sx[r * TWp + c3] = o;
-        sby[r * TW + c3] = (uint16_t)(b >> 16);
-        mloc = fmaxf(mloc, fabsf(o));
+        mloc = fmaxf(mloc, fabsf(o[k]));
       }
+      *reinterpret_cast<float4*>(sx + r * TQ + 4 * cq) = make_float4(o[0], o[1], o[2], o[3]);
+      // the Y bytes (b >> 16) of the four pixels as four u16
+      *reinterpret_cast<uint2*>(sby + r * TW + 4 * cq) =
+          make_uint2((Q.b.x >> 16) | (Q.b.y & 0xffff0000u), (Q.b.z >> 16) | (Q.b.w & 0xffff0000u));
     };
-    int r0 = r03;
-    while (r0 < SR) {
-      if (r0 + 2 * RS < SR) fetch(r0 + 2 * RS, QB);
-      compute(r0, QA);
-      r0 += 2 * RS;
-      if (r0 >= SR) break;
-      if (r0 + 2 * RS < SR) fetch(r0 + 2 * RS, QA);
-      compute(r0, QB);
-      r0 += 2 * RS;
+    int r = r3;
+    while (r < SR) {
+      if (r + RPP < SR) fetch(r + RPP, QB);
+      compute(r, QA);
+      r += RPP;
+      if (r >= SR) break;
+      if (r + RPP < SR) fetch(r + RPP, QA);
+      compute(r, QB);
+      r += RPP;
     }
     mloc = warp_max_nonneg(mloc);
     if (lane == 0) atomicMax(&smax[1], __float_as_uint(mloc));
   }
   __syncthreads();
-  // ---- 4. Y prefix per column in segments ---------------------------------------
+  // ---- 4. Y prefix: a warp per group of four columns, a lane per segment ---------
   const int Fy = fx_shift(__uint_as_float(smax[1]), lgy);
   const float sFy = pow2f(Fy), isFy = pow2f(-Fy);
-  const int c = tid % TW, sgi = tid / TW;
-  const int seg = (RY + NSEG - 1) / NSEG;
-  const int k0 = min(sgi * seg, RY), k1 = min(k0 + seg, RY);
-  unsigned acc = 0;
-  for (int k = k0; k < k1; ++k) {
-    if (k > 0) acc += fx_from(sx[(k - 1) * TWp + c], sFy);
-    Py[k * TW + c] = acc;
+  {
+    const int RY = SR + 1;
+    const int k0 = min(lane * L.seg, RY), k1 = min(k0 + L.seg, RY);
+    for (int q = warp; q < QW; q += NW) {
+      uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+      for (int k = k0; k < k1; ++k) {
+        if (k > 0) {
+          const float4 v = *reinterpret_cast<const float4*>(sx + (k - 1) * TQ + 4 * q);
+          acc.x += fx_from(v.x, sFy);
+          acc.y += fx_from(v.y, sFy);
+          acc.z += fx_from(v.z, sFy);
+          acc.w += fx_from(v.w, sFy);
+        }
+        *reinterpret_cast<uint4*>(Py + k * TQ + 4 * q) = acc;
+      }
+      uint4 off;
+      off.x = warp_incl_scan(acc.x, lane) - acc.x;
+      off.y = warp_incl_scan(acc.y, lane) - acc.y;
+      off.z = warp_incl_scan(acc.z, lane) - acc.z;
+      off.w = warp_incl_scan(acc.w, lane) - acc.w;
+      for (int k = k0; k < k1; ++k) {
+        uint4* pk = reinterpret_cast<uint4*>(Py + k * TQ + 4 * q);
+        uint4 w = *pk;
+        w.x += off.x;
+        w.y += off.y;
+        w.z += off.z;
+        w.w += off.w;
+        *pk = w;
+      }
+    }
   }
-  segy[sgi * TW + c] = acc;
   __syncthreads();
-  unsigned off = 0;
-  for (int s2 = 0; s2 < sgi; ++s2) off += segy[s2 * TW + c];
-  for (int k = k0; k < k1; ++k) Py[k * TW + c] += off;
-  __syncthreads();
-  // ---- 5. Y half-step, written coalesced ----------------------------------------
+  // ---- 5. Y half-step, four pixels per thread, vector stores --------------------
   const float slam = step * lambda;
-  const int x = t.x0 + c;
-  if (x >= W) return;
+  if (x3 >= W) return;
   const int jmax = min(TH, H - t.y0);
-  for (int j = sgi; j < jmax; j += NSEG) {
-    const uint32_t b = sby[(j + hy) * TW + c];
-    const int dl = min((int)(b & 0xff), hy + 1), du = min((int)(b >> 8), hy);
-    const int k = j + hy + 1;
-    const float Bv = fx_window(Py[(k + du) * TW + c], Py[(k - dl) * TW + c],
-                               rtab[dl + du] * isFy);
-    const float v = sx[(j + hy) * TWp + c];
-    vout_i[(t.y0 + j) * P + x] = __fmaf_rn(-slam, v - Bv, v);
+  for (int j = r3; j < jmax; j += RPP) {
+    const uint2 bq = *reinterpret_cast<const uint2*>(sby + (j + hy) * TW + 4 * cq);
+    const float4 v4 = *reinterpret_cast<const float4*>(sx + (j + hy) * TQ + 4 * cq);
+    const unsigned* c0 = Py + (j + hy + 1) * TQ + 4 * cq;
+    float o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const unsigned b = ((k < 2 ? bq.x : bq.y) >> (16 * (k & 1))) & 0xffffu;
+      const int dl = min((int)(b & 0xff), hy + 1), du = min((int)(b >> 8), hy);
+      const float Bv = fx_window(c0[du * TQ + k], c0[-dl * TQ + k], rtab[dl + du] * isFy);
+      const float v = f4_get(v4, k);
+      o[k] = __fmaf_rn(-slam, v - Bv, v);
+    }
+    float* dst = vout_i + (t.y0 + j) * P + x3;
+    if (x3 + 4 <= W) {
+      *reinterpret_cast<float4*>(dst) = make_float4(o[0], o[1], o[2], o[3]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (x3 + k < W) dst[k] = o[k];
+    }
   }
 }
 
@@ -483,7 +557,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
 // The same iteration for large halos (k_dts_iter_rows): shared memory grows
 // linearly with the halo instead of with its square, so every sigma_z below
 // 254 fits the 32 x 32 tiles.  Window sums from fixed-point prefix sums
-// (fixed_point.cuh) as in k_dts_iter_tile; the X scale comes from the
+// (fixed_point.cuh) as in k_dts_iter_vec; the X scale comes from the
 // largest magnitude in the row (X) or among the tile's X results (Y).
 //
 // X half-step: one warp per row of the tile plus the vertical halo; each
@@ -915,7 +989,7 @@ static int launch_iter_shape(const DtsLaunch& L, const float* vin, float* vout,
                              float overwrite, int hx, int hy, cudaStream_t s,
                              const StereoArgs& sa) {
   constexpr int NT = TW >= 64 ? 512 : 256;
-  const TileIterSmem<TW, TH, NT> lay(hx, hy);
+  const VecIterSmem<TW, TH, NT> lay(hx, hy);
   const size_t smem = (size_t)lay.total;
   const size_t smem_rows = PrefixIterSmem<TW, TH, NT>::bytes(hx, hy);
   if (smem > kMaxSmem && smem_rows > kMaxSmem)
@@ -936,10 +1010,10 @@ static int launch_iter_shape(const DtsLaunch& L, const float* vin, float* vout,
     DTSGB_CUDA(cudaGetLastError());
     return DTSGB_OK;
   }
-  int st = set_smem(k_dts_iter_tile<TS, MODE, TW, TH, NT, STEREO>, smem);
+  int st = set_smem(k_dts_iter_vec<TS, MODE, TW, TH, NT, STEREO>, smem);
   if (st) return st;
   ProfScope ps(s, DTSGB_K_DTS_ITER);
-  k_dts_iter_tile<TS, MODE, TW, TH, NT, STEREO><<<L.n_tiles, NT, smem, s>>>(
+  k_dts_iter_vec<TS, MODE, TW, TH, NT, STEREO><<<L.n_tiles, NT, smem, s>>>(
       L.d_inst, L.d_tiles, vin, vout, (const TS*)target, (const TS*)conf,
       bounds, lambda, step, overwrite, hx, hy, sa, lay);
   DTSGB_CUDA(cudaGetLastError());
@@ -956,7 +1030,7 @@ static int launch_iter_t(const DtsLaunch& L, const float* vin, float* vout,
     return launch_iter_shape<TS, MODE, kIterSmallTW, kIterSmallTH, STEREO>(
         L, vin, vout, target, conf, bounds, lambda, step, overwrite, hx, hy, s, sa);
   if (L.d_tiles_small &&
-      (size_t)TileIterSmem<kIterTW, kIterTH, 512>(hx, hy).total > kMaxSmem &&
+      (size_t)VecIterSmem<kIterTW, kIterTH, 512>(hx, hy).total > kMaxSmem &&
       PrefixIterSmem<kIterTW, kIterTH, 512>::bytes(hx, hy) > kMaxSmem)
     return launch_iter_shape<TS, MODE, kIterSmallTW, kIterSmallTH, STEREO>(
         L.as_small(), vin, vout, target, conf, bounds, lambda, step, overwrite, hx, hy,

@@ -287,7 +287,25 @@ __global__ void k_laplace(const HInst* __restrict__ insts, int axis,
   }
 }
 
-// InitZ<true> (src/hfbs.cu:337-353): z = blur(b) / (blur(c) + 1e-7); h = 0.
+// (float)((double)b / ((double)c + 1e-7)) without a double division, which
+// is slow on this part.  The double denominator d is split into floats
+// dh + dl (|dl| <= ulp(dh) / 2, exact to 2^-48 of d); q0 = b / dh is
+// correctly rounded, so b - q0 * dh is exact by FMA, and q0 + (b - q0 * d) / dh
+// carries the quotient to about 2^-46 of itself before the final rounding:
+// it can differ from the double quotient's rounding only when that lies
+// within about 2^-23 ulp of a float rounding midpoint.
+__device__ __forceinline__ float div_by_c_plus_eps(float b, float c) {
+  const double d = (double)c + 1e-7;
+  const float dh = (float)d;
+  const float dl = (float)(d - (double)dh);
+  const float q0 = __fdiv_rn(b, dh);
+  float r = __fmaf_rn(-q0, dh, b);
+  r = __fmaf_rn(-q0, dl, r);
+  return q0 + __fdiv_rn(r, dh);
+}
+
+// InitZ<true> (src/hfbs.cu:337-353): z = blur(b) / (blur(c) + 1e-7), the
+// division in double as the reference's double literal makes it; h = 0.
 __global__ void k_init_z(const HInst* __restrict__ insts,
                          const float* __restrict__ blur_b,
                          const float* __restrict__ blur_c, float* __restrict__ z,
@@ -297,7 +315,7 @@ __global__ void k_init_z(const HInst* __restrict__ insts,
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const long long g = I.grid_off + i;
-    z[g] = (float)((double)blur_b[g] / ((double)blur_c[g] + 1e-7));
+    z[g] = div_by_c_plus_eps(blur_b[g], blur_c[g]);
     h[g] = 0.f;
   }
 }
