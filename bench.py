@@ -8,8 +8,10 @@ solves with inputs already resident in HBM: for DTS the reference's timed
 window (src/edge_aware_solver.h:72-84: differential, integration, all
 iterations), for HFBS the whole HFBS::Optimize.  `e2e` times the same step
 through the public C ABI with pinned host buffers, the upload and the
-download included.  Under torchrun every rank solves its own copy of the
-workload (independent instances, no collective): weak scaling.
+download included (config 3: dtsgb_pipeline_run, which overlaps the copies
+of one chunk of instances with the solves of another; --e2e-chunks).
+Under torchrun every rank solves its own copy of the workload (independent
+instances, no collective): weak scaling.
 
 --impl reference times the reference algorithm's CPU restatement (the FP32
 oracle port, all host threads) on a bounded sample of the same workload; the
@@ -126,8 +128,9 @@ class Cfg3:
     name = "cfg3_batched_dts_hfbs_64_ragged_bf16"
     dtype = "bf16 storage, f32 math"
 
-    def __init__(self, rank: int, scale: float = 1.0):
+    def __init__(self, rank: int, scale: float = 1.0, e2e_chunks: int = 16):
         import domain_transform_solver_gb300 as D
+        self.e2e_chunks = e2e_chunks
         from domain_transform_solver_gb300 import workloads as W
         self.D, self.W = D, W
         # scale < 1 shrinks every instance (profiling captures of a smaller
@@ -164,6 +167,11 @@ class Cfg3:
         self._o1 = [_pinned_empty((h, w)) for w, h in self.sizes]
         self.h_rgba, self.h_t, self.h_c = _ptrs(self._rgba), _ptrs(self._t), _ptrs(self._c)
         self.h_o0, self.h_o1 = _ptrs(self._o0), _ptrs(self._o1)
+        # the host-to-host path: chunks of instances on their own streams
+        self.pipe = D.Pipeline(self.sizes, flags=D.FLAG_BF16_STORAGE,
+                               n_chunks=self.e2e_chunks)
+        self.pipe.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)
+        self.e2e_api = f"dtsgb_pipeline_run, {self.pipe.n_chunks} chunks"
 
     def step(self):
         from domain_transform_solver_gb300._lib import check
@@ -173,11 +181,10 @@ class Cfg3:
 
     def step_e2e(self):
         from domain_transform_solver_gb300._lib import check
-        h = self.b.handle
-        check(self.lib.dtsgb_batch_upload(h, 1, self.h_rgba, self.h_t, self.h_c))
-        self.step()
-        check(self.lib.dtsgb_batch_download(h, 0, self.h_o0))
-        check(self.lib.dtsgb_batch_download(h, 1, self.h_o1))
+        check(self.lib.dtsgb_pipeline_run(self.pipe.handle, 1, self.h_rgba, self.h_t,
+                                          self.h_c, ctypes.byref(self.fp),
+                                          ctypes.byref(self.op), ctypes.c_float(-1.0),
+                                          ctypes.byref(self.hpc), self.h_o0, self.h_o1))
 
     def e2e_bytes(self):
         return self.pixels * (4 + 4 + 4), self.pixels * 4 * 2
@@ -444,7 +451,7 @@ WORKLOADS = {"cfg3": Cfg3, "cfg0": Cfg0, "cfg1": Cfg1, "cfg4": Cfg4}
 # ---- arms ----------------------------------------------------------------------
 def make_workload(args, rank):
     if args.workload == "cfg3":
-        return Cfg3(rank, scale=args.scale)
+        return Cfg3(rank, scale=args.scale, e2e_chunks=args.e2e_chunks)
     return WORKLOADS[args.workload](rank)
 
 
@@ -656,7 +663,8 @@ def run_ours(args, world, rank, local):
                    "parallelism": f"independent instances x{world} GPUs",
                    "guide_state_reuse": "off (every step recomputes all of it)"},
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                **({"api": wl.e2e_api} if hasattr(wl, "e2e_api") else {})},
         "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": achieved,
                      "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None,
@@ -684,6 +692,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="cfg3")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="cfg3 only: shrink every instance (smaller profiling case)")
+    ap.add_argument("--e2e-chunks", type=int, default=16,
+                    help="cfg3 only: chunks of the overlapped host-to-host e2e run")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

@@ -137,6 +137,12 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_batch_get_tuning": ([vp, i, P(ll)], i),
         "dtsgb_batch_autotune": ([vp, P(FilterParams), P(OptimizeParams), f,
                                   P(HfbsParams), i], i),
+        "dtsgb_pipeline_create": ([i, P(i), P(i), u, i, pvp], i),
+        "dtsgb_pipeline_destroy": ([vp], i),
+        "dtsgb_pipeline_chunks": ([vp], i),
+        "dtsgb_pipeline_batch": ([vp, i, pvp], i),
+        "dtsgb_pipeline_run": ([vp, i, pvp, pvp, pvp, P(FilterParams), P(OptimizeParams), f,
+                                P(HfbsParams), pvp, pvp], i),
         "dtsgb_batch_enable_grad": ([vp, i, i], i),
         "dtsgb_png_unfilter": ([vp, i, i, i, vp], i),
         "dtsgb_batch_grad_info": ([vp, P(i), P(i)], i),

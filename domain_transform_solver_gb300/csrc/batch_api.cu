@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/dtsgb.h"
+#include "color.cuh"
 #include "dtsgb_internal.cuh"
 #include "hfbs_internal.cuh"
 
@@ -56,6 +57,13 @@ struct dtsgb_batch_s {
   float* v[2] = {nullptr, nullptr};
   float* hout = nullptr;
   float* scratch = nullptr;
+  // host uploads: every image is copied whole (one contiguous copy per
+  // plane) into a dense staging area, then one kernel writes the pitched
+  // planes; soff[i] = pixels of the instances before i
+  std::vector<long long> soff;
+  long long dense = 0;
+  long long* d_soff = nullptr;
+  unsigned char* stage = nullptr;  // dense x (rgba 4 B, target 4 B, conf 4 B)
   Inst* d_inst = nullptr;
   Tile* d_tb = nullptr;
   Tile* d_ti = nullptr;     // iteration tiles of the shape in use
@@ -145,6 +153,8 @@ void batch_free(dtsgb_batch_t b) {
   dfree(b->d_hinst);
   for (auto& p : b->hg) dfree(p);
   dfree(b->ovf);
+  dfree(b->d_soff);
+  dfree(b->stage);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
   b->stream = nullptr;
 }
@@ -242,8 +252,82 @@ int upload_plane(dtsgb_batch_t b, int i, const float* src, void* dst,
   return DTSGB_OK;
 }
 
+// Dense staged images -> pitched planes: the guide (color-converted; not
+// written when guide is null), target and confidence in the storage type.
+template <typename TS>
+__global__ void k_ingest(const Inst* __restrict__ insts, const long long* __restrict__ soff,
+                         const uchar4* __restrict__ s_rgba, const float* __restrict__ s_t,
+                         const float* __restrict__ s_c, uchar4* __restrict__ guide,
+                         TS* __restrict__ target, TS* __restrict__ conf, int cs) {
+  const Inst I = insts[blockIdx.y];
+  const long long so = soff[blockIdx.y];
+  for (int y = blockIdx.x; y < I.h; y += gridDim.x) {
+    const long long srow = so + (long long)y * I.w, drow = I.off + (long long)y * I.pitch;
+    for (int x = threadIdx.x; x < I.w; x += blockDim.x) {
+      if (guide) {
+        const uchar4 p = s_rgba[srow + x];
+        guide[drow + x] = cs == DTSGB_RGB ? p : convert_pixel(p, cs);
+      }
+      target[drow + x] = store_cast<TS>(s_t[srow + x]);
+      conf[drow + x] = store_cast<TS>(s_c[srow + x]);
+    }
+  }
+}
+
+// Host upload: one contiguous copy per image and plane into the staging
+// area (pinned host memory makes them asynchronous), ones for missing
+// confidences, then k_ingest.  rgba null: targets only (guides kept).
+int host_ingest(dtsgb_batch_t b, int cs, const void* const* rgba,
+                const float* const* target, const float* const* conf, bool sync_host) {
+  if (!b->stage) {
+    int st = dalloc(&b->stage, (size_t)b->dense * 12);
+    if (st) return st;
+  }
+  uchar4* s_rgba = reinterpret_cast<uchar4*>(b->stage);
+  float* s_t = reinterpret_cast<float*>(b->stage + (size_t)b->dense * 4);
+  float* s_c = reinterpret_cast<float*>(b->stage + (size_t)b->dense * 8);
+  for (int i = 0; i < b->n; ++i) {
+    const Inst& I = b->inst[i];
+    const size_t px = (size_t)I.w * I.h;
+    const long long o = b->soff[i];
+    if (rgba)
+      DTSGB_CUDA(cudaMemcpyAsync(s_rgba + o, rgba[i], px * 4, cudaMemcpyHostToDevice,
+                                 b->stream));
+    DTSGB_CUDA(cudaMemcpyAsync(s_t + o, target[i], px * 4, cudaMemcpyHostToDevice,
+                               b->stream));
+    if (conf && conf[i]) {
+      DTSGB_CUDA(cudaMemcpyAsync(s_c + o, conf[i], px * 4, cudaMemcpyHostToDevice,
+                                 b->stream));
+    } else {
+      int st = launch_fill_storage(Storage::F32, s_c + o, (long long)px, 1.f, b->stream);
+      if (st) return st;
+    }
+  }
+  const dim3 grid((unsigned)std::min(b->max_h, 512), (unsigned)b->n);
+  uchar4* g = rgba ? b->guide : nullptr;
+  if (b->st == Storage::F32)
+    k_ingest<float><<<grid, 256, 0, b->stream>>>(b->d_inst, b->d_soff, s_rgba, s_t, s_c, g,
+                                                 (float*)b->target, (float*)b->conf, cs);
+  else
+    k_ingest<__nv_bfloat16><<<grid, 256, 0, b->stream>>>(
+        b->d_inst, b->d_soff, s_rgba, s_t, s_c, g, (__nv_bfloat16*)b->target,
+        (__nv_bfloat16*)b->conf, cs);
+  DTSGB_CUDA(cudaGetLastError());
+  if (rgba) ++b->guide_gen;
+  b->dts_res = -1;
+  b->grad_n = -1;
+  b->hfbs_done = false;
+  if (sync_host) DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+  return DTSGB_OK;
+}
+
+// sync_host: a host upload returns only when the copies are done (the
+// reference's CopyTo semantics; the host buffers may be reused at once).
 int batch_upload_targets(dtsgb_batch_t b, const float* const* target,
-                         const float* const* conf, cudaMemcpyKind kind) {
+                         const float* const* conf, cudaMemcpyKind kind,
+                         bool sync_host = true) {
+  if (kind == cudaMemcpyHostToDevice)
+    return host_ingest(b, DTSGB_RGB, nullptr, target, conf, sync_host);
   int st;
   for (int i = 0; i < b->n; ++i)
     if ((st = upload_plane(b, i, target[i], b->target, kind))) return st;
@@ -273,19 +357,22 @@ int batch_upload_targets(dtsgb_batch_t b, const float* const* target,
   b->dts_res = -1;
   b->grad_n = -1;
   b->hfbs_done = false;
-  if (kind == cudaMemcpyHostToDevice) DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+  if (kind == cudaMemcpyHostToDevice && sync_host)
+    DTSGB_CUDA(cudaStreamSynchronize(b->stream));
   return DTSGB_OK;
 }
 
 int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
                  const float* const* target, const float* const* conf,
-                 cudaMemcpyKind kind) {
+                 cudaMemcpyKind kind, bool sync_host = true) {
   if (!b || !rgba || !target) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
   if (cs < DTSGB_RGB || cs > DTSGB_YYY)
     return fail(DTSGB_ERR_INVALID_ARGUMENT, "invalid color space");
   for (int i = 0; i < b->n; ++i)
     if (!rgba[i] || !target[i])
       return fail(DTSGB_ERR_INVALID_ARGUMENT, "null image pointer");
+  if (kind == cudaMemcpyHostToDevice)
+    return host_ingest(b, cs, rgba, target, conf, sync_host);
   for (int i = 0; i < b->n; ++i) {
     const Inst& I = b->inst[i];
     const size_t wb = (size_t)I.w * 4;
@@ -295,7 +382,7 @@ int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
   int st = launch_color_convert_flat(b->guide, b->total, cs, b->stream);
   if (st) return st;
   ++b->guide_gen;
-  return batch_upload_targets(b, target, conf, kind);
+  return batch_upload_targets(b, target, conf, kind, sync_host);
 }
 
 int ensure_hfbs_buffers(dtsgb_batch_t b, long long voxels, long long planes) {
@@ -375,6 +462,8 @@ DTSGB_API int dtsgb_batch_create(int n, const int* widths, const int* heights,
   for (int i = 0; i < n; ++i) {
     Inst I{widths[i], heights[i], round_up(widths[i], 32), 0, off};
     b->inst.push_back(I);
+    b->soff.push_back(b->dense);
+    b->dense += (long long)widths[i] * heights[i];
     off += (long long)I.pitch * I.h;
     b->max_w = std::max(b->max_w, I.w);
     b->max_h = std::max(b->max_h, I.h);
@@ -410,8 +499,11 @@ DTSGB_API int dtsgb_batch_create(int n, const int* widths, const int* heights,
   if (!st) st = dalloc(&b->d_ti_big, ti.size());
   if (!st) st = dalloc(&b->d_ti_small, ts.size());
   if (!st) st = dalloc(&b->d_hinst, (size_t)n);
+  if (!st) st = dalloc(&b->d_soff, (size_t)n);
   if (!st) {
     e = cudaMemcpy(b->d_inst, b->inst.data(), n * sizeof(Inst), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_soff, b->soff.data(), n * sizeof(long long), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
       e = cudaMemcpy(b->d_tb, tb.data(), tb.size() * sizeof(Tile), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
@@ -854,7 +946,7 @@ DTSGB_API int dtsgb_batch_autotune(dtsgb_batch_t b, const dtsgb_filter_params* f
 }
 
 static int batch_download(dtsgb_batch_t b, int which, float* const* dst,
-                          cudaMemcpyKind kind) {
+                          cudaMemcpyKind kind, bool sync_host = true) {
   if (!b || !dst) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
   const float* src = nullptr;
   if (which == 0) {
@@ -873,7 +965,8 @@ static int batch_download(dtsgb_batch_t b, int which, float* const* dst,
     DTSGB_CUDA(cudaMemcpy2DAsync(dst[i], wb, src + I.off, (size_t)I.pitch * 4, wb, I.h,
                                  kind, b->stream));
   }
-  if (kind == cudaMemcpyDeviceToHost) DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+  if (kind == cudaMemcpyDeviceToHost && sync_host)
+    DTSGB_CUDA(cudaStreamSynchronize(b->stream));
   return DTSGB_OK;
 }
 
@@ -884,6 +977,110 @@ DTSGB_API int dtsgb_batch_download(dtsgb_batch_t b, int which, float* const* dst
 DTSGB_API int dtsgb_batch_download_device(dtsgb_batch_t b, int which,
                                           float* const* dst) {
   return batch_download(b, which, dst, cudaMemcpyDeviceToDevice);
+}
+
+
+// ---------------------------------------------------------------------------
+// Overlapped host-to-host solves: chunks of the instances, each a batch on
+// its own stream; every chunk's upload, solves and downloads are enqueued
+// without waiting, so copies of one chunk overlap the solves of another.
+// ---------------------------------------------------------------------------
+struct dtsgb_pipeline_s {
+  std::vector<dtsgb_batch_t> chunk;
+  std::vector<int> first;  // index of each chunk's first instance
+  int n = 0;
+};
+
+DTSGB_API int dtsgb_pipeline_destroy(dtsgb_pipeline_t p) {
+  if (!p) return DTSGB_OK;
+  for (dtsgb_batch_t b : p->chunk) dtsgb_batch_destroy(b);
+  delete p;
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_pipeline_create(int n, const int* widths, const int* heights,
+                                    unsigned flags, int n_chunks, dtsgb_pipeline_t* out) {
+  if (!out || !widths || !heights || n <= 0 || n_chunks <= 0)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "bad pipeline description");
+  *out = nullptr;
+  long long total = 0;
+  for (int i = 0; i < n; ++i) {
+    if (widths[i] <= 0 || heights[i] <= 0)
+      return fail(DTSGB_ERR_INVALID_DIMS, "instance dims must be positive");
+    total += (long long)widths[i] * heights[i];
+  }
+  n_chunks = std::min(n_chunks, n);
+  dtsgb_pipeline_t p = new dtsgb_pipeline_s();
+  p->n = n;
+  // contiguous runs of instances, cut where the running pixel count passes
+  // k / n_chunks of the total
+  long long acc = 0;
+  int start = 0;
+  for (int i = 0; i < n; ++i) {
+    acc += (long long)widths[i] * heights[i];
+    const int k = (int)p->first.size() + 1;  // chunk being filled, 1-based
+    const bool last = i == n - 1;
+    const bool cut = acc * n_chunks >= total * k && n - (i + 1) >= n_chunks - k;
+    const bool must = n - (i + 1) == n_chunks - k;  // one instance per chunk left
+    if (last || ((cut || must) && k < n_chunks)) {
+      dtsgb_batch_t b = nullptr;
+      int st = dtsgb_batch_create(i + 1 - start, widths + start, heights + start, flags, &b);
+      if (st) {
+        dtsgb_pipeline_destroy(p);
+        return st;
+      }
+      p->chunk.push_back(b);
+      p->first.push_back(start);
+      start = i + 1;
+    }
+  }
+  *out = p;
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_pipeline_chunks(dtsgb_pipeline_t p) {
+  return p ? (int)p->chunk.size() : 0;
+}
+
+DTSGB_API int dtsgb_pipeline_batch(dtsgb_pipeline_t p, int k, dtsgb_batch_t* out) {
+  if (!p || !out || k < 0 || k >= (int)p->chunk.size())
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "no such chunk");
+  *out = p->chunk[k];
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_pipeline_run(dtsgb_pipeline_t p, int color_space,
+                                 const void* const* rgba, const float* const* target,
+                                 const float* const* conf,
+                                 const dtsgb_filter_params* filter,
+                                 const dtsgb_optimize_params* optimize,
+                                 float overwrite_target_above_conf,
+                                 const dtsgb_hfbs_params* hfbs, float* const* out_dts,
+                                 float* const* out_hfbs) {
+  if (!p || !rgba || !target) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  const bool dts = filter && optimize;
+  if ((dts && !out_dts) || (hfbs && !out_hfbs))
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "null output array");
+  int st = DTSGB_OK;
+  size_t k = 0;
+  for (; k < p->chunk.size() && !st; ++k) {
+    dtsgb_batch_t b = p->chunk[k];
+    const int f = p->first[k];
+    st = batch_upload(b, color_space, rgba + f, target + f, conf ? conf + f : nullptr,
+                      cudaMemcpyHostToDevice, false);
+    if (!st && dts)
+      st = dtsgb_batch_solve_dts(b, filter, optimize, overwrite_target_above_conf);
+    if (!st && hfbs) st = dtsgb_batch_solve_hfbs(b, hfbs);
+    if (!st && dts) st = batch_download(b, 0, out_dts + f, cudaMemcpyDeviceToHost, false);
+    if (!st && hfbs) st = batch_download(b, 1, out_hfbs + f, cudaMemcpyDeviceToHost, false);
+  }
+  // wait for every chunk enqueued so far, also after a failure (the host
+  // buffers must not be in use when this returns)
+  for (size_t j = 0; j < k; ++j) {
+    const cudaError_t e = cudaStreamSynchronize(p->chunk[j]->stream);
+    if (e != cudaSuccess && !st) st = cuda_fail(e, "cudaStreamSynchronize");
+  }
+  return st;
 }
 
 }  // extern "C"

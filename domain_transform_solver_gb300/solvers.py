@@ -37,7 +37,7 @@ __all__ = [
     "HfbsOptions", "Solve", "EdgeAwareOptimize", "DtsgbError",
     "FLAG_BF16_STORAGE", "FLAG_FIX_Y_LIMIT", "TUNE_DTS_TILE", "TUNE_HFBS_GROUP_VOXELS",
     "TUNE_REUSE_GUIDE_STATE",
-    "Batch", "DomainTransformStereo",
+    "Batch", "Pipeline", "DomainTransformStereo",
 ]
 
 FLAG_BF16_STORAGE = 0x1
@@ -518,6 +518,95 @@ class Batch:
         gc = None if grad_conf_ptrs is None else _vp_array(grad_conf_ptrs)
         check(self._lib.dtsgb_batch_dts_backward_device(self._h, _vp_array(grad_out_ptrs),
                                                         _vp_array(grad_target_ptrs), gc))
+
+
+class Pipeline:
+    """Host-to-host solves of many images with the copies of one chunk of
+    instances overlapping the solves of another (dtsgb_pipeline_*): each
+    chunk is a Batch-like set of consecutive instances on its own stream.
+    Copies overlap only from pinned host memory (e.g. torch's
+    pin_memory()); numpy arrays work but copy synchronously."""
+
+    def __init__(self, sizes, flags: int = 0, n_chunks: int = 4):
+        self._lib = _lib.load()
+        self.sizes = [(int(w), int(h)) for w, h in sizes]
+        n = len(self.sizes)
+        ws = (ctypes.c_int * n)(*[w for w, _ in self.sizes])
+        hs = (ctypes.c_int * n)(*[h for _, h in self.sizes])
+        p = ctypes.c_void_p()
+        check(self._lib.dtsgb_pipeline_create(n, ws, hs, flags, int(n_chunks),
+                                              ctypes.byref(p)))
+        self._h = p
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.dtsgb_pipeline_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def n_chunks(self) -> int:
+        return int(self._lib.dtsgb_pipeline_chunks(self._h))
+
+    def set_tuning(self, knob: int, value: int) -> None:
+        """Apply a batch tuning knob (TUNE_*) to every chunk."""
+        for k in range(self.n_chunks):
+            b = ctypes.c_void_p()
+            check(self._lib.dtsgb_pipeline_batch(self._h, k, ctypes.byref(b)))
+            check(self._lib.dtsgb_batch_set_tuning(b, int(knob), int(value)))
+
+    def run_ptrs(self, color_space: COLOR_SPACE, rgba_ptrs, target_ptrs, confidence_ptrs,
+                 filter_params: DomainFilterParams | None,
+                 optimize_params: DomainOptimizeParams | None,
+                 grid_params: HFBSGridParams | None, out_dts_ptrs, out_hfbs_ptrs,
+                 overwrite_target_above_conf: float = -1) -> None:
+        """The same on raw host pointers (integers), e.g. pinned buffers."""
+        dts = filter_params is not None and optimize_params is not None
+        check(self._lib.dtsgb_pipeline_run(
+            self._h, int(color_space), _vp_array(rgba_ptrs), _vp_array(target_ptrs),
+            None if confidence_ptrs is None else _vp_array(confidence_ptrs),
+            ctypes.byref(filter_params._c()) if dts else None,
+            ctypes.byref(optimize_params._c()) if dts else None,
+            float(overwrite_target_above_conf),
+            ctypes.byref(grid_params._c()) if grid_params is not None else None,
+            _vp_array(out_dts_ptrs) if dts else None,
+            _vp_array(out_hfbs_ptrs) if grid_params is not None else None))
+
+    def run(self, color_space: COLOR_SPACE, rgba, target, confidence=None,
+            filter_params: DomainFilterParams | None = None,
+            optimize_params: DomainOptimizeParams | None = None,
+            grid_params: HFBSGridParams | None = None, overwrite_target_above_conf=-1):
+        """Upload, DTS (given filter and optimize params) and HFBS (given grid
+        params), download.  Returns (dts results or None, hfbs results or
+        None), lists of HxW float32."""
+        rg = [_rgba(a, (h, w)) for a, (w, h) in zip(rgba, self.sizes)]
+        tg = [_f32(a, (h, w)) for a, (w, h) in zip(target, self.sizes)]
+        cf = None
+        if confidence is not None:
+            cf = [None if a is None else _f32(a, (h, w))
+                  for a, (w, h) in zip(confidence, self.sizes)]
+        dts = filter_params is not None and optimize_params is not None
+        od = [np.empty((h, w), np.float32) for w, h in self.sizes] if dts else None
+        oh = ([np.empty((h, w), np.float32) for w, h in self.sizes]
+              if grid_params is not None else None)
+        check(self._lib.dtsgb_pipeline_run(
+            self._h, int(color_space), _ptr_array(rg), _ptr_array(tg),
+            None if cf is None else _ptr_array(cf),
+            ctypes.byref(filter_params._c()) if dts else None,
+            ctypes.byref(optimize_params._c()) if dts else None,
+            float(overwrite_target_above_conf),
+            ctypes.byref(grid_params._c()) if grid_params is not None else None,
+            _ptr_array(od) if dts else None, _ptr_array(oh) if oh is not None else None))
+        return od, oh
 
 
 # ---- generic solve API, src/edge_aware_solver.h:13-90 (cv::Mat-free) -------

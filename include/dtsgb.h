@@ -349,6 +349,40 @@ DTSGB_API int dtsgb_batch_autotune(dtsgb_batch_t b, const dtsgb_filter_params* f
                                    float overwrite_target_above_conf,
                                    const dtsgb_hfbs_params* hfbs, int reps);
 
+/* ---- Overlapped host-to-host solves (new; the reference copies, solves
+ * and copies back one image at a time).  A pipeline splits n instances into
+ * n_chunks runs of consecutive instances of about equal pixel count, each a
+ * batch with its own stream (created with `flags`), and dtsgb_pipeline_run
+ * enqueues every chunk's upload, solves and downloads without waiting, so
+ * the copy engines move one chunk while another is solved.  The copies are
+ * asynchronous only from pinned host memory (cudaHostAlloc /
+ * cudaHostRegister); run returns when every result is on the host or, after
+ * a failure, when nothing enqueued is still running.  Arrays hold n
+ * pointers, as for dtsgb_batch_upload / dtsgb_batch_download.
+ * ===========================================================================*/
+typedef struct dtsgb_pipeline_s* dtsgb_pipeline_t;
+
+DTSGB_API int dtsgb_pipeline_create(int n, const int* widths, const int* heights,
+                                    unsigned flags, int n_chunks,
+                                    dtsgb_pipeline_t* out);
+DTSGB_API int dtsgb_pipeline_destroy(dtsgb_pipeline_t p);
+/* Number of chunks (min(n_chunks, n)). */
+DTSGB_API int dtsgb_pipeline_chunks(dtsgb_pipeline_t p);
+/* Chunk k's batch, owned by the pipeline (for dtsgb_batch_set_tuning and
+ * the like). */
+DTSGB_API int dtsgb_pipeline_batch(dtsgb_pipeline_t p, int k, dtsgb_batch_t* out);
+/* Upload, then DTS (when filter and optimize are both given; results into
+ * out_dts) and HFBS (when hfbs is given; results into out_hfbs), then
+ * download, for every instance. */
+DTSGB_API int dtsgb_pipeline_run(dtsgb_pipeline_t p, int color_space,
+                                 const void* const* rgba, const float* const* target,
+                                 const float* const* confidence,
+                                 const dtsgb_filter_params* filter,
+                                 const dtsgb_optimize_params* optimize,
+                                 float overwrite_target_above_conf,
+                                 const dtsgb_hfbs_params* hfbs, float* const* out_dts,
+                                 float* const* out_hfbs);
+
 /* ---- Gradients of the batched DTS solve (new; the reference has no
  * gradients).  With gradients enabled, dtsgb_batch_solve_dts also keeps the
  * iterate v_k every `segment` iterations (0 = automatic: the length that

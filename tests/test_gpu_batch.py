@@ -205,3 +205,38 @@ def test_large_halos(gpu_ready):
         assert np.abs(outs[64] - outs[32]).max() <= 1e-6 * rng_t
         if sz == 200.0:
             assert np.array_equal(outs[64], outs[32])
+
+
+@pytest.mark.parametrize("chunks", [1, 3, 10])
+def test_pipeline_matches_batch(gpu_ready, chunks):
+    """dtsgb_pipeline_run (chunks of instances on their own streams, copies
+    overlapping solves) gives the batch's results bitwise, for both solvers
+    and for one solver alone."""
+    D = gpu_ready
+    from domain_transform_solver_gb300 import workloads as W
+    insts = _instances()
+    sizes = [(i.width, i.height) for i in insts]
+    rgba = [i.rgba for i in insts]
+    tgt = [i.target for i in insts]
+    conf = [i.confidence for i in insts]
+    fp = D.DomainFilterParams(**W.CFG0_FILTER)
+    opt = D.DomainOptimizeParams(**dict(W.CFG0_OPT, num_iterations=5))
+    hp = D.HFBSGridParams(**dict(W.CFG1_HFBS, optim_iter_max=13))
+    b = D.Batch(sizes, flags=D.FLAG_BF16_STORAGE)
+    b.upload(D.COLOR_SPACE.YCbCr, rgba, tgt, conf)
+    b.solve_dts(fp, opt)
+    b.solve_hfbs(hp)
+    ref_d, ref_h = b.download(0), b.download(1)
+    p = D.Pipeline(sizes, flags=D.FLAG_BF16_STORAGE, n_chunks=chunks)
+    assert p.n_chunks == min(chunks, len(sizes))
+    for _ in range(2):  # the second run replays each chunk's graphs
+        od, oh = p.run(D.COLOR_SPACE.YCbCr, rgba, tgt, conf, fp, opt, hp)
+        for a, r in zip(od, ref_d):
+            assert np.array_equal(a, r)
+        for a, r in zip(oh, ref_h):
+            assert np.array_equal(a, r, equal_nan=True)
+    od, oh = p.run(D.COLOR_SPACE.YCbCr, rgba, tgt, conf, fp, opt, None)
+    assert oh is None and all(np.array_equal(a, r) for a, r in zip(od, ref_d))
+    od, oh = p.run(D.COLOR_SPACE.YCbCr, rgba, tgt, conf, grid_params=hp)
+    assert od is None and all(np.array_equal(a, r, equal_nan=True) for a, r in zip(oh, ref_h))
+    p.close()
