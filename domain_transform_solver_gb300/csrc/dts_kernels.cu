@@ -9,6 +9,7 @@
 // bounded-radius stencil over a tile plus halo held in shared memory: no
 // global prefix sums, no transposes, no long-row cancellation.
 #include <algorithm>
+#include <cmath>
 
 #include "../../include/dtsgb.h"
 #include "color.cuh"
@@ -43,99 +44,140 @@ __global__ void k_color_convert_flat(uchar4* __restrict__ g, long long n,
 }
 
 // ---------------------------------------------------------------------------
-// Window bounds (a4).  One CTA per TWxTH tile.  Shared memory holds dH for
-// the tile rows over columns [x0-rx+1, x0+TW+rx-1) and dV for the tile
-// columns over rows [y0-ry+1, y0+TH+ry-1), rx = floor(sigma_x)+1.
+// Window bounds (a4).  One CTA per TWxTH tile, 256 threads.
 // Lower bound: the largest i < p with sum_{j=i+1..p} w(j) > sigma, else p-1.
 // Upper bound: (the smallest i > p, i < limit, with sum_{j=p+1..i} w(j) >
 // sigma) - 1, else p.  limit is W for X and min(W,H) (reference quirk) or H
 // for Y.  A negative ratio stands for an all-zero domain transform (no
 // differential computed yet): every window is the pixel itself.
+//
+// The weights are clamped to sigma + 1 (a window holding a larger one
+// exceeds sigma either way) and converted to fixed point at 2^F with
+// r * (sigma + 1) * 2^F <= 2^30, so a window sum is the exact difference of
+// two wrapping 32-bit prefixes of the converted weights (each within 2^-F-1
+// of the float weight: decisions differ from float sums only within about
+// r * 2^-F of the threshold).  Shared memory holds the prefix of dH along
+// each tile row over [x0 - r, x0 + TW + r) and of dV along each tile column
+// over [y0 - r, y0 + TH + r).  As p moves forward, both window ends move
+// forward, so a thread walks a segment of 8 pixels with two pointers that
+// only advance: about two prefix reads per end and pixel instead of a search
+// over the whole radius.
 // ---------------------------------------------------------------------------
+constexpr int kBoundsSeg = 8;  // pixels per thread and axis
+
+// Lower and upper window ends along one axis for the n pixels starting at
+// prefix index j0 (S[j0 + k] for pixel p0 + k), coordinates p0.., axis length
+// `len` (lower limit 0), upper limit `lim`; stride between prefix entries s.
+// Writes dl | du << 8 to out[k * os].
+__device__ __forceinline__ void bounds_walk(const unsigned* __restrict__ S, int s, int j0,
+                                            int p0, int n, int r, int lim, int T,
+                                            uint16_t* out, int os) {
+  int q = 0, u = 0;
+  for (int k = 0; k < n; ++k) {
+    const int j = j0 + k, p = p0 + k;
+    const unsigned Sj = S[j * s];
+    // lower: the largest q in [j - K, j - 1] with S[j] - S[q] > T (K = min(r, p)),
+    // advanced from the previous pixel's (both only move forward)
+    const int qmin = j - min(r, p);
+    q = k == 0 ? qmin - 1 : max(q, qmin - 1);
+    while (q + 1 <= j - 1 && (int)(Sj - S[(q + 1) * s]) > T) ++q;
+    const int dl = q >= qmin ? j - q : 1;
+    // upper: the smallest u in [j + 1, j + K'] with S[u] - S[j] > T
+    // (K' = min(r, lim - 1 - p)); the first pixel starts from the far end
+    const int umax = j + min(r, lim - 1 - p);
+    if (k == 0) {
+      u = umax + 1;
+      while (u - 1 > j && (int)(S[(u - 1) * s] - Sj) > T) --u;
+    } else {
+      u = max(u, j + 1);
+      while (u <= umax && (int)(S[u * s] - Sj) <= T) ++u;
+    }
+    const int du = u <= umax ? u - j - 1 : 0;
+    out[k * os] = (uint16_t)(dl | (du << 8));
+  }
+}
+
 template <int TW, int TH>
 __global__ void __launch_bounds__(kThreads)
     k_bounds(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
              const uchar4* __restrict__ guide, uint32_t* __restrict__ bounds,
-             float ratio_x, float ratio_y, float sig_x, float sig_y, int rx,
-             int ry, int ref_y_limit) {
-  extern __shared__ float sm[];
+             float ratio_x, float ratio_y, int rx, int ry, int ref_y_limit,
+             float cap_x, float cap_y, float scale_x, float scale_y, int Tx, int Ty) {
+  static_assert(TW == 32 && TH == 32 && kThreads == 256, "bounds tile shape");
+  extern __shared__ unsigned smu[];
   const Tile t = tiles[blockIdx.x];
   const Inst in = insts[t.inst];
   const int W = in.w, H = in.h, P = in.pitch;
   const uchar4* g = guide + in.off;
-  const int DW = TW + 2 * rx - 1;
-  const int DR = TH + 2 * ry - 1;
-  float* sH = sm;            // TH x DW
-  float* sV = sm + TH * DW;  // DR x TW
+  const int DW = TW + 2 * rx, DWp = DW | 1;  // odd row stride: lanes on rows
+  const int DR = TH + 2 * ry;
+  unsigned* SH = smu;             // TH x DWp: prefix of dH, entry 0 = 0 at x0 - rx
+  unsigned* SV = SH + TH * DWp;   // DR x TW: prefix of dV, entry 0 = 0 at y0 - ry
+  uint16_t* BX = reinterpret_cast<uint16_t*>(SV + DR * TW);  // TH x TW
+  uint16_t* BY = BX + TH * TW;                               // TH x TW
   const uchar4 zero = make_uchar4(0, 0, 0, 0);
-  // dH: one warp per tile row, lanes along the row (no index divisions)
-  for (int r = threadIdx.x >> 5; r < TH; r += blockDim.x >> 5) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // ---- 1. weights in fixed point: dH one warp per row, dV lanes on columns
+  for (int r = warp; r < TH; r += kThreads / 32) {
     const int y = t.y0 + r;
-    for (int c = threadIdx.x & 31; c < DW; c += 32) {
-      const int x = t.x0 - rx + 1 + c;
-      float w = 0.f;
-      if (x >= 0 && x < W && y < H) {
+    for (int j = lane; j < DW; j += 32) {
+      const int x = t.x0 - rx + j;
+      unsigned q = 0u;
+      if (j > 0 && x >= 0 && x < W && y < H && ratio_x >= 0.f) {
         const uchar4 cur = g[y * P + x];
         const uchar4 prev = x > 0 ? g[y * P + x - 1] : zero;
-        w = ratio_x < 0.f ? 0.f : edge_weight(cur, prev, ratio_x);
+        q = (unsigned)__float2int_rn(fminf(edge_weight(cur, prev, ratio_x), cap_x) * scale_x);
       }
-      sH[r * DW + c] = w;
+      SH[r * DWp + j] = q;
     }
   }
-  for (int i = threadIdx.x; i < DR * TW; i += blockDim.x) {
-    const int r = i / TW, c = i - r * TW;
-    const int x = t.x0 + c, y = t.y0 - ry + 1 + r;
-    float w = 0.f;
-    if (x < W && y >= 0 && y < H) {
+  for (int i = tid; i < DR * TW; i += kThreads) {
+    const int j = i / TW, c = i % TW;
+    const int x = t.x0 + c, y = t.y0 - ry + j;
+    unsigned q = 0u;
+    if (j > 0 && x < W && y >= 0 && y < H && ratio_y >= 0.f) {
       const uchar4 cur = g[y * P + x];
       const uchar4 prev = y > 0 ? g[(y - 1) * P + x] : zero;
-      w = ratio_y < 0.f ? 0.f : edge_weight(cur, prev, ratio_y);
+      q = (unsigned)__float2int_rn(fminf(edge_weight(cur, prev, ratio_y), cap_y) * scale_y);
     }
-    sV[i] = w;
+    SV[i] = q;
   }
   __syncthreads();
+  // ---- 2. inclusive prefixes: a thread per row of SH, a thread per column of SV
+  if (tid < TH) {
+    unsigned* row = SH + tid * DWp;
+    unsigned acc = 0u;
+    for (int j = 0; j < DW; ++j) row[j] = acc += row[j];
+  } else if (tid >= 32 && tid < 32 + TW) {
+    unsigned* col = SV + (tid - 32);
+    unsigned acc = 0u;
+    for (int j = 0; j < DR; ++j) col[j * TW] = acc += col[j * TW];
+  }
+  __syncthreads();
+  // ---- 3. two-pointer walks: warps 0-3 rows (X), warps 4-7 columns (Y)
   const int ylim = ref_y_limit ? min(W, H) : H;
+  if (tid < 4 * 32) {
+    const int r = lane, sg = warp;  // lanes on rows
+    const int y = t.y0 + r, xs = t.x0 + sg * kBoundsSeg;
+    const int n = min(kBoundsSeg, W - xs);
+    if (y < H && n > 0)
+      bounds_walk(SH + r * DWp, 1, xs - t.x0 + rx, xs, n, rx, W, Tx,
+                  BX + r * TW + sg * kBoundsSeg, 1);
+  } else {
+    const int c = lane, sg = warp - 4;  // lanes on columns
+    const int x = t.x0 + c, ys = t.y0 + sg * kBoundsSeg;
+    const int n = min(kBoundsSeg, H - ys);
+    if (x < W && n > 0)
+      bounds_walk(SV + c, TW, ys - t.y0 + ry, ys, n, ry, ylim, Ty,
+                  BY + sg * kBoundsSeg * TW + c, TW);
+  }
+  __syncthreads();
+  // ---- 4. packed bounds, rows written coalesced
   uint32_t* bo = bounds + in.off;
-  for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
-    const int r = i / TW, c = i - r * TW;
+  for (int i = tid; i < TH * TW; i += kThreads) {
+    const int r = i / TW, c = i % TW;
     const int x = t.x0 + c, y = t.y0 + r;
-    if (x >= W || y >= H) continue;
-    const float* row = sH + r * DW + (c + rx - 1);  // row[0] = dH(x)
-    int dlx = 1, dux = 0, dly = 1, duy = 0;
-    float acc = 0.f;
-    for (int k = 1; k <= rx && x - k >= 0; ++k) {
-      acc += row[1 - k];
-      if (acc > sig_x) {
-        dlx = k;
-        break;
-      }
-    }
-    acc = 0.f;
-    for (int k = 1; k <= rx && x + k < W; ++k) {
-      acc += row[k];
-      if (acc > sig_x) {
-        dux = k - 1;
-        break;
-      }
-    }
-    const float* col = sV + (r + ry - 1) * TW + c;  // col[0] = dV(y)
-    acc = 0.f;
-    for (int k = 1; k <= ry && y - k >= 0; ++k) {
-      acc += col[(1 - k) * TW];
-      if (acc > sig_y) {
-        dly = k;
-        break;
-      }
-    }
-    acc = 0.f;
-    for (int k = 1; k <= ry && y + k < ylim; ++k) {
-      acc += col[k * TW];
-      if (acc > sig_y) {
-        duy = k - 1;
-        break;
-      }
-    }
-    bo[y * P + x] = pack_bounds(dlx, dux, dly, duy);
+    if (x < W && y < H) bo[y * P + x] = (uint32_t)BX[i] | ((uint32_t)BY[i] << 16);
   }
 }
 
@@ -969,15 +1011,27 @@ int launch_bounds(const DtsLaunch& L, const uchar4* guide, uint32_t* bounds,
   if (rx > 255 || ry > 255)
     return fail(DTSGB_ERR_UNSUPPORTED, "sigma >= 255 is not supported");
   const int TW = kBoundsTW, TH = kBoundsTH;
-  const size_t smem =
-      sizeof(float) * ((size_t)TH * (TW + 2 * rx - 1) + (size_t)(TH + 2 * ry - 1) * TW);
+  const size_t smem = sizeof(unsigned) * ((size_t)TH * ((TW + 2 * rx) | 1) +
+                                          (size_t)(TH + 2 * ry) * TW) +
+                      2 * sizeof(uint16_t) * TH * TW;
   if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "sigma too large");
+  // fixed point per axis: r * (sigma + 1) * 2^F <= 2^30; threshold floor(sigma 2^F)
+  auto fx = [](int r, float sigma, float* cap, float* scale, int* T) {
+    *cap = sigma + 1.f;
+    const int F = 30 - (int)std::ceil(std::log2((double)r * (double)*cap));
+    *scale = std::ldexp(1.f, F);
+    *T = (int)std::floor((double)sigma * std::ldexp(1.0, F));
+  };
+  float cap_x, cap_y, scale_x, scale_y;
+  int Tx, Ty;
+  fx(rx, sigma_x, &cap_x, &scale_x, &Tx);
+  fx(ry, sigma_y, &cap_y, &scale_y, &Ty);
   int st = set_smem(k_bounds<TW, TH>, smem);
   if (st) return st;
   ProfScope ps(s, DTSGB_K_BOUNDS);
   k_bounds<TW, TH><<<L.n_tiles, kThreads, smem, s>>>(
-      L.d_inst, L.d_tiles, guide, bounds, ratio_x, ratio_y, sigma_x, sigma_y,
-      rx, ry, ref_y_limit);
+      L.d_inst, L.d_tiles, guide, bounds, ratio_x, ratio_y, rx, ry, ref_y_limit, cap_x,
+      cap_y, scale_x, scale_y, Tx, Ty);
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
 }
