@@ -97,6 +97,8 @@ struct dtsgb_batch_s {
   long long gcap = 0;
   float* ovf = nullptr;
   long long ocap = 0;
+  float2* sgrid = nullptr;
+  long long scap = 0;
   // gradients of the DTS solve
   bool grad = false;
   int grad_seg_req = 0;          // 0: dts_checkpoint_segment(N)
@@ -153,6 +155,7 @@ void batch_free(dtsgb_batch_t b) {
   dfree(b->d_hinst);
   for (auto& p : b->hg) dfree(p);
   dfree(b->ovf);
+  dfree(b->sgrid);
   dfree(b->d_soff);
   dfree(b->stage);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
@@ -385,7 +388,8 @@ int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
   return batch_upload_targets(b, target, conf, kind, sync_host);
 }
 
-int ensure_hfbs_buffers(dtsgb_batch_t b, long long voxels, long long planes) {
+int ensure_hfbs_buffers(dtsgb_batch_t b, long long voxels, long long planes,
+                        long long slice_voxels) {
   if (voxels > b->gcap) {
     for (auto& p : b->hg) dfree(p);
     b->gcap = 0;
@@ -402,6 +406,13 @@ int ensure_hfbs_buffers(dtsgb_batch_t b, long long voxels, long long planes) {
     int st = dalloc(&b->ovf, (size_t)planes);
     if (st) return st;
     b->ocap = planes;
+    drop_graph(b, b->g_hfbs);
+  }
+  if (slice_voxels > b->scap) {
+    dfree(b->sgrid);
+    int st = dalloc(&b->sgrid, (size_t)slice_voxels);
+    if (st) return st;
+    b->scap = slice_voxels;
     drop_graph(b, b->g_hfbs);
   }
   return DTSGB_OK;
@@ -770,7 +781,8 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
   const int gl = (int)std::ceil(255.0 / (double)p->sigma_l);
   if (gl > 256) return fail(DTSGB_ERR_UNSUPPORTED, "more than 256 luma bins");
   std::vector<HInst> hi(b->n);
-  long long goff = 0, poff = 0, max_vox = 0, max_px = 0, max_cells = 0, max_lines = 0;
+  long long goff = 0, poff = 0, soff = 0, max_vox = 0, max_px = 0, max_cells = 0,
+            max_lines = 0;
   for (int i = 0; i < b->n; ++i) {
     const Inst& I = b->inst[i];
     HInst& H = hi[i];
@@ -787,6 +799,8 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
     H.pix_off = I.off;
     H.grid_off = goff;
     H.plane_off = poff;
+    H.slice_off = soff;
+    soff += round_up_ll((long long)(H.gx + 1) * (H.gy + 1) * (H.gl + 2), 32);
     const long long vox = (long long)H.gx * H.gy * H.gl;
     goff += round_up_ll(vox, 32);
     poff += round_up_ll((long long)H.gx * H.gy, 32);
@@ -796,7 +810,7 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
     max_lines = std::max({max_lines, (long long)H.gy * H.gl, (long long)H.gx * H.gl,
                           (long long)H.gx * H.gy});
   }
-  int st = ensure_hfbs_buffers(b, goff, poff);
+  int st = ensure_hfbs_buffers(b, goff, poff, soff);
   if (st) return st;
   const bool same_tables =
       b->hinst.size() == hi.size() &&
@@ -834,6 +848,7 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
   B.t0 = b->hg[HG_T0];
   B.t1 = b->hg[HG_T1];
   B.t2 = b->hg[HG_T2];
+  B.sgrid = b->sgrid;
   B.ovf = b->ovf;
   B.keep_debug = false;
   B.h_inst = b->hinst.data();

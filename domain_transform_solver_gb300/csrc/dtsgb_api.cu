@@ -663,6 +663,7 @@ struct dtsgb_hfbs_s {
   float *target = nullptr, *conf = nullptr, *out = nullptr;
   float* g[16] = {};
   float* ovf = nullptr;
+  float2* sgrid = nullptr;  // (max_gx + 1) x (max_gy + 1) x (max_gl + 2)
   HInst* d_inst = nullptr;
   dtsgb_hfbs_params p{};
   int gx = 0, gy = 0, gl = 0;
@@ -681,6 +682,7 @@ static void hfbs_free(dtsgb_hfbs_t h) {
   dfree(h->out);
   for (auto& p : h->g) dfree(p);
   dfree(h->ovf);
+  dfree(h->sgrid);
   dfree(h->d_inst);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   h->stream = nullptr;
@@ -719,6 +721,8 @@ DTSGB_API int dtsgb_hfbs_create(int max_w, int max_h, int max_gx, int max_gy,
   if (!st) st = dalloc(&h->out, h->plane);
   for (int i = 0; i < G_NUM && !st; ++i) st = dalloc(&h->g[i], h->gsize);
   if (!st) st = dalloc(&h->ovf, (size_t)max_gx * max_gy);
+  if (!st)
+    st = dalloc(&h->sgrid, (size_t)(max_gx + 1) * (max_gy + 1) * (max_gl + 2));
   if (!st) st = dalloc(&h->d_inst, 1);
   if (st) {
     if (g_last_error.find("memory") != std::string::npos)
@@ -867,6 +871,7 @@ DTSGB_API int dtsgb_hfbs_optimize(dtsgb_hfbs_t h) {
   I.pix_off = 0;
   I.grid_off = 0;
   I.plane_off = 0;
+  I.slice_off = 0;
   DTSGB_CUDA(cudaMemcpyAsync(h->d_inst, &I, sizeof(HInst),
                              cudaMemcpyHostToDevice, h->stream));
   HfbsBatch B{};
@@ -897,6 +902,7 @@ DTSGB_API int dtsgb_hfbs_optimize(dtsgb_hfbs_t h) {
   B.t0 = h->g[G_T0];
   B.t1 = h->g[G_T1];
   B.t2 = h->g[G_T2];
+  B.sgrid = h->sgrid;
   B.ovf = h->ovf;
   B.keep_debug = true;
   B.grid_bytes = (size_t)B.max_voxels * 4;

@@ -19,6 +19,10 @@ struct HInst {
   long long pix_off;    // element offset of pixel (0,0)
   long long grid_off;   // element offset of voxel (0,0,0)
   long long plane_off;  // element offset of the overflow count plane
+  // float2 offset of the slice grid: (count * z, count) over (gx + 1) x
+  // (gy + 1) x (gl + 2) voxels, zero past the grid and the overflow counts
+  // in plane gl (see k_slice_pack)
+  long long slice_off;
 };
 
 // Solver parameters shared by a batch (HFBSGridParams minus the grid dims).
@@ -48,6 +52,7 @@ struct HfbsBatch {
   Storage st;
   float* out;
   float *count, *csum, *b, *n0, *n1, *invA, *z0, *z1, *h, *t0, *t1, *t2, *ovf;
+  float2* sgrid;  // the instances' slice grids (HInst::slice_off)
   // optional debug copies (single-instance class API)
   bool keep_debug;
   size_t grid_bytes;

@@ -502,34 +502,60 @@ __global__ void __launch_bounds__(kTBThreads, 1)
 
 constexpr int kSliceXTable = 2048;
 
-__device__ __forceinline__ float slice_pixel(const HInst& I, const float* __restrict__ count,
-                                             const float* __restrict__ ovf,
-                                             const float* __restrict__ z, const HParams& p,
-                                             int x, float fy, float fz, const float* fxt) {
+// The slice's corner values, once per solve: (count * z, count) at every
+// voxel of (gx + 1) x (gy + 1) x (gl + 2), the overflow counts (times a zero
+// z, as the reference's read past the grid gives) in plane gl and zeros on
+// the faces past the grid, so that the slice reads its eight corners without
+// tests.  count * z is the product the reference forms first.  One warp per
+// (y, l) row of the padded grid.
+__global__ void k_slice_pack(const HInst* __restrict__ insts, const float* __restrict__ count,
+                             const float* __restrict__ ovf, const float* __restrict__ z,
+                             float2* __restrict__ sgrid) {
+  const HInst I = insts[blockIdx.y];
+  const int PX = I.gx + 1, PY = I.gy + 1, rows = PY * (I.gl + 2);
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < rows; row += nwarps) {
+    const int iz = row / PY, iy = row - iz * PY;
+    float2* out = sgrid + I.slice_off + (long long)row * PX;
+    for (int ix = lane; ix < PX; ix += 32) {
+      float2 v = make_float2(0.f, 0.f);
+      if (ix < I.gx && iy < I.gy) {
+        if (iz < I.gl) {
+          const long long g = gidx(I, ix, iy, iz);
+          const float c = count[g];
+          v = make_float2(c * z[g], c);
+        } else if (iz == I.gl) {
+          const float c = ovf[I.plane_off + (long long)iy * I.gx + ix];
+          v = make_float2(c * 0.f, c);
+        }
+      }
+      out[ix] = v;
+    }
+  }
+}
+
+__device__ __forceinline__ float slice_pixel(const HInst& I, const float2* __restrict__ sgrid,
+                                             const HParams& p, int x, float fy, float fz,
+                                             const float* fxt) {
   // x * 1.0f / sigma_x from the block's table where it covers x
   const float fx = x < kSliceXTable ? fxt[x] : (float)x * 1.0f / p.sigma_x;
   const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
   const float wx = fx - x0, wy = fy - y0, wz = fz - z0;
-  // the eight corners' loads are all issued before the weighting
-  float cnt[2][2][2], zv[2][2][2];
+  // x < W puts floor(x / sx) below gx (and likewise y, and L <= 255 puts
+  // floor(L / sl) at most gl); the clamps only keep the reads inside the
+  // padded grid
+  const int ix = min((int)x0, I.gx - 1), iy = min((int)y0, I.gy - 1),
+            iz = min((int)z0, I.gl);
+  const int PX = I.gx + 1, PXY = PX * (I.gy + 1);
+  const float2* c0 = sgrid + I.slice_off + (long long)iz * PXY + iy * PX + ix;
+  float2 v[2][2][2];  // the eight corners' loads, all issued before the weighting
 #pragma unroll
   for (int dz = 0; dz < 2; ++dz)
 #pragma unroll
     for (int dy = 0; dy < 2; ++dy)
 #pragma unroll
-      for (int dx = 0; dx < 2; ++dx) {
-        const int ix = (int)x0 + dx, iy = (int)y0 + dy, iz = (int)z0 + dz;
-        float c = 0.f, v = 0.f;
-        if (ix < I.gx && iy < I.gy && iz < I.gl) {
-          const long long g = gidx(I, ix, iy, iz);
-          c = count[g];
-          v = z[g];
-        } else if (ix < I.gx && iy < I.gy && iz == I.gl) {
-          c = ovf[I.plane_off + (long long)iy * I.gx + ix];
-        }
-        cnt[dz][dy][dx] = c;
-        zv[dz][dy][dx] = v;
-      }
+      for (int dx = 0; dx < 2; ++dx) v[dz][dy][dx] = c0[dz * PXY + dy * PX + dx];
   float num[2][2], den[2][2];
 #pragma unroll
   for (int dz = 0; dz < 2; ++dz)
@@ -539,17 +565,17 @@ __device__ __forceinline__ float slice_pixel(const HInst& I, const float* __rest
 #pragma unroll
       for (int dx = 0; dx < 2; ++dx) {
         const float w = dx ? wx : 1.f - wx;
-        ns += cnt[dz][dy][dx] * zv[dz][dy][dx] * w;
-        ds += cnt[dz][dy][dx] * w;
+        ns += v[dz][dy][dx].x * w;
+        ds += v[dz][dy][dx].y * w;
       }
       num[dz][dy] = ns;
       den[dz][dy] = ds;
     }
-  const float c0 = num[0][0] * (1.f - wy) + num[0][1] * wy;
-  const float c1 = num[1][0] * (1.f - wy) + num[1][1] * wy;
+  const float c0y = num[0][0] * (1.f - wy) + num[0][1] * wy;
+  const float c1y = num[1][0] * (1.f - wy) + num[1][1] * wy;
   const float c0m = den[0][0] * (1.f - wy) + den[0][1] * wy;
   const float c1m = den[1][0] * (1.f - wy) + den[1][1] * wy;
-  return __fdiv_rn(c0 * (1.f - wz) + c1 * wz, c0m * (1.f - wz) + c1m * wz);
+  return __fdiv_rn(c0y * (1.f - wz) + c1y * wz, c0m * (1.f - wz) + c1m * wz);
 }
 
 // a17: SliceSolution<true> (src/hfbs.cu:246-330): count-weighted trilinear
@@ -557,9 +583,7 @@ __device__ __forceinline__ float slice_pixel(const HInst& I, const float* __rest
 // along x, two pixels per lane per pass.
 __global__ void k_slice(const HInst* __restrict__ insts,
                         const uchar4* __restrict__ guide,
-                        const float* __restrict__ count,
-                        const float* __restrict__ ovf,
-                        const float* __restrict__ z, float* __restrict__ out,
+                        const float2* __restrict__ sgrid, float* __restrict__ out,
                         HParams p) {
   // the reference's x/sx and L/sl (correctly rounded divisions) are the same
   // for every row: computed once per block into tables
@@ -581,9 +605,9 @@ __global__ void k_slice(const HInst* __restrict__ insts,
       const int x1 = x0 + 32;
       const float z0 = fzt[g[row + x0].x];
       const float z1 = x1 < I.w ? fzt[g[row + x1].x] : 0.f;
-      const float r0 = slice_pixel(I, count, ovf, z, p, x0, fy, z0, fxt);
+      const float r0 = slice_pixel(I, sgrid, p, x0, fy, z0, fxt);
       if (x1 < I.w) {
-        const float r1 = slice_pixel(I, count, ovf, z, p, x1, fy, z1, fxt);
+        const float r1 = slice_pixel(I, sgrid, p, x1, fy, z1, fxt);
         o[row + x1] = r1;
       }
       o[row + x0] = r0;
@@ -761,7 +785,9 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
     DTSGB_CUDA(cudaMemcpyAsync(B.dbg_z_final, zs, B.grid_bytes,
                                cudaMemcpyDeviceToDevice, s));
   prof_begin(s, DTSGB_K_HFBS_SLICE);
-  k_slice<<<gp, kT, 0, s>>>(B.d_inst, B.guide, B.count, B.ovf, zs, B.out, p);
+  const dim3 gsl((unsigned)std::min<long long>(B.max_lines / 8 + 1, 4096), ni);
+  k_slice_pack<<<gsl, kT, 0, s>>>(B.d_inst, B.count, B.ovf, zs, B.sgrid);
+  k_slice<<<gp, kT, 0, s>>>(B.d_inst, B.guide, B.sgrid, B.out, p);
   prof_end(s, DTSGB_K_HFBS_SLICE);
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
