@@ -621,8 +621,18 @@ DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b, const dtsgb_filter_params* 
     if (iterate && over)
       return fail(DTSGB_ERR_UNSUPPORTED,
                   "gradients are not available with the confidence overwrite");
-    const int seg = b->grad_seg_req > 0 ? b->grad_seg_req
-                                        : dts_checkpoint_segment(std::max(n_kept, 1));
+    int seg = b->grad_seg_req;
+    if (seg <= 0) {
+      // automatic: every iterate kept (nothing recomputed by the backward)
+      // when its N + 4 planes fit in a quarter of the free device memory (or
+      // are held already), else the fewest planes
+      const int n = std::max(n_kept, 1);
+      const size_t need = (size_t)(n + 4) * (size_t)b->total * sizeof(float);
+      size_t free_b = 0, total_b = 0;
+      const bool held = b->grad_seg == 1 && b->gplanes.size() == (size_t)n + 4;
+      if (!held) DTSGB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+      seg = held || need <= free_b / 4 ? 1 : dts_checkpoint_segment(n);
+    }
     int st = ensure_grad_planes(b, n_kept, seg);
     if (st) return st;
   }

@@ -385,9 +385,10 @@ DTSGB_API int dtsgb_pipeline_run(dtsgb_pipeline_t p, int color_space,
 
 /* ---- Gradients of the batched DTS solve (new; the reference has no
  * gradients).  With gradients enabled, dtsgb_batch_solve_dts also keeps the
- * iterate v_k every `segment` iterations (0 = automatic: the length that
- * holds the fewest planes, near sqrt(num_iterations), and of those the
- * shortest),
+ * iterate v_k every `segment` iterations (0 = automatic: every iterate, so
+ * that the backward recomputes nothing, when those num_iterations + 4 planes
+ * fit in a quarter of the free device memory; else the length that holds
+ * the fewest planes, near sqrt(num_iterations), and of those the shortest),
  * and dtsgb_batch_dts_backward maps an upstream gradient dL/dv of each DTS
  * result to dL/dtarget and dL/dconfidence of the same solve.  The window
  * bounds found from the guide are held fixed: they are piecewise constant in

@@ -155,7 +155,8 @@ def test_checkpoint_segments_agree_bitwise(gpu_ready):
         b = _batch(D, data, opt, segment=seg, graphs=graphs)
         results.append(b.backward(go))
         seg_used, planes = b.grad_info()
-        want = seg if seg else 2  # fewest planes (5), then fewest recomputes
+        # automatic: every iterate kept (these few planes fit any free memory)
+        want = seg if seg else 1
         assert seg_used == want
         assert planes == -(-7 // want) - 1 + want + 4
         # the forward result is the plain solve's
@@ -171,12 +172,16 @@ def test_checkpoint_segments_agree_bitwise(gpu_ready):
 
 
 def test_memory_does_not_grow_with_iterations(gpu_ready):
+    """Checkpoint segments of about sqrt(N) hold ceil(N/K) - 1 + K + 4 planes;
+    the automatic choice keeps every iterate when that fits in free memory."""
     D = gpu_ready
     data = _inputs(990, sizes=[(40, 30)])
     for n, seg in ((16, 4), (100, 10)):
         opt = dict(num_iterations=n, loss=1, lambda_=0.99, sigma_z=4.0, step_size=0.99)
-        b = _batch(D, data, opt)
+        b = _batch(D, data, opt, segment=seg)
         assert b.grad_info() == (seg, -(-n // seg) - 1 + seg + 4)
+        b = _batch(D, data, opt)
+        assert b.grad_info() == (1, n + 4)
 
 
 def test_l1_and_zero_iterations_pass_the_gradient_to_the_target(gpu_ready):
