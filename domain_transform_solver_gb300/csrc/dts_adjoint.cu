@@ -185,13 +185,16 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   __syncthreads();
   // ---- X^T and the parameter gradients: one warp per tile row ----------------
   // A warp's global loads for its next row are issued before it works on the
-  // current one.
-  constexpr int CPL = TW / 32;  // tile columns per lane
+  // current one.  Each lane owns CPL adjacent tile columns (vector loads and
+  // stores; one warp scan per row).
+  constexpr int CPL = TW / 32;  // tile columns per lane, adjacent
   constexpr int BPL = 4;        // prefetched window columns per lane
+  static_assert(CPL == 1 || CPL == 2, "tile width 32 or 64");
   struct RowAdj {
     uint32_t bh[BPL];  // packed bounds of window columns lane + 32j
-    float v[CPL], tv[CPL], cv[CPL], gt[CPL], gc[CPL];  // tile columns lane + 32k
+    float v[CPL], tv[CPL], cv[CPL], gt[CPL], gc[CPL];  // tile columns CPL*lane + k
   };
+  const int xl = t.x0 + CPL * lane;  // first tile column of this lane
   auto fetch = [&](int rr, RowAdj& R) {
     const int row = (t.y0 + rr) * P;
 #pragma unroll
@@ -199,16 +202,32 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
       const int c = lane + 32 * j, x = gx0 + c;
       R.bh[j] = (c < SWc && (unsigned)x < (unsigned)W) ? __ldg(bnd_i + row + x) : 0u;
     }
+    const int p = row + xl;
+    if (CPL == 2 && xl + 1 < W) {  // both columns inside: 8-byte aligned pairs
+      const float2 v = __ldg(reinterpret_cast<const float2*>(vk_i + p));
+      const float2 g0 = *reinterpret_cast<const float2*>(gt_i + p);
+      const float2 g1 = *reinterpret_cast<const float2*>(gc_i + p);
+      R.v[0] = v.x;
+      R.v[CPL - 1] = v.y;
+      R.gt[0] = g0.x;
+      R.gt[CPL - 1] = g0.y;
+      R.gc[0] = g1.x;
+      R.gc[CPL - 1] = g1.y;
 #pragma unroll
-    for (int k = 0; k < CPL; ++k) {
-      const int x = t.x0 + lane + 32 * k;
-      const bool ok = x < W;
-      const int p = row + x;
-      R.v[k] = ok ? __ldg(vk_i + p) : 0.f;
-      R.tv[k] = ok ? load_f(tgt_i + p) : 0.f;
-      R.cv[k] = ok ? load_f(cnf_i + p) : 0.f;
-      R.gt[k] = ok ? gt_i[p] : 0.f;
-      R.gc[k] = ok ? gc_i[p] : 0.f;
+      for (int k = 0; k < CPL; ++k) {
+        R.tv[k] = load_f(tgt_i + p + k);
+        R.cv[k] = load_f(cnf_i + p + k);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < CPL; ++k) {
+        const bool ok = xl + k < W;
+        R.v[k] = ok ? __ldg(vk_i + p + k) : 0.f;
+        R.tv[k] = ok ? load_f(tgt_i + p + k) : 0.f;
+        R.cv[k] = ok ? load_f(cnf_i + p + k) : 0.f;
+        R.gt[k] = ok ? gt_i[p + k] : 0.f;
+        R.gc[k] = ok ? gc_i[p + k] : 0.f;
+      }
     }
   };
   const int rows = min(TH, H - t.y0);
@@ -251,18 +270,21 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
       atomicAdd(xb + hi + 1, 0u - A);
     });
     __syncwarp();
-    unsigned carry = 0;
+    // inclusive prefix of the difference array over this lane's columns
+    unsigned incl[CPL];
+    incl[0] = xb[CPL * lane];
+#pragma unroll
+    for (int k = 1; k < CPL; ++k) incl[k] = incl[k - 1] + xb[CPL * lane + k];
+    const unsigned off = warp_incl_scan(incl[CPL - 1], lane) - incl[CPL - 1];
+    float go[CPL], gtn[CPL], gcn[CPL];
 #pragma unroll
     for (int k = 0; k < CPL; ++k) {
-      const int cc = lane + 32 * k;
-      const unsigned incl = warp_incl_scan(xb[cc], lane) + carry;
-      carry = __shfl_sync(0xffffffffu, incl, 31);
-      const int x = t.x0 + cc;
+      const int x = xl + k;
+      go[k] = gtn[k] = gcn[k] = 0.f;
       if (x >= W) continue;
-      const int p = row + x;
-      const float bt = fx_window(incl, 0u, isF);
-      const float g1 = g1r[hx + cc];
-      const uint32_t b = __ldg(bnd_i + p);
+      const float bt = fx_window(incl[k] + off, 0u, isF);
+      const float g1 = g1r[hx + CPL * lane + k];
+      const uint32_t b = __ldg(bnd_i + row + x);
       const float rn = rtab[min((int)(b & 0xff), hx + 1) + min((int)((b >> 8) & 0xff), hx)];
       const float v = cur.v[k], tv = cur.tv[k], cv = cur.cv[k];
       const float d = v - tv;
@@ -275,9 +297,23 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
         dh_dv = __fdiv_rn(0.5f * (cv * rn) * 1e-6f, rt * rt * rt);
         dh_dc = __fdiv_rn(0.5f * d * rn, rt);
       }
-      gout_i[p] = __fmaf_rn(1.f - slam - step * dh_dv, g1, slam * bt);
-      gt_i[p] = cur.gt[k] + step * dh_dv * g1;
-      gc_i[p] = cur.gc[k] - step * dh_dc * g1;
+      go[k] = __fmaf_rn(1.f - slam - step * dh_dv, g1, slam * bt);
+      gtn[k] = cur.gt[k] + step * dh_dv * g1;
+      gcn[k] = cur.gc[k] - step * dh_dc * g1;
+    }
+    const int p = row + xl;
+    if (CPL == 2 && xl + 1 < W) {
+      *reinterpret_cast<float2*>(gout_i + p) = make_float2(go[0], go[CPL - 1]);
+      *reinterpret_cast<float2*>(gt_i + p) = make_float2(gtn[0], gtn[CPL - 1]);
+      *reinterpret_cast<float2*>(gc_i + p) = make_float2(gcn[0], gcn[CPL - 1]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < CPL; ++k)
+        if (xl + k < W) {
+          gout_i[p + k] = go[k];
+          gt_i[p + k] = gtn[k];
+          gc_i[p + k] = gcn[k];
+        }
     }
     __syncwarp();  // the warp's buffer is cleared for its next row
     cur = nxt;
