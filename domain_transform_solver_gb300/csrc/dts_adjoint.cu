@@ -40,11 +40,16 @@ struct AdjSmem {
     const size_t SR = TH + 2 * hy, SWc = TW + 2 * hx;
     const size_t nseg = std::max<size_t>(1, NT / SWc);
     auto up = [](size_t v) { return (v + 15) / 16 * 16; };
+    // The Y bounds (By), the Y segment totals and the X buffers are alive in
+    // turn (By until the scatter, the totals in the column prefix, the X
+    // buffers in X^T) and share one region; this keeps the 64 x 128 tile of
+    // sigma_z = 8 within two CTAs per SM.
     s2 = 0;                                                    // SR x SWc f32
-    by = up(s2 + SR * SWc * 4);                                // SR x SWc u16 | X buffers
-    d = up(by + std::max(SR * SWc * 2, (size_t)(NT / 32) * (TW + 1) * 4));
-    seg = up(d + (size_t)(TH + 1) * SWc * 4);                  // (TH+1) x SWc u32
-    rt = up(seg + nseg * SWc * 4);                             // nseg x SWc u32
+    by = up(s2 + SR * SWc * 4);                                // By | totals | X buffers
+    seg = by;                                                  // nseg x SWc u32
+    d = up(by + std::max({SR * SWc * 2, (size_t)(NT / 32) * (TW + 1) * 4,
+                          nseg * SWc * 4}));
+    rt = up(d + (size_t)(TH + 1) * SWc * 4);                   // (TH+1) x SWc u32 at d
     mx = up(rt + (size_t)(2 * std::max(hx, hy) + 2) * 4);
     total = mx + 16;
   }
