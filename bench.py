@@ -1,7 +1,7 @@
 """Benchmark of the DTS / HFBS hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg3|cfg0|cfg1|cfg4]
+                    [--workload cfg3|cfg0|cfg1|cfg2|cfg4]
 
 One JSON line on stdout (rank 0).  A step is one pass of the workload's
 solves with inputs already resident in HBM: for DTS the reference's timed
@@ -276,6 +276,65 @@ class Cfg0:
         return self.pixels, "one full solve"
 
 
+class Cfg2:
+    """DTS with a given confidence, 1280x384 RGB, Charbonnier, sigma_z 30, 15
+    iterations, BF16 storage of target and confidence (config 2)."""
+
+    name = "cfg2_dts_charbonnier_1280x384_bf16"
+    dtype = "bf16 storage, f32 math"
+
+    def __init__(self, rank: int):
+        import domain_transform_solver_gb300 as D
+        from domain_transform_solver_gb300 import workloads as W
+        self.D, self.W = D, W
+        self.inst = W.stereo_instance()
+        self.pixels = self.inst.width * self.inst.height
+        self.iters = W.CFG2_OPT["num_iterations"]
+        self.voxels = 0
+
+    def setup(self, stream_handle: int):
+        D, W = self.D, self.W
+        w, h = self.inst.width, self.inst.height
+        self.s = D.DomainTransformSolver(D.ImageDim(w, h), flags=D.FLAG_BF16_STORAGE)
+        self.s.SetStream(stream_handle)
+        self.s.ClearAll()
+        self.s.InitFrame(D.COLOR_SPACE.RGB, self.inst.rgba, self.inst.target,
+                         self.inst.confidence)
+        self.fp = D.DomainFilterParams(**W.CFG2_FILTER)
+        self.op = D.DomainOptimizeParams(**W.CFG2_OPT)
+        self.h_rgba = _pinned_copy(self.inst.rgba)
+        self.h_t = _pinned_copy(self.inst.target)
+        self.h_c = _pinned_copy(self.inst.confidence)
+        self.h_out = _pinned_empty((h, w))
+
+    def step(self):
+        self.s.ComputeColorSpaceDifferential(self.fp)
+        self.s.IntegrateColorDifferentials()
+        self.s.Optimize(self.op)
+
+    def step_e2e(self):
+        from domain_transform_solver_gb300._lib import check
+        lib, h = self.s._lib, self.s.handle
+        check(lib.dtsgb_dts_init_frame(h, 0, ctypes.c_void_p(self.h_rgba.ctypes.data),
+                                       ctypes.c_void_p(self.h_t.ctypes.data),
+                                       ctypes.c_void_p(self.h_c.ctypes.data)))
+        self.step()
+        check(lib.dtsgb_dts_download(h, 5, ctypes.c_void_p(self.h_out.ctypes.data)))
+
+    def e2e_bytes(self):
+        return self.pixels * 12, self.pixels * 4
+
+    def algorithmic_bytes(self):
+        return {0: 8 * self.pixels, 1: 16 * self.pixels, 8: 6 * self.pixels}
+
+    def cpu_sample(self, real="f32"):
+        import oracle as O
+        W = self.W
+        O.dts_solve(self.inst.rgba, self.inst.target, self.inst.confidence, 0,
+                    W.CFG2_FILTER, W.CFG2_OPT, real=real)
+        return self.pixels, "one full solve"
+
+
 class Cfg1:
     """HFBS colorization 640x480, U and V channels, 64 iterations (config 1)."""
 
@@ -445,7 +504,7 @@ class Cfg4:
         return inst.width * inst.height, "1 of the 16 instances, forward + adjoint"
 
 
-WORKLOADS = {"cfg3": Cfg3, "cfg0": Cfg0, "cfg1": Cfg1, "cfg4": Cfg4}
+WORKLOADS = {"cfg3": Cfg3, "cfg0": Cfg0, "cfg1": Cfg1, "cfg2": Cfg2, "cfg4": Cfg4}
 
 
 # ---- arms ----------------------------------------------------------------------
