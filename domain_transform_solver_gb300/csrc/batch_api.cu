@@ -277,15 +277,51 @@ __global__ void k_ingest(const Inst* __restrict__ insts, const long long* __rest
   }
 }
 
+// Dense staged plane -> pitched plane (gradient uploads).  Downloads stay
+// row-by-row DMA copies: those need no SM, so in a pipeline they do not wait
+// behind another chunk's solve.
+__global__ void k_unstage(const Inst* __restrict__ insts, const long long* __restrict__ soff,
+                          const float* __restrict__ src, float* __restrict__ dst) {
+  const Inst I = insts[blockIdx.y];
+  const long long so = soff[blockIdx.y];
+  for (int y = blockIdx.x; y < I.h; y += gridDim.x) {
+    const long long drow = so + (long long)y * I.w, prow = I.off + (long long)y * I.pitch;
+    for (int x = threadIdx.x; x < I.w; x += blockDim.x) dst[prow + x] = src[drow + x];
+  }
+}
+
+int ensure_stage(dtsgb_batch_t b) {
+  if (b->stage) return DTSGB_OK;
+  return dalloc(&b->stage, (size_t)b->dense * 12);
+}
+
+// Float region k (0..2) of the staging area.
+float* stage_plane(dtsgb_batch_t b, int k) {
+  return reinterpret_cast<float*>(b->stage + (size_t)b->dense * 4 * k);
+}
+
+// n host images -> pitched device plane, through staging region `region`.
+int host_upload_plane(dtsgb_batch_t b, const float* const* src, float* dst, int region) {
+  int st = ensure_stage(b);
+  if (st) return st;
+  float* d = stage_plane(b, region);
+  for (int i = 0; i < b->n; ++i) {
+    const Inst& I = b->inst[i];
+    DTSGB_CUDA(cudaMemcpyAsync(d + b->soff[i], src[i], (size_t)I.w * I.h * 4,
+                               cudaMemcpyHostToDevice, b->stream));
+  }
+  const dim3 grid((unsigned)std::min(b->max_h, 512), (unsigned)b->n);
+  k_unstage<<<grid, 256, 0, b->stream>>>(b->d_inst, b->d_soff, d, dst);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
 // Host upload: one contiguous copy per image and plane into the staging
 // area (pinned host memory makes them asynchronous), ones for missing
 // confidences, then k_ingest.  rgba null: targets only (guides kept).
 int host_ingest(dtsgb_batch_t b, int cs, const void* const* rgba,
                 const float* const* target, const float* const* conf, bool sync_host) {
-  if (!b->stage) {
-    int st = dalloc(&b->stage, (size_t)b->dense * 12);
-    if (st) return st;
-  }
+  if (int st = ensure_stage(b)) return st;
   uchar4* s_rgba = reinterpret_cast<uchar4*>(b->stage);
   float* s_t = reinterpret_cast<float*>(b->stage + (size_t)b->dense * 4);
   float* s_c = reinterpret_cast<float*>(b->stage + (size_t)b->dense * 8);
@@ -728,11 +764,15 @@ static int batch_backward(dtsgb_batch_t b, const float* const* grad_out,
     if (!grad_out[i]) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null gradient pointer");
   const int n_iter = b->grad_n;
   DtsGrad G = grad_view(b, n_iter);
-  for (int i = 0; i < b->n; ++i) {
-    const Inst& I = b->inst[i];
-    const size_t wb = (size_t)I.w * 4;
-    DTSGB_CUDA(cudaMemcpy2DAsync(G.g[0] + I.off, (size_t)I.pitch * 4, grad_out[i], wb, wb,
-                                 I.h, up, b->stream));
+  if (up == cudaMemcpyHostToDevice) {
+    if (int st = host_upload_plane(b, grad_out, G.g[0], 0)) return st;
+  } else {
+    for (int i = 0; i < b->n; ++i) {
+      const Inst& I = b->inst[i];
+      const size_t wb = (size_t)I.w * 4;
+      DTSGB_CUDA(cudaMemcpy2DAsync(G.g[0] + I.off, (size_t)I.pitch * 4, grad_out[i], wb, wb,
+                                   I.h, up, b->stream));
+    }
   }
   const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n, b->small, b->d_ti_small,
                      b->nti_small};
@@ -983,8 +1023,9 @@ static int batch_download(dtsgb_batch_t b, int which, float* const* dst,
   } else {
     return fail(DTSGB_ERR_INVALID_ARGUMENT, "which must be 0 (DTS) or 1 (HFBS)");
   }
-  for (int i = 0; i < b->n; ++i) {
+  for (int i = 0; i < b->n; ++i)
     if (!dst[i]) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null output pointer");
+  for (int i = 0; i < b->n; ++i) {
     const Inst& I = b->inst[i];
     const size_t wb = (size_t)I.w * 4;
     DTSGB_CUDA(cudaMemcpy2DAsync(dst[i], wb, src + I.off, (size_t)I.pitch * 4, wb, I.h,
