@@ -875,6 +875,7 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
   B.d_inst = b->d_hinst;
   B.n_inst = b->n;
   B.max_voxels = max_vox;
+  B.total_voxels = goff;
   B.max_pixels = max_px;
   B.max_cells = max_cells;
   B.max_lines = max_lines;

@@ -879,6 +879,7 @@ DTSGB_API int dtsgb_hfbs_optimize(dtsgb_hfbs_t h) {
   B.h_inst = &I;
   B.n_inst = 1;
   B.max_voxels = (long long)I.gx * I.gy * I.gl;
+  B.total_voxels = B.max_voxels;
   B.max_pixels = (long long)I.w * I.h;
   B.max_cells = (long long)I.gx * I.gy;
   B.max_rows = (long long)I.gy * I.gl;

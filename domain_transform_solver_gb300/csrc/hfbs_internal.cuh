@@ -44,6 +44,9 @@ struct HfbsBatch {
   // bistoch_iter_max) is that of the same guide and grid: skip recomputing it
   bool reuse_norm = false;
   long long max_voxels, max_pixels, max_cells, max_lines;
+  // voxels of the whole grid arena (instances and the gaps that round each
+  // instance's grid to 32 voxels): the span of the elementwise kernels
+  long long total_voxels;
   long long max_rows;  // max over instances of gy * gl (grid rows along x)
   int max_gl;
   const uchar4* guide;

@@ -93,12 +93,12 @@ __global__ void __launch_bounds__(64)
   }
 }
 
-__global__ void k_fill_ones(const HInst* __restrict__ insts, float* __restrict__ a) {
-  const HInst I = insts[blockIdx.y];
-  const long long n = (long long)I.gx * I.gy * I.gl;
+// The elementwise kernels below run flat over the whole grid arena: the
+// voxels in the gaps between instances are computed too and never read.
+__global__ void k_fill_ones(float* __restrict__ a, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    a[I.grid_off + i] = 1.f;
+    a[i] = 1.f;
 }
 
 // a13: one BistochastasizeOptimize step (src/hfbs.cu:126-155):
@@ -162,16 +162,11 @@ __global__ void k_bistoch(const HInst* __restrict__ insts,
 // midpoint), so the FP64 division is replaced by __frcp_rn.  d >= 1e-3f is
 // the float form of (double)d > 1e-3, and 1/1e-3 rounds to 1000 (NaN too,
 // as fmax returns the other operand).
-__global__ void k_inv_diag(const HInst* __restrict__ insts,
-                           const float* __restrict__ count,
-                           const float* __restrict__ csum,
-                           const float* __restrict__ norm,
-                           float* __restrict__ invA, float lambda) {
-  const HInst I = insts[blockIdx.y];
-  const long long n = (long long)I.gx * I.gy * I.gl;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long g = I.grid_off + i;
+__global__ void k_inv_diag(const float* __restrict__ count, const float* __restrict__ csum,
+                           const float* __restrict__ norm, float* __restrict__ invA,
+                           float lambda, long long n) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+       g += (long long)gridDim.x * blockDim.x) {
     const float nv = norm[g];
     const float diag = lambda * (count[g] - 2.f * nv * nv) + csum[g];
     invA[g] = diag >= 1e-3f ? __frcp_rn(diag) : 1000.f;
@@ -287,17 +282,23 @@ __global__ void k_laplace(const HInst* __restrict__ insts, int axis,
   }
 }
 
-// (float)((double)b / ((double)c + 1e-7)) without a double division, which
-// is slow on this part.  The double denominator d is split into floats
-// dh + dl (|dl| <= ulp(dh) / 2, exact to 2^-48 of d); q0 = b / dh is
-// correctly rounded, so b - q0 * dh is exact by FMA, and q0 + (b - q0 * d) / dh
-// carries the quotient to about 2^-46 of itself before the final rounding:
-// it can differ from the double quotient's rounding only when that lies
-// within about 2^-23 ulp of a float rounding midpoint.
+// (float)((double)b / ((double)c + 1e-7)) without double arithmetic, which
+// is slow on this part.  The denominator c + 1e-7 is carried as floats
+// dh + dl to about 2^-48 of itself: an exact two-sum of c and the float
+// nearest 1e-7, plus the rest of the double 1e-7.  q0 = b / dh is correctly
+// rounded, so b - q0 * dh is exact by FMA, and q0 + (b - q0 * d) / dh carries
+// the quotient to about 2^-46 of itself before the final rounding: it can
+// differ from the double quotient's rounding only when that lies within
+// about 2^-22 ulp of a float rounding midpoint.
 __device__ __forceinline__ float div_by_c_plus_eps(float b, float c) {
-  const double d = (double)c + 1e-7;
-  const float dh = (float)d;
-  const float dl = (float)(d - (double)dh);
+  constexpr float e_hi = 1e-7f;
+  constexpr float e_lo = (float)(1e-7 - (double)1e-7f);
+  const float s = c + e_hi;
+  const float bb = s - c;
+  const float err = (c - (s - bb)) + (e_hi - bb);  // c + e_hi == s + err exactly
+  const float dl0 = err + e_lo;
+  const float dh = s + dl0;
+  const float dl = dl0 - (dh - s);
   const float q0 = __fdiv_rn(b, dh);
   float r = __fmaf_rn(-q0, dh, b);
   r = __fmaf_rn(-q0, dl, r);
@@ -306,15 +307,10 @@ __device__ __forceinline__ float div_by_c_plus_eps(float b, float c) {
 
 // InitZ<true> (src/hfbs.cu:337-353): z = blur(b) / (blur(c) + 1e-7), the
 // division in double as the reference's double literal makes it; h = 0.
-__global__ void k_init_z(const HInst* __restrict__ insts,
-                         const float* __restrict__ blur_b,
-                         const float* __restrict__ blur_c, float* __restrict__ z,
-                         float* __restrict__ h) {
-  const HInst I = insts[blockIdx.y];
-  const long long n = (long long)I.gx * I.gy * I.gl;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long g = I.grid_off + i;
+__global__ void k_init_z(const float* __restrict__ blur_b, const float* __restrict__ blur_c,
+                         float* __restrict__ z, float* __restrict__ h, long long n) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+       g += (long long)gridDim.x * blockDim.x) {
     z[g] = div_by_c_plus_eps(blur_b[g], blur_c[g]);
     h[g] = 0.f;
   }
@@ -625,7 +621,6 @@ int blocks_for(long long n) {
 
 int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   const int ni = B.n_inst;
-  const dim3 gv(blocks_for(B.max_voxels), ni);
   // row kernels: one warp per grid row, 8 warps per block
   const dim3 gr((unsigned)std::min<long long>((B.max_rows + 7) / 8, 4096), ni);
   // slice: one warp per image row, 8 rows per block
@@ -657,7 +652,8 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   prof_end(s, DTSGB_K_HFBS_SPLAT);
   // bistochastization ping-pong: even iterations read the buffer filled with
   // ones, whose covered pad faces hold 1
-  if (!B.reuse_norm) k_fill_ones<<<gv, kT, 0, s>>>(B.d_inst, B.n0);
+  const int gflat = blocks_for(B.total_voxels);
+  if (!B.reuse_norm) k_fill_ones<<<gflat, kT, 0, s>>>(B.n0, B.total_voxels);
   // The iterative stages (bistochastization, heavy-ball) touch only their own
   // instance's grid, so they run group by group: all iterations of a group
   // of consecutive instances whose grids fit in L2 before the next group,
@@ -710,8 +706,8 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   float* norm = src;
   float* spare = dst;
   prof_begin(s, DTSGB_K_HFBS_OTHER);
-  k_inv_diag<<<gv, kT, 0, s>>>(B.d_inst, B.count, B.csum, norm, B.invA,
-                               p.lambda);
+  k_inv_diag<<<gflat, kT, 0, s>>>(B.count, B.csum, norm, B.invA, p.lambda,
+                                  B.total_voxels);
   // Laplace blur of (c, b): X -> Y -> Z.
   const dim3 gl_lines(blocks_for(B.max_lines), ni);
   k_laplace_x<<<gr, kT, 0, s>>>(B.d_inst, B.csum, B.t0, B.b, B.t1, p.neg_exp_beta);
@@ -720,7 +716,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   k_laplace<<<gl_lines, kT, 0, s>>>(B.d_inst, 2, B.t2, B.t0, spare, B.t1,
                                     p.neg_exp_beta);
   // blur_c = t0, blur_b = t1
-  k_init_z<<<gv, kT, 0, s>>>(B.d_inst, B.t1, B.t0, B.z0, B.h);
+  k_init_z<<<gflat, kT, 0, s>>>(B.t1, B.t0, B.z0, B.h, B.total_voxels);
   prof_end(s, DTSGB_K_HFBS_OTHER);
   if (B.keep_debug) {
     DTSGB_CUDA(cudaMemcpyAsync(B.dbg_blur_c, B.t0, B.grid_bytes,
@@ -785,7 +781,11 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
     DTSGB_CUDA(cudaMemcpyAsync(B.dbg_z_final, zs, B.grid_bytes,
                                cudaMemcpyDeviceToDevice, s));
   prof_begin(s, DTSGB_K_HFBS_SLICE);
-  const dim3 gsl((unsigned)std::min<long long>(B.max_lines / 8 + 1, 4096), ni);
+  long long prows = 1;  // rows of the largest padded slice grid
+  for (int i = 0; B.h_inst && i < ni; ++i)
+    prows = std::max<long long>(prows, (long long)(B.h_inst[i].gy + 1) * (B.h_inst[i].gl + 2));
+  if (!B.h_inst) prows = B.max_lines + 2 * B.max_rows + 260;
+  const dim3 gsl((unsigned)std::min<long long>((prows + 7) / 8, 4096), ni);
   k_slice_pack<<<gsl, kT, 0, s>>>(B.d_inst, B.count, B.ovf, zs, B.sgrid);
   k_slice<<<gp, kT, 0, s>>>(B.d_inst, B.guide, B.sgrid, B.out, p);
   prof_end(s, DTSGB_K_HFBS_SLICE);
