@@ -67,22 +67,57 @@ __global__ void __launch_bounds__(64)
     const int bx = cell % I.gx, by = cell / I.gx;
     const int xs = cell_start(bx, p.sigma_x, I.w), xe = cell_start(bx + 1, p.sigma_x, I.w);
     const int ys = cell_start(by, p.sigma_y, I.h), ye = cell_start(by + 1, p.sigma_y, I.h);
+    // a run of pixels in the same luma bin is summed in registers and added
+    // to the cell's histogram when the bin changes (a fixed order: the
+    // result is deterministic)
+    int run = -1;
+    float r_ct = 0.f, r_c = 0.f, r_n = 0.f;
+    auto flush = [&]() {
+      if (run < 0) return;
+      if (run < gl) {
+        hist[(3 * run + 0) * T + threadIdx.x] += r_ct;
+        hist[(3 * run + 1) * T + threadIdx.x] += r_c;
+        hist[(3 * run + 2) * T + threadIdx.x] += r_n;
+      } else {
+        ovf_cnt += r_n;
+      }
+    };
+    constexpr int U = 8;  // pixels whose loads are issued together
     for (int y = ys; y < ye; ++y) {
       const long long row = I.pix_off + (long long)y * I.pitch;
-      for (int x = xs; x < xe; ++x) {
-        const uchar4 g = guide[row + x];
-        const int bl = lbin[g.x];
-        const float c = load_f(cnf + row + x);
-        const float ct = c * load_f(tgt + row + x);
-        if (bl < gl) {
-          hist[(3 * bl + 0) * T + threadIdx.x] += ct;
-          hist[(3 * bl + 1) * T + threadIdx.x] += c;
-          hist[(3 * bl + 2) * T + threadIdx.x] += 1.f;
-        } else {
-          ovf_cnt += 1.f;
+      for (int x0 = xs; x0 < xe; x0 += U) {
+        int lum[U];
+        float cv[U], tv[U];
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+          lum[k] = 0;
+          cv[k] = tv[k] = 0.f;
+          if (x0 + k < xe) {
+            lum[k] = guide[row + x0 + k].x;
+            cv[k] = load_f(cnf + row + x0 + k);
+            tv[k] = load_f(tgt + row + x0 + k);
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+          if (x0 + k >= xe) break;
+          const int bl = lbin[lum[k]];
+          const float ct = cv[k] * tv[k];
+          if (bl != run) {
+            flush();
+            run = bl;
+            r_ct = ct;
+            r_c = cv[k];
+            r_n = 1.f;
+          } else {
+            r_ct += ct;
+            r_c += cv[k];
+            r_n += 1.f;
+          }
         }
       }
     }
+    flush();
     for (int z = 0; z < gl; ++z) {
       const long long gi = gidx(I, bx, by, z);
       b[gi] = hist[(3 * z + 0) * T + threadIdx.x];
