@@ -30,6 +30,7 @@ namespace dtsgb {
 namespace {
 
 constexpr int kT = 256;
+constexpr int kAdjFirst = 1, kAdjLast = 2;
 
 
 // Shared-memory layout (byte offsets, 16-byte aligned regions).
@@ -62,7 +63,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
                   const float* __restrict__ vk, const TS* __restrict__ tgt,
                   const TS* __restrict__ cnf, const uint32_t* __restrict__ bnd,
                   float* __restrict__ grad_t, float* __restrict__ grad_c,
-                  float lambda, float step, int hx, int hy, AdjSmem<TW, TH, NT> L) {
+                  float lambda, float step, int hx, int hy, int flags,
+                  AdjSmem<TW, TH, NT> L) {
+  // flags: kAdjFirst, the first adjoint of a backward (dL/dt and dL/dc start
+  // at zero: not read); kAdjLast, the last (its dL/dv_0 goes into dL/dt, as
+  // v_0 = t, instead of to gout)
+  const bool first = flags & kAdjFirst, last = flags & kAdjLast;
   constexpr int NW = NT / 32;
   extern __shared__ __align__(16) unsigned char smraw[];
   const Tile t = tiles[blockIdx.x];
@@ -210,8 +216,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
     const int p = row + xl;
     if (CPL == 2 && xl + 1 < W) {  // both columns inside: 8-byte aligned pairs
       const float2 v = __ldg(reinterpret_cast<const float2*>(vk_i + p));
-      const float2 g0 = *reinterpret_cast<const float2*>(gt_i + p);
-      const float2 g1 = *reinterpret_cast<const float2*>(gc_i + p);
+      const float2 g0 =
+          first ? make_float2(0.f, 0.f) : *reinterpret_cast<const float2*>(gt_i + p);
+      const float2 g1 =
+          first ? make_float2(0.f, 0.f) : *reinterpret_cast<const float2*>(gc_i + p);
       R.v[0] = v.x;
       R.v[CPL - 1] = v.y;
       R.gt[0] = g0.x;
@@ -230,8 +238,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
         R.v[k] = ok ? __ldg(vk_i + p + k) : 0.f;
         R.tv[k] = ok ? load_f(tgt_i + p + k) : 0.f;
         R.cv[k] = ok ? load_f(cnf_i + p + k) : 0.f;
-        R.gt[k] = ok ? gt_i[p + k] : 0.f;
-        R.gc[k] = ok ? gc_i[p + k] : 0.f;
+        R.gt[k] = ok && !first ? gt_i[p + k] : 0.f;
+        R.gc[k] = ok && !first ? gc_i[p + k] : 0.f;
       }
     }
   };
@@ -305,17 +313,18 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
       go[k] = __fmaf_rn(1.f - slam - step * dh_dv, g1, slam * bt);
       gtn[k] = cur.gt[k] + step * dh_dv * g1;
       gcn[k] = cur.gc[k] - step * dh_dc * g1;
+      if (last) gtn[k] += go[k];
     }
     const int p = row + xl;
     if (CPL == 2 && xl + 1 < W) {
-      *reinterpret_cast<float2*>(gout_i + p) = make_float2(go[0], go[CPL - 1]);
+      if (!last) *reinterpret_cast<float2*>(gout_i + p) = make_float2(go[0], go[CPL - 1]);
       *reinterpret_cast<float2*>(gt_i + p) = make_float2(gtn[0], gtn[CPL - 1]);
       *reinterpret_cast<float2*>(gc_i + p) = make_float2(gcn[0], gcn[CPL - 1]);
     } else {
 #pragma unroll
       for (int k = 0; k < CPL; ++k)
         if (xl + k < W) {
-          gout_i[p + k] = go[k];
+          if (!last) gout_i[p + k] = go[k];
           gt_i[p + k] = gtn[k];
           gc_i[p + k] = gcn[k];
         }
@@ -337,7 +346,8 @@ __global__ void k_axpy_planes(const Inst* __restrict__ insts, const float* __res
 template <typename TS, int MODE, int TW, int TH>
 int launch_adj_shape(const DtsLaunch& L, const float* gin, float* gout, const float* vk,
                      const void* t, const void* c, const uint32_t* bounds, float* gt,
-                     float* gc, float lambda, float step, int hx, int hy, cudaStream_t s) {
+                     float* gc, float lambda, float step, int hx, int hy, int flags,
+                     cudaStream_t s) {
   constexpr int NT = TW >= 64 ? 512 : 256;
   const AdjSmem<TW, TH, NT> lay(hx, hy);
   if (lay.total > 227 * 1024)
@@ -348,7 +358,7 @@ int launch_adj_shape(const DtsLaunch& L, const float* gin, float* gout, const fl
                                     (int)lay.total));
   k_dts_adjoint<TS, MODE, TW, TH, NT><<<L.n_tiles, NT, lay.total, s>>>(
       L.d_inst, L.d_tiles, gin, gout, vk, (const TS*)t, (const TS*)c, bounds, gt, gc,
-      lambda, step, hx, hy, lay);
+      lambda, step, hx, hy, flags, lay);
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
 }
@@ -356,34 +366,34 @@ int launch_adj_shape(const DtsLaunch& L, const float* gin, float* gout, const fl
 template <typename TS, int MODE>
 int launch_adj_t(const DtsLaunch& L, const float* gin, float* gout, const float* vk,
                  const void* t, const void* c, const uint32_t* bounds, float* gt, float* gc,
-                 float lambda, float step, int hx, int hy, cudaStream_t s) {
+                 float lambda, float step, int hx, int hy, int flags, cudaStream_t s) {
   if (L.small)
     return launch_adj_shape<TS, MODE, kIterSmallTW, kIterSmallTH>(
-        L, gin, gout, vk, t, c, bounds, gt, gc, lambda, step, hx, hy, s);
+        L, gin, gout, vk, t, c, bounds, gt, gc, lambda, step, hx, hy, flags, s);
   if (L.d_tiles_small && AdjSmem<kIterTW, kIterTH, 512>(hx, hy).total > 227 * 1024)
     return launch_adj_shape<TS, MODE, kIterSmallTW, kIterSmallTH>(
-        L.as_small(), gin, gout, vk, t, c, bounds, gt, gc, lambda, step, hx, hy, s);
+        L.as_small(), gin, gout, vk, t, c, bounds, gt, gc, lambda, step, hx, hy, flags, s);
   return launch_adj_shape<TS, MODE, kIterTW, kIterTH>(L, gin, gout, vk, t, c, bounds, gt,
-                                                      gc, lambda, step, hx, hy, s);
+                                                      gc, lambda, step, hx, hy, flags, s);
 }
 
 int launch_adjoint(const DtsLaunch& L, Storage st, IterMode mode, const float* gin,
                    float* gout, const float* vk, const void* t, const void* c,
                    const uint32_t* bounds, float* gt, float* gc, float lambda,
-                   float step, int hx, int hy, cudaStream_t s) {
+                   float step, int hx, int hy, int flags, cudaStream_t s) {
   ProfScope ps(s, DTSGB_K_DTS_ADJOINT);
   if (st == Storage::F32) {
     if (mode == IterMode::L2)
       return launch_adj_t<float, 0>(L, gin, gout, vk, t, c, bounds, gt, gc, lambda, step,
-                                    hx, hy, s);
+                                    hx, hy, flags, s);
     return launch_adj_t<float, 1>(L, gin, gout, vk, t, c, bounds, gt, gc, lambda, step, hx,
-                                  hy, s);
+                                  hy, flags, s);
   }
   if (mode == IterMode::L2)
     return launch_adj_t<__nv_bfloat16, 0>(L, gin, gout, vk, t, c, bounds, gt, gc, lambda,
-                                          step, hx, hy, s);
+                                          step, hx, hy, flags, s);
   return launch_adj_t<__nv_bfloat16, 1>(L, gin, gout, vk, t, c, bounds, gt, gc, lambda,
-                                        step, hx, hy, s);
+                                        step, hx, hy, flags, s);
 }
 
 }  // namespace
@@ -447,8 +457,15 @@ int dts_backward(const DtsLaunch& L, const Inst* d_inst, int n_inst, long long p
                  const void* conf, const uint32_t* bounds, float lambda, float step,
                  int halo, int num_iterations, float* grad_t, float* grad_c,
                  cudaStream_t s) {
-  DTSGB_CUDA(cudaMemsetAsync(grad_t, 0, plane * sizeof(float), s));
-  DTSGB_CUDA(cudaMemsetAsync(grad_c, 0, plane * sizeof(float), s));
+  if (num_iterations <= 0) {  // v = t: dL/dt = dL/dv, dL/dc = 0
+    DTSGB_CUDA(cudaMemsetAsync(grad_t, 0, plane * sizeof(float), s));
+    DTSGB_CUDA(cudaMemsetAsync(grad_c, 0, plane * sizeof(float), s));
+    k_axpy_planes<<<dim3(64, n_inst), kT, 0, s>>>(d_inst, G.g[0], grad_t);
+    DTSGB_CUDA(cudaGetLastError());
+    return DTSGB_OK;
+  }
+  // the first adjoint writes dL/dt and dL/dc (no zeroing pass), the last
+  // adds dL/dv_0 to dL/dt (no final pass)
   float* g = G.g[0];  // holds dL/dv_N on entry
   float* gn = G.g[1];
   const int nseg = (num_iterations + G.seg - 1) / G.seg;
@@ -468,16 +485,14 @@ int dts_backward(const DtsLaunch& L, const Inst* d_inst, int n_inst, long long p
       if (st_) return st_;
     }
     for (int k = len - 1; k >= 0; --k) {
+      const int flags = (j == nseg - 1 && k == len - 1 ? kAdjFirst : 0) |
+                        (j == 0 && k == 0 ? kAdjLast : 0);
       int st_ = launch_adjoint(L, st, mode, g, gn, k == 0 ? x0 : G.segbuf[k], target, conf,
-                               bounds, grad_t,
-                               grad_c, lambda, step, halo, halo, s);
+                               bounds, grad_t, grad_c, lambda, step, halo, halo, flags, s);
       if (st_) return st_;
       std::swap(g, gn);
     }
   }
-  // v_0 = t
-  k_axpy_planes<<<dim3(64, n_inst), kT, 0, s>>>(d_inst, g, grad_t);
-  DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
 }
 
