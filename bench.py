@@ -397,11 +397,11 @@ class Cfg1:
 
 class Cfg4:
     """Differentiable DTS: 16 x 1024x768 config-0-style instances, FP32,
-    L2, 10 iterations, forward with checkpoints (the automatic segment
-    length: 2 for 10 iterations, 10 planes held instead of 10 + 4 iterates)
-    plus the adjoint (dL/dtarget, dL/dconfidence) for an N(0,1) upstream
-    gradient.  One step = forward + backward; the guide's window
-    bounds are held fixed (piecewise constant in the guide)."""
+    L2, 10 iterations, the forward keeping its iterates (the automatic
+    checkpoint choice: every iterate, as 14 planes fit in free memory) plus
+    the adjoint (dL/dtarget, dL/dconfidence) for an N(0,1) upstream
+    gradient.  One step = forward + backward; the guide's window bounds
+    are held fixed (piecewise constant in the guide)."""
 
     name = "cfg4_dts_fwd_bwd_16x1024x768_f32"
     dtype = "f32"
