@@ -765,13 +765,10 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   float* zd = B.z1;
   if (B.max_gl <= kTBMaxGL && B.h_inst) {
     // K heavy-ball steps per pass; h ping-pongs through the free blur
-    // temporary t2 (its final value is not needed)
-    static bool attr = false;
-    if (!attr) {
-      DTSGB_CUDA(cudaFuncSetAttribute(k_solve_tb, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)kTBSmem));
-      attr = true;
-    }
+    // temporary t2 (its final value is not needed).  The shared-memory limit
+    // is a per-device attribute: set on every call (host-side, cheap).
+    DTSGB_CUDA(cudaFuncSetAttribute(k_solve_tb, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kTBSmem));
     for (const Group& g : groups) {
       zs = B.z0;
       zd = B.z1;
