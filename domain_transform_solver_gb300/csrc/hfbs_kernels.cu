@@ -632,16 +632,23 @@ __global__ void k_slice(const HInst* __restrict__ insts,
   for (int y = blockIdx.x * wpb + (threadIdx.x >> 5); y < I.h; y += gridDim.x * wpb) {
     const int row = y * I.pitch;
     const float fy = (float)y * 1.0f / p.sigma_y;
-    for (int x0 = lane; x0 < I.w; x0 += 64) {
-      const int x1 = x0 + 32;
-      const float z0 = fzt[g[row + x0].x];
-      const float z1 = x1 < I.w ? fzt[g[row + x1].x] : 0.f;
-      const float r0 = slice_pixel(I, sgrid, p, x0, fy, z0, fxt);
-      if (x1 < I.w) {
-        const float r1 = slice_pixel(I, sgrid, p, x1, fy, z1, fxt);
-        o[row + x1] = r1;
+    // four pixels per lane per pass: their 32 corner loads are in flight
+    // together
+    for (int xb = lane; xb < I.w; xb += 128) {
+      float zq[4], rq[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int x = xb + 32 * u;
+        zq[u] = x < I.w ? fzt[g[row + x].x] : 0.f;
       }
-      o[row + x0] = r0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int x = min(xb + 32 * u, I.w - 1);  // past the width: a copy of the last
+        rq[u] = slice_pixel(I, sgrid, p, x, fy, zq[u], fxt);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (xb + 32 * u < I.w) o[row + xb + 32 * u] = rq[u];
     }
   }
 }
