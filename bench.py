@@ -8,8 +8,9 @@ solves with inputs already resident in HBM: for DTS the reference's timed
 window (src/edge_aware_solver.h:72-84: differential, integration, all
 iterations), for HFBS the whole HFBS::Optimize.  `e2e` times the same step
 through the public C ABI with pinned host buffers, the upload and the
-download included (config 3: dtsgb_pipeline_run, which overlaps the copies
-of one chunk of instances with the solves of another; --e2e-chunks).
+download included (configs 3 and 4: dtsgb_pipeline_run / _run_grad, which
+overlap the copies of one chunk of instances with the solves of another;
+--e2e-chunks).
 Under torchrun every rank solves its own copy of the workload (independent
 instances, no collective): weak scaling.
 
@@ -406,7 +407,8 @@ class Cfg4:
     name = "cfg4_dts_fwd_bwd_16x1024x768_f32"
     dtype = "f32"
 
-    def __init__(self, rank: int):
+    def __init__(self, rank: int, e2e_chunks: int = 4):
+        self.e2e_chunks = e2e_chunks
         import domain_transform_solver_gb300 as D
         from domain_transform_solver_gb300 import workloads as W
         self.D, self.W = D, W
@@ -448,6 +450,10 @@ class Cfg4:
         self.h_g, self.h_v = _ptrs(self._g), _ptrs(self._v)
         self.h_gt, self.h_gc = _ptrs(self._ogt), _ptrs(self._ogc)
         # the plain forward (no checkpoints) of the same batch, for the ratio
+        # the host-to-host path: chunks of instances on their own streams
+        self.pipe = D.Pipeline(self.sizes, n_chunks=self.e2e_chunks)
+        self.pipe.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)
+        self.e2e_api = f"dtsgb_pipeline_run_grad, {self.pipe.n_chunks} chunks"
         self.fwd = D.Batch(self.sizes)
         self.fwd.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)
         self.fwd.set_stream(stream_handle)
@@ -468,12 +474,10 @@ class Cfg4:
 
     def step_e2e(self):
         from domain_transform_solver_gb300._lib import check
-        h = self.b.handle
-        check(self.lib.dtsgb_batch_upload(h, 1, self.h_rgba, self.h_t, self.h_c))
-        check(self.lib.dtsgb_batch_solve_dts(h, ctypes.byref(self.fp), ctypes.byref(self.op),
-                                             ctypes.c_float(-1.0)))
-        check(self.lib.dtsgb_batch_download(h, 0, self.h_v))
-        check(self.lib.dtsgb_batch_dts_backward(h, self.h_g, self.h_gt, self.h_gc))
+        check(self.lib.dtsgb_pipeline_run_grad(self.pipe.handle, 1, self.h_rgba, self.h_t,
+                                               self.h_c, ctypes.byref(self.fp),
+                                               ctypes.byref(self.op), self.h_g, self.h_v,
+                                               self.h_gt, self.h_gc))
 
     def e2e_bytes(self):
         # rgba, target, confidence, upstream gradient in; v, dL/dt, dL/dc out
@@ -511,6 +515,8 @@ WORKLOADS = {"cfg3": Cfg3, "cfg0": Cfg0, "cfg1": Cfg1, "cfg2": Cfg2, "cfg4": Cfg
 def make_workload(args, rank):
     if args.workload == "cfg3":
         return Cfg3(rank, scale=args.scale, e2e_chunks=args.e2e_chunks)
+    if args.workload == "cfg4":
+        return Cfg4(rank, e2e_chunks=args.e2e_chunks if args.e2e_chunks_set else 4)
     return WORKLOADS[args.workload](rank)
 
 
@@ -751,9 +757,12 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="cfg3")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="cfg3 only: shrink every instance (smaller profiling case)")
-    ap.add_argument("--e2e-chunks", type=int, default=16,
-                    help="cfg3 only: chunks of the overlapped host-to-host e2e run")
+    ap.add_argument("--e2e-chunks", type=int, default=None,
+                    help="chunks of the overlapped host-to-host e2e run (cfg3: 16, cfg4: 4)")
     args = ap.parse_args()
+    args.e2e_chunks_set = args.e2e_chunks is not None
+    if args.e2e_chunks is None:
+        args.e2e_chunks = 16
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)

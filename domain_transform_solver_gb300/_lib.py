@@ -143,6 +143,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_pipeline_batch": ([vp, i, pvp], i),
         "dtsgb_pipeline_run": ([vp, i, pvp, pvp, pvp, P(FilterParams), P(OptimizeParams), f,
                                 P(HfbsParams), pvp, pvp], i),
+        "dtsgb_pipeline_run_grad": ([vp, i, pvp, pvp, pvp, P(FilterParams), P(OptimizeParams),
+                                     pvp, pvp, pvp, pvp], i),
         "dtsgb_batch_enable_grad": ([vp, i, i], i),
         "dtsgb_png_unfilter": ([vp, i, i, i, vp], i),
         "dtsgb_batch_grad_info": ([vp, P(i), P(i)], i),

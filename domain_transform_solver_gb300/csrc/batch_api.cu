@@ -755,7 +755,7 @@ DTSGB_API int dtsgb_batch_grad_info(dtsgb_batch_t b, int* segment, int* planes) 
 
 static int batch_backward(dtsgb_batch_t b, const float* const* grad_out,
                           float* const* grad_t, float* const* grad_c,
-                          cudaMemcpyKind up, cudaMemcpyKind down) {
+                          cudaMemcpyKind up, cudaMemcpyKind down, bool sync_host = true) {
   if (!b || !grad_out) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
   if (b->grad_n < 0)
     return fail(DTSGB_ERR_INVALID_ARGUMENT,
@@ -803,7 +803,8 @@ static int batch_backward(dtsgb_batch_t b, const float* const* grad_out,
                                    down, b->stream));
     }
   }
-  if (down == cudaMemcpyDeviceToHost) DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+  if (down == cudaMemcpyDeviceToHost && sync_host)
+    DTSGB_CUDA(cudaStreamSynchronize(b->stream));
   return DTSGB_OK;
 }
 
@@ -1103,6 +1104,39 @@ DTSGB_API int dtsgb_pipeline_create(int n, const int* widths, const int* heights
   }
   *out = p;
   return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_pipeline_run_grad(dtsgb_pipeline_t p, int color_space,
+                                      const void* const* rgba, const float* const* target,
+                                      const float* const* conf,
+                                      const dtsgb_filter_params* filter,
+                                      const dtsgb_optimize_params* optimize,
+                                      const float* const* grad_out, float* const* out_v,
+                                      float* const* grad_target,
+                                      float* const* grad_confidence) {
+  if (!p || !rgba || !target || !filter || !optimize || !grad_out || !out_v)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  int st = DTSGB_OK;
+  size_t k = 0;
+  for (; k < p->chunk.size() && !st; ++k) {
+    dtsgb_batch_t b = p->chunk[k];
+    const int f = p->first[k];
+    if (!b->grad) st = dtsgb_batch_enable_grad(b, 1, 0);
+    if (!st)
+      st = batch_upload(b, color_space, rgba + f, target + f, conf ? conf + f : nullptr,
+                        cudaMemcpyHostToDevice, false);
+    if (!st) st = dtsgb_batch_solve_dts(b, filter, optimize, -1.f);
+    if (!st) st = batch_download(b, 0, out_v + f, cudaMemcpyDeviceToHost, false);
+    if (!st)
+      st = batch_backward(b, grad_out + f, grad_target ? grad_target + f : nullptr,
+                          grad_confidence ? grad_confidence + f : nullptr,
+                          cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost, false);
+  }
+  for (size_t j = 0; j < k; ++j) {
+    const cudaError_t e = cudaStreamSynchronize(p->chunk[j]->stream);
+    if (e != cudaSuccess && !st) st = cuda_fail(e, "cudaStreamSynchronize");
+  }
+  return st;
 }
 
 DTSGB_API int dtsgb_pipeline_chunks(dtsgb_pipeline_t p) {

@@ -608,6 +608,27 @@ class Pipeline:
             _ptr_array(od) if dts else None, _ptr_array(oh) if oh is not None else None))
         return od, oh
 
+    def run_grad(self, color_space: COLOR_SPACE, rgba, target, confidence,
+                 filter_params: DomainFilterParams, optimize_params: DomainOptimizeParams,
+                 grad_out):
+        """Differentiable solve: returns (v, dL/dtarget, dL/dconfidence), lists
+        of HxW float32, for the upstream gradients grad_out = dL/dv."""
+        rg = [_rgba(a, (h, w)) for a, (w, h) in zip(rgba, self.sizes)]
+        tg = [_f32(a, (h, w)) for a, (w, h) in zip(target, self.sizes)]
+        cf = None
+        if confidence is not None:
+            cf = [None if a is None else _f32(a, (h, w))
+                  for a, (w, h) in zip(confidence, self.sizes)]
+        go = [_f32(a, (h, w)) for a, (w, h) in zip(grad_out, self.sizes)]
+        v = [np.empty((h, w), np.float32) for w, h in self.sizes]
+        gt = [np.empty((h, w), np.float32) for w, h in self.sizes]
+        gc = [np.empty((h, w), np.float32) for w, h in self.sizes]
+        check(self._lib.dtsgb_pipeline_run_grad(
+            self._h, int(color_space), _ptr_array(rg), _ptr_array(tg),
+            None if cf is None else _ptr_array(cf), ctypes.byref(filter_params._c()),
+            ctypes.byref(optimize_params._c()), _ptr_array(go), _ptr_array(v),
+            _ptr_array(gt), _ptr_array(gc)))
+        return v, gt, gc
 
 # ---- generic solve API, src/edge_aware_solver.h:13-90 (cv::Mat-free) -------
 @dataclass

@@ -382,6 +382,19 @@ DTSGB_API int dtsgb_pipeline_run(dtsgb_pipeline_t p, int color_space,
                                  float overwrite_target_above_conf,
                                  const dtsgb_hfbs_params* hfbs, float* const* out_dts,
                                  float* const* out_hfbs);
+/* The same for a differentiable solve: upload, DTS with gradients on (the
+ * automatic checkpoint choice of dtsgb_batch_enable_grad), download of the
+ * results into out_v, then the backward of the upstream gradients grad_out
+ * into grad_target / grad_confidence (either may be NULL or hold NULL
+ * entries), chunk by chunk without waiting. */
+DTSGB_API int dtsgb_pipeline_run_grad(dtsgb_pipeline_t p, int color_space,
+                                      const void* const* rgba, const float* const* target,
+                                      const float* const* confidence,
+                                      const dtsgb_filter_params* filter,
+                                      const dtsgb_optimize_params* optimize,
+                                      const float* const* grad_out, float* const* out_v,
+                                      float* const* grad_target,
+                                      float* const* grad_confidence);
 
 /* ---- Gradients of the batched DTS solve (new; the reference has no
  * gradients).  With gradients enabled, dtsgb_batch_solve_dts also keeps the

@@ -251,3 +251,24 @@ def test_torch_autograd_binding(gpu_ready):
         assert np.array_equal(v[i].detach().cpu().numpy(), b.download(0)[i])
         assert np.array_equal(t.grad[i].cpu().numpy(), gts[i])
         assert np.array_equal(c.grad[i].cpu().numpy(), gcs[i])
+
+
+def test_pipeline_run_grad_matches_batch(gpu_ready):
+    """dtsgb_pipeline_run_grad (chunks on their own streams) gives the batch's
+    results and gradients bitwise."""
+    D = gpu_ready
+    data = _inputs(1010)
+    opt = dict(num_iterations=6, loss=1, lambda_=0.99, sigma_z=8.0, step_size=0.99)
+    go = [g for _, _, _, g in data]
+    b = _batch(D, data, opt)
+    ref_v = b.download(0)
+    ref_gt, ref_gc = b.backward(go)
+    sizes = [(t.shape[1], t.shape[0]) for _, t, _, _ in data]
+    p = D.Pipeline(sizes, n_chunks=2)
+    for _ in range(2):
+        v, gt, gc = p.run_grad(D.COLOR_SPACE.YCbCr, [r for r, _, _, _ in data],
+                               [t for _, t, _, _ in data], [c for _, _, c, _ in data],
+                               D.DomainFilterParams(**FILT), D.DomainOptimizeParams(**opt), go)
+        for a, r in zip(v + gt + gc, ref_v + ref_gt + ref_gc):
+            assert np.array_equal(a, r)
+    p.close()
