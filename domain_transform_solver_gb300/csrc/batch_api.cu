@@ -63,6 +63,8 @@ struct dtsgb_batch_s {
   std::vector<long long> soff;
   long long dense = 0;
   long long* d_soff = nullptr;
+  // device copies of caller pointer arrays (3 x n), for the _device calls
+  float** d_uptr = nullptr;
   unsigned char* stage = nullptr;  // dense x (rgba 4 B, target 4 B, conf 4 B)
   Inst* d_inst = nullptr;
   Tile* d_tb = nullptr;
@@ -157,6 +159,7 @@ void batch_free(dtsgb_batch_t b) {
   dfree(b->ovf);
   dfree(b->sgrid);
   dfree(b->d_soff);
+  dfree(b->d_uptr);
   dfree(b->stage);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
   b->stream = nullptr;
@@ -312,6 +315,42 @@ int host_upload_plane(dtsgb_batch_t b, const float* const* src, float* dst, int 
   }
   const dim3 grid((unsigned)std::min(b->max_h, 512), (unsigned)b->n);
   k_unstage<<<grid, 256, 0, b->stream>>>(b->d_inst, b->d_soff, d, dst);
+  DTSGB_CUDA(cudaGetLastError());
+  return DTSGB_OK;
+}
+
+// Caller device images (dense W x H, one pointer each; null: skipped) <->
+// pitched arena plane: one kernel instead of a row-by-row copy per image.
+template <bool TO_ARENA>
+__global__ void k_user_copy(const Inst* __restrict__ insts, float* const* __restrict__ user,
+                            float* __restrict__ arena) {
+  const Inst I = insts[blockIdx.y];
+  float* u = user[blockIdx.y];
+  if (!u) return;
+  for (int y = blockIdx.x; y < I.h; y += gridDim.x) {
+    float* urow = u + (long long)y * I.w;
+    float* arow = arena + I.off + (long long)y * I.pitch;
+    for (int x = threadIdx.x; x < I.w; x += blockDim.x) {
+      if (TO_ARENA)
+        arow[x] = urow[x];
+      else
+        urow[x] = arow[x];
+    }
+  }
+}
+
+// Copies between n caller device images and an arena plane (slot 0..2 of the
+// pointer table, so that up to three such copies can be in flight in order).
+int user_plane_copy(dtsgb_batch_t b, float* const* user, float* arena, bool to_arena,
+                    int slot) {
+  float** d = b->d_uptr + (size_t)slot * b->n;
+  DTSGB_CUDA(cudaMemcpyAsync(d, user, sizeof(float*) * b->n, cudaMemcpyHostToDevice,
+                             b->stream));
+  const dim3 grid((unsigned)std::min(b->max_h, 512), (unsigned)b->n);
+  if (to_arena)
+    k_user_copy<true><<<grid, 256, 0, b->stream>>>(b->d_inst, d, arena);
+  else
+    k_user_copy<false><<<grid, 256, 0, b->stream>>>(b->d_inst, d, arena);
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
 }
@@ -547,6 +586,7 @@ DTSGB_API int dtsgb_batch_create(int n, const int* widths, const int* heights,
   if (!st) st = dalloc(&b->d_ti_small, ts.size());
   if (!st) st = dalloc(&b->d_hinst, (size_t)n);
   if (!st) st = dalloc(&b->d_soff, (size_t)n);
+  if (!st) st = dalloc(&b->d_uptr, (size_t)3 * n);
   if (!st) {
     e = cudaMemcpy(b->d_inst, b->inst.data(), n * sizeof(Inst), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
@@ -767,12 +807,8 @@ static int batch_backward(dtsgb_batch_t b, const float* const* grad_out,
   if (up == cudaMemcpyHostToDevice) {
     if (int st = host_upload_plane(b, grad_out, G.g[0], 0)) return st;
   } else {
-    for (int i = 0; i < b->n; ++i) {
-      const Inst& I = b->inst[i];
-      const size_t wb = (size_t)I.w * 4;
-      DTSGB_CUDA(cudaMemcpy2DAsync(G.g[0] + I.off, (size_t)I.pitch * 4, grad_out[i], wb, wb,
-                                   I.h, up, b->stream));
-    }
+    if (int st = user_plane_copy(b, const_cast<float* const*>(grad_out), G.g[0], true, 0))
+      return st;
   }
   const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n, b->small, b->d_ti_small,
                      b->nti_small};
@@ -795,6 +831,10 @@ static int batch_backward(dtsgb_batch_t b, const float* const* grad_out,
     float* const* dst = k == 0 ? grad_t : grad_c;
     const float* src = k == 0 ? grad_plane_t(b) : grad_plane_c(b);
     if (!dst) continue;
+    if (down == cudaMemcpyDeviceToDevice) {
+      if (int st = user_plane_copy(b, dst, const_cast<float*>(src), false, 1 + k)) return st;
+      continue;
+    }
     for (int i = 0; i < b->n; ++i) {
       if (!dst[i]) continue;
       const Inst& I = b->inst[i];
@@ -1027,6 +1067,8 @@ static int batch_download(dtsgb_batch_t b, int which, float* const* dst,
   }
   for (int i = 0; i < b->n; ++i)
     if (!dst[i]) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null output pointer");
+  if (kind == cudaMemcpyDeviceToDevice)
+    return user_plane_copy(b, dst, const_cast<float*>(src), false, 0);
   for (int i = 0; i < b->n; ++i) {
     const Inst& I = b->inst[i];
     const size_t wb = (size_t)I.w * 4;
