@@ -204,6 +204,8 @@ __device__ __forceinline__ float x_update(float v, float B, float tv, float cv,
                                           float extra = 0.f) {
   const float cn = cv * rn;
   const float d = v - tv;
+  // L2: 0.5 * (2 (c/n) d) is (c/n) d exactly (scaling by 2 is exact)
+  if (MODE == 0 && !STEREO) return __fmaf_rn(step, -__fmaf_rn(lambda, v - B, cn * d), v);
   float g;
   if (MODE == 0) {
     g = 2.f * cn * d;
@@ -281,7 +283,7 @@ __device__ __forceinline__ int fast_div(int i, unsigned m) {
 
 template <int TW, int TH, int NT>
 struct VecIterSmem {
-  int ha, sw, sws, sr, nsx, seg, sx_off, sby_off, rt_off, mx_off, total;
+  int ha, sw, sws, sr, nsx, seg, sx_off, sby_off, rt_off, ry_off, mx_off, total;
   unsigned sw4_magic, sr_magic;  // fast_div_magic(sw / 4), fast_div_magic(sr)
   __host__ VecIterSmem(int hx, int hy) {
     constexpr int TQ = TW + 4;  // sx / Py row stride: 16 bytes mod 128
@@ -297,8 +299,10 @@ struct VecIterSmem {
     seg = ((sr + 1 + 31) / 32) | 1;
     sx_off = max(sr * sws, (sr + 1) * TQ) * 4;  // X prefix, later the Y prefix
     sby_off = sx_off + sr * TQ * 4;
-    rt_off = sby_off + sr * TW * 2;
-    mx_off = rt_off + ((2 * max(hx, hy) + 2) * 4 + 15) / 16 * 16;
+    rt_off = sby_off + sr * TW * 2;  // (1/n, 1/n 2^-F) for X
+    const int nrt = 2 * max(hx, hy) + 2;
+    ry_off = rt_off + (nrt * 8 + 15) / 16 * 16;  // 1/n 2^-Fy for Y
+    mx_off = ry_off + (nrt * 4 + 15) / 16 * 16;
     total = mx_off + 16;
     sw4_magic = fast_div_magic((unsigned)(sw >> 2));
     sr_magic = fast_div_magic((unsigned)sr);
@@ -364,11 +368,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   unsigned* Py = XP;                                    // (SR + 1) x TQ, phase 4
   float* sx = reinterpret_cast<float*>(smraw + L.sx_off);          // SR x TQ
   uint16_t* sby = reinterpret_cast<uint16_t*>(smraw + L.sby_off);  // SR x TW
-  float* rtab = reinterpret_cast<float*>(smraw + L.rt_off);
+  float2* rtx = reinterpret_cast<float2*>(smraw + L.rt_off);  // (1/n, 1/n 2^-F)
+  float* rsy = reinterpret_cast<float*>(smraw + L.ry_off);     // 1/n 2^-Fy
   unsigned* smax = reinterpret_cast<unsigned*>(smraw + L.mx_off);  // [0] X, [1] Y
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nrt = 2 * max(hx, hy) + 2;
-  for (int i = tid; i < nrt; i += NT) rtab[i] = i ? __frcp_rn((float)i) : 0.f;
+  for (int i = tid; i < nrt; i += NT) rtx[i].x = i ? __frcp_rn((float)i) : 0.f;
   if (tid < 2) smax[tid] = 0u;
   const bool over = overwrite > 0.f && overwrite < 1.f;  // v itself is already
                                                           // overwritten
@@ -444,6 +449,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   // ---- 2. X prefix: a thread per 16-entry segment of a row, then offsets -------
   {
     const float sF = pow2f(fx_shift(__uint_as_float(smax[0]), lgx));
+    const float isF = pow2f(-fx_shift(__uint_as_float(smax[0]), lgx));
+    for (int i = tid; i < nrt; i += NT) rtx[i].y = rtx[i].x * isF;
     const int NSX = L.nsx, n = SR * NSX, SW4 = SW >> 2;
     unsigned* segx = reinterpret_cast<unsigned*>(sx);  // SR x NSX totals (sx is free)
     for (int i = tid; i < n; i += NT) {
@@ -490,7 +497,6 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   __syncthreads();
   // ---- 3. X half-step for the tile columns over all rows -----------------------
   {
-    const float isF = pow2f(-fx_shift(__uint_as_float(smax[0]), lgx));
     float mloc = 0.f;
     auto compute = [&](int r, const Quad& Q) {
       const unsigned* e0 = XP + r * SWS + HA + 4 * cq;  // e0[k]: prefix at x3 + k
@@ -502,8 +508,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
         if (b) {  // inside the image (a window always holds its own pixel)
           const int dl = min((int)(b & 0xff), hx + 1);
           const int du = min((int)((b >> 8) & 0xff), hx);
-          const float rn = rtab[dl + du];
-          const float B = fx_window(e0[k + du], e0[k - dl], rn * isF);
+          const float2 rr = rtx[dl + du];
+          const float rn = rr.x;
+          const float B = fx_window(e0[k + du], e0[k - dl], rr.y);
           const float vv = f4_get(Q.vv, k), tv = Q.tv[k], cv = Q.cv[k];
           float extra = 0.f;
           if (STEREO)
@@ -535,6 +542,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   // ---- 4. Y prefix: a warp per group of four columns, a lane per segment ---------
   const int Fy = fx_shift(__uint_as_float(smax[1]), lgy);
   const float sFy = pow2f(Fy), isFy = pow2f(-Fy);
+  for (int i = tid; i < nrt; i += NT) rsy[i] = rtx[i].x * isFy;
   {
     const int RY = SR + 1;
     const int k0 = min(lane * L.seg, RY), k1 = min(k0 + L.seg, RY);
@@ -580,7 +588,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
     for (int k = 0; k < 4; ++k) {
       const unsigned b = ((k < 2 ? bq.x : bq.y) >> (16 * (k & 1))) & 0xffffu;
       const int dl = min((int)(b & 0xff), hy + 1), du = min((int)(b >> 8), hy);
-      const float Bv = fx_window(c0[du * TQ + k], c0[-dl * TQ + k], rtab[dl + du] * isFy);
+      const float Bv = fx_window(c0[du * TQ + k], c0[-dl * TQ + k], rsy[dl + du]);
       const float v = f4_get(v4, k);
       o[k] = __fmaf_rn(-slam, v - Bv, v);
     }
