@@ -1,7 +1,7 @@
 """Benchmark of the DTS / HFBS hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg3|cfg0|cfg1|cfg2|cfg4]
+                    [--workload cfg3|cfg3dts|cfg0|cfg1|cfg2|cfg4]
 
 One JSON line on stdout (rank 0).  A step is one pass of the workload's
 solves with inputs already resident in HBM: for DTS the reference's timed
@@ -217,6 +217,47 @@ class Cfg3:
                          max_grid=(inst.width, inst.height, 64), real=real)
             px += inst.width * inst.height
         return px, "4 smallest of the 64 instances, DTS + HFBS each"
+
+
+class Cfg3Dts(Cfg3):
+    """Config 3's DTS solve alone (64 ragged instances, BF16 storage, 10
+    iterations): the batched form of config 0, for the batched versus
+    single-image comparison."""
+
+    name = "cfg3dts_batched_dts_64_ragged_bf16"
+
+    def __init__(self, rank: int, scale: float = 1.0, e2e_chunks: int = 16):
+        super().__init__(rank, scale=scale, e2e_chunks=e2e_chunks)
+        self.voxels = 0
+        if scale != 1.0:
+            self.name = f"{Cfg3Dts.name}_scale{scale:g}"
+
+    def step(self):
+        from domain_transform_solver_gb300._lib import check
+        check(self.lib.dtsgb_batch_solve_dts(self.b.handle, ctypes.byref(self.fp),
+                                             ctypes.byref(self.op), ctypes.c_float(-1.0)))
+
+    def step_e2e(self):
+        from domain_transform_solver_gb300._lib import check
+        check(self.lib.dtsgb_pipeline_run(self.pipe.handle, 1, self.h_rgba, self.h_t,
+                                          self.h_c, ctypes.byref(self.fp),
+                                          ctypes.byref(self.op), ctypes.c_float(-1.0), None,
+                                          self.h_o0, None))
+
+    def e2e_bytes(self):
+        return self.pixels * (4 + 4 + 4), self.pixels * 4
+
+    def cpu_sample(self, real="f32"):
+        import oracle as O
+        W = self.W
+        order = sorted(range(len(self.insts)), key=lambda i: self.sizes[i][0] * self.sizes[i][1])
+        px = 0
+        for i in order[:4]:
+            inst = self.insts[i]
+            O.dts_solve(inst.rgba, inst.target, inst.confidence, 1, W.CFG0_FILTER,
+                        W.CFG0_OPT, real=real)
+            px += inst.width * inst.height
+        return px, "4 smallest of the 64 instances, DTS"
 
 
 class Cfg0:
@@ -508,13 +549,16 @@ class Cfg4:
         return inst.width * inst.height, "1 of the 16 instances, forward + adjoint"
 
 
-WORKLOADS = {"cfg3": Cfg3, "cfg0": Cfg0, "cfg1": Cfg1, "cfg2": Cfg2, "cfg4": Cfg4}
+WORKLOADS = {"cfg3": Cfg3, "cfg3dts": Cfg3Dts, "cfg0": Cfg0, "cfg1": Cfg1, "cfg2": Cfg2,
+             "cfg4": Cfg4}
 
 
 # ---- arms ----------------------------------------------------------------------
 def make_workload(args, rank):
     if args.workload == "cfg3":
         return Cfg3(rank, scale=args.scale, e2e_chunks=args.e2e_chunks)
+    if args.workload == "cfg3dts":
+        return Cfg3Dts(rank, scale=args.scale, e2e_chunks=args.e2e_chunks)
     if args.workload == "cfg4":
         return Cfg4(rank, e2e_chunks=args.e2e_chunks if args.e2e_chunks_set else 4)
     return WORKLOADS[args.workload](rank)
