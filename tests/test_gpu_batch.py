@@ -240,3 +240,36 @@ def test_pipeline_matches_batch(gpu_ready, chunks):
     od, oh = p.run(D.COLOR_SPACE.YCbCr, rgba, tgt, conf, grid_params=hp)
     assert od is None and all(np.array_equal(a, r, equal_nan=True) for a, r in zip(oh, ref_h))
     p.close()
+
+
+def test_pipeline_pinned_buffers(gpu_ready):
+    """The asynchronous path of dtsgb_pipeline_run (pinned host buffers passed
+    as raw pointers) gives the pageable path's results bitwise."""
+    torch = pytest.importorskip("torch")
+    D = gpu_ready
+    from domain_transform_solver_gb300 import workloads as W
+    insts = _instances()
+    sizes = [(i.width, i.height) for i in insts]
+    fp = D.DomainFilterParams(**W.CFG0_FILTER)
+    opt = D.DomainOptimizeParams(**dict(W.CFG0_OPT, num_iterations=4))
+    hp = D.HFBSGridParams(**dict(W.CFG1_HFBS, optim_iter_max=9))
+    p = D.Pipeline(sizes, flags=D.FLAG_BF16_STORAGE, n_chunks=3)
+    ref_d, ref_h = p.run(D.COLOR_SPACE.YCbCr, [i.rgba for i in insts],
+                         [i.target for i in insts], [i.confidence for i in insts], fp, opt, hp)
+
+    def pin(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+
+    rg = [pin(i.rgba) for i in insts]
+    tg = [pin(i.target) for i in insts]
+    cf = [pin(i.confidence) for i in insts]
+    od = [torch.empty((h, w), dtype=torch.float32).pin_memory() for w, h in sizes]
+    oh = [torch.empty((h, w), dtype=torch.float32).pin_memory() for w, h in sizes]
+    ptrs = lambda ts: [t.data_ptr() for t in ts]  # noqa: E731
+    p.run_ptrs(D.COLOR_SPACE.YCbCr, ptrs(rg), ptrs(tg), ptrs(cf), fp, opt, hp, ptrs(od),
+               ptrs(oh))
+    for a, r in zip(od, ref_d):
+        assert np.array_equal(a.numpy(), r)
+    for a, r in zip(oh, ref_h):
+        assert np.array_equal(a.numpy(), r, equal_nan=True)
+    p.close()
