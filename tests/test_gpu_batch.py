@@ -273,3 +273,26 @@ def test_pipeline_pinned_buffers(gpu_ready):
     for a, r in zip(oh, ref_h):
         assert np.array_equal(a.numpy(), r, equal_nan=True)
     p.close()
+
+
+@pytest.mark.parametrize("flags", [0, 1])
+def test_missing_confidences_are_ones(gpu_ready, flags):
+    """A host upload without confidences, or with None entries, solves as
+    with explicit ones (the staged upload fills them on the device), for FP32
+    and BF16 storage."""
+    D = gpu_ready
+    from domain_transform_solver_gb300 import workloads as W
+    insts = _instances()
+    sizes = [(i.width, i.height) for i in insts]
+    fp = D.DomainFilterParams(**W.CFG0_FILTER)
+    opt = D.DomainOptimizeParams(**dict(W.CFG0_OPT, num_iterations=3))
+    ones = [np.ones((h, w), np.float32) for w, h in sizes]
+    outs = []
+    for conf in (ones, None, [None if k % 2 else o for k, o in enumerate(ones)]):
+        b = D.Batch(sizes, flags=flags)
+        b.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in insts], [i.target for i in insts], conf)
+        b.solve_dts(fp, opt)
+        outs.append(b.download(0))
+    for res in outs[1:]:
+        for a, r in zip(res, outs[0]):
+            assert np.array_equal(a, r)
