@@ -278,5 +278,6 @@ def hfbs_solve(guide, t, c, p, max_grid):
                         zz = zs[iz + 1, iy + 1, ix + 1] if iz < gl else 0.0
                         num += cc * zz * w
                         den += cc * w
-            out[y, x] = num / den
+            with np.errstate(invalid="ignore", divide="ignore"):  # 0/0: NaN, as the reference
+                out[y, x] = num / den
     return out, dict(count=cnt[I], norm=n[I], invA=invA, z=zs[I], dims=(gx, gy, gl))
