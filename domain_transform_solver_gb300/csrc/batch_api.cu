@@ -355,6 +355,66 @@ int user_plane_copy(dtsgb_batch_t b, float* const* user, float* arena, bool to_a
   return DTSGB_OK;
 }
 
+// Caller device images -> pitched planes (the _device uploads): the guide
+// (color-converted; not written when rgba is null), target and confidence in
+// the storage type; a null confidence image stands for ones.
+template <typename TS>
+__global__ void k_ingest_ptr(const Inst* __restrict__ insts, uchar4* const* __restrict__ rgba,
+                             float* const* __restrict__ tgt, float* const* __restrict__ cnf,
+                             uchar4* __restrict__ guide, TS* __restrict__ target,
+                             TS* __restrict__ conf, int cs) {
+  const Inst I = insts[blockIdx.y];
+  const uchar4* g = rgba ? rgba[blockIdx.y] : nullptr;
+  const float* t = tgt[blockIdx.y];
+  const float* c = cnf ? cnf[blockIdx.y] : nullptr;
+  for (int y = blockIdx.x; y < I.h; y += gridDim.x) {
+    const long long srow = (long long)y * I.w, drow = I.off + (long long)y * I.pitch;
+    for (int x = threadIdx.x; x < I.w; x += blockDim.x) {
+      if (g) {
+        const uchar4 p = g[srow + x];
+        guide[drow + x] = cs == DTSGB_RGB ? p : convert_pixel(p, cs);
+      }
+      target[drow + x] = store_cast<TS>(t[srow + x]);
+      conf[drow + x] = store_cast<TS>(c ? c[srow + x] : 1.f);
+    }
+  }
+}
+
+int device_ingest(dtsgb_batch_t b, int cs, const void* const* rgba,
+                  const float* const* target, const float* const* conf) {
+  const size_t n = (size_t)b->n;
+  float** slots = b->d_uptr;  // [rgba | target | confidence]
+  std::vector<const void*> cf(n, nullptr);
+  if (conf)
+    for (size_t i = 0; i < n; ++i) cf[i] = conf[i];
+  if (rgba)
+    DTSGB_CUDA(cudaMemcpyAsync(slots, rgba, sizeof(void*) * n, cudaMemcpyHostToDevice,
+                               b->stream));
+  DTSGB_CUDA(cudaMemcpyAsync(slots + n, target, sizeof(void*) * n, cudaMemcpyHostToDevice,
+                             b->stream));
+  DTSGB_CUDA(cudaMemcpyAsync(slots + 2 * n, cf.data(), sizeof(void*) * n,
+                             cudaMemcpyHostToDevice, b->stream));
+  // the pointer copies come from pageable host memory: the calls return
+  // once the arrays are copied out, so cf may go out of scope
+  const dim3 grid((unsigned)std::min(b->max_h, 512), (unsigned)b->n);
+  uchar4* const* rp = rgba ? reinterpret_cast<uchar4* const*>(slots) : nullptr;
+  uchar4* g = rgba ? b->guide : nullptr;
+  if (b->st == Storage::F32)
+    k_ingest_ptr<float><<<grid, 256, 0, b->stream>>>(b->d_inst, rp, slots + n, slots + 2 * n,
+                                                     g, (float*)b->target, (float*)b->conf,
+                                                     cs);
+  else
+    k_ingest_ptr<__nv_bfloat16><<<grid, 256, 0, b->stream>>>(
+        b->d_inst, rp, slots + n, slots + 2 * n, g, (__nv_bfloat16*)b->target,
+        (__nv_bfloat16*)b->conf, cs);
+  DTSGB_CUDA(cudaGetLastError());
+  if (rgba) ++b->guide_gen;
+  b->dts_res = -1;
+  b->grad_n = -1;
+  b->hfbs_done = false;
+  return DTSGB_OK;
+}
+
 // Host upload: one contiguous copy per image and plane into the staging
 // area (pinned host memory makes them asynchronous), ones for missing
 // confidences, then k_ingest.  rgba null: targets only (guides kept).
@@ -406,6 +466,7 @@ int batch_upload_targets(dtsgb_batch_t b, const float* const* target,
                          bool sync_host = true) {
   if (kind == cudaMemcpyHostToDevice)
     return host_ingest(b, DTSGB_RGB, nullptr, target, conf, sync_host);
+  if (kind == cudaMemcpyDeviceToDevice) return device_ingest(b, DTSGB_RGB, nullptr, target, conf);
   int st;
   for (int i = 0; i < b->n; ++i)
     if ((st = upload_plane(b, i, target[i], b->target, kind))) return st;
@@ -451,6 +512,7 @@ int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
       return fail(DTSGB_ERR_INVALID_ARGUMENT, "null image pointer");
   if (kind == cudaMemcpyHostToDevice)
     return host_ingest(b, cs, rgba, target, conf, sync_host);
+  if (kind == cudaMemcpyDeviceToDevice) return device_ingest(b, cs, rgba, target, conf);
   for (int i = 0; i < b->n; ++i) {
     const Inst& I = b->inst[i];
     const size_t wb = (size_t)I.w * 4;
