@@ -296,3 +296,31 @@ def test_missing_confidences_are_ones(gpu_ready, flags):
     for res in outs[1:]:
         for a, r in zip(res, outs[0]):
             assert np.array_equal(a, r)
+
+
+@pytest.mark.parametrize("flags", [0, 1])
+def test_device_uploads_match_host_uploads(gpu_ready, flags):
+    """Uploads from device pointers (FP32 and BF16 storage, some confidences
+    missing) solve exactly as the same images uploaded from the host."""
+    torch = pytest.importorskip("torch")
+    D = gpu_ready
+    from domain_transform_solver_gb300 import workloads as W
+    insts = _instances()
+    sizes = [(i.width, i.height) for i in insts]
+    fp = D.DomainFilterParams(**W.CFG0_FILTER)
+    opt = D.DomainOptimizeParams(**dict(W.CFG0_OPT, num_iterations=3))
+    conf = [None if k % 2 else i.confidence for k, i in enumerate(insts)]
+    ref = D.Batch(sizes, flags=flags)
+    ref.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in insts], [i.target for i in insts], conf)
+    ref.solve_dts(fp, opt)
+    dev = torch.device("cuda:0")
+    rg = [torch.from_numpy(np.ascontiguousarray(i.rgba)).to(dev) for i in insts]
+    tg = [torch.from_numpy(i.target).to(dev) for i in insts]
+    cf = [None if c is None else torch.from_numpy(c).to(dev) for c in conf]
+    torch.cuda.synchronize()
+    b = D.Batch(sizes, flags=flags)
+    b.upload_device(D.COLOR_SPACE.YCbCr, [x.data_ptr() for x in rg],
+                    [x.data_ptr() for x in tg], [0 if x is None else x.data_ptr() for x in cf])
+    b.solve_dts(fp, opt)
+    for a, r in zip(b.download(0), ref.download(0)):
+        assert np.array_equal(a, r)
