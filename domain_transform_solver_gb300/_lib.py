@@ -118,6 +118,10 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_dts_synchronize": ([vp], i),
         "dtsgb_hfbs_synchronize": ([vp], i),
         "dtsgb_hfbs_debug_grid": ([vp, i, vp], i),
+        "dtsgb_hfbs_enable_grad": ([vp, i, i], i),
+        "dtsgb_hfbs_grad_info": ([vp, ctypes.POINTER(i), ctypes.POINTER(i)], i),
+        "dtsgb_hfbs_backward": ([vp, vp, vp, vp], i),
+        "dtsgb_hfbs_backward_device": ([vp, vp, vp, vp], i),
         "dtsgb_profile_enable": ([i], i),
         "dtsgb_profile_reset": ([], i),
         "dtsgb_profile_read": ([i, P(i), P(ctypes.c_double)], i),

@@ -1,10 +1,11 @@
-"""torch.autograd binding of the batched DTS solve and its adjoint.
+"""torch.autograd bindings of the DTS and HFBS solves and their adjoints.
 
-The reference has no gradients; this is the thin binding over
-dtsgb_batch_dts_backward_device (include/dtsgb.h) that lets a PyTorch graph
-differentiate through the fixed-iteration DTS solve with respect to the
-target and the confidence.  The window bounds come from the guide and are
-held fixed: the guide gets no gradient.
+The reference has no gradients; these are thin bindings over
+dtsgb_batch_dts_backward_device and dtsgb_hfbs_backward_device
+(include/dtsgb.h) that let a PyTorch graph differentiate through the
+fixed-iteration solves with respect to the target and the confidence.  DTS
+window bounds and HFBS bins, counts and normalisation come from the guide
+and are held fixed: the guide gets no gradient.
 
 Tensors stay on the GPU: the solve reads the caller's device buffers and
 writes its result into a tensor allocated by PyTorch.  The library's launch
@@ -17,11 +18,13 @@ from __future__ import annotations
 
 import threading
 
+import numpy as np
 import torch
 
-from .solvers import (COLOR_SPACE, Batch, DomainFilterParams, DomainOptimizeParams)
+from .solvers import (COLOR_SPACE, HFBS, Batch, DomainFilterParams, DomainOptimizeParams,
+                      HFBSGridParams, ImageDim, ImageType)
 
-__all__ = ["DtsSolveFunction", "dts_solve"]
+__all__ = ["DtsSolveFunction", "dts_solve", "HfbsSolveFunction", "hfbs_solve"]
 
 _pool: dict = {}
 _pool_lock = threading.Lock()
@@ -123,3 +126,95 @@ def dts_solve(rgba: torch.Tensor, target: torch.Tensor, confidence: torch.Tensor
     op = optimize_params or DomainOptimizeParams()
     return DtsSolveFunction.apply(target, confidence, rgba, fp, op, color_space, segment,
                                   flags)
+
+
+def _hfbs_max_grid(w, h, p: HFBSGridParams):
+    """The grid of Optimize for (w, h, p) (src/hfbs.cu:589-591)."""
+    import math
+    return (int(math.ceil(np.float32(w) / np.float32(p.sigma_x))),
+            int(math.ceil(np.float32(h) / np.float32(p.sigma_y))),
+            int(math.ceil(255.0 / float(np.float32(p.sigma_l)))))
+
+
+def _take_hfbs(key):
+    with _pool_lock:
+        free = _pool.get(key)
+        if free:
+            return free.pop()
+    _, h, w, gx, gy, gl = key
+    return HFBS(ImageDim(w, h), gx, gy, gl)
+
+
+class HfbsSolveFunction(torch.autograd.Function):
+    """out = HFBS(guide; target, confidence) for a batch of equal-size images,
+    each solved by its own HFBS handle.
+
+    forward(target [B,H,W] f32, confidence [B,H,W] f32, rgba [B,H,W,4] u8,
+    grid_params, color_space, segment, max_grid) -> [B,H,W] f32
+    """
+
+    @staticmethod
+    def forward(ctx, target, confidence, rgba, grid_params, color_space=COLOR_SPACE.YCbCr,
+                segment=0, max_grid=None):
+        if not (target.is_cuda and confidence.is_cuda and rgba.is_cuda):
+            raise ValueError("HfbsSolveFunction wants CUDA tensors")
+        if target.dtype != torch.float32 or confidence.dtype != torch.float32:
+            raise ValueError("target and confidence must be float32")
+        if rgba.dtype != torch.uint8 or rgba.shape[-1] != 4:
+            raise ValueError("rgba must be uint8 [B,H,W,4]")
+        B, H, W = target.shape
+        if confidence.shape != target.shape or tuple(rgba.shape[:3]) != (B, H, W):
+            raise ValueError("target, confidence and rgba shapes differ")
+        t = target.contiguous()
+        c = confidence.contiguous()
+        g = rgba.contiguous()
+        gx, gy, gl = max_grid or _hfbs_max_grid(W, H, grid_params)
+        key = ("hfbs", H, W, gx, gy, gl)
+        out = torch.empty_like(t)
+        cur = torch.cuda.current_stream(t.device)
+        side = _side_stream(t.device)
+        side.wait_stream(cur)
+        solvers = []
+        for i in range(B):
+            s = _take_hfbs(key)
+            s.SetStream(side.cuda_stream)
+            s.EnableGrad(True, int(segment))
+            s.InitFrameDevice(color_space, g[i].data_ptr(), t[i].data_ptr(), c[i].data_ptr())
+            s.SetFilterParams(grid_params)
+            s.Optimize()
+            s.DownloadDevice(ImageType.OPTIMIZED_QUANTITY, out[i].data_ptr())
+            solvers.append(s)
+        cur.wait_stream(side)
+        ctx.solvers, ctx.key = solvers, key
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        go = grad_out.contiguous().float()
+        need_t, need_c = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        gt = torch.empty_like(go)
+        gc = torch.empty_like(go)
+        cur = torch.cuda.current_stream(go.device)
+        side = _side_stream(go.device)
+        side.wait_stream(cur)
+        for i, s in enumerate(ctx.solvers):
+            s.SetStream(side.cuda_stream)
+            s.BackwardDevice(go[i].data_ptr(), gt[i].data_ptr() if need_t else None,
+                             gc[i].data_ptr() if need_c else None)
+        cur.wait_stream(side)
+        with _pool_lock:
+            _pool.setdefault(ctx.key, []).extend(ctx.solvers)
+        ctx.solvers = None
+        return (gt if need_t else None, gc if need_c else None, None, None, None, None, None)
+
+
+def hfbs_solve(rgba: torch.Tensor, target: torch.Tensor, confidence: torch.Tensor,
+               grid_params: HFBSGridParams | None = None,
+               color_space: COLOR_SPACE = COLOR_SPACE.YCbCr, segment: int = 0,
+               max_grid=None) -> torch.Tensor:
+    """Differentiable HFBS solve (InitFrame + SetFilterParams + Optimize on
+    every image).  max_grid: the handles' (max_grid_x, max_grid_y,
+    max_grid_l), by default the solve's own grid."""
+    gp = grid_params or HFBSGridParams()
+    return HfbsSolveFunction.apply(target, confidence, rgba, gp, color_space, segment,
+                                   max_grid)

@@ -668,6 +668,17 @@ struct dtsgb_hfbs_s {
   dtsgb_hfbs_params p{};
   int gx = 0, gy = 0, gl = 0;
   bool solved = false;
+  // gradients (dtsgb_hfbs_enable_grad): the requested and the chosen
+  // checkpoint segment, one arena for the kept iterates, the adjoint's grids
+  // and three pixel planes (upstream gradient, dL/dtarget, dL/dconfidence)
+  bool grad = false;
+  int grad_seg_req = 0, grad_seg = 0, grad_planes = 0;
+  float* gbuf = nullptr;
+  size_t gbuf_cap = 0;  // floats
+  float *gout = nullptr, *gtgt = nullptr, *gcnf = nullptr;
+  HfbsGradState gs{};
+  HInst inst{};
+  bool grad_ready = false;  // the last optimize kept its iterates
 };
 
 enum {
@@ -684,8 +695,112 @@ static void hfbs_free(dtsgb_hfbs_t h) {
   dfree(h->ovf);
   dfree(h->sgrid);
   dfree(h->d_inst);
+  dfree(h->gbuf);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   h->stream = nullptr;
+}
+
+// The single-instance batch of a handle (instance table already on the device).
+static void hfbs_fill_batch(dtsgb_hfbs_t h, const HInst* hi, HfbsBatch& B) {
+  const HInst& I = *hi;
+  B.d_inst = h->d_inst;
+  B.h_inst = hi;
+  B.n_inst = 1;
+  B.max_voxels = (long long)I.gx * I.gy * I.gl;
+  B.total_voxels = B.max_voxels;
+  B.max_pixels = (long long)I.w * I.h;
+  B.max_cells = (long long)I.gx * I.gy;
+  B.max_rows = (long long)I.gy * I.gl;
+  B.max_lines = std::max({(long long)I.gy * I.gl, (long long)I.gx * I.gl,
+                          (long long)I.gx * I.gy});
+  B.max_gl = I.gl;
+  B.guide = h->guide;
+  B.target = h->target;
+  B.conf = h->conf;
+  B.st = Storage::F32;
+  B.out = h->out;
+  B.count = h->g[G_COUNT];
+  B.csum = h->g[G_CSUM];
+  B.b = h->g[G_B];
+  B.n0 = h->g[G_N0];
+  B.n1 = h->g[G_N1];
+  B.invA = h->g[G_INVA];
+  B.z0 = h->g[G_Z0];
+  B.z1 = h->g[G_Z1];
+  B.h = h->g[G_H];
+  B.t0 = h->g[G_T0];
+  B.t1 = h->g[G_T1];
+  B.t2 = h->g[G_T2];
+  B.sgrid = h->sgrid;
+  B.ovf = h->ovf;
+  B.keep_debug = true;
+  B.grid_bytes = (size_t)B.max_voxels * 4;
+  B.dbg_norm = h->g[G_DBG_NORM];
+  B.dbg_blur_c = h->g[G_DBG_BLUR_C];
+  B.dbg_z_init = h->g[G_DBG_Z_INIT];
+  B.dbg_z_final = h->g[G_DBG_Z_FINAL];
+}
+
+// Carve the gradient arena for K heavy-ball steps over tv voxels: the
+// adjoint's six grids, the kept iterates of the chosen segment and three
+// pixel planes.  Segment 0 (automatic): every iterate when that fits in a
+// quarter of the free device memory (the arena already held counts as free),
+// else about sqrt(K) steps per segment.
+static int hfbs_prepare_grad(dtsgb_hfbs_t h, int K, long long tv) {
+  auto planes_for = [&](int S) -> long long {
+    if (S == 1) return 6 + std::max(K - 1, 0);
+    const long long nck = (K + S - 1) / S;
+    return 6 + 2 * nck + (S - 1) + 1;
+  };
+  const long long pix = 3 * (long long)h->plane;
+  int S = h->grad_seg_req;
+  if (K <= 1) S = 1;
+  if (S <= 0) {
+    size_t fr = 0, tot = 0;
+    DTSGB_CUDA(cudaMemGetInfo(&fr, &tot));
+    const double avail = (double)fr + (double)h->gbuf_cap * 4.0;
+    const double need1 = ((double)planes_for(1) * tv + pix) * 4.0;
+    S = need1 <= avail / 4 ? 1 : std::max(2, (int)std::ceil(std::sqrt((double)K)));
+  }
+  S = std::min(S, std::max(K, 1));
+  const long long need = planes_for(S) * tv + pix;
+  if ((size_t)need > h->gbuf_cap) {
+    dfree(h->gbuf);
+    h->gbuf_cap = 0;
+    int st = dalloc(&h->gbuf, (size_t)need);
+    if (st) return st;
+    h->gbuf_cap = (size_t)need;
+  }
+  float* q = h->gbuf;
+  auto take = [&](long long planes) {
+    float* r = q;
+    q += planes * tv;
+    return r;
+  };
+  HfbsGradState& G = h->gs;
+  G = HfbsGradState{};
+  G.segment = S;
+  G.gz = take(1);
+  G.gh = take(1);
+  G.gg = take(1);
+  G.gw = take(1);
+  G.gb = take(1);
+  G.ginv = take(1);
+  if (S == 1) {
+    G.hist = take(std::max(K - 1, 0));
+  } else {
+    const long long nck = (K + S - 1) / S;
+    G.ckz = take(nck);
+    G.ckh = take(nck);
+    G.seg = take(S - 1);
+    G.hrec = take(1);
+  }
+  h->gout = q;
+  h->gtgt = q + h->plane;
+  h->gcnf = q + 2 * h->plane;
+  h->grad_seg = S;
+  h->grad_planes = (int)planes_for(S);
+  return DTSGB_OK;
 }
 
 extern "C" {
@@ -770,6 +885,7 @@ DTSGB_API int dtsgb_hfbs_set_image_dim(dtsgb_hfbs_t h, int w, int hh) {
                 "Image size is more than the reserved Cuda memory in constructor.");
   h->w = w;
   h->h = hh;
+  h->grad_ready = false;
   return DTSGB_OK;
 }
 
@@ -796,6 +912,7 @@ static int hfbs_init_frame(dtsgb_hfbs_t h, int cs, const void* rgba,
                              h->stream);
     if (st) return st;
   }
+  h->grad_ready = false;
   if (kind == cudaMemcpyHostToDevice) DTSGB_CUDA(cudaStreamSynchronize(h->stream));
   return DTSGB_OK;
 }
@@ -815,6 +932,7 @@ DTSGB_API int dtsgb_hfbs_set_filter_params(dtsgb_hfbs_t h,
                                            const dtsgb_hfbs_params* p) {
   if (!h || !p) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
   h->p = *p;
+  h->grad_ready = false;
   return DTSGB_OK;
 }
 
@@ -828,6 +946,7 @@ DTSGB_API int dtsgb_hfbs_clear_all(dtsgb_hfbs_t h) {
   DTSGB_CUDA(cudaMemsetAsync(h->ovf, 0, (size_t)h->max_gx * h->max_gy * 4,
                              h->stream));
   h->solved = false;
+  h->grad_ready = false;
   return DTSGB_OK;
 }
 
@@ -875,47 +994,20 @@ DTSGB_API int dtsgb_hfbs_optimize(dtsgb_hfbs_t h) {
   DTSGB_CUDA(cudaMemcpyAsync(h->d_inst, &I, sizeof(HInst),
                              cudaMemcpyHostToDevice, h->stream));
   HfbsBatch B{};
-  B.d_inst = h->d_inst;
-  B.h_inst = &I;
-  B.n_inst = 1;
-  B.max_voxels = (long long)I.gx * I.gy * I.gl;
-  B.total_voxels = B.max_voxels;
-  B.max_pixels = (long long)I.w * I.h;
-  B.max_cells = (long long)I.gx * I.gy;
-  B.max_rows = (long long)I.gy * I.gl;
-  B.max_lines = std::max({(long long)I.gy * I.gl, (long long)I.gx * I.gl,
-                          (long long)I.gx * I.gy});
-  B.max_gl = I.gl;
-  B.guide = h->guide;
-  B.target = h->target;
-  B.conf = h->conf;
-  B.st = Storage::F32;
-  B.out = h->out;
-  B.count = h->g[G_COUNT];
-  B.csum = h->g[G_CSUM];
-  B.b = h->g[G_B];
-  B.n0 = h->g[G_N0];
-  B.n1 = h->g[G_N1];
-  B.invA = h->g[G_INVA];
-  B.z0 = h->g[G_Z0];
-  B.z1 = h->g[G_Z1];
-  B.h = h->g[G_H];
-  B.t0 = h->g[G_T0];
-  B.t1 = h->g[G_T1];
-  B.t2 = h->g[G_T2];
-  B.sgrid = h->sgrid;
-  B.ovf = h->ovf;
-  B.keep_debug = true;
-  B.grid_bytes = (size_t)B.max_voxels * 4;
-  B.dbg_norm = h->g[G_DBG_NORM];
-  B.dbg_blur_c = h->g[G_DBG_BLUR_C];
-  B.dbg_z_init = h->g[G_DBG_Z_INIT];
-  B.dbg_z_final = h->g[G_DBG_Z_FINAL];
+  hfbs_fill_batch(h, &I, B);
+  h->grad_ready = false;
+  if (h->grad) {
+    int gst = hfbs_prepare_grad(h, p.optim_iter_max, B.total_voxels);
+    if (gst) return gst;
+    B.grad = &h->gs;
+  }
   HParams hp{p.sigma_x, p.sigma_y, p.sigma_l, p.lambda, p.alpha, p.beta,
              p.bistoch_iter_max, p.optim_iter_max, p.neg_exp_beta};
   int st = hfbs_enqueue_solve(B, hp, h->stream);
   if (st) return st;
+  h->inst = I;
   h->solved = true;
+  h->grad_ready = h->grad;
   return DTSGB_OK;
 }
 
@@ -964,6 +1056,68 @@ DTSGB_API int dtsgb_hfbs_debug_grid(dtsgb_hfbs_t h, int which, float* dst) {
                              cudaMemcpyDeviceToHost, h->stream));
   DTSGB_CUDA(cudaStreamSynchronize(h->stream));
   return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_hfbs_enable_grad(dtsgb_hfbs_t h, int enable, int segment) {
+  if (!h) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null handle");
+  if (segment < 0) return fail(DTSGB_ERR_INVALID_ARGUMENT, "segment must be >= 0");
+  h->grad = enable != 0;
+  h->grad_seg_req = segment;
+  h->grad_ready = false;
+  if (!h->grad) {
+    DTSGB_CUDA(cudaStreamSynchronize(h->stream));
+    dfree(h->gbuf);
+    h->gbuf_cap = 0;
+    h->grad_seg = h->grad_planes = 0;
+  }
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_hfbs_grad_info(dtsgb_hfbs_t h, int* segment, int* planes) {
+  if (!h) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null handle");
+  if (segment) *segment = h->grad_seg;
+  if (planes) *planes = h->grad_planes;
+  return DTSGB_OK;
+}
+
+static int hfbs_backward_impl(dtsgb_hfbs_t h, const float* grad_out, float* grad_target,
+                              float* grad_confidence, cudaMemcpyKind up,
+                              cudaMemcpyKind down) {
+  if (!h || !grad_out) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  if (!h->grad_ready)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT,
+                "no optimize with gradients enabled since the last change of frame, "
+                "dims or parameters");
+  const size_t wb = (size_t)h->w * 4, pb = (size_t)h->pitch * 4;
+  DTSGB_CUDA(cudaMemcpy2DAsync(h->gout, pb, grad_out, wb, wb, h->h, up, h->stream));
+  HfbsBatch B{};
+  hfbs_fill_batch(h, &h->inst, B);
+  B.grad = &h->gs;
+  const dtsgb_hfbs_params& p = h->p;
+  HParams hp{p.sigma_x, p.sigma_y, p.sigma_l, p.lambda, p.alpha, p.beta,
+             p.bistoch_iter_max, p.optim_iter_max, p.neg_exp_beta};
+  int st = hfbs_enqueue_backward(B, hp, h->gout, grad_target ? h->gtgt : nullptr,
+                                 grad_confidence ? h->gcnf : nullptr, h->stream);
+  if (st) return st;
+  if (grad_target)
+    DTSGB_CUDA(cudaMemcpy2DAsync(grad_target, wb, h->gtgt, pb, wb, h->h, down, h->stream));
+  if (grad_confidence)
+    DTSGB_CUDA(cudaMemcpy2DAsync(grad_confidence, wb, h->gcnf, pb, wb, h->h, down,
+                                 h->stream));
+  if (down == cudaMemcpyDeviceToHost) DTSGB_CUDA(cudaStreamSynchronize(h->stream));
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_hfbs_backward(dtsgb_hfbs_t h, const float* grad_out, float* grad_target,
+                                  float* grad_confidence) {
+  return hfbs_backward_impl(h, grad_out, grad_target, grad_confidence,
+                            cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost);
+}
+
+DTSGB_API int dtsgb_hfbs_backward_device(dtsgb_hfbs_t h, const float* grad_out,
+                                         float* grad_target, float* grad_confidence) {
+  return hfbs_backward_impl(h, grad_out, grad_target, grad_confidence,
+                            cudaMemcpyDeviceToDevice, cudaMemcpyDeviceToDevice);
 }
 
 }  // extern "C"

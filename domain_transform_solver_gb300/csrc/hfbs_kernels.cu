@@ -28,17 +28,6 @@ __device__ __forceinline__ long long gidx(const HInst& I, int x, int y, int z) {
   return I.grid_off + ((long long)z * I.gy + y) * I.gx + x;
 }
 
-// First pixel index p >= 0 with floorf(p * 1.0f / sigma) >= cell (the
-// reference's bin of pixel p, src/hfbs.cu:82-83); n if none.
-__device__ __forceinline__ int cell_start(int cell, float sigma, int n) {
-  int p = (int)ceilf((float)cell * sigma) - 2;
-  if (p < 0) p = 0;
-  if (p > n) p = n;
-  while (p < n && (int)floorf((float)p * 1.0f / sigma) < cell) ++p;
-  while (p > 0 && (int)floorf((float)(p - 1) * 1.0f / sigma) >= cell) --p;
-  return p;
-}
-
 // a12: SplatBAndC + BistochastasizeSetup (src/hfbs.cu:72-120).  Bins
 // (floor(x/sx), floor(y/sy), floor(L/sl)) with L the .x channel; sums of
 // c*t, c and 1 per bin.  Luma bin == gl lands in the overflow plane.
@@ -661,6 +650,24 @@ int blocks_for(long long n) {
 
 }  // namespace
 
+void hfbs_launch_step(const HfbsBatch& B, const HParams& p, const float* zs, float* zd,
+                      float* h, const float* norm, cudaStream_t s) {
+  // one warp per grid row (y, l) of the largest grid
+  const dim3 gr((unsigned)std::min<long long>((B.max_rows + 7) / 8, 4096), B.n_inst);
+  k_solve<<<gr, kT, 0, s>>>(B.d_inst, zs, zd, h, norm, B.b, B.invA, p.lambda, p.alpha,
+                            p.beta);
+}
+
+void hfbs_launch_blur_pair(const HfbsBatch& B, const HParams& p, const float* s0,
+                           const float* s1, float* x0, float* x1, float* y0, float* y1,
+                           cudaStream_t s) {
+  const dim3 gr((unsigned)std::min<long long>((B.max_rows + 7) / 8, 4096), B.n_inst);
+  const dim3 gl_lines(blocks_for(B.max_lines), B.n_inst);
+  k_laplace_x<<<gr, kT, 0, s>>>(B.d_inst, s0, x0, s1, x1, p.neg_exp_beta);
+  k_laplace<<<gl_lines, kT, 0, s>>>(B.d_inst, 1, x0, y0, x1, y1, p.neg_exp_beta);
+  k_laplace<<<gl_lines, kT, 0, s>>>(B.d_inst, 2, y0, x0, y1, x1, p.neg_exp_beta);
+}
+
 int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   const int ni = B.n_inst;
   // row kernels: one warp per grid row, 8 warps per block
@@ -705,7 +712,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
     long long cols;  // max over the group of gx * gy
   };
   std::vector<Group> groups;
-  if (B.h_inst && B.group_voxels > 0) {
+  if (B.h_inst && B.group_voxels > 0 && !B.grad) {
     Group g{0, 0, 0};
     long long vox = 0;
     for (int i = 0; i < ni; ++i) {
@@ -770,7 +777,31 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   }
   float* zs = B.z0;
   float* zd = B.z1;
-  if (B.max_gl <= kTBMaxGL && B.h_inst) {
+  if (B.grad) {
+    // iterates kept for the adjoint (HfbsGradState): one-step passes
+    const HfbsGradState& G = *B.grad;
+    const int K = p.optim_iter_max, S = G.segment;
+    const long long tv = B.total_voxels;
+    const size_t gbytes = (size_t)tv * sizeof(float);
+    for (int k = 0; k < K; ++k) {
+      float* nxt;
+      if (S == 1) {
+        nxt = k + 1 < K ? G.hist + (size_t)k * tv : (zs == B.z1 ? B.z0 : B.z1);
+      } else {
+        if (k % S == 0) {
+          DTSGB_CUDA(cudaMemcpyAsync(G.ckz + (size_t)(k / S) * tv, zs, gbytes,
+                                     cudaMemcpyDeviceToDevice, s));
+          DTSGB_CUDA(cudaMemcpyAsync(G.ckh + (size_t)(k / S) * tv, B.h, gbytes,
+                                     cudaMemcpyDeviceToDevice, s));
+        }
+        nxt = zs == B.z0 ? B.z1 : B.z0;
+      }
+      prof_begin(s, DTSGB_K_HFBS_SOLVE);
+      hfbs_launch_step(B, p, zs, nxt, B.h, norm, s);
+      prof_end(s, DTSGB_K_HFBS_SOLVE);
+      zs = nxt;
+    }
+  } else if (B.max_gl <= kTBMaxGL && B.h_inst) {
     // K heavy-ball steps per pass; h ping-pongs through the free blur
     // temporary t2 (its final value is not needed).  The shared-memory limit
     // is a per-device attribute: set on every call (host-side, cheap).

@@ -348,6 +348,18 @@ class HFBS:
         if st == _lib.DTSGB_WARN_GRID_TOO_LARGE:
             warnings.warn(self._lib.dtsgb_last_error().decode())
 
+    def InitFrameDevice(self, color_space: COLOR_SPACE, rgba_ptr: int, target_ptr: int,
+                        confidence_ptr: int | None = None) -> None:
+        """InitFrame from device buffers (W*H uchar4 / float32), enqueued on
+        the handle's stream."""
+        check(self._lib.dtsgb_hfbs_init_frame_device(
+            self._h, int(color_space), ctypes.c_void_p(rgba_ptr), ctypes.c_void_p(target_ptr),
+            ctypes.c_void_p(confidence_ptr) if confidence_ptr else None))
+
+    def DownloadDevice(self, image_type: ImageType, dst_ptr: int) -> None:
+        check(self._lib.dtsgb_hfbs_download_device(self._h, int(image_type),
+                                                   ctypes.c_void_p(dst_ptr)))
+
     def GridDims(self):
         gx, gy, gl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(self._lib.dtsgb_hfbs_grid_dims(self._h, ctypes.byref(gx),
@@ -364,6 +376,37 @@ class HFBS:
         out = np.zeros(self._shape(), np.float32)
         check(self._lib.dtsgb_hfbs_download(self._h, int(image_type), _ptr(out)))
         return out
+
+    # ---- gradients (an addition; the reference has none) ------------------
+    def EnableGrad(self, enable: bool = True, segment: int = 0) -> None:
+        """Keep what the adjoint needs in the following Optimize calls
+        (segment 0: automatic checkpoint choice)."""
+        check(self._lib.dtsgb_hfbs_enable_grad(self._h, int(bool(enable)), int(segment)))
+
+    def GradInfo(self):
+        """(checkpoint segment, grid planes) of the last Optimize."""
+        seg, planes = ctypes.c_int(), ctypes.c_int()
+        check(self._lib.dtsgb_hfbs_grad_info(self._h, ctypes.byref(seg),
+                                             ctypes.byref(planes)))
+        return seg.value, planes.value
+
+    def Backward(self, grad_out):
+        """dL/dtarget, dL/dconfidence of the last Optimize for dL/doutput."""
+        shape = self._shape()
+        g = _f32(grad_out, shape)
+        gt = np.empty(shape, np.float32)
+        gc = np.empty(shape, np.float32)
+        check(self._lib.dtsgb_hfbs_backward(self._h, _ptr(g), _ptr(gt), _ptr(gc)))
+        return gt, gc
+
+    def BackwardDevice(self, grad_out_ptr: int, grad_target_ptr: int | None,
+                       grad_confidence_ptr: int | None) -> None:
+        """Device-pointer backward (W*H float32 planes, enqueued on the
+        handle's stream)."""
+        check(self._lib.dtsgb_hfbs_backward_device(
+            self._h, ctypes.c_void_p(grad_out_ptr),
+            ctypes.c_void_p(grad_target_ptr) if grad_target_ptr else None,
+            ctypes.c_void_p(grad_confidence_ptr) if grad_confidence_ptr else None))
 
 
 def _ptr_array(arrays):

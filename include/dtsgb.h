@@ -118,7 +118,8 @@ enum {
   DTSGB_K_HFBS_SLICE = 7,
   DTSGB_K_DTS_OTHER = 8, /* iterate init, conversions                 */
   DTSGB_K_DTS_ADJOINT = 9, /* adjoint of one fused iteration          */
-  DTSGB_K_COUNT = 10
+  DTSGB_K_HFBS_ADJOINT = 10, /* the whole HFBS adjoint                  */
+  DTSGB_K_COUNT = 11
 };
 DTSGB_API int dtsgb_profile_enable(int enable);
 DTSGB_API int dtsgb_profile_reset(void);
@@ -241,6 +242,27 @@ DTSGB_API int dtsgb_hfbs_grid_dims(dtsgb_hfbs_t h, int* gx, int* gy, int* gl);
  * gx*gy*gl floats, x fastest: 0 splat count, 1 splat of c, 2 b,
  * 3 splat_norm, 4 inv_diag_A, 5 blurred c, 6 initial z, 7 final z. */
 DTSGB_API int dtsgb_hfbs_debug_grid(dtsgb_hfbs_t h, int which, float* dst);
+
+/* Gradients of the HFBS solve (an addition: the reference has no gradients).
+ * With gradients enabled, dtsgb_hfbs_optimize keeps what the adjoint needs:
+ * every heavy-ball iterate (segment 1), or z and h at every segment-th step
+ * with the segment's iterates recomputed by the backward (segment > 1);
+ * segment 0 chooses every iterate when those optim_iter_max planes fit in a
+ * quarter of the free device memory, else about sqrt(optim_iter_max) steps
+ * per segment.  The forward then runs one heavy-ball step per launch.
+ * dtsgb_hfbs_backward maps dL/d(output) of the last optimize (W*H floats) to
+ * dL/dtarget and dL/dconfidence (W*H floats each; either may be NULL).  Bins,
+ * splat counts and the bistochastized normalisation are held fixed (the
+ * guide gets no gradient), the Huber clamp of the heavy-ball step enters by
+ * its mask.  InitFrame, SetImageDim, SetFilterParams or ClearAll after the
+ * optimize make the backward return DTSGB_ERR_INVALID_ARGUMENT. */
+DTSGB_API int dtsgb_hfbs_enable_grad(dtsgb_hfbs_t h, int enable, int segment);
+/* the segment and the number of grid planes of the last optimize */
+DTSGB_API int dtsgb_hfbs_grad_info(dtsgb_hfbs_t h, int* segment, int* planes);
+DTSGB_API int dtsgb_hfbs_backward(dtsgb_hfbs_t h, const float* grad_out,
+                                  float* grad_target, float* grad_confidence);
+DTSGB_API int dtsgb_hfbs_backward_device(dtsgb_hfbs_t h, const float* grad_out,
+                                         float* grad_target, float* grad_confidence);
 
 /* ===========================================================================
  * Allocation-free DTS solve (no counterpart in the reference).

@@ -918,6 +918,15 @@ EXPORT void ora_hfbs_init_frame(ora_hfbs* s, int color_space,
   }
 }
 
+/* target / confidence at REAL precision (finite-difference checks); NULL
+ * keeps a plane. */
+EXPORT void ora_hfbs_set_target_conf(ora_hfbs* s, const REAL* target,
+                                     const REAL* confidence) {
+  const size_t n = (size_t)s->w * s->h;
+  if (target) memcpy(s->target, target, n * sizeof(REAL));
+  if (confidence) memcpy(s->conf, confidence, n * sizeof(REAL));
+}
+
 #define GI(x, y, z) (((size_t)(z) * gy + (y)) * gx + (x))
 
 /* Laplace sweeps -- src/hfbs.cu:355-427: along one axis,
@@ -949,6 +958,36 @@ static void ora_laplace(const REAL* src, REAL* dst, int gx, int gy, int gl,
         r = r + src[base + i * stride];
       }
     }
+}
+
+/* One SolveHFBS heavy-ball step, src/hfbs.cu:201-239: zd = zs - alpha*h'
+ * with h' = beta*h + Huber(zs - q), q = (b + lambda*norm*N(norm*zs))*invA and
+ * N the six-neighbour sum.  Neighbours outside the interior read 0. */
+static void ora_hfbs_step(const REAL* zs, REAL* zd, REAL* h, const REAL* norm,
+                          const REAL* b, const REAL* invA, int gx, int gy, int gl,
+                          const ora_hfbs_params* p) {
+  const REAL lam = p->lambda, beta = p->beta, alpha = p->alpha;
+#pragma omp parallel for schedule(static)
+  for (int z = 0; z < gl; ++z)
+    for (int y = 0; y < gy; ++y)
+      for (int x = 0; x < gx; ++x) {
+        REAL d = 0;
+        if (x > 0) d += zs[GI(x - 1, y, z)] * norm[GI(x - 1, y, z)];
+        if (x + 1 < gx) d += zs[GI(x + 1, y, z)] * norm[GI(x + 1, y, z)];
+        if (y > 0) d += zs[GI(x, y - 1, z)] * norm[GI(x, y - 1, z)];
+        if (y + 1 < gy) d += zs[GI(x, y + 1, z)] * norm[GI(x, y + 1, z)];
+        if (z > 0) d += zs[GI(x, y, z - 1)] * norm[GI(x, y, z - 1)];
+        if (z + 1 < gl) d += zs[GI(x, y, z + 1)] * norm[GI(x, y, z + 1)];
+        const size_t g = GI(x, y, z);
+        const REAL q = (b[g] + lam * norm[g] * d) * invA[g];
+        const REAL zc = zs[g];
+        const REAL grad = zc - q;
+        const REAL gc = fabs((double)grad) > 1.345 ? (grad > 0 ? (REAL)1 : (REAL)-1)
+                                                   : grad;
+        const REAL hn = beta * h[g] + gc;
+        h[g] = hn;
+        zd[g] = zc - alpha * hn;
+      }
 }
 
 /* HFBS::Optimize -- src/hfbs.cu:586-743. */
@@ -1053,35 +1092,13 @@ EXPORT int ora_hfbs_optimize(ora_hfbs* s) {
   ora_laplace(src, zinit, gx, gy, gl, 2, nb_beta);
   for (size_t i = 0; i < ng; ++i) zinit[i] = zinit[i] / (blur_c[i] + (REAL)1e-7);
 
-  /* a16. SolveHFBS heavy-ball iterations, hfbs.cu:201-239 and :720-732.
-   * Neighbours outside the interior read 0. */
+  /* a16. SolveHFBS heavy-ball iterations, hfbs.cu:201-239 and :720-732. */
   REAL* h = ora_alloc_real(ng);
   REAL* zs = src;
   REAL* zd = dst;
   memcpy(zs, zinit, ng * sizeof(REAL));
-  const REAL lam = p->lambda, beta = p->beta, alpha = p->alpha;
   for (int it = 0; it < p->optim_iter_max; ++it) {
-#pragma omp parallel for schedule(static)
-    for (int z = 0; z < gl; ++z)
-      for (int y = 0; y < gy; ++y)
-        for (int x = 0; x < gx; ++x) {
-          REAL d = 0;
-          if (x > 0) d += zs[GI(x - 1, y, z)] * norm[GI(x - 1, y, z)];
-          if (x + 1 < gx) d += zs[GI(x + 1, y, z)] * norm[GI(x + 1, y, z)];
-          if (y > 0) d += zs[GI(x, y - 1, z)] * norm[GI(x, y - 1, z)];
-          if (y + 1 < gy) d += zs[GI(x, y + 1, z)] * norm[GI(x, y + 1, z)];
-          if (z > 0) d += zs[GI(x, y, z - 1)] * norm[GI(x, y, z - 1)];
-          if (z + 1 < gl) d += zs[GI(x, y, z + 1)] * norm[GI(x, y, z + 1)];
-          const size_t g = GI(x, y, z);
-          const REAL q = (b[g] + lam * norm[g] * d) * invA[g];
-          const REAL zc = zs[g];
-          const REAL grad = zc - q;
-          const REAL gc = fabs((double)grad) > 1.345 ? (grad > 0 ? (REAL)1 : (REAL)-1)
-                                                     : grad;
-          const REAL hn = beta * h[g] + gc;
-          h[g] = hn;
-          zd[g] = zc - alpha * hn;
-        }
+    ora_hfbs_step(zs, zd, h, norm, b, invA, gx, gy, gl, p);
     REAL* t = zs;
     zs = zd;
     zd = t;
@@ -1128,6 +1145,177 @@ EXPORT int ora_hfbs_optimize(ora_hfbs* s) {
       const REAL c1m = den[1][0] * ((REAL)1 - wy) + den[1][1] * wy;
       s->optim[k] = (c0 * ((REAL)1 - wz) + c1 * wz) / (c0m * ((REAL)1 - wz) + c1m * wz);
     }
+  return 0;
+}
+
+/* Three-axis Laplace blur (X -> Y -> Z) of src into dst; t0, t1 scratch. */
+static void ora_laplace3(const REAL* src, REAL* dst, REAL* t0, REAL* t1, int gx,
+                         int gy, int gl, REAL beta) {
+  ora_laplace(src, t0, gx, gy, gl, 0, beta);
+  ora_laplace(t0, t1, gx, gy, gl, 1, beta);
+  ora_laplace(t1, dst, gx, gy, gl, 2, beta);
+}
+
+/* Adjoint of HFBS::Optimize (src/hfbs.cu:586-743) with respect to the
+ * target and the confidence, for an upstream gradient grad_out = dL/d(output)
+ * (W*H).  Bins, splat counts and the bistochastized normalisation do not
+ * depend on target or confidence; the Huber clamp of the heavy-ball step
+ * enters by its mask (|grad| <= 1.345), the invA floor (diag <= 1e-3) by a
+ * zero derivative.  Steps, last to first:
+ *  slice^T:  gz += gout * w * count / den at each in-grid corner (den = 0:
+ *            the pixel contributes nothing);
+ *  step^T:   u = gh - alpha*gz;  gg = mask*u;  gh = beta*u;
+ *            gb -= invA*gg;  ginvA -= (b + lambda*norm*d)*gg;
+ *            gz += gg - lambda*norm*N(norm*invA*gg)   (N symmetric);
+ *  InitZ^T:  z0 = blur_b / (blur_c + 1e-7);
+ *  blur^T:   the three-axis Laplace blur is symmetric;
+ *  invA^T:   dinvA/dcsum = -invA^2 where diag > 1e-3;
+ *  splat^T:  b = S(c*t), csum = S(c): gt = c*gb[bin], gc = t*gb[bin] + gcsum[bin]
+ *            (pixels in the overflow bin get 0).
+ * Needs the grids of a completed ora_hfbs_optimize of the same frame; the
+ * forward iterates are recomputed and all kept. */
+EXPORT int ora_hfbs_backward(ora_hfbs* s, const REAL* grad_out, REAL* grad_t,
+                             REAL* grad_c) {
+  if (!s->grids[ORA_G_B]) return -1;
+  const int W = s->w, H = s->h, gx = s->gx, gy = s->gy, gl = s->gl;
+  const ora_hfbs_params* p = &s->p;
+  const size_t ng = (size_t)gx * gy * gl;
+  const int K = p->optim_iter_max;
+  const REAL* count = s->grids[ORA_G_SPLAT_SUM];
+  const REAL* csum = s->grids[ORA_G_SPLAT_C];
+  const REAL* b = s->grids[ORA_G_B];
+  const REAL* norm = s->grids[ORA_G_SPLAT_NORM];
+  const REAL* invA = s->grids[ORA_G_INV_DIAG_A];
+  const REAL* blur_c = s->grids[ORA_G_BLUR_C];
+  const REAL* zinit = s->grids[ORA_G_Z_INIT];
+  const int ovf_stored = gl < s->max_gl;
+  const REAL lam = p->lambda, alpha = p->alpha, beta = p->beta;
+  /* forward iterates z_0 .. z_{K-1} */
+  REAL* zh = ora_alloc_real(ng * (size_t)(K > 0 ? K : 1));
+  REAL* hv = ora_alloc_real(ng);
+  REAL* ztmp = ora_alloc_real(ng);
+  memcpy(zh, zinit, ng * sizeof(REAL));
+  for (int it = 0; it + 1 < K; ++it)
+    ora_hfbs_step(zh + ng * it, zh + ng * (it + 1), hv, norm, b, invA, gx, gy, gl, p);
+  REAL* gz = ora_alloc_real(ng);
+  REAL* gh = ora_alloc_real(ng);
+  REAL* gb = ora_alloc_real(ng);
+  REAL* ginv = ora_alloc_real(ng);
+  REAL* gg = ora_alloc_real(ng);
+  REAL* wv = ora_alloc_real(ng);
+  /* slice^T (same positions and weights as the forward slice) */
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const size_t k = (size_t)y * W + x;
+      const float fxp = (float)x * 1.0f / p->sigma_x;
+      const float fyp = (float)y * 1.0f / p->sigma_y;
+      const float fzp = (float)s->color[4 * k] * 1.0f / p->sigma_l;
+      const float x0 = floorf(fxp), y0 = floorf(fyp), z0 = floorf(fzp);
+      const REAL wx = (REAL)(fxp - x0), wy = (REAL)(fyp - y0), wz = (REAL)(fzp - z0);
+      REAL wgt[8], cnt[8];
+      size_t gidx[8];
+      int in[8];
+      REAL den = 0;
+      for (int c = 0; c < 8; ++c) {
+        const int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
+        const int ix = (int)x0 + dx, iy = (int)y0 + dy, iz = (int)z0 + dz;
+        wgt[c] = (dx ? wx : 1 - wx) * (dy ? wy : 1 - wy) * (dz ? wz : 1 - wz);
+        cnt[c] = 0;
+        in[c] = 0;
+        gidx[c] = 0;
+        if (ix < gx && iy < gy && iz < gl) {
+          gidx[c] = GI(ix, iy, iz);
+          cnt[c] = count[gidx[c]];
+          in[c] = 1;
+        } else if (ix < gx && iy < gy && iz == gl && ovf_stored) {
+          cnt[c] = s->overflow_count[(size_t)iy * gx + ix];
+        }
+        den += wgt[c] * cnt[c];
+      }
+      if (den == 0) continue;
+      for (int c = 0; c < 8; ++c)
+        if (in[c]) gz[gidx[c]] += grad_out[k] * wgt[c] * cnt[c] / den;
+    }
+  /* heavy-ball steps, last to first */
+  for (int it = K - 1; it >= 0; --it) {
+    const REAL* z = zh + ng * it;
+#pragma omp parallel for schedule(static)
+    for (int zz = 0; zz < gl; ++zz)
+      for (int y = 0; y < gy; ++y)
+        for (int x = 0; x < gx; ++x) {
+          REAL d = 0;
+          if (x > 0) d += z[GI(x - 1, y, zz)] * norm[GI(x - 1, y, zz)];
+          if (x + 1 < gx) d += z[GI(x + 1, y, zz)] * norm[GI(x + 1, y, zz)];
+          if (y > 0) d += z[GI(x, y - 1, zz)] * norm[GI(x, y - 1, zz)];
+          if (y + 1 < gy) d += z[GI(x, y + 1, zz)] * norm[GI(x, y + 1, zz)];
+          if (zz > 0) d += z[GI(x, y, zz - 1)] * norm[GI(x, y, zz - 1)];
+          if (zz + 1 < gl) d += z[GI(x, y, zz + 1)] * norm[GI(x, y, zz + 1)];
+          const size_t g = GI(x, y, zz);
+          const REAL bq = b[g] + lam * norm[g] * d;
+          const REAL grad = z[g] - bq * invA[g];
+          const REAL u = gh[g] - alpha * gz[g];
+          const REAL v = fabs((double)grad) > 1.345 ? (REAL)0 : u;
+          gh[g] = beta * u;
+          gb[g] -= invA[g] * v;
+          ginv[g] -= bq * v;
+          gg[g] = v;
+          wv[g] = norm[g] * invA[g] * v;
+        }
+#pragma omp parallel for schedule(static)
+    for (int zz = 0; zz < gl; ++zz)
+      for (int y = 0; y < gy; ++y)
+        for (int x = 0; x < gx; ++x) {
+          REAL a = 0;
+          if (x > 0) a += wv[GI(x - 1, y, zz)];
+          if (x + 1 < gx) a += wv[GI(x + 1, y, zz)];
+          if (y > 0) a += wv[GI(x, y - 1, zz)];
+          if (y + 1 < gy) a += wv[GI(x, y + 1, zz)];
+          if (zz > 0) a += wv[GI(x, y, zz - 1)];
+          if (zz + 1 < gl) a += wv[GI(x, y, zz + 1)];
+          const size_t g = GI(x, y, zz);
+          gz[g] += gg[g] - lam * norm[g] * a;
+        }
+  }
+  /* InitZ^T: gg = d/d blur_b, wv = d/d blur_c */
+  for (size_t i = 0; i < ng; ++i) {
+    const REAL e = blur_c[i] + (REAL)1e-7;
+    gg[i] = gz[i] / e;
+    wv[i] = -gz[i] * zinit[i] / e;
+  }
+  /* blur^T (symmetric): gb += blur(gg); gcsum = blur(wv) (into gh) */
+  ora_laplace3(gg, ztmp, gz, hv, gx, gy, gl, p->neg_exp_beta);
+  for (size_t i = 0; i < ng; ++i) gb[i] += ztmp[i];
+  ora_laplace3(wv, gh, gz, hv, gx, gy, gl, p->neg_exp_beta);
+  /* invA^T */
+  for (size_t i = 0; i < ng; ++i) {
+    const REAL diag = lam * (count[i] - 2 * norm[i] * norm[i]) + csum[i];
+    if (diag > (REAL)1e-3) gh[i] -= ginv[i] * invA[i] * invA[i];
+  }
+  /* splat^T */
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const size_t k = (size_t)y * W + x;
+      const int bx = (int)floorf((float)x * 1.0f / p->sigma_x);
+      const int by = (int)floorf((float)y * 1.0f / p->sigma_y);
+      const int bl = (int)floorf((float)s->color[4 * k] * 1.0f / p->sigma_l);
+      if (bl < gl) {
+        const size_t g = GI(bx, by, bl);
+        if (grad_t) grad_t[k] = s->conf[k] * gb[g];
+        if (grad_c) grad_c[k] = s->target[k] * gb[g] + gh[g];
+      } else {
+        if (grad_t) grad_t[k] = 0;
+        if (grad_c) grad_c[k] = 0;
+      }
+    }
+  free(zh);
+  free(hv);
+  free(ztmp);
+  free(gz);
+  free(gh);
+  free(gb);
+  free(ginv);
+  free(gg);
+  free(wv);
   return 0;
 }
 

@@ -126,6 +126,11 @@ void ora_hfbs_init_frame(ora_hfbs* s, int color_space, const uint8_t* rgba,
 /* returns 0 on a solve, 1 when the grid exceeded the allocation and the
  * target was copied to the output (src/hfbs.cu:594-611). */
 int ora_hfbs_optimize(ora_hfbs* s);
+/* target / confidence at REAL precision (NULL keeps a plane) */
+void ora_hfbs_set_target_conf(ora_hfbs* s, const REAL* target, const REAL* confidence);
+/* adjoint of the last optimize w.r.t. target and confidence (0 on success,
+ * -1 without a completed optimize); grad_t / grad_c may be NULL */
+int ora_hfbs_backward(ora_hfbs* s, const REAL* grad_out, REAL* grad_t, REAL* grad_c);
 void ora_hfbs_download(const ora_hfbs* s, int image_type, REAL* dst);
 /* grid dims of the last Optimize (gx, gy, gl). */
 void ora_hfbs_grid_dims(const ora_hfbs* s, int* gx, int* gy, int* gl);

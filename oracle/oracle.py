@@ -76,6 +76,8 @@ def lib(real: str = "f64") -> ctypes.CDLL:
             "ora_hfbs_clear_all": ([vp], None),
             "ora_hfbs_init_frame": ([vp, i, vp, vp, vp], None),
             "ora_hfbs_optimize": ([vp], i),
+            "ora_hfbs_set_target_conf": ([vp, vp, vp], None),
+            "ora_hfbs_backward": ([vp, vp, vp, vp], i),
             "ora_hfbs_download": ([vp, i, vp], None),
             "ora_hfbs_grid_dims": ([vp, ctypes.POINTER(i), ctypes.POINTER(i),
                                     ctypes.POINTER(i)], None),
@@ -253,6 +255,20 @@ class OracleHFBS:
 
     def optimize(self) -> int:
         return self.L.ora_hfbs_optimize(self.h)
+
+    def set_target_conf(self, target=None, conf=None):
+        t = None if target is None else np.ascontiguousarray(target, self.dt)
+        c = None if conf is None else np.ascontiguousarray(conf, self.dt)
+        self.L.ora_hfbs_set_target_conf(self.h, _p(t), _p(c))
+
+    def backward(self, grad_out):
+        """dL/dtarget, dL/dconfidence of the last optimize for dL/doutput."""
+        g = np.ascontiguousarray(grad_out, self.dt)
+        gt = np.empty((self.hh, self.w), self.dt)
+        gc = np.empty((self.hh, self.w), self.dt)
+        if self.L.ora_hfbs_backward(self.h, _p(g), _p(gt), _p(gc)) != 0:
+            raise ValueError("no completed optimize to differentiate")
+        return gt, gc
 
     def download(self, image_type):
         out = np.empty((self.hh, self.w), self.dt)

@@ -326,3 +326,63 @@ def test_oracle_adjoint_matches_central_differences(oracle_mod, loss):
             args_m = (b, c) if arr is t else (t, b)
             fd = (L(*args_p) - L(*args_m)) / (2 * float(h))
             assert abs(fd - grad[y, x]) <= 2e-3 * max(1.0, abs(fd)), (k, fd, grad[y, x])
+
+
+# ---- HFBS adjoint --------------------------------------------------------------
+def _hfbs_fd_case(oracle_mod, seed, scale, K, sl=32.0, mg=(16, 16, 16), W_=48, H_=40):
+    rng = np.random.default_rng(seed)
+    g = rng.integers(0, 256, (H_, W_, 4)).astype(np.uint8)
+    g[..., 3] = 255
+    g[0, :8, 0] = 255  # luma-overflow bin when sigma_l divides 255
+    t = rng.uniform(-0.5, 0.5, (H_, W_)) * scale
+    c = rng.uniform(0.1, 1.0, (H_, W_)) * (rng.random((H_, W_)) < 0.5)
+    gout = rng.standard_normal((H_, W_))
+    o = oracle_mod.OracleHFBS(W_, H_, *mg)
+    o.clear_all()
+    o.init_frame(0, g, t.astype(np.float32), c.astype(np.float32))
+    o.set_params(sigma_x=8.0, sigma_y=8.0, sigma_l=sl, lambda_=8.0, alpha=1.0, beta=0.9,
+                 bistoch_iter_max=5, optim_iter_max=K, neg_exp_beta=0.9)
+
+    def loss(tt, cc):
+        o.set_target_conf(tt, cc)
+        assert o.optimize() == 0
+        return float(np.sum(gout * o.download(5)))
+
+    loss(t, c)
+    gt, gc = o.backward(gout)
+    return rng, t, c, loss, gt, gc, o, gout
+
+
+@pytest.mark.parametrize("scale,K,sl,mg", [(1.0, 12, 32.0, (16, 16, 16)),
+                                          (20.0, 20, 32.0, (16, 16, 16)),  # Huber clamp active
+                                          (1.0, 9, 17.0, (8, 8, 32))])    # overflow bin stored
+def test_oracle_hfbs_adjoint_matches_central_differences(oracle_mod, scale, K, sl, mg):
+    """ora_hfbs_backward against FP64 central differences of ora_hfbs_optimize
+    (bins, counts and normalisation do not move under these perturbations)."""
+    rng, t, c, loss, gt, gc, _, _ = _hfbs_fd_case(oracle_mod, 5, scale, K, sl, mg)
+    H_, W_ = t.shape
+    h = 1e-6
+    for _ in range(20):
+        y, x = int(rng.integers(0, H_)), int(rng.integers(0, W_))
+        for which, an in ((0, gt[y, x]), (1, gc[y, x])):
+            a = (t if which == 0 else c).copy()
+            a[y, x] += h
+            lp = loss(a, c) if which == 0 else loss(t, a)
+            a[y, x] -= 2 * h
+            lm = loss(a, c) if which == 0 else loss(t, a)
+            fd = (lp - lm) / (2 * h)
+            assert abs(fd - an) <= 1e-5 * max(1e-2, abs(fd)), (which, y, x, fd, an)
+
+
+def test_oracle_hfbs_adjoint_is_linear_in_the_upstream_gradient(oracle_mod):
+    """The adjoint is linear in dL/doutput: backward(2*g1 - g2) equals
+    2*backward(g1) - backward(g2), and a zero upstream gradient gives zero."""
+    rng, t, c, loss, gt1, gc1, o, g1 = _hfbs_fd_case(oracle_mod, 7, 1.0, 10)
+    g2 = rng.standard_normal(g1.shape)
+    gt2, gc2 = o.backward(g2)
+    gt3, gc3 = o.backward(2 * g1 - g2)
+    assert np.allclose(gt3, 2 * gt1 - gt2, rtol=0, atol=1e-12)
+    assert np.allclose(gc3, 2 * gc1 - gc2, rtol=0, atol=1e-12)
+    gt0, gc0 = o.backward(np.zeros_like(g1))
+    assert not gt0.any() and not gc0.any()
+    assert np.abs(gt1).max() > 0 and np.abs(gc1).max() > 0
