@@ -42,7 +42,8 @@ FALLBACK_HBM_GBS = 6800.0
 L2_FLUSH_BYTES = 256 << 20
 KERNEL_NAMES = {0: "k_bounds", 1: "k_dts_iter", 2: "k_filter", 3: "k_splat",
                 4: "k_bistoch", 5: "k_solve (HFBS heavy-ball)", 6: "hfbs setup kernels",
-                7: "k_slice", 8: "k_to_float", 9: "k_dts_adjoint"}
+                7: "k_slice", 8: "k_to_float", 9: "k_dts_adjoint",
+                10: "hfbs adjoint (whole backward)"}
 
 
 def peaks():
@@ -396,6 +397,7 @@ class Cfg1:
         D, W = self.D, self.W
         w, h = self.u.width, self.u.height
         self.b = D.Batch([(w, h), (w, h)])
+        self.b.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)  # full work every step
         self.b.set_stream(stream_handle)
         self.b.upload(D.COLOR_SPACE.RGB, [self.u.rgba, self.u.rgba],
                       [self.u.target, self.v], [self.u.confidence, self.u.confidence])
@@ -435,6 +437,89 @@ class Cfg1:
             O.hfbs_solve(self.u.rgba, t, self.u.confidence, 0, W.CFG1_HFBS,
                          max_grid=(96, 96, 32), real=real)
         return self.pixels, "U and V solves"
+
+
+class Cfg1Grad(Cfg1):
+    """Differentiable HFBS: the config-1 colorization (U and V, 640x480, 64
+    iterations), FP32, the batched forward keeping every heavy-ball iterate
+    (the automatic checkpoint choice) plus the adjoint (dL/dtarget,
+    dL/dconfidence) for an N(0,1) upstream gradient, both replayed from CUDA
+    graphs.  One step = forward + backward of both channels; bins, counts
+    and normalisation are held fixed (piecewise constant in the guide)."""
+
+    name = "cfg1grad_hfbs_fwd_bwd_640x480_uv_f32"
+
+    def setup(self, stream_handle: int):
+        import torch
+        super().setup(stream_handle)  # the plain batched forward, for the ratio
+        D, W = self.D, self.W
+        w, h = self.u.width, self.u.height
+        rng = np.random.default_rng(7)
+        self.grads = [rng.standard_normal((h, w)).astype(np.float32) for _ in range(2)]
+        self.gb = D.Batch([(w, h), (w, h)])
+        self.gb.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)  # full work every step
+        self.gb.set_stream(stream_handle)
+        self.gb.enable_grad(True, 0)
+        self.gb.upload(D.COLOR_SPACE.RGB, [self.u.rgba, self.u.rgba], [self.u.target, self.v],
+                       [self.u.confidence, self.u.confidence])
+        dev = torch.device("cuda")
+        self.d_g = torch.from_numpy(np.stack(self.grads)).to(dev)
+        self.d_gt = torch.empty_like(self.d_g)
+        self.d_gc = torch.empty_like(self.d_g)
+        self.p_g = (ctypes.c_void_p * 2)(*[self.d_g[i].data_ptr() for i in range(2)])
+        self.p_gt = (ctypes.c_void_p * 2)(*[self.d_gt[i].data_ptr() for i in range(2)])
+        self.p_gc = (ctypes.c_void_p * 2)(*[self.d_gc[i].data_ptr() for i in range(2)])
+        self._g = [_pinned_copy(g) for g in self.grads]
+        self._gt = [_pinned_empty((h, w)) for _ in range(2)]
+        self._gc = [_pinned_empty((h, w)) for _ in range(2)]
+        self.h_g, self.h_gt, self.h_gc = _ptrs(self._g), _ptrs(self._gt), _ptrs(self._gc)
+        self.e2e_api = ("dtsgb_batch_upload, dtsgb_batch_solve_hfbs, dtsgb_batch_download, "
+                        "dtsgb_batch_hfbs_backward")
+
+    def step(self):
+        from domain_transform_solver_gb300._lib import check
+        h = self.gb.handle
+        check(self.lib.dtsgb_batch_solve_hfbs(h, ctypes.byref(self.hpc)))
+        check(self.lib.dtsgb_batch_hfbs_backward_device(h, self.p_g, self.p_gt, self.p_gc))
+
+    def forward_only(self):
+        Cfg1.step(self)
+
+    def step_e2e(self):
+        from domain_transform_solver_gb300._lib import check
+        h = self.gb.handle
+        check(self.lib.dtsgb_batch_upload(h, 0, self.h_rgba, self.h_t, self.h_c))
+        check(self.lib.dtsgb_batch_solve_hfbs(h, ctypes.byref(self.hpc)))
+        check(self.lib.dtsgb_batch_download(h, 1, self.h_o))
+        check(self.lib.dtsgb_batch_hfbs_backward(h, self.h_g, self.h_gt, self.h_gc))
+
+    def e2e_bytes(self):
+        # rgba, target, confidence, upstream gradient in; result, dL/dt, dL/dc out
+        return self.pixels * 16, self.pixels * 12
+
+    def algorithmic_bytes(self):
+        px, vx, k = self.pixels, self.voxels, self.iters
+        return {
+            3: 12 * px + 12 * vx,
+            # four heavy-ball steps: read z, h, norm, b, invA; write z, h and
+            # the three kept iterates
+            5: 40 * vx,
+            7: 8 * px,
+            # the whole adjoint: read dL/dout, guide, target, confidence and
+            # write dL/dt, dL/dc per pixel; per step 10 grid reads, 6 writes
+            10: 24 * px + 64 * vx * k,
+        }
+
+    def cpu_sample(self, real="f32"):
+        import oracle as O
+        W = self.W
+        o = O.OracleHFBS(self.u.width, self.u.height, 96, 96, 32, real=real)
+        o.clear_all()
+        o.init_frame(0, self.u.rgba, self.u.target, self.u.confidence)
+        o.set_params(**W.CFG1_HFBS)
+        o.optimize()
+        o.backward(self.grads[0])
+        return self.pixels // 2, "the U channel, forward + adjoint"
 
 
 class Cfg4:
@@ -550,7 +635,7 @@ class Cfg4:
 
 
 WORKLOADS = {"cfg3": Cfg3, "cfg3dts": Cfg3Dts, "cfg0": Cfg0, "cfg1": Cfg1, "cfg2": Cfg2,
-             "cfg4": Cfg4}
+             "cfg4": Cfg4, "cfg1grad": Cfg1Grad}
 
 
 # ---- arms ----------------------------------------------------------------------

@@ -154,6 +154,9 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_batch_grad_info": ([vp, P(i), P(i)], i),
         "dtsgb_batch_dts_backward": ([vp, pvp, pvp, pvp], i),
         "dtsgb_batch_dts_backward_device": ([vp, pvp, pvp, pvp], i),
+        "dtsgb_batch_hfbs_backward": ([vp, pvp, pvp, pvp], i),
+        "dtsgb_batch_hfbs_backward_device": ([vp, pvp, pvp, pvp], i),
+        "dtsgb_batch_hfbs_grad_info": ([vp, ctypes.POINTER(i), ctypes.POINTER(i)], i),
         "dtsgb_dts_solve_noalloc": ([i, i, i, vp, vp, vp, P(FilterParams),
                                      P(OptimizeParams), f, vp, vp], i),
         "dtsgb_dts_init_right_frame": ([vp, f, i, vp], i),

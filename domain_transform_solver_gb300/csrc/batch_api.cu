@@ -110,6 +110,18 @@ struct dtsgb_batch_s {
   dtsgb_optimize_params gopt{};  // parameters of the solve the planes belong to
   float ghalo = 0.f;
   Graph g_bwd;
+  // gradients of the HFBS solve (the same enable_grad switch): the kept
+  // iterates and adjoint grids (hfbs_grad_planes) in hgbuf; three pixel
+  // planes (dL/dout, dL/dtarget, dL/dconfidence) in hpix
+  float* hgbuf = nullptr;
+  size_t hgcap = 0;  // floats
+  float* hpix = nullptr;
+  HfbsGradState hgs{};
+  int hgrad_seg = 0, hgrad_planes = 0;
+  bool hgrad_ready = false;  // the last HFBS solve kept its iterates
+  HfbsBatch hB{};            // that solve's batch description and parameters
+  HParams hhp{};
+  Graph g_hbwd;
 
   size_t tsize() const { return st == Storage::F32 ? 4 : 2; }
 };
@@ -140,7 +152,10 @@ void batch_free(dtsgb_batch_t b) {
   drop_graph(b, b->g_dts);
   drop_graph(b, b->g_hfbs);
   drop_graph(b, b->g_bwd);
+  drop_graph(b, b->g_hbwd);
   free_grad_planes(b);
+  dfree(b->hgbuf);
+  dfree(b->hpix);
   dfree(b->guide);
   dfree(b->target);
   dfree(b->conf);
@@ -412,6 +427,7 @@ int device_ingest(dtsgb_batch_t b, int cs, const void* const* rgba,
   b->dts_res = -1;
   b->grad_n = -1;
   b->hfbs_done = false;
+  b->hgrad_ready = false;
   return DTSGB_OK;
 }
 
@@ -455,6 +471,7 @@ int host_ingest(dtsgb_batch_t b, int cs, const void* const* rgba,
   b->dts_res = -1;
   b->grad_n = -1;
   b->hfbs_done = false;
+  b->hgrad_ready = false;
   if (sync_host) DTSGB_CUDA(cudaStreamSynchronize(b->stream));
   return DTSGB_OK;
 }
@@ -496,6 +513,7 @@ int batch_upload_targets(dtsgb_batch_t b, const float* const* target,
   b->dts_res = -1;
   b->grad_n = -1;
   b->hfbs_done = false;
+  b->hgrad_ready = false;
   if (kind == cudaMemcpyHostToDevice && sync_host)
     DTSGB_CUDA(cudaStreamSynchronize(b->stream));
   return DTSGB_OK;
@@ -523,6 +541,40 @@ int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
   if (st) return st;
   ++b->guide_gen;
   return batch_upload_targets(b, target, conf, kind, sync_host);
+}
+
+// The HFBS gradient arena for K heavy-ball steps over tv voxels (the choice
+// of segment as for the DTS checkpoints: every iterate when that fits in a
+// quarter of the free device memory, else about sqrt(K) steps), and the
+// three pixel planes of the backward.
+int hfbs_prepare_grad(dtsgb_batch_t b, int K, long long tv) {
+  int S = b->grad_seg_req;
+  if (K <= 1) S = 1;
+  if (S <= 0) {
+    size_t fr = 0, tot = 0;
+    DTSGB_CUDA(cudaMemGetInfo(&fr, &tot));
+    const double avail = (double)fr + (double)b->hgcap * 4.0;
+    S = (double)hfbs_grad_planes(K, 1) * tv * 4.0 <= avail / 4
+            ? 1
+            : std::max(2, (int)std::ceil(std::sqrt((double)K)));
+  }
+  S = std::min(S, std::max(K, 1));
+  const long long need = hfbs_grad_planes(K, S) * tv;
+  if ((size_t)need > b->hgcap) {
+    DTSGB_CUDA(cudaStreamSynchronize(b->stream));  // a backward may still read it
+    dfree(b->hgbuf);
+    b->hgcap = 0;
+    if (int st = dalloc(&b->hgbuf, (size_t)need)) return st;
+    b->hgcap = (size_t)need;
+    drop_graph(b, b->g_hbwd);
+  }
+  if (!b->hpix) {
+    if (int st = dalloc(&b->hpix, (size_t)(3 * b->total))) return st;
+  }
+  hfbs_carve_grad(b->hgs, b->hgbuf, K, S, tv);
+  b->hgrad_seg = S;
+  b->hgrad_planes = (int)hfbs_grad_planes(K, S);
+  return DTSGB_OK;
 }
 
 int ensure_hfbs_buffers(dtsgb_batch_t b, long long voxels, long long planes,
@@ -840,11 +892,20 @@ DTSGB_API int dtsgb_batch_enable_grad(dtsgb_batch_t b, int enable, int segment) 
     DTSGB_CUDA(cudaStreamSynchronize(b->stream));
     drop_graph(b, b->g_dts);
     drop_graph(b, b->g_bwd);
+    drop_graph(b, b->g_hfbs);
+    drop_graph(b, b->g_hbwd);
   }
   b->grad = enable != 0;
   b->grad_seg_req = segment;
   b->grad_n = -1;
-  if (!b->grad) free_grad_planes(b);
+  b->hgrad_ready = false;
+  if (!b->grad) {
+    free_grad_planes(b);
+    dfree(b->hgbuf);
+    dfree(b->hpix);
+    b->hgcap = 0;
+    b->hgrad_seg = b->hgrad_planes = 0;
+  }
   return DTSGB_OK;
 }
 
@@ -1013,10 +1074,17 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
   B.reuse_norm = b->reuse && same_tables && std::memcmp(&nk, &b->nkey, sizeof nk) == 0;
   HParams hp{p->sigma_x, p->sigma_y, p->sigma_l, p->lambda, p->alpha, p->beta,
              p->bistoch_iter_max, p->optim_iter_max, p->neg_exp_beta};
+  b->hgrad_ready = false;
+  if (b->grad) {
+    if ((st = hfbs_prepare_grad(b, p->optim_iter_max, goff))) return st;
+    B.grad = &b->hgs;
+  }
   std::vector<char> key;
   key_append(key, hp);
   key_append(key, b->hfbs_group_voxels);
   key_append(key, B.reuse_norm);
+  key_append(key, b->grad ? b->hgbuf : nullptr);  // the kept iterates' arena
+  key_append(key, b->grad ? b->hgrad_seg : 0);
   st = run_graph(b, b->g_hfbs, key, [&]() { return hfbs_enqueue_solve(B, hp, b->stream); });
   if (st) {
     b->nkey.gen = ~0ull;
@@ -1024,6 +1092,81 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
   }
   b->nkey = nk;
   b->hfbs_done = true;
+  if (b->grad) {
+    b->hB = B;
+    b->hhp = hp;
+    b->hgrad_ready = true;
+  }
+  return DTSGB_OK;
+}
+
+// Adjoint of the last differentiable dtsgb_batch_solve_hfbs (the HFBS
+// counterpart of batch_backward): upstream gradients in, dL/dtarget and
+// dL/dconfidence out, the launch sequence replayed from a CUDA graph.
+static int batch_hfbs_backward(dtsgb_batch_t b, const float* const* grad_out,
+                               float* const* grad_t, float* const* grad_c,
+                               cudaMemcpyKind up, cudaMemcpyKind down) {
+  if (!b || !grad_out) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  if (!b->hgrad_ready)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT,
+                "no HFBS solve with gradients enabled since the last upload");
+  for (int i = 0; i < b->n; ++i)
+    if (!grad_out[i]) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null gradient pointer");
+  float* gout = b->hpix;
+  float* gt = b->hpix + b->total;
+  float* gc = b->hpix + 2 * b->total;
+  if (up == cudaMemcpyHostToDevice) {
+    if (int st = host_upload_plane(b, grad_out, gout, 0)) return st;
+  } else {
+    if (int st = user_plane_copy(b, const_cast<float* const*>(grad_out), gout, true, 0))
+      return st;
+  }
+  std::vector<char> key;
+  key_append(key, b->hhp);
+  key_append(key, b->hgbuf);
+  key_append(key, b->hgrad_seg);
+  key_append(key, b->hB.total_voxels);
+  int st = run_graph(b, b->g_hbwd, key,
+                     [&]() { return hfbs_enqueue_backward(b->hB, b->hhp, gout, gt, gc, b->stream); });
+  if (st) return st;
+  for (int k = 0; k < 2; ++k) {
+    float* const* dst = k == 0 ? grad_t : grad_c;
+    const float* src = k == 0 ? gt : gc;
+    if (!dst) continue;
+    if (down == cudaMemcpyDeviceToDevice) {
+      if (int st = user_plane_copy(b, dst, const_cast<float*>(src), false, 1 + k)) return st;
+      continue;
+    }
+    for (int i = 0; i < b->n; ++i) {
+      if (!dst[i]) continue;
+      const Inst& I = b->inst[i];
+      const size_t wb = (size_t)I.w * 4;
+      DTSGB_CUDA(cudaMemcpy2DAsync(dst[i], wb, src + I.off, (size_t)I.pitch * 4, wb, I.h,
+                                   down, b->stream));
+    }
+  }
+  if (down == cudaMemcpyDeviceToHost) DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_batch_hfbs_backward(dtsgb_batch_t b, const float* const* grad_out,
+                                        float* const* grad_target,
+                                        float* const* grad_confidence) {
+  return batch_hfbs_backward(b, grad_out, grad_target, grad_confidence,
+                             cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost);
+}
+
+DTSGB_API int dtsgb_batch_hfbs_backward_device(dtsgb_batch_t b, const float* const* grad_out,
+                                               float* const* grad_target,
+                                               float* const* grad_confidence) {
+  return batch_hfbs_backward(b, grad_out, grad_target, grad_confidence,
+                             cudaMemcpyDeviceToDevice, cudaMemcpyDeviceToDevice);
+}
+
+DTSGB_API int dtsgb_batch_hfbs_grad_info(dtsgb_batch_t b, int* segment, int* planes) {
+  if (!b || !segment || !planes) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  *segment = b->hgrad_ready ? b->hgrad_seg : 0;
+  *planes = b->hgrad_ready ? b->hgrad_planes : 0;
   return DTSGB_OK;
 }
 

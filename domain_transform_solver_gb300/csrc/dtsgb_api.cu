@@ -741,17 +741,12 @@ static void hfbs_fill_batch(dtsgb_hfbs_t h, const HInst* hi, HfbsBatch& B) {
   B.dbg_z_final = h->g[G_DBG_Z_FINAL];
 }
 
-// Carve the gradient arena for K heavy-ball steps over tv voxels: the
-// adjoint's six grids, the kept iterates of the chosen segment and three
-// pixel planes.  Segment 0 (automatic): every iterate when that fits in a
-// quarter of the free device memory (the arena already held counts as free),
-// else about sqrt(K) steps per segment.
+// Carve the gradient arena for K heavy-ball steps over tv voxels: the kept
+// iterates and the adjoint's grids (hfbs_grad_planes) and three pixel planes.
+// Segment 0 (automatic): every iterate when that fits in a quarter of the
+// free device memory (the arena already held counts as free), else about
+// sqrt(K) steps per segment.
 static int hfbs_prepare_grad(dtsgb_hfbs_t h, int K, long long tv) {
-  auto planes_for = [&](int S) -> long long {
-    if (S == 1) return 6 + std::max(K - 1, 0);
-    const long long nck = (K + S - 1) / S;
-    return 6 + 2 * nck + (S - 1) + 1;
-  };
   const long long pix = 3 * (long long)h->plane;
   int S = h->grad_seg_req;
   if (K <= 1) S = 1;
@@ -759,12 +754,13 @@ static int hfbs_prepare_grad(dtsgb_hfbs_t h, int K, long long tv) {
     size_t fr = 0, tot = 0;
     DTSGB_CUDA(cudaMemGetInfo(&fr, &tot));
     const double avail = (double)fr + (double)h->gbuf_cap * 4.0;
-    const double need1 = ((double)planes_for(1) * tv + pix) * 4.0;
+    const double need1 = ((double)hfbs_grad_planes(K, 1) * tv + pix) * 4.0;
     S = need1 <= avail / 4 ? 1 : std::max(2, (int)std::ceil(std::sqrt((double)K)));
   }
   S = std::min(S, std::max(K, 1));
-  const long long need = planes_for(S) * tv + pix;
+  const long long need = hfbs_grad_planes(K, S) * tv + pix;
   if ((size_t)need > h->gbuf_cap) {
+    DTSGB_CUDA(cudaStreamSynchronize(h->stream));  // a backward may still read it
     dfree(h->gbuf);
     h->gbuf_cap = 0;
     int st = dalloc(&h->gbuf, (size_t)need);
@@ -772,34 +768,13 @@ static int hfbs_prepare_grad(dtsgb_hfbs_t h, int K, long long tv) {
     h->gbuf_cap = (size_t)need;
   }
   float* q = h->gbuf;
-  auto take = [&](long long planes) {
-    float* r = q;
-    q += planes * tv;
-    return r;
-  };
-  HfbsGradState& G = h->gs;
-  G = HfbsGradState{};
-  G.segment = S;
-  G.gz = take(1);
-  G.gh = take(1);
-  G.gg = take(1);
-  G.gw = take(1);
-  G.gb = take(1);
-  G.ginv = take(1);
-  if (S == 1) {
-    G.hist = take(std::max(K - 1, 0));
-  } else {
-    const long long nck = (K + S - 1) / S;
-    G.ckz = take(nck);
-    G.ckh = take(nck);
-    G.seg = take(S - 1);
-    G.hrec = take(1);
-  }
+  hfbs_carve_grad(h->gs, q, K, S, tv);
+  q += hfbs_grad_planes(K, S) * tv;
   h->gout = q;
   h->gtgt = q + h->plane;
   h->gcnf = q + 2 * h->plane;
   h->grad_seg = S;
-  h->grad_planes = (int)planes_for(S);
+  h->grad_planes = (int)hfbs_grad_planes(K, S);
   return DTSGB_OK;
 }
 

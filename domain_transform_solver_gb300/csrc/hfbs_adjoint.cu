@@ -126,71 +126,76 @@ __global__ void k_hb_slice_gather(const HInst* __restrict__ insts,
   }
 }
 
-// step^T, first half: per voxel, with the forward iterate z_k of the step.
-// The neighbour sum and q are formed exactly as in the forward step, so the
-// Huber mask is the forward's.
-__global__ void k_hb_step_adj_a(const HInst* __restrict__ insts, const float* __restrict__ zk,
-                                const float* __restrict__ gz, float* __restrict__ gh,
-                                float* __restrict__ gg, float* __restrict__ gw,
-                                const float* __restrict__ norm, const float* __restrict__ b,
-                                const float* __restrict__ invA, float* __restrict__ gb,
-                                float* __restrict__ ginv, float lambda, float alpha,
-                                float beta) {
+// step^T, one launch per step.  finish: complete the previous (later) step,
+// gz += gg_in - lambda*norm*N(gw_in) (N: the six-neighbour sum; gw_in of the
+// neighbours comes from the previous launch).  step: the adjoint of step k
+// with its forward iterate z_k, into gh, gb, ginv and gg_out, gw_out.  The
+// neighbour sum and q are formed as in the forward step (kRounded: the
+// temporally blocked kernel's rounded z * n products), so the Huber mask is
+// the forward's.
+template <bool kRounded>
+__global__ void k_hb_step_adj(const HInst* __restrict__ insts, const float* __restrict__ zk,
+                              float* __restrict__ gz, float* __restrict__ gh,
+                              const float* __restrict__ gg_in, const float* __restrict__ gw_in,
+                              float* __restrict__ gg_out, float* __restrict__ gw_out,
+                              const float* __restrict__ norm, const float* __restrict__ b,
+                              const float* __restrict__ invA, float* __restrict__ gb,
+                              float* __restrict__ ginv, float lambda, float alpha, float beta,
+                              int finish, int step) {
   const HInst I = insts[blockIdx.y];
   const int gx = I.gx, gy = I.gy, gl = I.gl;
   const long long nv = (long long)gx * gy * gl;
   const int sy = gx, sz = gx * gy;
-  const float* z = zk + I.grid_off;
   const float* nn = norm + I.grid_off;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nv;
        v += (long long)gridDim.x * blockDim.x) {
     const int r = (int)(v / gx), x = (int)(v - (long long)r * gx);
     const int zz = r / gy, y = r - zz * gy;
     const int i = (int)v;
-    float a = 0.f;
-    if (x > 0) a += z[i - 1] * nn[i - 1];
-    if (x + 1 < gx) a += z[i + 1] * nn[i + 1];
-    if (y > 0) a += z[i - sy] * nn[i - sy];
-    if (y + 1 < gy) a += z[i + sy] * nn[i + sy];
-    if (zz > 0) a += z[i - sz] * nn[i - sz];
-    if (zz + 1 < gl) a += z[i + sz] * nn[i + sz];
     const long long g = I.grid_off + v;
-    const float nc = nn[i], bc = b[g], ic = invA[g];
-    const float q = (bc + lambda * nc * a) * ic;
-    const float grad = z[i] - q;
-    const float u = gh[g] - alpha * gz[g];
-    const float m = fabsf(grad) >= 1.345f ? 0.f : u;
-    gh[g] = beta * u;
-    gb[g] -= ic * m;
-    ginv[g] -= (bc + lambda * nc * a) * m;
-    gg[g] = m;
-    gw[g] = nc * ic * m;
-  }
-}
-
-// step^T, second half: gz += gg - lambda*norm*N(gw).
-__global__ void k_hb_step_adj_b(const HInst* __restrict__ insts, float* __restrict__ gz,
-                                const float* __restrict__ gg, const float* __restrict__ gw,
-                                const float* __restrict__ norm, float lambda) {
-  const HInst I = insts[blockIdx.y];
-  const int gx = I.gx, gy = I.gy, gl = I.gl;
-  const long long nv = (long long)gx * gy * gl;
-  const int sy = gx, sz = gx * gy;
-  const float* w = gw + I.grid_off;
-  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nv;
-       v += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(v / gx), x = (int)(v - (long long)r * gx);
-    const int zz = r / gy, y = r - zz * gy;
-    const int i = (int)v;
-    float a = 0.f;
-    if (x > 0) a += w[i - 1];
-    if (x + 1 < gx) a += w[i + 1];
-    if (y > 0) a += w[i - sy];
-    if (y + 1 < gy) a += w[i + sy];
-    if (zz > 0) a += w[i - sz];
-    if (zz + 1 < gl) a += w[i + sz];
-    const long long g = I.grid_off + v;
-    gz[g] += gg[g] - lambda * norm[g] * a;
+    float gzv = gz[g];
+    const float nc = nn[i];
+    if (finish) {
+      const float* w = gw_in + I.grid_off;
+      float a = 0.f;
+      if (x > 0) a += w[i - 1];
+      if (x + 1 < gx) a += w[i + 1];
+      if (y > 0) a += w[i - sy];
+      if (y + 1 < gy) a += w[i + sy];
+      if (zz > 0) a += w[i - sz];
+      if (zz + 1 < gl) a += w[i + sz];
+      gzv += gg_in[g] - lambda * nc * a;
+      gz[g] = gzv;
+    }
+    if (step) {
+      const float* z = zk + I.grid_off;
+      float a = 0.f;
+      if (kRounded) {
+        if (x > 0) a = a + __fmul_rn(z[i - 1], nn[i - 1]);
+        if (x + 1 < gx) a = a + __fmul_rn(z[i + 1], nn[i + 1]);
+        if (y > 0) a = a + __fmul_rn(z[i - sy], nn[i - sy]);
+        if (y + 1 < gy) a = a + __fmul_rn(z[i + sy], nn[i + sy]);
+        if (zz > 0) a = a + __fmul_rn(z[i - sz], nn[i - sz]);
+        if (zz + 1 < gl) a = a + __fmul_rn(z[i + sz], nn[i + sz]);
+      } else {
+        if (x > 0) a += z[i - 1] * nn[i - 1];
+        if (x + 1 < gx) a += z[i + 1] * nn[i + 1];
+        if (y > 0) a += z[i - sy] * nn[i - sy];
+        if (y + 1 < gy) a += z[i + sy] * nn[i + sy];
+        if (zz > 0) a += z[i - sz] * nn[i - sz];
+        if (zz + 1 < gl) a += z[i + sz] * nn[i + sz];
+      }
+      const float bc = b[g], ic = invA[g];
+      const float q = (bc + lambda * nc * a) * ic;
+      const float grad = z[i] - q;
+      const float u = gh[g] - alpha * gzv;
+      const float m = fabsf(grad) >= 1.345f ? 0.f : u;
+      gh[g] = beta * u;
+      gb[g] -= ic * m;
+      ginv[g] -= (bc + lambda * nc * a) * m;
+      gg_out[g] = m;
+      gw_out[g] = nc * ic * m;
+    }
   }
 }
 
@@ -264,8 +269,8 @@ int hfbs_enqueue_backward(const HfbsBatch& B, const HParams& p, const float* gou
   const float* norm = (p.bistoch_iter_max % 2) ? B.n1 : B.n0;
   const int K = p.optim_iter_max;
   const int S = G.segment;
-  // z_0: checkpoint slot 0 when the forward ping-ponged its iterates
-  const float* z0 = (S == 1 || K == 0) ? B.z0 : G.ckz;
+  // z_0: hist plane 0 or checkpoint slot 0 (the z0 buffer is overwritten)
+  const float* z0 = K == 0 ? B.z0 : (S == 1 ? G.hist : G.ckz);
   float* sp = grad_t ? grad_t : grad_c;
   if (!sp) return DTSGB_OK;  // no gradient asked for
   prof_begin(s, DTSGB_K_HFBS_ADJOINT);
@@ -285,13 +290,26 @@ int hfbs_enqueue_backward(const HfbsBatch& B, const HParams& p, const float* gou
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsmem));
   const dim3 gcol((unsigned)((B.max_cells + kSliceCols - 1) / kSliceCols), ni);
   k_hb_slice_gather<<<gcol, kSliceCols, hsmem, s>>>(B.d_inst, B.guide, sp, B.count, G.gz, p);
+  const bool tb = hfbs_uses_tb(B);
+  // (gg, gw) ping-pong: a launch reads the pair the previous one wrote
+  float* pg[2] = {G.gg, G.gg2};
+  float* pw[2] = {G.gw, G.gw2};
+  int cur = 0, launched = 0;
   auto step_adj = [&](const float* zk) {
-    k_hb_step_adj_a<<<gv, kA, 0, s>>>(B.d_inst, zk, G.gz, G.gh, G.gg, G.gw, norm, B.b,
-                                      B.invA, G.gb, G.ginv, p.lambda, p.alpha, p.beta);
-    k_hb_step_adj_b<<<gv, kA, 0, s>>>(B.d_inst, G.gz, G.gg, G.gw, norm, p.lambda);
+    const int fin = launched > 0, nx = cur ^ 1;
+    if (tb)
+      k_hb_step_adj<true><<<gv, kA, 0, s>>>(B.d_inst, zk, G.gz, G.gh, pg[cur], pw[cur], pg[nx],
+                                            pw[nx], norm, B.b, B.invA, G.gb, G.ginv,
+                                            p.lambda, p.alpha, p.beta, fin, 1);
+    else
+      k_hb_step_adj<false><<<gv, kA, 0, s>>>(B.d_inst, zk, G.gz, G.gh, pg[cur], pw[cur],
+                                             pg[nx], pw[nx], norm, B.b, B.invA, G.gb,
+                                             G.ginv, p.lambda, p.alpha, p.beta, fin, 1);
+    cur = nx;
+    ++launched;
   };
   if (S == 1) {
-    for (int k = K - 1; k >= 0; --k) step_adj(k == 0 ? B.z0 : G.hist + (size_t)(k - 1) * tv);
+    for (int k = K - 1; k >= 0; --k) step_adj(G.hist + (size_t)k * tv);
   } else {
     const int nseg = (K + S - 1) / S;
     for (int j = nseg - 1; j >= 0; --j) {
@@ -299,11 +317,30 @@ int hfbs_enqueue_backward(const HfbsBatch& B, const HParams& p, const float* gou
       auto zk = [&](int k) -> float* {
         return k == start ? G.ckz + (size_t)j * tv : G.seg + (size_t)(k - start - 1) * tv;
       };
-      DTSGB_CUDA(cudaMemcpyAsync(G.hrec, G.ckh + (size_t)j * tv, gbytes,
-                                 cudaMemcpyDeviceToDevice, s));
-      for (int k = start; k + 1 < end; ++k) hfbs_launch_step(B, p, zk(k), zk(k + 1), G.hrec, norm, s);
+      // recompute z_{start+1} .. z_{end-1} from the segment's checkpoint
+      const float* hin = G.ckh + (size_t)j * tv;
+      float* hbuf[2] = {G.hrec, G.hrec2};
+      int hb = 0;
+      if (!tb) {  // the one-step kernel updates h in place
+        DTSGB_CUDA(cudaMemcpyAsync(G.hrec, hin, gbytes, cudaMemcpyDeviceToDevice, s));
+        hin = G.hrec;
+      }
+      for (int k = start; k + 1 < end;) {
+        const int steps = tb ? std::min(kHfbsTBSteps, end - 1 - k) : 1;
+        float* hout = tb ? hbuf[hb] : G.hrec;
+        hfbs_launch_steps(B, p, norm, zk(k), zk(k + steps), hin, hout, steps,
+                          tb ? zk(k + 1) : nullptr, tb ? steps : 0, s);
+        hin = hout;
+        hb ^= 1;
+        k += steps;
+      }
       for (int k = end - 1; k >= start; --k) step_adj(zk(k));
     }
+  }
+  if (launched > 0) {  // finish step 0
+    k_hb_step_adj<false><<<gv, kA, 0, s>>>(B.d_inst, nullptr, G.gz, G.gh, pg[cur], pw[cur],
+                                           nullptr, nullptr, norm, B.b, B.invA, G.gb, G.ginv,
+                                           p.lambda, p.alpha, p.beta, 1, 0);
   }
   k_hb_initz_adj<<<gflat, kA, 0, s>>>(B.t0, z0, G.gz, G.gg, G.gw, tv);
   // blur^T of (gg, gw), gz and gh as scratch: results in t1 (for gb), t2 (gcsum)

@@ -44,18 +44,56 @@ struct HParams {
 };
 
 // Forward iterates kept for the HFBS adjoint, and its scratch grids (all
-// total_voxels floats per plane).  segment 1: z_0 stays in the z0 buffer and
-// z_k (1 <= k < K) is written to hist + (k - 1) planes, nothing is recomputed.
-// segment S > 1: z and h at the start of every S-step segment go to slot j of
-// ckz / ckh (step j*S), and the backward recomputes a segment's iterates into
-// seg (S - 1 planes) with h in hrec.
+// total_voxels floats per plane).  segment 1: z_k (0 <= k < K) in hist plane
+// k, nothing is recomputed.  segment S > 1: z and h at the start of every
+// S-step segment go to slot j of ckz / ckh (step j*S), and the backward
+// recomputes a segment's iterates into seg (S - 1 planes) with h ping-ponging
+// through hrec / hrec2.  The adjoint's scratch: gz, gh, gb, ginv and two
+// (gg, gw) pairs.
 struct HfbsGradState {
   int segment = 1;
   float* hist = nullptr;
-  float *ckz = nullptr, *ckh = nullptr, *seg = nullptr, *hrec = nullptr;
-  float *gz = nullptr, *gh = nullptr, *gg = nullptr, *gw = nullptr, *gb = nullptr,
-        *ginv = nullptr;
+  float *ckz = nullptr, *ckh = nullptr, *seg = nullptr, *hrec = nullptr, *hrec2 = nullptr;
+  float *gz = nullptr, *gh = nullptr, *gb = nullptr, *ginv = nullptr;
+  float *gg = nullptr, *gw = nullptr, *gg2 = nullptr, *gw2 = nullptr;
 };
+
+// Grid planes of an HfbsGradState for K steps and segment S.
+inline long long hfbs_grad_planes(int K, int S) {
+  if (S == 1) return 8 + (K > 0 ? K : 0);
+  const long long nck = (K + S - 1) / S;
+  return 8 + 2 * nck + (S - 1) + 2;
+}
+
+// Point G's planes into an arena of hfbs_grad_planes(K, S) * tv floats.
+inline void hfbs_carve_grad(HfbsGradState& G, float* arena, int K, int S, long long tv) {
+  float* q = arena;
+  auto take = [&](long long planes) {
+    float* r = q;
+    q += planes * tv;
+    return r;
+  };
+  G = HfbsGradState{};
+  G.segment = S;
+  G.gz = take(1);
+  G.gh = take(1);
+  G.gb = take(1);
+  G.ginv = take(1);
+  G.gg = take(1);
+  G.gw = take(1);
+  G.gg2 = take(1);
+  G.gw2 = take(1);
+  if (S == 1) {
+    G.hist = take(K > 0 ? K : 0);
+  } else {
+    const long long nck = (K + S - 1) / S;
+    G.ckz = take(nck);
+    G.ckh = take(nck);
+    G.seg = take(S - 1);
+    G.hrec = take(1);
+    G.hrec2 = take(1);
+  }
+}
 
 // Device buffers and sizes of a batch of HFBS instances.
 struct HfbsBatch {
@@ -93,9 +131,22 @@ struct HfbsBatch {
 // Enqueue the whole HFBS::Optimize sequence (splat .. slice) on a stream.
 int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s);
 
-// One heavy-ball step of every instance: zs -> zd, h in place.
-void hfbs_launch_step(const HfbsBatch& B, const HParams& p, const float* zs, float* zd,
-                      float* h, const float* norm, cudaStream_t s);
+// Heavy-ball steps per launch of the temporally blocked kernel.
+constexpr int kHfbsTBSteps = 4;
+
+// Whether the batch's heavy-ball steps run temporally blocked (every grid
+// at most 16 levels, host instance table given).  Its neighbour sums add
+// rounded z * n products; the one-step kernel's fuse them (FMA).
+bool hfbs_uses_tb(const HfbsBatch& B);
+
+// `steps` heavy-ball steps of every instance from (zs, hs) to (zd, hd): one
+// temporally blocked launch (steps <= kHfbsTBSteps), else one one-step launch
+// (steps == 1, h updated in place in hd: the caller passes hs == hd).  rec:
+// z after each of the first rec_steps steps, plane stride total_voxels
+// (temporally blocked launches only).
+void hfbs_launch_steps(const HfbsBatch& B, const HParams& p, const float* norm,
+                       const float* zs, float* zd, const float* hs, float* hd, int steps,
+                       float* rec, int rec_steps, cudaStream_t s);
 
 // X -> Y -> Z Laplace blur of two grids s0, s1 into x0, x1 (y0, y1 scratch).
 void hfbs_launch_blur_pair(const HfbsBatch& B, const HParams& p, const float* s0,

@@ -425,6 +425,7 @@ __global__ void k_solve(const HInst* __restrict__ insts,
 // the space the z * n buffers use afterwards.  Every thread reads and writes
 // only its own column there, so the reuse needs no barrier.
 constexpr int kTBT = 16, kTBK = 4, kTBL = kTBT + 2 * kTBK;
+static_assert(kTBK == kHfbsTBSteps, "steps per temporally blocked launch");
 constexpr int kTBMaxGL = 16;
 constexpr int kTBThreads = kTBL * kTBL;  // one thread per (x, y) column
 constexpr int kTBPlane = kTBMaxGL * kTBThreads;  // floats per staged array
@@ -451,7 +452,7 @@ __global__ void __launch_bounds__(kTBThreads, 1)
                float* __restrict__ zd, const float* __restrict__ hs, float* __restrict__ hd,
                const float* __restrict__ norm, const float* __restrict__ b,
                const float* __restrict__ invA, float lambda, float alpha, float beta,
-               int steps) {
+               int steps, float* __restrict__ rec, long long rec_stride, int rec_steps) {
   extern __shared__ float tb_s[];
   float* Bs = tb_s;
   float* As = Bs + kTBPlane;
@@ -506,6 +507,14 @@ __global__ void __launch_bounds__(kTBThreads, 1)
         below = cur;
         cur = above;
       }
+    }
+    // iterates kept for the adjoint: z after step k of the tile's columns
+    if (k <= rec_steps && in && xx >= kTBK && xx < kTBK + kTBT && yy >= kTBK &&
+        yy < kTBK + kTBT) {
+      float* zr = rec + (long long)(k - 1) * rec_stride + g0;
+#pragma unroll
+      for (int l = 0; l < kTBMaxGL; ++l)
+        if (l < gl) zr[l * plane] = z[l];
     }
   }
   if (in && xx >= kTBK && xx < kTBK + kTBT && yy >= kTBK && yy < kTBK + kTBT) {
@@ -650,12 +659,29 @@ int blocks_for(long long n) {
 
 }  // namespace
 
-void hfbs_launch_step(const HfbsBatch& B, const HParams& p, const float* zs, float* zd,
-                      float* h, const float* norm, cudaStream_t s) {
-  // one warp per grid row (y, l) of the largest grid
-  const dim3 gr((unsigned)std::min<long long>((B.max_rows + 7) / 8, 4096), B.n_inst);
-  k_solve<<<gr, kT, 0, s>>>(B.d_inst, zs, zd, h, norm, B.b, B.invA, p.lambda, p.alpha,
-                            p.beta);
+bool hfbs_uses_tb(const HfbsBatch& B) { return B.max_gl <= kTBMaxGL && B.h_inst; }
+
+void hfbs_launch_steps(const HfbsBatch& B, const HParams& p, const float* norm,
+                       const float* zs, float* zd, const float* hs, float* hd, int steps,
+                       float* rec, int rec_steps, cudaStream_t s) {
+  prof_begin(s, DTSGB_K_HFBS_SOLVE);
+  if (hfbs_uses_tb(B)) {
+    long long tiles = 1;
+    for (int i = 0; i < B.n_inst; ++i) {
+      const HInst& H = B.h_inst[i];
+      tiles = std::max(tiles, (long long)((H.gx + kTBT - 1) / kTBT) * ((H.gy + kTBT - 1) / kTBT));
+    }
+    cudaFuncSetAttribute(k_solve_tb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTBSmem);
+    k_solve_tb<<<dim3((unsigned)tiles, B.n_inst), kTBThreads, kTBSmem, s>>>(
+        B.d_inst, zs, zd, hs, hd, norm, B.b, B.invA, p.lambda, p.alpha, p.beta, steps, rec,
+        B.total_voxels, rec_steps);
+  } else {
+    // one step; h in place (hs == hd)
+    const dim3 gr((unsigned)std::min<long long>((B.max_rows + 7) / 8, 4096), B.n_inst);
+    k_solve<<<gr, kT, 0, s>>>(B.d_inst, zs, zd, hd, norm, B.b, B.invA, p.lambda, p.alpha,
+                              p.beta);
+  }
+  prof_end(s, DTSGB_K_HFBS_SOLVE);
 }
 
 void hfbs_launch_blur_pair(const HfbsBatch& B, const HParams& p, const float* s0,
@@ -778,28 +804,45 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   float* zs = B.z0;
   float* zd = B.z1;
   if (B.grad) {
-    // iterates kept for the adjoint (HfbsGradState): one-step passes
+    // iterates kept for the adjoint (HfbsGradState)
     const HfbsGradState& G = *B.grad;
     const int K = p.optim_iter_max, S = G.segment;
+    const bool tb = hfbs_uses_tb(B);
     const long long tv = B.total_voxels;
     const size_t gbytes = (size_t)tv * sizeof(float);
-    for (int k = 0; k < K; ++k) {
-      float* nxt;
-      if (S == 1) {
-        nxt = k + 1 < K ? G.hist + (size_t)k * tv : (zs == B.z1 ? B.z0 : B.z1);
-      } else {
-        if (k % S == 0) {
-          DTSGB_CUDA(cudaMemcpyAsync(G.ckz + (size_t)(k / S) * tv, zs, gbytes,
+    if (S == 1) {
+      // z_k in hist plane k; h ping-pongs through the free blur temporary t2
+      if (K > 0)
+        DTSGB_CUDA(cudaMemcpyAsync(G.hist, B.z0, gbytes, cudaMemcpyDeviceToDevice, s));
+      float* hs = B.h;
+      float* hd = tb ? B.t2 : B.h;
+      for (int it = 0; it < K;) {
+        const int steps = tb ? std::min(kTBK, K - it) : 1;
+        float* zout = it + steps < K ? G.hist + (size_t)(it + steps) * tv : B.z1;
+        const int rec_steps = tb ? std::min(steps, K - 1 - it) : 0;
+        hfbs_launch_steps(B, p, norm, G.hist + (size_t)it * tv, zout, hs, hd, steps,
+                          G.hist + (size_t)(it + 1) * tv, rec_steps, s);
+        std::swap(hs, hd);
+        it += steps;
+      }
+      zs = K > 0 ? B.z1 : B.z0;
+    } else {
+      // z and h at the start of every segment
+      float* hs = B.h;
+      float* hd = tb ? B.t2 : B.h;
+      for (int it = 0; it < K;) {
+        if (it % S == 0) {
+          DTSGB_CUDA(cudaMemcpyAsync(G.ckz + (size_t)(it / S) * tv, zs, gbytes,
                                      cudaMemcpyDeviceToDevice, s));
-          DTSGB_CUDA(cudaMemcpyAsync(G.ckh + (size_t)(k / S) * tv, B.h, gbytes,
+          DTSGB_CUDA(cudaMemcpyAsync(G.ckh + (size_t)(it / S) * tv, hs, gbytes,
                                      cudaMemcpyDeviceToDevice, s));
         }
-        nxt = zs == B.z0 ? B.z1 : B.z0;
+        const int steps = tb ? std::min({kTBK, K - it, S - it % S}) : 1;
+        hfbs_launch_steps(B, p, norm, zs, zd, hs, hd, steps, nullptr, 0, s);
+        std::swap(zs, zd);
+        std::swap(hs, hd);
+        it += steps;
       }
-      prof_begin(s, DTSGB_K_HFBS_SOLVE);
-      hfbs_launch_step(B, p, zs, nxt, B.h, norm, s);
-      prof_end(s, DTSGB_K_HFBS_SOLVE);
-      zs = nxt;
     }
   } else if (B.max_gl <= kTBMaxGL && B.h_inst) {
     // K heavy-ball steps per pass; h ping-pongs through the free blur
@@ -823,7 +866,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
         prof_begin(s, DTSGB_K_HFBS_SOLVE);
         k_solve_tb<<<gt, kTBThreads, kTBSmem, s>>>(B.d_inst + g.first, zs, zd, hs, hd, norm,
                                                     B.b, B.invA, p.lambda, p.alpha, p.beta,
-                                                    steps);
+                                                    steps, nullptr, 0, 0);
         prof_end(s, DTSGB_K_HFBS_SOLVE);
         std::swap(zs, zd);
         std::swap(hs, hd);

@@ -562,6 +562,30 @@ class Batch:
         check(self._lib.dtsgb_batch_dts_backward_device(self._h, _vp_array(grad_out_ptrs),
                                                         _vp_array(grad_target_ptrs), gc))
 
+    def hfbs_grad_info(self):
+        """(segment length, grid planes) of the last differentiable
+        solve_hfbs ((0, 0): none)."""
+        seg, planes = ctypes.c_int(), ctypes.c_int()
+        check(self._lib.dtsgb_batch_hfbs_grad_info(self._h, ctypes.byref(seg),
+                                                   ctypes.byref(planes)))
+        return seg.value, planes.value
+
+    def hfbs_backward(self, grad_out):
+        """dL/dtarget, dL/dconfidence (lists of HxW float32) for the upstream
+        gradients of the last solve_hfbs results."""
+        go = [_f32(a, (h, w)) for a, (w, h) in zip(grad_out, self.sizes)]
+        gt = [np.empty((h, w), np.float32) for w, h in self.sizes]
+        gc = [np.empty((h, w), np.float32) for w, h in self.sizes]
+        check(self._lib.dtsgb_batch_hfbs_backward(self._h, _ptr_array(go), _ptr_array(gt),
+                                                  _ptr_array(gc)))
+        return gt, gc
+
+    def hfbs_backward_device(self, grad_out_ptrs, grad_target_ptrs,
+                             grad_conf_ptrs=None) -> None:
+        gc = None if grad_conf_ptrs is None else _vp_array(grad_conf_ptrs)
+        check(self._lib.dtsgb_batch_hfbs_backward_device(
+            self._h, _vp_array(grad_out_ptrs), _vp_array(grad_target_ptrs), gc))
+
 
 class Pipeline:
     """Host-to-host solves of many images with the copies of one chunk of

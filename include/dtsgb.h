@@ -448,6 +448,20 @@ DTSGB_API int dtsgb_batch_dts_backward_device(dtsgb_batch_t b,
                                               const float* const* grad_out,
                                               float* const* grad_target,
                                               float* const* grad_confidence);
+/* The HFBS counterpart: with gradients enabled (dtsgb_batch_enable_grad),
+ * dtsgb_batch_solve_hfbs keeps its heavy-ball iterates (the same segment
+ * choice; the forward result is unchanged) and dtsgb_batch_hfbs_backward maps
+ * the upstream gradients of its results to dL/dtarget and dL/dconfidence of
+ * every instance, as dtsgb_hfbs_backward does for one. */
+DTSGB_API int dtsgb_batch_hfbs_backward(dtsgb_batch_t b, const float* const* grad_out,
+                                        float* const* grad_target,
+                                        float* const* grad_confidence);
+DTSGB_API int dtsgb_batch_hfbs_backward_device(dtsgb_batch_t b,
+                                               const float* const* grad_out,
+                                               float* const* grad_target,
+                                               float* const* grad_confidence);
+/* segment and grid planes of the last differentiable HFBS solve (0, 0: none) */
+DTSGB_API int dtsgb_batch_hfbs_grad_info(dtsgb_batch_t b, int* segment, int* planes);
 
 /* ---- Host-side image helper (no counterpart: the reference's drivers decode
  * PNG with OpenCV).  Undoes the PNG row filters (types 0-4) of `height` rows

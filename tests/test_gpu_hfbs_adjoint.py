@@ -137,8 +137,8 @@ def test_hfbs_adjoint_matches_fp64_central_differences(gpu_ready, oracle_mod):
 
 def test_hfbs_checkpoint_segments_agree_bitwise(gpu_ready):
     """Every iterate kept (segment 1) and segments recomputed from (z, h)
-    checkpoints give the same gradients bit for bit; the forward result of a
-    differentiable solve matches the plain solve."""
+    checkpoints give the same gradients bit for bit, and the forward result
+    of a differentiable solve is the plain solve's."""
     D = gpu_ready
     params = dict(BASE, optim_iter_max=30)
     g, t, c, gout = _inputs(41, 96, 64, "graded")
@@ -147,21 +147,22 @@ def test_hfbs_checkpoint_segments_agree_bitwise(gpu_ready):
         assert np.array_equal(out, res[0][0])
         assert np.array_equal(gt, res[0][1])
         assert np.array_equal(gc, res[0][2])
-    assert res[1][3].GradInfo() == (4, 6 + 2 * 8 + 3 + 1)
+    # 8 adjoint grids, (z, h) at 8 checkpoints, 3 segment planes, 2 for h
+    assert res[1][3].GradInfo() == (4, 8 + 2 * 8 + 3 + 2)
     plain = D.HFBS(D.ImageDim(96, 64), 12, 8, 16)
     plain.SetFilterParams(D.HFBSGridParams(**params))
     plain.ClearAll()
     plain.InitFrame(D.COLOR_SPACE.RGB, g, t, c)
     plain.Optimize()
     ref = plain.Download(D.ImageType.OPTIMIZED_QUANTITY)
-    assert np.abs(res[0][0] - ref).max() <= 1e-6 * P.target_range(t)
+    assert np.array_equal(res[0][0], ref)  # the same heavy-ball kernel
 
 
 def test_hfbs_automatic_segment_keeps_every_iterate(gpu_ready):
     D = gpu_ready
     g, t, c, gout = _inputs(51, 64, 48, "sparse")
     _, _, _, s = _gpu(D, g, t, c, dict(BASE, optim_iter_max=40), (8, 6, 16), gout)
-    assert s.GradInfo() == (1, 6 + 39)
+    assert s.GradInfo() == (1, 8 + 40)  # 8 adjoint grids, every iterate
 
 
 def test_hfbs_backward_needs_a_gradient_solve(gpu_ready):
@@ -199,3 +200,36 @@ def test_hfbs_torch_autograd_binding(gpu_ready):
         assert np.array_equal(out[i].detach().cpu().numpy(), ref_out)
         assert np.array_equal(t.grad[i].cpu().numpy(), rt)
         assert np.array_equal(c.grad[i].cpu().numpy(), rc)
+
+
+@pytest.mark.parametrize("bf16", [0, 1])
+def test_batch_hfbs_backward_matches_single_handles(gpu_ready, bf16):
+    """dtsgb_batch_hfbs_backward over ragged instances (one graph-replayed
+    launch sequence) against one HFBS handle per instance.  The batch stores
+    the overflow bin and pads like a handle whose max grid exceeds the grid;
+    BF16 storage is compared on BF16-rounded inputs."""
+    D = gpu_ready
+    sizes = [(96, 64), (71, 53), (40, 24)]
+    params = dict(BASE, optim_iter_max=24)
+    data = [_inputs(81 + i, w, h, "graded") for i, (w, h) in enumerate(sizes)]
+    b = D.Batch(sizes, flags=D.FLAG_BF16_STORAGE if bf16 else 0)
+    b.enable_grad(True, 0)
+    b.upload(D.COLOR_SPACE.RGB, [d[0] for d in data], [d[1] for d in data],
+             [d[2] for d in data])
+    b.solve_hfbs(D.HFBSGridParams(**params))
+    outs = b.download(1)
+    for rep in range(2):  # the second backward replays the captured graph
+        gts, gcs = b.hfbs_backward([d[3] for d in data])
+    assert b.hfbs_grad_info() == (1, 8 + 24)
+    for i, ((w, h), (g, t, c, gout)) in enumerate(zip(sizes, data)):
+        if bf16:
+            t, c = P.bf16_round(t), P.bf16_round(c)
+        gx, gy = -(-w // 8), -(-h // 8)
+        out, gt, gc, _ = _gpu(D, g, t, c, params, (gx + 8, gy + 8, 24), gout)
+        assert np.abs(outs[i] - out).max() <= 1e-6 * P.target_range(t)
+        _close(gts[i], gt, 1e-5)
+        _close(gcs[i], gc, 1e-5)
+    b.upload(D.COLOR_SPACE.RGB, [d[0] for d in data], [d[1] for d in data],
+             [d[2] for d in data])
+    with pytest.raises(D.DtsgbError):  # new inputs: no differentiable solve
+        b.hfbs_backward([d[3] for d in data])
