@@ -1,7 +1,7 @@
 """Benchmark of the DTS / HFBS hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg3|cfg3dts|cfg0|cfg1|cfg2|cfg4]
+                    [--workload cfg3|cfg3dts|cfg0|cfg1|cfg2|cfg4|cfg1grad]
 
 One JSON line on stdout (rank 0).  A step is one pass of the workload's
 solves with inputs already resident in HBM: for DTS the reference's timed
@@ -11,8 +11,10 @@ through the public C ABI with pinned host buffers, the upload and the
 download included (configs 3 and 4: dtsgb_pipeline_run / _run_grad, which
 overlap the copies of one chunk of instances with the solves of another;
 --e2e-chunks).
-Under torchrun every rank solves its own copy of the workload (independent
-instances, no collective): weak scaling.
+Steps are timed with the library's per-kernel profiler off; a second pass of
+the same steps with it on gives the kernel table and the roofline (its events
+slow steps of small kernels).  Under torchrun every rank solves its own copy
+of the workload (independent instances, no collective): weak scaling.
 
 --impl reference times the reference algorithm's CPU restatement (the FP32
 oracle port, all host threads) on a bounded sample of the same workload; the
@@ -751,12 +753,9 @@ def run_ours(args, world, rank, local):
         dev_id = uid if uid.startswith("GPU-") else "GPU-" + uid
     except Exception:
         dev_id = str(local)
-    lib.dtsgb_profile_reset()
-    lib.dtsgb_profile_enable(1)
     for _ in range(max(args.warmup, 3)):
         wl.step()
     torch.cuda.synchronize()
-    lib.dtsgb_profile_reset()
     sampler = ClockSampler(dev_id)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
@@ -776,9 +775,26 @@ def run_ours(args, world, rank, local):
     ms_per_step = total_ms / args.steps
     value = world * wl.pixels / (ms_per_step * 1e-3) / 1e6
 
-    # per-kernel launch durations inside the timed region (CUDA events recorded
-    # on the launching stream by the library; graph replays keep the events of
-    # the latest replay, i.e. the last step)
+    # per-kernel launch durations: the same steps again with the library's
+    # profiler on (CUDA events recorded on the launching stream around every
+    # launch; graph replays keep the events of the latest replay, i.e. the
+    # last step).  The events themselves slow a step of small kernels, so
+    # the profiled pass is timed apart from the steps above and its shares
+    # are of its own step time.
+    lib.dtsgb_profile_enable(1)
+    wl.step()  # captures the profiled graphs
+    torch.cuda.synchronize()
+    lib.dtsgb_profile_reset()
+    pev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    for k in range(args.steps):
+        if flush is not None:
+            flush.zero_()
+        pev[k][0].record(stream)
+        wl.step()
+        pev[k][1].record(stream)
+    torch.cuda.synchronize()
+    prof_ms_per_step = sum(a.elapsed_time(b) for a, b in pev) / args.steps
     per_kernel = {}
     for kid in range(len(KERNEL_NAMES)):
         n, t = ctypes.c_int(), ctypes.c_double()
@@ -796,7 +812,7 @@ def run_ours(args, world, rank, local):
     for kid, (n, t) in per_kernel.items():
         avg = t / n
         rec = {"launches_per_step": n / steps_seen, "avg_launch_ms": avg,
-               "share_of_step": (t / steps_seen) / ms_per_step}
+               "share_of_step": (t / steps_seen) / prof_ms_per_step}
         if kid in algo:
             rec["achieved_gbs"] = algo[kid] / (avg * 1e-3) / 1e9
             rec["frac_of_measured_hbm"] = rec["achieved_gbs"] / peak
@@ -866,6 +882,7 @@ def run_ours(args, world, rank, local):
                      "traffic": traffic, "avg_launch_ms": avg_dom,
                      "algorithmic_bytes_per_launch": algo.get(dom)},
         "kernels": kernels,
+        "profiled_ms_per_step": prof_ms_per_step,
         "gpu_launches": int(round(launches_per_step * args.steps)),
         "clocks": clocks,
     }
