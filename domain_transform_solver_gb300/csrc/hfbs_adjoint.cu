@@ -78,51 +78,71 @@ __global__ void k_hb_slice_scale(const HInst* __restrict__ insts,
 }
 
 // slice^T, pass 2: gz(ix, iy, l) = count * sum over the pixels of cells
-// ix-1..ix, iy-1..iy of sp * (x weight) * (y weight) * (l weight).  One
-// thread per (ix, iy) column gathers in a fixed pixel order into its own
-// level histogram in shared memory (hist[level * 64 + thread]): no atomics,
-// bitwise-reproducible gradients.
-constexpr int kSliceCols = 64;
+// ix-1..ix, iy-1..iy of sp * (x weight) * (y weight) * (l weight).  Four
+// threads per (ix, iy) column, one per source cell, each gathering its
+// cell's pixels in a fixed order (loads issued eight pixels ahead) into its
+// own level histogram in shared memory (hist[level * kGatherThreads +
+// thread]); the column's first thread then adds the four histograms in
+// cell order.  No atomics: bitwise-reproducible gradients.
+constexpr int kGatherCols = 32;
+constexpr int kGatherThreads = 4 * kGatherCols;
 
-__global__ void k_hb_slice_gather(const HInst* __restrict__ insts,
-                                  const uchar4* __restrict__ guide,
-                                  const float* __restrict__ sp,
-                                  const float* __restrict__ count, float* __restrict__ gz,
-                                  HParams p) {
-  extern __shared__ float hist[];  // (gl + 2) x kSliceCols
+__global__ void __launch_bounds__(kGatherThreads)
+    k_hb_slice_gather(const HInst* __restrict__ insts, const uchar4* __restrict__ guide,
+                      const float* __restrict__ sp, const float* __restrict__ count,
+                      float* __restrict__ gz, HParams p) {
+  extern __shared__ float hist[];  // (gl + 2) x kGatherThreads
   const HInst I = insts[blockIdx.y];
-  const int col = blockIdx.x * kSliceCols + threadIdx.x;
-  if (col >= I.gx * I.gy) return;
-  const int iy = col / I.gx, ix = col - iy * I.gx;
+  const int col = blockIdx.x * kGatherCols + (threadIdx.x >> 2), q = threadIdx.x & 3;
+  const bool live = col < I.gx * I.gy;
+  const int iy = live ? col / I.gx : 0, ix = live ? col - iy * I.gx : 0;
   float* hcol = hist + threadIdx.x;
-  for (int l = 0; l < I.gl + 2; ++l) hcol[l * kSliceCols] = 0.f;
-  const int xs = cell_start(max(ix - 1, 0), p.sigma_x, I.w);
-  const int xe = cell_start(ix + 1, p.sigma_x, I.w);
-  const int ys = cell_start(max(iy - 1, 0), p.sigma_y, I.h);
-  const int ye = cell_start(iy + 1, p.sigma_y, I.h);
-  for (int y = ys; y < ye; ++y) {
-    const float fy = (float)y * 1.0f / p.sigma_y;
-    const float y0 = floorf(fy);
-    const float wyy = (int)y0 == iy ? 1.f - (fy - y0) : fy - y0;
-    const long long row = I.pix_off + (long long)y * I.pitch;
-    for (int x = xs; x < xe; ++x) {
-      const float s = sp[row + x];
-      if (s == 0.f) continue;
-      const float fx = (float)x * 1.0f / p.sigma_x;
-      const float x0 = floorf(fx);
-      const float wxx = (int)x0 == ix ? 1.f - (fx - x0) : fx - x0;
-      const float fz = (float)guide[row + x].x * 1.0f / p.sigma_l;
-      const float z0 = floorf(fz);
-      const float wz = fz - z0;
-      const int iz = (int)z0;  // <= gl
-      const float a = s * wxx * wyy;
-      hcol[iz * kSliceCols] += a * (1.f - wz);
-      hcol[(iz + 1) * kSliceCols] += a * wz;
+  for (int l = 0; l < I.gl + 2; ++l) hcol[l * kGatherThreads] = 0.f;
+  const int cx = ix - 1 + (q & 1), cy = iy - 1 + (q >> 1);  // this thread's cell
+  if (live && cx >= 0 && cy >= 0) {
+    const int xs = cell_start(cx, p.sigma_x, I.w), xe = cell_start(cx + 1, p.sigma_x, I.w);
+    const int ys = cell_start(cy, p.sigma_y, I.h), ye = cell_start(cy + 1, p.sigma_y, I.h);
+    const int nx = xe - xs, n = nx * (ye - ys);
+    for (int k0 = 0; k0 < n; k0 += 8) {
+      float sv[8];
+      unsigned char lv[8];
+      int xv[8], yv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = min(k0 + u, n - 1);
+        const int dy = k / nx;
+        yv[u] = ys + dy;
+        xv[u] = xs + (k - dy * nx);
+        const long long pix = I.pix_off + (long long)yv[u] * I.pitch + xv[u];
+        sv[u] = k0 + u < n ? sp[pix] : 0.f;
+        lv[u] = guide[pix].x;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (sv[u] == 0.f) continue;
+        const float fx = (float)xv[u] * 1.0f / p.sigma_x;
+        const float fy = (float)yv[u] * 1.0f / p.sigma_y;
+        const float fx0 = floorf(fx), fy0 = floorf(fy);
+        const float wxx = cx == ix ? 1.f - (fx - fx0) : fx - fx0;
+        const float wyy = cy == iy ? 1.f - (fy - fy0) : fy - fy0;
+        const float fz = (float)lv[u] * 1.0f / p.sigma_l;
+        const float z0 = floorf(fz);
+        const float wz = fz - z0;
+        const int iz = (int)z0;  // <= gl
+        const float a = sv[u] * wxx * wyy;
+        hcol[iz * kGatherThreads] += a * (1.f - wz);
+        hcol[(iz + 1) * kGatherThreads] += a * wz;
+      }
     }
   }
-  for (int l = 0; l < I.gl; ++l) {
-    const long long g = I.grid_off + ((long long)l * I.gy + iy) * I.gx + ix;
-    gz[g] = count[g] * hcol[l * kSliceCols];
+  __syncthreads();
+  if (live && q == 0) {
+    for (int l = 0; l < I.gl; ++l) {
+      const float* r = hcol + l * kGatherThreads;
+      const float v = ((r[0] + r[1]) + r[2]) + r[3];
+      const long long g = I.grid_off + ((long long)l * I.gy + iy) * I.gx + ix;
+      gz[g] = count[g] * v;
+    }
   }
 }
 
@@ -284,12 +304,13 @@ int hfbs_enqueue_backward(const HfbsBatch& B, const HParams& p, const float* gou
   // slice^T: the per-pixel scale goes to an output plane (the last kernel
   // overwrites it)
   k_hb_slice_scale<<<gp, kA, 0, s>>>(B.d_inst, B.guide, B.count, B.ovf, gout, sp, p);
-  const size_t hsmem = sizeof(float) * (size_t)(B.max_gl + 2) * kSliceCols;
+  const size_t hsmem = sizeof(float) * (size_t)(B.max_gl + 2) * kGatherThreads;
   if (hsmem > 48 * 1024)
     DTSGB_CUDA(cudaFuncSetAttribute(k_hb_slice_gather,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsmem));
-  const dim3 gcol((unsigned)((B.max_cells + kSliceCols - 1) / kSliceCols), ni);
-  k_hb_slice_gather<<<gcol, kSliceCols, hsmem, s>>>(B.d_inst, B.guide, sp, B.count, G.gz, p);
+  const dim3 gcol((unsigned)((B.max_cells + kGatherCols - 1) / kGatherCols), ni);
+  k_hb_slice_gather<<<gcol, kGatherThreads, hsmem, s>>>(B.d_inst, B.guide, sp, B.count, G.gz,
+                                                        p);
   const bool tb = hfbs_uses_tb(B);
   // (gg, gw) ping-pong: a launch reads the pair the previous one wrote
   float* pg[2] = {G.gg, G.gg2};

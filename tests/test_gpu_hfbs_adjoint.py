@@ -69,6 +69,8 @@ CASES = [
     (71, 53, dict(BASE, sigma_l=17.0, optim_iter_max=20), (9, 7, 32), "graded"),  # overflow bin stored
     (64, 48, dict(BASE, sigma_l=32.0, optim_iter_max=12), (8, 6, 8), None),  # default confidence
     (40, 24, dict(BASE, optim_iter_max=0), (5, 3, 16), "graded"),  # no heavy-ball step
+    # 32 luma levels: the one-step heavy-ball kernel (FMA neighbour sums)
+    (64, 40, dict(BASE, sigma_l=8.0, optim_iter_max=16), (8, 5, 40), "graded"),
 ]
 
 
@@ -156,6 +158,25 @@ def test_hfbs_checkpoint_segments_agree_bitwise(gpu_ready):
     plain.Optimize()
     ref = plain.Download(D.ImageType.OPTIMIZED_QUANTITY)
     assert np.array_equal(res[0][0], ref)  # the same heavy-ball kernel
+
+
+def test_hfbs_one_step_path_segments_agree_bitwise(gpu_ready):
+    """Grids of more than 16 levels run one heavy-ball step per launch (h in
+    place); checkpointed segments recompute with the same kernel."""
+    D = gpu_ready
+    params = dict(BASE, sigma_l=8.0, optim_iter_max=13)
+    g, t, c, gout = _inputs(45, 64, 40, "graded")
+    res = [_gpu(D, g, t, c, params, (8, 5, 40), gout, segment=s) for s in (1, 3, 5)]
+    for out, gt, gc, _ in res[1:]:
+        assert np.array_equal(out, res[0][0])
+        assert np.array_equal(gt, res[0][1])
+        assert np.array_equal(gc, res[0][2])
+    plain = D.HFBS(D.ImageDim(64, 40), 8, 5, 40)
+    plain.SetFilterParams(D.HFBSGridParams(**params))
+    plain.ClearAll()
+    plain.InitFrame(D.COLOR_SPACE.RGB, g, t, c)
+    plain.Optimize()
+    assert np.array_equal(res[0][0], plain.Download(D.ImageType.OPTIMIZED_QUANTITY))
 
 
 def test_hfbs_automatic_segment_keeps_every_iterate(gpu_ready):
