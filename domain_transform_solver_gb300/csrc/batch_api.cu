@@ -63,8 +63,12 @@ struct dtsgb_batch_s {
   std::vector<long long> soff;
   long long dense = 0;
   long long* d_soff = nullptr;
-  // device copies of caller pointer arrays (3 x n), for the _device calls
+  // device copies of caller pointer arrays (3 x n), for the _device calls,
+  // and the host copy of what each slot holds (a slot is re-sent only when
+  // the caller's pointers change)
   float** d_uptr = nullptr;
+  std::vector<const void*> uptr_host;
+  bool uptr_valid[3] = {false, false, false};
   unsigned char* stage = nullptr;  // dense x (rgba 4 B, target 4 B, conf 4 B)
   Inst* d_inst = nullptr;
   Tile* d_tb = nullptr;
@@ -356,11 +360,25 @@ __global__ void k_user_copy(const Inst* __restrict__ insts, float* const* __rest
 
 // Copies between n caller device images and an arena plane (slot 0..2 of the
 // pointer table, so that up to three such copies can be in flight in order).
+// Send n caller pointers to device slot `slot` unless it already holds them.
+// The copy comes from pageable host memory, so the call may wait for the
+// stream's earlier work; repeated calls with the same buffers skip it.
+int upload_slot(dtsgb_batch_t b, int slot, const void* const* ptrs) {
+  const size_t n = (size_t)b->n;
+  if (b->uptr_host.size() != 3 * n) b->uptr_host.assign(3 * n, nullptr);
+  const void** h = b->uptr_host.data() + slot * n;
+  if (b->uptr_valid[slot] && std::memcmp(h, ptrs, sizeof(void*) * n) == 0) return DTSGB_OK;
+  DTSGB_CUDA(cudaMemcpyAsync(b->d_uptr + slot * n, ptrs, sizeof(void*) * n,
+                             cudaMemcpyHostToDevice, b->stream));
+  std::memcpy(h, ptrs, sizeof(void*) * n);
+  b->uptr_valid[slot] = true;
+  return DTSGB_OK;
+}
+
 int user_plane_copy(dtsgb_batch_t b, float* const* user, float* arena, bool to_arena,
                     int slot) {
   float** d = b->d_uptr + (size_t)slot * b->n;
-  DTSGB_CUDA(cudaMemcpyAsync(d, user, sizeof(float*) * b->n, cudaMemcpyHostToDevice,
-                             b->stream));
+  if (int st = upload_slot(b, slot, reinterpret_cast<const void* const*>(user))) return st;
   const dim3 grid((unsigned)std::min(b->max_h, 512), (unsigned)b->n);
   if (to_arena)
     k_user_copy<true><<<grid, 256, 0, b->stream>>>(b->d_inst, d, arena);
@@ -402,13 +420,11 @@ int device_ingest(dtsgb_batch_t b, int cs, const void* const* rgba,
   std::vector<const void*> cf(n, nullptr);
   if (conf)
     for (size_t i = 0; i < n; ++i) cf[i] = conf[i];
-  if (rgba)
-    DTSGB_CUDA(cudaMemcpyAsync(slots, rgba, sizeof(void*) * n, cudaMemcpyHostToDevice,
-                               b->stream));
-  DTSGB_CUDA(cudaMemcpyAsync(slots + n, target, sizeof(void*) * n, cudaMemcpyHostToDevice,
-                             b->stream));
-  DTSGB_CUDA(cudaMemcpyAsync(slots + 2 * n, cf.data(), sizeof(void*) * n,
-                             cudaMemcpyHostToDevice, b->stream));
+  int st = DTSGB_OK;
+  if (rgba) st = upload_slot(b, 0, rgba);
+  if (!st) st = upload_slot(b, 1, reinterpret_cast<const void* const*>(target));
+  if (!st) st = upload_slot(b, 2, cf.data());
+  if (st) return st;
   // the pointer copies come from pageable host memory: the calls return
   // once the arrays are copied out, so cf may go out of scope
   const dim3 grid((unsigned)std::min(b->max_h, 512), (unsigned)b->n);
@@ -550,6 +566,8 @@ int batch_upload(dtsgb_batch_t b, int cs, const void* const* rgba,
 int hfbs_prepare_grad(dtsgb_batch_t b, int K, long long tv) {
   int S = b->grad_seg_req;
   if (K <= 1) S = 1;
+  if (S <= 0 && b->hgrad_seg == 1 && b->hgcap >= (size_t)(hfbs_grad_planes(K, 1) * tv))
+    S = 1;  // every iterate already held: no memory query
   if (S <= 0) {
     size_t fr = 0, tot = 0;
     DTSGB_CUDA(cudaMemGetInfo(&fr, &tot));
