@@ -33,3 +33,16 @@ def test_error_string_before_any_call(dts):
     assert b"null" in lib.dtsgb_last_error()
     assert lib.dtsgb_hfbs_optimize(None) == _lib.DTSGB_ERR_INVALID_ARGUMENT
     assert lib.dtsgb_dts_create(0, 10, 0, None) == _lib.DTSGB_ERR_INVALID_ARGUMENT
+
+
+def test_gradient_entry_points_reject_null_handles(dts):
+    """The HFBS gradient calls validate their arguments before any CUDA call."""
+    lib = _lib.load()
+    bad = _lib.DTSGB_ERR_INVALID_ARGUMENT
+    assert lib.dtsgb_hfbs_enable_grad(None, 1, 0) == bad
+    assert lib.dtsgb_hfbs_grad_info(None, None, None) == bad
+    assert lib.dtsgb_hfbs_backward(None, None, None, None) == bad
+    assert lib.dtsgb_hfbs_backward_device(None, None, None, None) == bad
+    assert lib.dtsgb_batch_hfbs_backward(None, None, None, None) == bad
+    assert lib.dtsgb_batch_hfbs_backward_device(None, None, None, None) == bad
+    assert lib.dtsgb_batch_hfbs_grad_info(None, None, None) == bad
