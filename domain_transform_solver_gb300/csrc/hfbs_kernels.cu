@@ -447,6 +447,92 @@ __device__ __forceinline__ void cp_async_f32(float* dst, const float* src, bool 
                : "memory");
 }
 
+// a13, up to K bistochastization iterations per pass (temporal blocking as
+// in k_solve_tb): a thread per (x, y) column of a 24 x 24 block keeps its
+// column's v in registers (its counts in shared memory), and v goes through
+// shared memory to the x and y neighbours.  Columns past the grid hold what
+// the one-step kernel reads there: the covered pad faces (x = gx, y = gy,
+// and level gl when covered) the pad value of the iteration's parity (1 on
+// even iterations, 0 on odd ones), everything else 0.  The neighbour order
+// and the arithmetic are k_bistoch's, so the result is bitwise that of the
+// one-step passes.  it0: the global index of the pass's first iteration.
+constexpr size_t kTBBistochSmem = sizeof(float) * 3 * kTBPlane;  // v x 2, count
+// Small grids only: there one-step passes are launch-latency-bound (about
+// 12 us each on GB300 whatever the size) and four iterations per pass win
+// (config 1, 2 x 76,800 voxels: 0.097 against 0.246 ms).  At 11.7 M voxels
+// the one-step kernel's 0.056 ms per iteration beats this kernel's 0.063 (one
+// 576-thread CTA per SM, a division and a square root per voxel and
+// iteration), and batches of a few hundred thousand voxels solved side by
+// side on several streams (the pipeline's chunks) hide the one-step
+// latency, where this kernel's large blocks only crowd the SMs.
+constexpr long long kBistochTBMaxVoxels = 1ll << 18;
+
+__global__ void __launch_bounds__(kTBThreads, 1)
+    k_bistoch_tb(const HInst* __restrict__ insts, const float* __restrict__ src,
+                 float* __restrict__ dst, const float* __restrict__ count, int it0,
+                 int steps) {
+  extern __shared__ float tb_s[];
+  float* Cs = tb_s + 2 * kTBPlane;  // counts of the block's columns
+  const HInst I = insts[blockIdx.y];
+  const int gx = I.gx, gy = I.gy, gl = I.gl;  // gl <= kTBMaxGL (host checks)
+  const int tiles_x = (gx + kTBT - 1) / kTBT;
+  if ((int)blockIdx.x >= tiles_x * ((gy + kTBT - 1) / kTBT)) return;
+  const int ty = blockIdx.x / tiles_x, tx = blockIdx.x - ty * tiles_x;
+  const int c = threadIdx.x, yy = c / kTBL, xx = c - yy * kTBL;
+  const int x = tx * kTBT - kTBK + xx, y = ty * kTBT - kTBK + yy;
+  const bool in = x >= 0 && x < gx && y >= 0 && y < gy;
+  const bool face = (I.cov_x && x == gx && y >= 0 && y < gy) ||
+                    (I.cov_y && y == gy && x >= 0 && x < gx);
+  const int plane = gx * gy, col = in ? y * gx + x : 0;
+  const long long g0 = I.grid_off + col;
+#pragma unroll
+  for (int l = 0; l < kTBMaxGL; ++l) {
+    const bool v = in && l < gl;
+    const long long i = g0 + (v ? (long long)l * plane : 0);
+    cp_async_f32(tb_s + l * kTBThreads + c, src + i, v);
+    cp_async_f32(Cs + l * kTBThreads + c, count + i, v);
+  }
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+  float v[kTBMaxGL];
+#pragma unroll
+  for (int l = 0; l < kTBMaxGL; ++l) v[l] = tb_s[l * kTBThreads + c];
+  for (int k = 1; k <= steps; ++k) {
+    const float pad = ((it0 + k - 1) & 1) ? 0.f : 1.f;
+    const float pz = I.cov_l ? pad : 0.f;
+    float* P = tb_s + (k & 1) * kTBPlane;
+#pragma unroll
+    for (int l = 0; l < kTBMaxGL; ++l)
+      P[l * kTBThreads + c] = in ? v[l] : (face && l < gl ? pad : 0.f);
+    __syncthreads();
+    if (in && tb_active(xx, yy, k)) {
+      float below = 0.f;
+#pragma unroll
+      for (int l = 0; l < kTBMaxGL; ++l) {
+        if (l < gl) {
+          const float* q = P + l * kTBThreads + c;
+          const float vc = v[l];
+          float a = q[-1];
+          a += q[1];
+          a += q[-kTBL];
+          a += q[kTBL];
+          a += below;
+          a += l + 1 < gl ? v[l + 1] : pz;
+          const float blurred = 2.f * vc + a;
+          v[l] = __fsqrt_rn(
+              __fdiv_rn(vc * (Cs[l * kTBThreads + c] + 0.00001f), blurred + 0.00001f));
+          below = vc;
+        }
+      }
+    }
+  }
+  if (in && xx >= kTBK && xx < kTBK + kTBT && yy >= kTBK && yy < kTBK + kTBT) {
+    float* o = dst + g0;
+#pragma unroll
+    for (int l = 0; l < kTBMaxGL; ++l)
+      if (l < gl) o[l * plane] = v[l];
+  }
+}
+
 __global__ void __launch_bounds__(kTBThreads, 1)
     k_solve_tb(const HInst* __restrict__ insts, const float* __restrict__ zs,
                float* __restrict__ zd, const float* __restrict__ hs, float* __restrict__ hd,
@@ -770,12 +856,50 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
       if (p.bistoch_iter_max % 2) std::swap(src, dst);
       continue;
     }
-    for (int it = 0; it < p.bistoch_iter_max; ++it) {
-      prof_begin(s, DTSGB_K_HFBS_BISTOCH);
-      k_bistoch<<<col_grid(g), kT, 0, s>>>(B.d_inst + g.first, src, dst, B.count,
-                                           (it % 2 == 0) ? 1.f : 0.f);
-      prof_end(s, DTSGB_K_HFBS_BISTOCH);
-      std::swap(src, dst);
+    long long gvox = 0;  // the group's voxels
+    for (int i = 0; B.h_inst && i < g.count; ++i) {
+      const HInst& H = B.h_inst[g.first + i];
+      gvox += (long long)H.gx * H.gy * H.gl;
+    }
+    if (hfbs_uses_tb(B) && gvox <= kBistochTBMaxVoxels) {
+      // up to kTBK iterations per pass; one pass split in two when the number
+      // of passes and of iterations differ in parity, so that the result
+      // lands in the buffer the one-step ping-pong leaves it in
+      std::vector<int> plan;
+      for (int r = p.bistoch_iter_max; r > 0; r -= kTBK) plan.push_back(std::min(kTBK, r));
+      if ((int)(plan.size() % 2) != p.bistoch_iter_max % 2) {
+        for (int i = (int)plan.size() - 1; i >= 0; --i)
+          if (plan[i] >= 2) {
+            const int a = plan[i] / 2;
+            plan[i] -= a;
+            plan.insert(plan.begin() + i + 1, a);
+            break;
+          }
+      }
+      long long tiles = 1;
+      for (int i = 0; i < g.count; ++i) {
+        const HInst& H = B.h_inst[g.first + i];
+        tiles = std::max(tiles, (long long)((H.gx + kTBT - 1) / kTBT) * ((H.gy + kTBT - 1) / kTBT));
+      }
+      DTSGB_CUDA(cudaFuncSetAttribute(k_bistoch_tb, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kTBBistochSmem));
+      int it0 = 0;
+      for (int steps : plan) {
+        prof_begin(s, DTSGB_K_HFBS_BISTOCH);
+        k_bistoch_tb<<<dim3((unsigned)tiles, g.count), kTBThreads, kTBBistochSmem, s>>>(
+            B.d_inst + g.first, src, dst, B.count, it0, steps);
+        prof_end(s, DTSGB_K_HFBS_BISTOCH);
+        std::swap(src, dst);
+        it0 += steps;
+      }
+    } else {
+      for (int it = 0; it < p.bistoch_iter_max; ++it) {
+        prof_begin(s, DTSGB_K_HFBS_BISTOCH);
+        k_bistoch<<<col_grid(g), kT, 0, s>>>(B.d_inst + g.first, src, dst, B.count,
+                                             (it % 2 == 0) ? 1.f : 0.f);
+        prof_end(s, DTSGB_K_HFBS_BISTOCH);
+        std::swap(src, dst);
+      }
     }
   }
   float* norm = src;

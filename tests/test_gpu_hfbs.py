@@ -111,3 +111,30 @@ def test_deterministic(gpu_ready):
     a, _ = _run(gpu_ready, u.rgba, u.target, u.confidence, 0, PARAMS, (80, 60, 16))
     b, _ = _run(gpu_ready, u.rgba, u.target, u.confidence, 0, PARAMS, (80, 60, 16))
     assert np.array_equal(a, b)
+
+
+def test_blocked_bistochastization_matches_one_step_passes(gpu_ready):
+    """Small groups bistochastize four iterations per pass, large ones one
+    per pass; both give the same normalisation bit for bit.  The same
+    instance is solved alone (blocked passes) and beside a 2.4 M-voxel
+    instance in one group (one-step passes); its result must not change."""
+    D = gpu_ready
+    rng = np.random.default_rng(5)
+    w, h = 137, 91  # pad faces covered on x and y, luma bins 0..15
+    g = rng.integers(0, 256, (h, w, 4)).astype(np.uint8)
+    t = rng.uniform(-0.5, 0.5, (h, w)).astype(np.float32)
+    c = (rng.random((h, w)) < 0.3).astype(np.float32)
+    big = (4000, 2400)
+    gb = rng.integers(0, 256, (big[1], big[0], 4)).astype(np.uint8)
+    tb = np.zeros((big[1], big[0]), np.float32)
+    params = D.HFBSGridParams(**dict(PARAMS, bistoch_iter_max=11, optim_iter_max=8))
+    outs = []
+    for sizes, gs, ts, cs in (([(w, h)], [g], [t], [c]),
+                              ([(w, h), big], [g, gb], [t, tb], [c, np.ones_like(tb)])):
+        b = D.Batch(sizes)
+        b.set_tuning(D.TUNE_HFBS_GROUP_VOXELS, 0)  # one group
+        b.upload(D.COLOR_SPACE.RGB, gs, ts, cs)
+        b.solve_hfbs(params)
+        outs.append(b.download(1)[0])
+        b.close()
+    assert np.array_equal(outs[0], outs[1], equal_nan=True)
