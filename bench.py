@@ -125,9 +125,11 @@ def _ptrs(arrays):
 # ---- workloads ---------------------------------------------------------------
 class Cfg3:
     """64 ragged instances (W~U[256,1920], H~U[256,1080]), each solved by DTS
-    (config-0 parameters, 10 iterations) and HFBS (config-1 parameters, luma
-    from YCbCr, 64 iterations), BF16 target/confidence storage, FP32 math,
-    one launch per kernel across all instances, CUDA-graph replay."""
+    (the depth super-resolution parameters: sigma 8/8/0.1, lambda 0.99,
+    sigma_z 8, 10 iterations) and HFBS (the colorization parameters: 8x8
+    spatial, sigma_l 16, 64 iterations; luma from YCbCr), BF16
+    target/confidence storage, FP32 math, one launch per kernel across all
+    instances, CUDA-graph replay."""
 
     name = "cfg3_batched_dts_hfbs_64_ragged_bf16"
     dtype = "bf16 storage, f32 math"
@@ -223,9 +225,9 @@ class Cfg3:
 
 
 class Cfg3Dts(Cfg3):
-    """Config 3's DTS solve alone (64 ragged instances, BF16 storage, 10
-    iterations): the batched form of config 0, for the batched versus
-    single-image comparison."""
+    """The 64-instance batch's DTS solve alone (BF16 storage, 10
+    iterations): the batched form of the 640x480 depth super-resolution, for
+    the batched versus single-image comparison."""
 
     name = "cfg3dts_batched_dts_64_ragged_bf16"
 
@@ -264,7 +266,7 @@ class Cfg3Dts(Cfg3):
 
 
 class Cfg0:
-    """DTS depth super-resolution 640x480, FP32, 10 iterations (config 0)."""
+    """DTS depth super-resolution 640x480, FP32, 10 iterations."""
 
     name = "cfg0_dts_depth_superres_640x480"
     dtype = "f32"
@@ -323,7 +325,7 @@ class Cfg0:
 
 class Cfg2:
     """DTS with a given confidence, 1280x384 RGB, Charbonnier, sigma_z 30, 15
-    iterations, BF16 storage of target and confidence (config 2)."""
+    iterations, BF16 storage of target and confidence."""
 
     name = "cfg2_dts_charbonnier_1280x384_bf16"
     dtype = "bf16 storage, f32 math"
@@ -381,7 +383,7 @@ class Cfg2:
 
 
 class Cfg1:
-    """HFBS colorization 640x480, U and V channels, 64 iterations (config 1)."""
+    """HFBS colorization 640x480, U and V channels, 64 iterations."""
 
     name = "cfg1_hfbs_colorization_640x480_uv"
     dtype = "f32"
@@ -442,7 +444,7 @@ class Cfg1:
 
 
 class Cfg1Grad(Cfg1):
-    """Differentiable HFBS: the config-1 colorization (U and V, 640x480, 64
+    """Differentiable HFBS: the 640x480 colorization (U and V, 64
     iterations), FP32, the batched forward keeping every heavy-ball iterate
     (the automatic checkpoint choice) plus the adjoint (dL/dtarget,
     dL/dconfidence) for an N(0,1) upstream gradient, both replayed from CUDA
@@ -525,7 +527,7 @@ class Cfg1Grad(Cfg1):
 
 
 class Cfg4:
-    """Differentiable DTS: 16 x 1024x768 config-0-style instances, FP32,
+    """Differentiable DTS: 16 x 1024x768 depth super-resolution instances, FP32,
     L2, 10 iterations, the forward keeping its iterates (the automatic
     checkpoint choice: every iterate, as 14 planes fit in free memory) plus
     the adjoint (dL/dtarget, dL/dconfidence) for an N(0,1) upstream

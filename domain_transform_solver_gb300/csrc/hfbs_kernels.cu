@@ -459,7 +459,7 @@ __device__ __forceinline__ void cp_async_f32(float* dst, const float* src, bool 
 constexpr size_t kTBBistochSmem = sizeof(float) * 3 * kTBPlane;  // v x 2, count
 // Small grids only: there one-step passes are launch-latency-bound (about
 // 12 us each on GB300 whatever the size) and four iterations per pass win
-// (config 1, 2 x 76,800 voxels: 0.097 against 0.246 ms).  At 11.7 M voxels
+// (a 640x480 colorization's two 80x60x16 grids: 0.097 against 0.246 ms).  At 11.7 M voxels
 // the one-step kernel's 0.056 ms per iteration beats this kernel's 0.063 (one
 // 576-thread CTA per SM, a division and a square root per voxel and
 // iteration), and batches of a few hundred thousand voxels solved side by

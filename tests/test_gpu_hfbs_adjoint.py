@@ -65,7 +65,7 @@ def _close(a, r, tol=TOL_GRAD):
 
 CASES = [
     # (w, h, params, max grid, confidence)
-    (96, 80, dict(BASE), (12, 10, 16), "sparse"),             # config-1 style, 64 steps
+    (96, 80, dict(BASE), (12, 10, 16), "sparse"),             # colorization-style, 64 steps
     (71, 53, dict(BASE, sigma_l=17.0, optim_iter_max=20), (9, 7, 32), "graded"),  # overflow bin stored
     (64, 48, dict(BASE, sigma_l=32.0, optim_iter_max=12), (8, 6, 8), None),  # default confidence
     (40, 24, dict(BASE, optim_iter_max=0), (5, 3, 16), "graded"),  # no heavy-ball step
