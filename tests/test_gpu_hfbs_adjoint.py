@@ -254,3 +254,35 @@ def test_batch_hfbs_backward_matches_single_handles(gpu_ready, bf16):
              [d[2] for d in data])
     with pytest.raises(D.DtsgbError):  # new inputs: no differentiable solve
         b.hfbs_backward([d[3] for d in data])
+
+
+def test_batch_hfbs_backward_device_matches_host(gpu_ready):
+    """dtsgb_batch_hfbs_backward_device (caller device buffers, here torch
+    tensors) returns what the host-pointer call returns, bit for bit, and a
+    null confidence-gradient pointer array is skipped."""
+    torch = pytest.importorskip("torch")
+    D = gpu_ready
+    sizes = [(96, 64), (71, 53)]
+    params = dict(BASE, optim_iter_max=12)
+    data = [_inputs(91 + i, w, h, "graded") for i, (w, h) in enumerate(sizes)]
+    b = D.Batch(sizes)
+    b.enable_grad(True, 0)
+    b.upload(D.COLOR_SPACE.RGB, [d[0] for d in data], [d[1] for d in data],
+             [d[2] for d in data])
+    b.solve_hfbs(D.HFBSGridParams(**params))
+    gts, gcs = b.hfbs_backward([d[3] for d in data])
+    dev = torch.device("cuda:0")
+    go = [torch.tensor(d[3], device=dev) for d in data]
+    gt = [torch.empty_like(g) for g in go]
+    gc = [torch.empty_like(g) for g in go]
+    b.hfbs_backward_device([g.data_ptr() for g in go], [g.data_ptr() for g in gt],
+                           [g.data_ptr() for g in gc])
+    torch.cuda.synchronize()
+    for i in range(2):
+        assert np.array_equal(gt[i].cpu().numpy(), gts[i])
+        assert np.array_equal(gc[i].cpu().numpy(), gcs[i])
+    gt2 = [torch.zeros_like(g) for g in go]
+    b.hfbs_backward_device([g.data_ptr() for g in go], [g.data_ptr() for g in gt2], None)
+    torch.cuda.synchronize()
+    for i in range(2):
+        assert np.array_equal(gt2[i].cpu().numpy(), gts[i])
