@@ -286,3 +286,25 @@ def test_batch_hfbs_backward_device_matches_host(gpu_ready):
     torch.cuda.synchronize()
     for i in range(2):
         assert np.array_equal(gt2[i].cpu().numpy(), gts[i])
+
+
+@pytest.mark.parametrize("w,h,conf,K,segment", [
+    (40, 24, "zero", 12, 0),  # no data term: dL/dtarget = 0, dL/dconfidence is not
+    (1, 1, "graded", 6, 0),   # a one-pixel image, a 1 x 1 x 16 grid
+    (5, 3, "graded", 9, 4),   # a partial cell, segments of 4 steps
+    (17, 9, "graded", 1, 3),  # a single step: the segment request is clamped
+])
+def test_hfbs_adjoint_edge_cases(gpu_ready, oracle_mod, w, h, conf, K, segment):
+    params = dict(BASE, optim_iter_max=K, bistoch_iter_max=7)
+    g, t, c, gout = _inputs(101 + w, w, h, "graded")
+    if conf == "zero":
+        c = np.zeros_like(t)
+    mg = (-(-w // 8) + 1, -(-h // 8) + 1, 17)
+    _, gt, gc, s = _gpu(gpu_ready, g, t, c, params, mg, gout, segment=segment)
+    _, rt, rc, _ = _oracle(oracle_mod, g, t, c, params, mg, gout)
+    if conf == "zero":
+        assert not gt.any() and not rt.any()
+    else:
+        _close(gt, rt)
+    _close(gc, rc)
+    assert s.GradInfo()[0] == (1 if K <= 1 else (segment or 1))
