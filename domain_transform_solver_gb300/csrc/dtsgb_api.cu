@@ -750,6 +750,9 @@ static int hfbs_prepare_grad(dtsgb_hfbs_t h, int K, long long tv) {
   const long long pix = 3 * (long long)h->plane;
   int S = h->grad_seg_req;
   if (K <= 1) S = 1;
+  if (S <= 0 && h->grad_seg == 1 &&
+      h->gbuf_cap >= (size_t)(hfbs_grad_planes(K, 1) * tv + pix))
+    S = 1;  // every iterate already held: no memory query
   if (S <= 0) {
     size_t fr = 0, tot = 0;
     DTSGB_CUDA(cudaMemGetInfo(&fr, &tot));
