@@ -261,6 +261,15 @@ class HFBS {
   void SetStream(void* cuda_stream) {
     detail::on_status(dtsgb_hfbs_set_stream(h_, cuda_stream));
   }
+  // Gradients (an addition: the reference has none; dtsgb_hfbs_enable_grad).
+  // segment 0 chooses the checkpoint segment; Backward maps dL/d(output) of
+  // the last Optimize to dL/dtarget and dL/dconfidence (either may be null).
+  void EnableGrad(bool enable = true, int segment = 0) {
+    detail::on_status(dtsgb_hfbs_enable_grad(h_, enable ? 1 : 0, segment));
+  }
+  void Backward(const float* grad_out, float* grad_target, float* grad_confidence) {
+    detail::on_status(dtsgb_hfbs_backward(h_, grad_out, grad_target, grad_confidence));
+  }
   dtsgb_hfbs_t handle() const { return h_; }
 
  protected:

@@ -89,6 +89,13 @@ int main(int argc, char** argv) {
   const float ms = EdgeAwareOptimize(rgba.data(), target.data(), conf.data(), ho, &hfbs,
                                      hout.data());
   write_all(dir + "/hfbs.bin", hout);
+  // the HFBS adjoint through the facade (an addition): dL/d(output) = target
+  hfbs.EnableGrad(true, 0);
+  hfbs.Optimize();
+  std::vector<float> hgt(n), hgc(n);
+  hfbs.Backward(target.data(), hgt.data(), hgc.data());
+  write_all(dir + "/hfbs_gt.bin", hgt);
+  write_all(dir + "/hfbs_gc.bin", hgc);
   std::printf("facade ok: hfbs solve %.3f ms\n", ms);
   return 0;
 }

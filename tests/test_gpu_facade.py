@@ -66,3 +66,8 @@ def test_cpp_facade_matches_python(gpu_ready, oracle_mod, tmp_path):
     ref = hb.Download(D.ImageType.OPTIMIZED_QUANTITY)
     assert np.array_equal(np.isnan(hf), np.isnan(ref))
     assert np.array_equal(hf[~np.isnan(hf)], ref[~np.isnan(ref)])
+    hb.EnableGrad(True, 0)
+    hb.Optimize()
+    gt, gc = hb.Backward(inst.target)
+    assert np.array_equal(np.fromfile(tmp_path / "hfbs_gt.bin", np.float32).reshape(h, w), gt)
+    assert np.array_equal(np.fromfile(tmp_path / "hfbs_gc.bin", np.float32).reshape(h, w), gc)
