@@ -13,20 +13,26 @@ overlap the copies of one chunk of instances with the solves of another;
 --e2e-chunks).
 Steps are timed with the library's per-kernel profiler off; a second pass of
 the same steps with it on gives the kernel table and the roofline (its events
-slow steps of small kernels).  Under torchrun every rank solves its own copy
-of the workload (independent instances, no collective): weak scaling.
+slow steps of small kernels).  Under torchrun the batched workloads (64
+ragged instances, 16 differentiable instances) are split over the ranks by
+pixel count (sharding.partition_lpt; independent instances, no collective):
+strong scaling.  Single-image workloads run one replica per rank.
 
 --impl reference times the reference algorithm's CPU restatement (the FP32
-oracle port, all host threads) on a bounded sample of the same workload; the
-reference's own CUDA build cannot be built with this toolchain.
+oracle port, all host threads, plus one single-thread sample) on the same
+workload; the reference's own CUDA build cannot be built with this
+toolchain.  That arm never loads the product library: the input generators
+are loaded from their file, not through the package.
 """
 from __future__ import annotations
 
 import argparse
 import ctypes
+import importlib.util
 import json
 import math
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -46,6 +52,7 @@ KERNEL_NAMES = {0: "k_bounds", 1: "k_dts_iter", 2: "k_filter", 3: "k_splat",
                 4: "k_bistoch", 5: "k_solve (HFBS heavy-ball)", 6: "hfbs setup kernels",
                 7: "k_slice", 8: "k_to_float", 9: "k_dts_adjoint",
                 10: "hfbs adjoint (whole backward)"}
+HFBS_TB_STEPS = 4  # heavy-ball steps per launch of the temporally blocked kernel
 
 
 def peaks():
@@ -54,6 +61,46 @@ def peaks():
         d = json.loads(p.read_text())
         return float(d["hbm_gbs"]), "measured"
     return FALLBACK_HBM_GBS, "fallback"
+
+
+_W = None
+
+
+def workloads_module():
+    """domain_transform_solver_gb300/workloads.py loaded from its file: the
+    input generators without the package (whose import loads libdtsgb.so)."""
+    global _W
+    if _W is None:
+        path = ROOT / "domain_transform_solver_gb300" / "workloads.py"
+        spec = importlib.util.spec_from_file_location("dtsgb_bench_workloads", path)
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        _W = mod
+    return _W
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.processor() or platform.machine()
+
+
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
 
 
 # ---- clocks ------------------------------------------------------------------
@@ -122,8 +169,54 @@ def _ptrs(arrays):
     return arr
 
 
+def _check(status):
+    from domain_transform_solver_gb300._lib import check
+    check(status)
+
+
+def _stratified(sizes, k: int) -> list[int]:
+    """Every k-th instance in order of pixel count (a sample with the
+    batch's size distribution and about 1/k of its pixels)."""
+    order = sorted(range(len(sizes)), key=lambda i: (sizes[i][0] * sizes[i][1], i))
+    return sorted(order[k // 2::k]) if k > 1 else list(range(len(sizes)))
+
+
 # ---- workloads ---------------------------------------------------------------
-class Cfg3:
+# Byte models per step, by kernel id (one step's launches together):
+#   pass_model_bytes: the reference's pass model (each pass reads each input
+#     once and writes each output once at the storage format used): DTS
+#     setup 4 + 2*s_dH B/px, per iteration X (read v, t, c, dH; write v) and
+#     Y (read v, dV; write v); HFBS splat (guide, t, c) + 12 B/vx, per
+#     bistochastization step 12 B/vx, invA 16 + blur 48 + init 12 B/vx, per
+#     heavy-ball step 28 B/vx, slice 8 B/px.  Kernels it does not describe
+#     (the iterate initialisation, the adjoints) use the fused contract.
+#   fused_bytes: what the fused kernels here must move at minimum (the DTS
+#     iteration reads v, t, c and the packed bounds once and writes v; the
+#     temporally blocked heavy-ball launch reads z, n, b, invA, h once and
+#     writes h, z for four steps).
+class Batched:
+    """Shared parts of the many-instance workloads."""
+
+    scaling = "strong"
+    reuse_note = "off (every step recomputes all of it)"
+
+    def config(self, world):
+        c = {"workload": self.name, "pixels_per_step": self.total_pixels,
+             "voxels_per_step": self.total_voxels, "iterations": self.iters,
+             "instances": self.n_total,
+             "l2": ("inputs larger than L2" if self.total_pixels * 16 > 2 * (129 << 20)
+                    else "flushed between steps (256 MB write)"),
+             "parallelism": (f"{world} GPUs, instances split by pixel count "
+                             "(longest first to the least loaded)" if world > 1
+                             else "1 GPU"),
+             "guide_state_reuse": self.reuse_note}
+        return c
+
+    def reference_subset(self):
+        return None  # the whole workload per step
+
+
+class Cfg3(Batched):
     """64 ragged instances (W~U[256,1920], H~U[256,1080]), each solved by DTS
     (the depth super-resolution parameters: sigma 8/8/0.1, lambda 0.99,
     sigma_z 8, 10 iterations) and HFBS (the colorization parameters: 8x8
@@ -133,27 +226,43 @@ class Cfg3:
 
     name = "cfg3_batched_dts_hfbs_64_ragged_bf16"
     dtype = "bf16 storage, f32 math"
+    solvers = ("dts", "hfbs")
 
-    def __init__(self, rank: int, scale: float = 1.0, e2e_chunks: int = 16):
-        import domain_transform_solver_gb300 as D
+    def __init__(self, rank: int = 0, world: int = 1, scale: float = 1.0,
+                 e2e_chunks: int = 16):
+        W = workloads_module()
+        self.W = W
         self.e2e_chunks = e2e_chunks
-        from domain_transform_solver_gb300 import workloads as W
-        self.D, self.W = D, W
         # scale < 1 shrinks every instance (profiling captures of a smaller
         # case); the reported workload is scale 1
-        self.insts = W.batched_instances(scale=scale)
         if scale != 1.0:
             self.name = f"{self.name}_scale{scale:g}"
+        all_sizes = [W.scaled_size(w, h, scale) for w, h in W.batched_sizes()]
+        self.n_total = len(all_sizes)
+        if world > 1:
+            from domain_transform_solver_gb300.sharding import partition_lpt
+            share = partition_lpt(all_sizes, world)[rank]
+        else:
+            share = list(range(len(all_sizes)))
+        self.share = share
+        self.insts = W.batched_instances(scale=scale, indices=set(share))
         self.sizes = [(i.width, i.height) for i in self.insts]
         self.pixels = sum(w * h for w, h in self.sizes)
+        self.total_pixels = sum(w * h for w, h in all_sizes)
         self.iters = W.CFG0_OPT["num_iterations"]
         self.hp = dict(W.CFG1_HFBS)
-        self.voxels = sum(math.ceil(np.float32(w) / np.float32(8.0)) *
-                          math.ceil(np.float32(h) / np.float32(8.0)) * 16
-                          for w, h in self.sizes)
+
+        def vox(sz):
+            return sum(math.ceil(np.float32(w) / np.float32(8.0)) *
+                       math.ceil(np.float32(h) / np.float32(8.0)) * 16 for w, h in sz)
+        hf = "hfbs" in self.solvers
+        self.voxels = vox(self.sizes) if hf else 0
+        self.total_voxels = vox(all_sizes) if hf else 0
 
     def setup(self, stream_handle: int):
-        D, W = self.D, self.W
+        import domain_transform_solver_gb300 as D
+        W = self.W
+        self.D = D
         self.b = D.Batch(self.sizes, flags=D.FLAG_BF16_STORAGE)
         # every step solves the same inputs: keeping the guide-derived windows
         # and HFBS normalisation across steps would skip work, so it is off
@@ -179,49 +288,87 @@ class Cfg3:
         self.pipe.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)
         self.e2e_api = f"dtsgb_pipeline_run, {self.pipe.n_chunks} chunks"
 
+    def autotune(self):
+        """The batch's tuning knobs chosen by timing (outside the timed
+        region); returns the chosen values."""
+        D = self.D
+        self.b.autotune(D.DomainFilterParams(**self.W.CFG0_FILTER),
+                        D.DomainOptimizeParams(**self.W.CFG0_OPT),
+                        D.HFBSGridParams(**self.hp) if "hfbs" in self.solvers else None,
+                        reps=2)
+        return self.b.tuning()
+
     def step(self):
-        from domain_transform_solver_gb300._lib import check
-        check(self.lib.dtsgb_batch_solve_dts(self.b.handle, ctypes.byref(self.fp),
-                                             ctypes.byref(self.op), ctypes.c_float(-1.0)))
-        check(self.lib.dtsgb_batch_solve_hfbs(self.b.handle, ctypes.byref(self.hpc)))
+        if "dts" in self.solvers:
+            _check(self.lib.dtsgb_batch_solve_dts(self.b.handle, ctypes.byref(self.fp),
+                                                  ctypes.byref(self.op), ctypes.c_float(-1.0)))
+        if "hfbs" in self.solvers:
+            _check(self.lib.dtsgb_batch_solve_hfbs(self.b.handle, ctypes.byref(self.hpc)))
 
     def step_e2e(self):
-        from domain_transform_solver_gb300._lib import check
-        check(self.lib.dtsgb_pipeline_run(self.pipe.handle, 1, self.h_rgba, self.h_t,
-                                          self.h_c, ctypes.byref(self.fp),
-                                          ctypes.byref(self.op), ctypes.c_float(-1.0),
-                                          ctypes.byref(self.hpc), self.h_o0, self.h_o1))
+        dts, hfbs = "dts" in self.solvers, "hfbs" in self.solvers
+        _check(self.lib.dtsgb_pipeline_run(
+            self.pipe.handle, 1, self.h_rgba, self.h_t, self.h_c,
+            ctypes.byref(self.fp) if dts else None, ctypes.byref(self.op) if dts else None,
+            ctypes.c_float(-1.0), ctypes.byref(self.hpc) if hfbs else None,
+            self.h_o0 if dts else None, self.h_o1 if hfbs else None))
 
     def e2e_bytes(self):
-        return self.pixels * (4 + 4 + 4), self.pixels * 4 * 2
+        return self.pixels * (4 + 4 + 4), self.pixels * 4 * len(self.solvers)
 
-    def algorithmic_bytes(self):
-        """Bytes each launch of a kernel must move at minimum, per kernel id."""
-        px, vx = self.pixels, self.voxels
-        return {
-            0: 8 * px,            # read guide, write packed bounds
-            1: 16 * px,           # read v f32, t bf16, c bf16, bounds; write v f32
-            3: 8 * px + 12 * vx,  # read guide, t, c; write b, sum c, count
-            4: 12 * vx,           # read n, count; write n
-            5: 28 * vx,           # read z, n, b, invA, h; write h, z
-            7: 8 * px,            # read guide, write result (grid reads cached)
-            8: 6 * px,            # read t bf16, write v f32
-        }
+    def fused_bytes(self):
+        px, vx, it = self.pixels, self.voxels, self.iters
+        k = self.hp["optim_iter_max"]
+        b = {}
+        if "dts" in self.solvers:
+            b.update({0: 8 * px,            # read guide, write packed bounds
+                      1: 16 * px * it,      # read v f32, t bf16, c bf16, bounds; write v f32
+                      8: 6 * px})           # read t bf16, write v f32
+        if "hfbs" in self.solvers:
+            b.update({3: 8 * px + 12 * vx,  # read guide, t, c; write b, sum c, count
+                      4: 12 * vx * self.hp["bistoch_iter_max"],
+                      5: 28 * vx * math.ceil(k / HFBS_TB_STEPS),
+                      6: 76 * vx,
+                      7: 8 * px})           # read guide, write result (grid reads cached)
+        return b
 
-    def cpu_sample(self, real="f32"):
-        """A bounded sample: the four smallest instances, DTS + HFBS each."""
+    def pass_model_bytes(self):
+        px, vx, it = self.pixels, self.voxels, self.iters
+        b = {}
+        if "dts" in self.solvers:
+            b.update({0: (4 + 2 * 2) * px,            # guide in, dH and dV (bf16) out
+                      1: (14 + 10) * px * it,         # X: v4 t2 c2 dH2 + v4; Y: v4 dV2 + v4
+                      8: 6 * px})
+        if "hfbs" in self.solvers:
+            b.update({3: 8 * px + 12 * vx, 4: 12 * vx * self.hp["bistoch_iter_max"],
+                      5: 28 * vx * self.hp["optim_iter_max"], 6: 76 * vx, 7: 8 * px})
+        return b
+
+    def cpu_sizes(self):
+        return self.sizes
+
+    def cpu_sample(self, real="f32", subset=None):
+        """The FP32 oracle port over the instances of `subset` (default: all),
+        DTS and/or HFBS each, as the batch solves them."""
         import oracle as O
         W = self.W
-        order = sorted(range(len(self.insts)), key=lambda i: self.sizes[i][0] * self.sizes[i][1])
+        idx = range(len(self.insts)) if subset is None else subset
         px = 0
-        for i in order[:4]:
+        for i in idx:
             inst = self.insts[i]
-            O.dts_solve(inst.rgba, inst.target, inst.confidence, 1, W.CFG0_FILTER,
-                        W.CFG0_OPT, real=real)
-            O.hfbs_solve(inst.rgba, inst.target, inst.confidence, 1, self.hp,
-                         max_grid=(inst.width, inst.height, 64), real=real)
+            if "dts" in self.solvers:
+                O.dts_solve(inst.rgba, inst.target, inst.confidence, 1, W.CFG0_FILTER,
+                            W.CFG0_OPT, real=real)
+            if "hfbs" in self.solvers:
+                O.hfbs_solve(inst.rgba, inst.target, inst.confidence, 1, self.hp,
+                             max_grid=(inst.width, inst.height, 64), real=real)
             px += inst.width * inst.height
-        return px, "4 smallest of the 64 instances, DTS + HFBS each"
+        what = " + ".join(s.upper() for s in self.solvers)
+        if subset is None or len(idx) == len(self.insts):
+            return px, f"all {len(self.insts)} instances, {what} each"
+        return px, (f"{len(idx)} of the {len(self.insts)} instances (every "
+                    f"{max(1, round(len(self.insts) / max(1, len(idx))))}th by pixel "
+                    f"count), {what} each")
 
 
 class Cfg3Dts(Cfg3):
@@ -230,175 +377,138 @@ class Cfg3Dts(Cfg3):
     the batched versus single-image comparison."""
 
     name = "cfg3dts_batched_dts_64_ragged_bf16"
+    solvers = ("dts",)
 
-    def __init__(self, rank: int, scale: float = 1.0, e2e_chunks: int = 16):
-        super().__init__(rank, scale=scale, e2e_chunks=e2e_chunks)
-        self.voxels = 0
-        if scale != 1.0:
-            self.name = f"{Cfg3Dts.name}_scale{scale:g}"
+
+class Single:
+    """Shared parts of the single-image workloads (one replica per rank)."""
+
+    scaling = "weak"
+    n_total = 1
+
+    def config(self, world):
+        return {"workload": self.name, "pixels_per_step": self.pixels,
+                "voxels_per_step": self.voxels, "iterations": self.iters,
+                "l2": "flushed between steps (256 MB write)",
+                "parallelism": (f"{world} independent replicas (a single image does not "
+                                "shard)" if world > 1 else "1 GPU"),
+                "guide_state_reuse": "off (every step recomputes all of it)"}
+
+    @property
+    def total_pixels(self):
+        return self.pixels
+
+    def reference_subset(self):
+        return None
+
+    def cpu_sizes(self):
+        return [(self.inst.width, self.inst.height)]
+
+
+class _DtsSingle(Single):
+    """Single-image DTS through the class API."""
+
+    voxels = 0
+    color_space = 1
+    bf16 = False
+
+    def setup(self, stream_handle: int):
+        import domain_transform_solver_gb300 as D
+        w, h = self.inst.width, self.inst.height
+        self.s = D.DomainTransformSolver(D.ImageDim(w, h),
+                                         flags=D.FLAG_BF16_STORAGE if self.bf16 else 0)
+        self.s.SetStream(stream_handle)
+        self.s.ClearAll()
+        self.s.InitFrame(D.COLOR_SPACE(self.color_space), self.inst.rgba, self.inst.target,
+                         self.inst.confidence)
+        self.fpar = D.DomainFilterParams(**self.filt)
+        self.opar = D.DomainOptimizeParams(**self.opt)
+        self.h_rgba = _pinned_copy(self.inst.rgba)
+        self.h_t = _pinned_copy(self.inst.target)
+        self.h_c = _pinned_copy(self.inst.confidence)
+        self.h_out = _pinned_empty((h, w))
 
     def step(self):
-        from domain_transform_solver_gb300._lib import check
-        check(self.lib.dtsgb_batch_solve_dts(self.b.handle, ctypes.byref(self.fp),
-                                             ctypes.byref(self.op), ctypes.c_float(-1.0)))
+        self.s.ComputeColorSpaceDifferential(self.fpar)
+        self.s.IntegrateColorDifferentials()
+        self.s.Optimize(self.opar)
 
     def step_e2e(self):
-        from domain_transform_solver_gb300._lib import check
-        check(self.lib.dtsgb_pipeline_run(self.pipe.handle, 1, self.h_rgba, self.h_t,
-                                          self.h_c, ctypes.byref(self.fp),
-                                          ctypes.byref(self.op), ctypes.c_float(-1.0), None,
-                                          self.h_o0, None))
+        lib, h = self.s._lib, self.s.handle
+        _check(lib.dtsgb_dts_init_frame(h, self.color_space,
+                                        ctypes.c_void_p(self.h_rgba.ctypes.data),
+                                        ctypes.c_void_p(self.h_t.ctypes.data),
+                                        ctypes.c_void_p(self.h_c.ctypes.data)))
+        self.step()
+        _check(lib.dtsgb_dts_download(h, 5, ctypes.c_void_p(self.h_out.ctypes.data)))
 
     def e2e_bytes(self):
-        return self.pixels * (4 + 4 + 4), self.pixels * 4
+        return self.pixels * 12, self.pixels * 4
 
-    def cpu_sample(self, real="f32"):
+    def fused_bytes(self):
+        px, it, s = self.pixels, self.iters, 2 if self.bf16 else 4
+        return {0: 8 * px, 1: (12 + 2 * s) * px * it, 8: (4 + s) * px}
+
+    def pass_model_bytes(self):
+        px, it, s = self.pixels, self.iters, 2 if self.bf16 else 4
+        return {0: (4 + 2 * s) * px, 1: (16 + 4 * s) * px * it, 8: (4 + s) * px}
+
+    def cpu_sample(self, real="f32", subset=None):
         import oracle as O
-        W = self.W
-        order = sorted(range(len(self.insts)), key=lambda i: self.sizes[i][0] * self.sizes[i][1])
-        px = 0
-        for i in order[:4]:
-            inst = self.insts[i]
-            O.dts_solve(inst.rgba, inst.target, inst.confidence, 1, W.CFG0_FILTER,
-                        W.CFG0_OPT, real=real)
-            px += inst.width * inst.height
-        return px, "4 smallest of the 64 instances, DTS"
+        O.dts_solve(self.inst.rgba, self.inst.target, self.inst.confidence,
+                    self.color_space, self.filt, self.opt, real=real)
+        return self.pixels, "one full solve"
 
 
-class Cfg0:
+class Cfg0(_DtsSingle):
     """DTS depth super-resolution 640x480, FP32, 10 iterations."""
 
     name = "cfg0_dts_depth_superres_640x480"
     dtype = "f32"
 
-    def __init__(self, rank: int):
-        import domain_transform_solver_gb300 as D
-        from domain_transform_solver_gb300 import workloads as W
-        self.D, self.W = D, W
+    def __init__(self, rank: int = 0, world: int = 1):
+        W = workloads_module()
         self.inst = W.depth_sr_instance(W.SEED_BASE)
         self.pixels = self.inst.width * self.inst.height
-        self.iters = W.CFG0_OPT["num_iterations"]
-        self.voxels = 0
-
-    def setup(self, stream_handle: int):
-        D, W = self.D, self.W
-        w, h = self.inst.width, self.inst.height
-        self.s = D.DomainTransformSolver(D.ImageDim(w, h))
-        self.s.SetStream(stream_handle)
-        self.s.ClearAll()
-        self.s.InitFrame(D.COLOR_SPACE.YCbCr, self.inst.rgba, self.inst.target,
-                         self.inst.confidence)
-        self.fp = D.DomainFilterParams(**W.CFG0_FILTER)
-        self.op = D.DomainOptimizeParams(**W.CFG0_OPT)
-        self.h_rgba = _pinned_copy(self.inst.rgba)
-        self.h_t = _pinned_copy(self.inst.target)
-        self.h_c = _pinned_copy(self.inst.confidence)
-        self.h_out = _pinned_empty((h, w))
-
-    def step(self):
-        self.s.ComputeColorSpaceDifferential(self.fp)
-        self.s.IntegrateColorDifferentials()
-        self.s.Optimize(self.op)
-
-    def step_e2e(self):
-        from domain_transform_solver_gb300._lib import check
-        lib, h = self.s._lib, self.s.handle
-        check(lib.dtsgb_dts_init_frame(h, 1, ctypes.c_void_p(self.h_rgba.ctypes.data),
-                                       ctypes.c_void_p(self.h_t.ctypes.data),
-                                       ctypes.c_void_p(self.h_c.ctypes.data)))
-        self.step()
-        check(lib.dtsgb_dts_download(h, 5, ctypes.c_void_p(self.h_out.ctypes.data)))
-
-    def e2e_bytes(self):
-        return self.pixels * 12, self.pixels * 4
-
-    def algorithmic_bytes(self):
-        return {0: 8 * self.pixels, 1: 20 * self.pixels, 8: 8 * self.pixels}
-
-    def cpu_sample(self, real="f32"):
-        import oracle as O
-        W = self.W
-        O.dts_solve(self.inst.rgba, self.inst.target, self.inst.confidence, 1,
-                    W.CFG0_FILTER, W.CFG0_OPT, real=real)
-        return self.pixels, "one full solve"
+        self.filt, self.opt = W.CFG0_FILTER, W.CFG0_OPT
+        self.iters = self.opt["num_iterations"]
 
 
-class Cfg2:
+class Cfg2(_DtsSingle):
     """DTS with a given confidence, 1280x384 RGB, Charbonnier, sigma_z 30, 15
     iterations, BF16 storage of target and confidence."""
 
     name = "cfg2_dts_charbonnier_1280x384_bf16"
     dtype = "bf16 storage, f32 math"
+    color_space = 0
+    bf16 = True
 
-    def __init__(self, rank: int):
-        import domain_transform_solver_gb300 as D
-        from domain_transform_solver_gb300 import workloads as W
-        self.D, self.W = D, W
+    def __init__(self, rank: int = 0, world: int = 1):
+        W = workloads_module()
         self.inst = W.stereo_instance()
         self.pixels = self.inst.width * self.inst.height
-        self.iters = W.CFG2_OPT["num_iterations"]
-        self.voxels = 0
-
-    def setup(self, stream_handle: int):
-        D, W = self.D, self.W
-        w, h = self.inst.width, self.inst.height
-        self.s = D.DomainTransformSolver(D.ImageDim(w, h), flags=D.FLAG_BF16_STORAGE)
-        self.s.SetStream(stream_handle)
-        self.s.ClearAll()
-        self.s.InitFrame(D.COLOR_SPACE.RGB, self.inst.rgba, self.inst.target,
-                         self.inst.confidence)
-        self.fp = D.DomainFilterParams(**W.CFG2_FILTER)
-        self.op = D.DomainOptimizeParams(**W.CFG2_OPT)
-        self.h_rgba = _pinned_copy(self.inst.rgba)
-        self.h_t = _pinned_copy(self.inst.target)
-        self.h_c = _pinned_copy(self.inst.confidence)
-        self.h_out = _pinned_empty((h, w))
-
-    def step(self):
-        self.s.ComputeColorSpaceDifferential(self.fp)
-        self.s.IntegrateColorDifferentials()
-        self.s.Optimize(self.op)
-
-    def step_e2e(self):
-        from domain_transform_solver_gb300._lib import check
-        lib, h = self.s._lib, self.s.handle
-        check(lib.dtsgb_dts_init_frame(h, 0, ctypes.c_void_p(self.h_rgba.ctypes.data),
-                                       ctypes.c_void_p(self.h_t.ctypes.data),
-                                       ctypes.c_void_p(self.h_c.ctypes.data)))
-        self.step()
-        check(lib.dtsgb_dts_download(h, 5, ctypes.c_void_p(self.h_out.ctypes.data)))
-
-    def e2e_bytes(self):
-        return self.pixels * 12, self.pixels * 4
-
-    def algorithmic_bytes(self):
-        return {0: 8 * self.pixels, 1: 16 * self.pixels, 8: 6 * self.pixels}
-
-    def cpu_sample(self, real="f32"):
-        import oracle as O
-        W = self.W
-        O.dts_solve(self.inst.rgba, self.inst.target, self.inst.confidence, 0,
-                    W.CFG2_FILTER, W.CFG2_OPT, real=real)
-        return self.pixels, "one full solve"
+        self.filt, self.opt = W.CFG2_FILTER, W.CFG2_OPT
+        self.iters = self.opt["num_iterations"]
 
 
-class Cfg1:
+class Cfg1(Single):
     """HFBS colorization 640x480, U and V channels, 64 iterations."""
 
     name = "cfg1_hfbs_colorization_640x480_uv"
     dtype = "f32"
 
-    def __init__(self, rank: int):
-        import domain_transform_solver_gb300 as D
-        from domain_transform_solver_gb300 import workloads as W
-        self.D, self.W = D, W
+    def __init__(self, rank: int = 0, world: int = 1):
+        W = workloads_module()
+        self.W = W
         self.u, self.v = W.colorization_instance()
+        self.inst = self.u
         self.pixels = 2 * self.u.width * self.u.height
         self.iters = W.CFG1_HFBS["optim_iter_max"]
         self.voxels = 2 * 80 * 60 * 16
 
     def setup(self, stream_handle: int):
-        D, W = self.D, self.W
+        import domain_transform_solver_gb300 as D
+        W = self.W
         w, h = self.u.width, self.u.height
         self.b = D.Batch([(w, h), (w, h)])
         self.b.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)  # full work every step
@@ -417,24 +527,29 @@ class Cfg1:
         self.h_o = _ptrs([o0, o1])
 
     def step(self):
-        from domain_transform_solver_gb300._lib import check
-        check(self.lib.dtsgb_batch_solve_hfbs(self.b.handle, ctypes.byref(self.hpc)))
+        _check(self.lib.dtsgb_batch_solve_hfbs(self.b.handle, ctypes.byref(self.hpc)))
 
     def step_e2e(self):
-        from domain_transform_solver_gb300._lib import check
         h = self.b.handle
-        check(self.lib.dtsgb_batch_upload(h, 0, self.h_rgba, self.h_t, self.h_c))
+        _check(self.lib.dtsgb_batch_upload(h, 0, self.h_rgba, self.h_t, self.h_c))
         self.step()
-        check(self.lib.dtsgb_batch_download(h, 1, self.h_o))
+        _check(self.lib.dtsgb_batch_download(h, 1, self.h_o))
 
     def e2e_bytes(self):
         return self.pixels * 12, self.pixels * 4
 
-    def algorithmic_bytes(self):
-        px, vx = self.pixels, self.voxels
-        return {3: 12 * px + 12 * vx, 4: 12 * vx, 5: 28 * vx, 7: 8 * px}
+    def fused_bytes(self):
+        px, vx, hp = self.pixels, self.voxels, self.W.CFG1_HFBS
+        return {3: 12 * px + 12 * vx, 4: 12 * vx * hp["bistoch_iter_max"],
+                5: 28 * vx * math.ceil(hp["optim_iter_max"] / HFBS_TB_STEPS), 6: 76 * vx,
+                7: 8 * px}
 
-    def cpu_sample(self, real="f32"):
+    def pass_model_bytes(self):
+        px, vx, hp = self.pixels, self.voxels, self.W.CFG1_HFBS
+        return {3: 12 * px + 12 * vx, 4: 12 * vx * hp["bistoch_iter_max"],
+                5: 28 * vx * hp["optim_iter_max"], 6: 76 * vx, 7: 8 * px}
+
+    def cpu_sample(self, real="f32", subset=None):
         import oracle as O
         W = self.W
         for t in (self.u.target, self.v):
@@ -455,8 +570,8 @@ class Cfg1Grad(Cfg1):
 
     def setup(self, stream_handle: int):
         import torch
+        import domain_transform_solver_gb300 as D
         super().setup(stream_handle)  # the plain batched forward, for the ratio
-        D, W = self.D, self.W
         w, h = self.u.width, self.u.height
         rng = np.random.default_rng(7)
         self.grads = [rng.standard_normal((h, w)).astype(np.float32) for _ in range(2)]
@@ -481,40 +596,41 @@ class Cfg1Grad(Cfg1):
                         "dtsgb_batch_hfbs_backward")
 
     def step(self):
-        from domain_transform_solver_gb300._lib import check
         h = self.gb.handle
-        check(self.lib.dtsgb_batch_solve_hfbs(h, ctypes.byref(self.hpc)))
-        check(self.lib.dtsgb_batch_hfbs_backward_device(h, self.p_g, self.p_gt, self.p_gc))
+        _check(self.lib.dtsgb_batch_solve_hfbs(h, ctypes.byref(self.hpc)))
+        _check(self.lib.dtsgb_batch_hfbs_backward_device(h, self.p_g, self.p_gt, self.p_gc))
 
     def forward_only(self):
         Cfg1.step(self)
 
     def step_e2e(self):
-        from domain_transform_solver_gb300._lib import check
         h = self.gb.handle
-        check(self.lib.dtsgb_batch_upload(h, 0, self.h_rgba, self.h_t, self.h_c))
-        check(self.lib.dtsgb_batch_solve_hfbs(h, ctypes.byref(self.hpc)))
-        check(self.lib.dtsgb_batch_download(h, 1, self.h_o))
-        check(self.lib.dtsgb_batch_hfbs_backward(h, self.h_g, self.h_gt, self.h_gc))
+        _check(self.lib.dtsgb_batch_upload(h, 0, self.h_rgba, self.h_t, self.h_c))
+        _check(self.lib.dtsgb_batch_solve_hfbs(h, ctypes.byref(self.hpc)))
+        _check(self.lib.dtsgb_batch_download(h, 1, self.h_o))
+        _check(self.lib.dtsgb_batch_hfbs_backward(h, self.h_g, self.h_gt, self.h_gc))
 
     def e2e_bytes(self):
         # rgba, target, confidence, upstream gradient in; result, dL/dt, dL/dc out
         return self.pixels * 16, self.pixels * 12
 
-    def algorithmic_bytes(self):
+    def fused_bytes(self):
         px, vx, k = self.pixels, self.voxels, self.iters
-        return {
-            3: 12 * px + 12 * vx,
-            # four heavy-ball steps: read z, h, norm, b, invA; write z, h and
-            # the three kept iterates
-            5: 40 * vx,
-            7: 8 * px,
-            # the whole adjoint: read dL/dout, guide, target, confidence and
-            # write dL/dt, dL/dc per pixel; per step 10 grid reads, 6 writes
-            10: 24 * px + 64 * vx * k,
-        }
+        b = super().fused_bytes()
+        # four heavy-ball steps per launch: read z, h, norm, b, invA; write z,
+        # h and the three kept iterates
+        b[5] = 40 * vx * math.ceil(k / HFBS_TB_STEPS)
+        # the whole adjoint: read dL/dout, guide, target, confidence and
+        # write dL/dt, dL/dc per pixel; per step 10 grid reads, 6 writes
+        b[10] = 24 * px + 64 * vx * k
+        return b
 
-    def cpu_sample(self, real="f32"):
+    def pass_model_bytes(self):
+        b = super().pass_model_bytes()
+        b[10] = self.fused_bytes()[10]  # the model has no adjoint: the fused contract
+        return b
+
+    def cpu_sample(self, real="f32", subset=None):
         import oracle as O
         W = self.W
         o = O.OracleHFBS(self.u.width, self.u.height, 96, 96, 32, real=real)
@@ -522,11 +638,12 @@ class Cfg1Grad(Cfg1):
         o.init_frame(0, self.u.rgba, self.u.target, self.u.confidence)
         o.set_params(**W.CFG1_HFBS)
         o.optimize()
-        o.backward(self.grads[0])
+        rng = np.random.default_rng(7)
+        o.backward(rng.standard_normal((self.u.height, self.u.width)).astype(np.float32))
         return self.pixels // 2, "the U channel, forward + adjoint"
 
 
-class Cfg4:
+class Cfg4(Batched):
     """Differentiable DTS: 16 x 1024x768 depth super-resolution instances, FP32,
     L2, 10 iterations, the forward keeping its iterates (the automatic
     checkpoint choice: every iterate, as 14 planes fit in free memory) plus
@@ -537,20 +654,29 @@ class Cfg4:
     name = "cfg4_dts_fwd_bwd_16x1024x768_f32"
     dtype = "f32"
 
-    def __init__(self, rank: int, e2e_chunks: int = 4):
+    def __init__(self, rank: int = 0, world: int = 1, e2e_chunks: int = 4):
+        W = workloads_module()
+        self.W = W
         self.e2e_chunks = e2e_chunks
-        import domain_transform_solver_gb300 as D
-        from domain_transform_solver_gb300 import workloads as W
-        self.D, self.W = D, W
-        self.insts, self.grads = W.grad_instances()
+        n, w, h = 16, 1024, 768
+        self.n_total = n
+        if world > 1:
+            from domain_transform_solver_gb300.sharding import partition_lpt
+            share = partition_lpt([(w, h)] * n, world)[rank]
+        else:
+            share = list(range(n))
+        self.insts, self.grads = W.grad_instances(indices=share)
         self.sizes = [(i.width, i.height) for i in self.insts]
         self.pixels = sum(w * h for w, h in self.sizes)
+        self.total_pixels = n * w * h
         self.iters = W.CFG0_OPT["num_iterations"]
-        self.voxels = 0
+        self.voxels = self.total_voxels = 0
 
     def setup(self, stream_handle: int):
         import torch
-        D, W = self.D, self.W
+        import domain_transform_solver_gb300 as D
+        W = self.W
+        self.D = D
         self.b = D.Batch(self.sizes)
         self.b.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)  # full work every step
         self.b.set_stream(stream_handle)
@@ -579,63 +705,83 @@ class Cfg4:
         self.h_rgba, self.h_t, self.h_c = _ptrs(self._rgba), _ptrs(self._t), _ptrs(self._c)
         self.h_g, self.h_v = _ptrs(self._g), _ptrs(self._v)
         self.h_gt, self.h_gc = _ptrs(self._ogt), _ptrs(self._ogc)
-        # the plain forward (no checkpoints) of the same batch, for the ratio
         # the host-to-host path: chunks of instances on their own streams
         self.pipe = D.Pipeline(self.sizes, n_chunks=self.e2e_chunks)
         self.pipe.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)
         self.e2e_api = f"dtsgb_pipeline_run_grad, {self.pipe.n_chunks} chunks"
+        # the plain forward (no checkpoints) of the same batch, for the ratio
         self.fwd = D.Batch(self.sizes)
         self.fwd.set_tuning(D.TUNE_REUSE_GUIDE_STATE, 0)
         self.fwd.set_stream(stream_handle)
         self.fwd.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in self.insts],
                         [i.target for i in self.insts], [i.confidence for i in self.insts])
 
+    def autotune(self):
+        D = self.D
+        self.b.autotune(D.DomainFilterParams(**self.W.CFG0_FILTER),
+                        D.DomainOptimizeParams(**self.W.CFG0_OPT), None, reps=2)
+        self.fwd.set_tuning(D.TUNE_DTS_TILE, self.b.get_tuning(D.TUNE_DTS_TILE))
+        return self.b.tuning()
+
     def step(self):
-        from domain_transform_solver_gb300._lib import check
-        check(self.lib.dtsgb_batch_solve_dts(self.b.handle, ctypes.byref(self.fp),
-                                             ctypes.byref(self.op), ctypes.c_float(-1.0)))
-        check(self.lib.dtsgb_batch_dts_backward_device(self.b.handle, self.p_g, self.p_gt,
-                                                       self.p_gc))
+        _check(self.lib.dtsgb_batch_solve_dts(self.b.handle, ctypes.byref(self.fp),
+                                              ctypes.byref(self.op), ctypes.c_float(-1.0)))
+        _check(self.lib.dtsgb_batch_dts_backward_device(self.b.handle, self.p_g, self.p_gt,
+                                                        self.p_gc))
 
     def forward_only(self):
-        from domain_transform_solver_gb300._lib import check
-        check(self.lib.dtsgb_batch_solve_dts(self.fwd.handle, ctypes.byref(self.fp),
-                                             ctypes.byref(self.op), ctypes.c_float(-1.0)))
+        _check(self.lib.dtsgb_batch_solve_dts(self.fwd.handle, ctypes.byref(self.fp),
+                                              ctypes.byref(self.op), ctypes.c_float(-1.0)))
 
     def step_e2e(self):
-        from domain_transform_solver_gb300._lib import check
-        check(self.lib.dtsgb_pipeline_run_grad(self.pipe.handle, 1, self.h_rgba, self.h_t,
-                                               self.h_c, ctypes.byref(self.fp),
-                                               ctypes.byref(self.op), self.h_g, self.h_v,
-                                               self.h_gt, self.h_gc))
+        _check(self.lib.dtsgb_pipeline_run_grad(self.pipe.handle, 1, self.h_rgba, self.h_t,
+                                                self.h_c, ctypes.byref(self.fp),
+                                                ctypes.byref(self.op), self.h_g, self.h_v,
+                                                self.h_gt, self.h_gc))
 
     def e2e_bytes(self):
         # rgba, target, confidence, upstream gradient in; v, dL/dt, dL/dc out
         return self.pixels * 16, self.pixels * 12
 
-    def algorithmic_bytes(self):
-        px = self.pixels
+    def fused_bytes(self):
+        px, it = self.pixels, self.iters
         return {
-            0: 8 * px,   # read guide, write packed bounds
-            1: 20 * px,  # read v, t, c, bounds; write v (f32)
-            8: 8 * px,   # read t, write v
-            9: 40 * px,  # read g, v_k, t, c, bounds; read+write dL/dt, dL/dc; write g
+            0: 8 * px,        # read guide, write packed bounds
+            1: 20 * px * it,  # read v, t, c, bounds; write v (f32)
+            8: 8 * px,        # read t, write v
+            9: 40 * px * it,  # read g, v_k, t, c, bounds; read+write dL/dt, dL/dc; write g
         }
 
-    def cpu_sample(self, real="f32"):
-        """A bounded sample: one instance, forward + adjoint by the FP32 port."""
+    def pass_model_bytes(self):
+        px, it = self.pixels, self.iters
+        b = self.fused_bytes()  # the adjoint and the init: the fused contract
+        b.update({0: 12 * px, 1: 32 * px * it})
+        return b
+
+    def reference_subset(self):
+        return [0, 5, 10, 15]  # 4 of the 16 (identical sizes) keep a step near 3 s
+
+    def cpu_sizes(self):
+        return self.sizes
+
+    def cpu_sample(self, real="f32", subset=None):
+        """The FP32 port: forward + adjoint of the instances of `subset`."""
         import oracle as O
         W = self.W
-        inst, g = self.insts[0], self.grads[0]
-        o = O.OracleDTS(inst.width, inst.height, real=real)
-        o.init_frame(1, inst.rgba, inst.target, inst.confidence)
-        o.differential(W.CFG0_FILTER["sigma_x"], W.CFG0_FILTER["sigma_y"],
-                       W.CFG0_FILTER["sigma_r"])
-        o.integrate()
         op = W.CFG0_OPT
-        o.backward(op["num_iterations"], op["loss"], op["lambda_"], op["sigma_z"],
-                   op["step_size"], g)
-        return inst.width * inst.height, "1 of the 16 instances, forward + adjoint"
+        idx = range(len(self.insts)) if subset is None else subset
+        px = 0
+        for i in idx:
+            inst, g = self.insts[i], self.grads[i]
+            o = O.OracleDTS(inst.width, inst.height, real=real)
+            o.init_frame(1, inst.rgba, inst.target, inst.confidence)
+            o.differential(W.CFG0_FILTER["sigma_x"], W.CFG0_FILTER["sigma_y"],
+                           W.CFG0_FILTER["sigma_r"])
+            o.integrate()
+            o.backward(op["num_iterations"], op["loss"], op["lambda_"], op["sigma_z"],
+                       op["step_size"], g)
+            px += inst.width * inst.height
+        return px, f"{len(idx)} of the {len(self.insts)} instances, forward + adjoint"
 
 
 WORKLOADS = {"cfg3": Cfg3, "cfg3dts": Cfg3Dts, "cfg0": Cfg0, "cfg1": Cfg1, "cfg2": Cfg2,
@@ -643,14 +789,13 @@ WORKLOADS = {"cfg3": Cfg3, "cfg3dts": Cfg3Dts, "cfg0": Cfg0, "cfg1": Cfg1, "cfg2
 
 
 # ---- arms ----------------------------------------------------------------------
-def make_workload(args, rank):
-    if args.workload == "cfg3":
-        return Cfg3(rank, scale=args.scale, e2e_chunks=args.e2e_chunks)
-    if args.workload == "cfg3dts":
-        return Cfg3Dts(rank, scale=args.scale, e2e_chunks=args.e2e_chunks)
+def make_workload(args, rank, world):
+    if args.workload in ("cfg3", "cfg3dts"):
+        return WORKLOADS[args.workload](rank, world, scale=args.scale,
+                                        e2e_chunks=args.e2e_chunks or 16)
     if args.workload == "cfg4":
-        return Cfg4(rank, e2e_chunks=args.e2e_chunks if args.e2e_chunks_set else 4)
-    return WORKLOADS[args.workload](rank)
+        return Cfg4(rank, world, e2e_chunks=args.e2e_chunks or 4)
+    return WORKLOADS[args.workload](rank, world)
 
 
 def dist_setup():
@@ -671,70 +816,116 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(world, value):
+def reduce_over_ranks(world, value, op="max"):
     if world == 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    t = torch.tensor([float(value)], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
     return float(t.item())
 
 
-def cores_used():
-    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-
-
-def cpu_baseline(wl, budget_s=12.0, real="f32"):
-    import oracle as O
-    O.build()
-    wl.cpu_sample(real)  # warm-up (page-in, thread pool)
-    px, t0, n = 0, time.perf_counter(), 0
-    desc = ""
+def _time_cpu(wl, subset, budget_s, min_runs=1):
+    px, n, t0, desc = 0, 0, time.perf_counter(), ""
     while True:
-        p, desc = wl.cpu_sample(real)
+        p, desc = wl.cpu_sample("f32", subset)
         px += p
         n += 1
         el = time.perf_counter() - t0
-        if el >= budget_s or n >= 500:
+        if n >= min_runs and el >= budget_s:
             break
-    return {"value": px / el / 1e6, "unit": "Mpix/s", "cores": cores_used(), "kind": "port",
-            "sample": f"{n} x ({desc}) of {wl.name} by the FP32 oracle port "
-                      f"(OpenMP, {cores_used()} threads), {el:.1f} s"}
+    return px / el / 1e6, n, el, desc
+
+
+def single_thread_sample(wl, s_per_pass_all, threads, budget_s=15.0):
+    """One thread over a sample with the workload's size distribution (every
+    k-th instance by pixel count), k chosen so that the estimated time fits
+    budget_s; s_per_pass_all: seconds of one all-thread pass."""
+    import oracle as O
+    subset = wl.reference_subset()
+    base = list(range(len(wl.cpu_sizes()))) if subset is None else list(subset)
+    est = s_per_pass_all * threads
+    k = max(1, min(len(base), math.ceil(est / budget_s)))
+    sizes = [wl.cpu_sizes()[i] for i in base]
+    single = [base[j] for j in _stratified(sizes, k)]
+    O.set_threads(1)
+    try:
+        v, n, el, desc = _time_cpu(wl, single, 0.0)
+    finally:
+        O.set_threads(0)
+    return {"value": v, "unit": "Mpix/s", "cores": 1, "sample": f"{n} x ({desc}), {el:.1f} s"}
+
+
+def cpu_baseline(wl, budget_s=10.0):
+    """The FP32 oracle port on the host: all threads over the workload (its
+    reference subset for cfg 4), then one thread over a sample."""
+    import oracle as O
+    O.build()
+    threads = O.set_threads(0)
+    subset = wl.reference_subset()
+    wl.cpu_sample("f32", subset)  # warm-up (page-in, thread pool)
+    v_all, n_all, el_all, desc = _time_cpu(wl, subset, budget_s)
+    return {"value": v_all, "unit": "Mpix/s", "cores": threads, "kind": "port",
+            "sample": f"{n_all} x ({desc}) of {wl.name} by the FP32 oracle port "
+                      f"(OpenMP, {threads} threads), {el_all:.1f} s",
+            "single_thread": single_thread_sample(wl, el_all / n_all, threads),
+            "cpu_model": cpu_model(), "nproc": host_threads()}
 
 
 def run_reference(args, world, rank):
+    """The reference algorithm's CPU restatement (the FP32 oracle port) on
+    this host's cores: every timed step solves the workload (cfg 3: all 64
+    instances, DTS + HFBS each) with all threads.  Rank 0 only."""
     if rank != 0:
         return
-    wl = make_workload(args, rank)
+    wl = make_workload(args, 0, 1)
     import oracle as O
     O.build()
-    desc = ""
+    threads = O.set_threads(0)
+    subset = wl.reference_subset()
     for _ in range(args.warmup):
-        wl.cpu_sample()
+        wl.cpu_sample("f32", subset)
     t0 = time.perf_counter()
-    px = 0
+    px, desc = 0, ""
     for _ in range(args.steps):
-        p, desc = wl.cpu_sample()
+        p, desc = wl.cpu_sample("f32", subset)
         px += p
     el = time.perf_counter() - t0
     value = px / el / 1e6
+    single = single_thread_sample(wl, el / args.steps, threads)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpix/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": wl.name, "pixels_per_step": wl.pixels,
-                   "iterations": wl.iters, "sample_per_step": desc},
-        "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": cores_used(),
-                         "kind": "port", "sample": f"{args.steps} x ({desc})"},
+        "scaling": wl.scaling, "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded, shapes of the reference's datasets)",
+        "config": wl.config(world),
+        "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": threads, "kind": "port",
+                         "sample": f"every step: {desc}",
+                         "single_thread": single, "cpu_model": cpu_model(),
+                         "nproc": host_threads()},
         "e2e": {"value": value, "unit": "Mpix/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "note": "the reference's CUDA build cannot be built with this toolchain (empty "
                 "libcua/CUB submodules, CUDA 8/9-era CUB API); its algorithm's CPU "
-                "restatement is timed on all host threads",
+                "restatement (FP32) is timed on the host's threads",
     }
     print(json.dumps(line), flush=True)
+
+
+def _timed_steps(fn, stream, steps, flush):
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for k in range(steps):
+        if flush is not None:
+            flush.zero_()  # L2 flush between steps, outside the step's events
+        ev[k][0].record(stream)
+        fn()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev)
 
 
 def run_ours(args, world, rank, local):
@@ -743,11 +934,12 @@ def run_ours(args, world, rank, local):
     import domain_transform_solver_gb300 as D  # noqa: F401  (loads libdtsgb.so)
     from domain_transform_solver_gb300 import _lib
     lib = _lib.load()
-    wl = make_workload(args, rank)
+    wl = make_workload(args, rank, world)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     wl.setup(stream.cuda_stream)
-    big = wl.pixels * 16 > 2 * (129 << 20)
+    tuning = wl.autotune() if hasattr(wl, "autotune") and not args.no_autotune else None
+    big = wl.total_pixels * 16 > 2 * (129 << 20)
     flush = None if big else torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32,
                                          device="cuda")
     try:
@@ -759,23 +951,15 @@ def run_ours(args, world, rank, local):
         wl.step()
     torch.cuda.synchronize()
     sampler = ClockSampler(dev_id)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
     barrier(world)
     torch.cuda.synchronize()
-    for k in range(args.steps):
-        if flush is not None:
-            flush.zero_()  # L2 flush between steps, outside the step's events
-        ev[k][0].record(stream)
-        wl.step()
-        ev[k][1].record(stream)
-    torch.cuda.synchronize()
+    step_total = _timed_steps(wl.step, stream, args.steps, flush)
     barrier(world)
     clocks = sampler.stop()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = max_over_ranks(world, sum(step_ms))
+    total_ms = reduce_over_ranks(world, step_total, "max")
     ms_per_step = total_ms / args.steps
-    value = world * wl.pixels / (ms_per_step * 1e-3) / 1e6
+    all_pixels = reduce_over_ranks(world, wl.pixels, "sum")
+    value = all_pixels / (ms_per_step * 1e-3) / 1e6
 
     # per-kernel launch durations: the same steps again with the library's
     # profiler on (CUDA events recorded on the launching stream around every
@@ -787,16 +971,7 @@ def run_ours(args, world, rank, local):
     wl.step()  # captures the profiled graphs
     torch.cuda.synchronize()
     lib.dtsgb_profile_reset()
-    pev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    for k in range(args.steps):
-        if flush is not None:
-            flush.zero_()
-        pev[k][0].record(stream)
-        wl.step()
-        pev[k][1].record(stream)
-    torch.cuda.synchronize()
-    prof_ms_per_step = sum(a.elapsed_time(b) for a, b in pev) / args.steps
+    prof_ms_per_step = _timed_steps(wl.step, stream, args.steps, flush) / args.steps
     per_kernel = {}
     for kid in range(len(KERNEL_NAMES)):
         n, t = ctypes.c_int(), ctypes.c_double()
@@ -808,25 +983,57 @@ def run_ours(args, world, rank, local):
     graph_replayed = hasattr(wl, "b")
     steps_seen = 1 if graph_replayed else args.steps
     launches_per_step = sum(n for n, _ in per_kernel.values()) / steps_seen
-    algo = wl.algorithmic_bytes()
+    model, fused = wl.pass_model_bytes(), wl.fused_bytes()
     peak, peak_kind = peaks()
+    traffic_rec = {}
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic_rec = json.loads(tf.read_text()).get(wl.name, {})
     kernels = {}
     for kid, (n, t) in per_kernel.items():
         avg = t / n
-        rec = {"launches_per_step": n / steps_seen, "avg_launch_ms": avg,
+        per_step = n / steps_seen
+        rec = {"launches_per_step": per_step, "avg_launch_ms": avg,
                "share_of_step": (t / steps_seen) / prof_ms_per_step}
-        if kid in algo:
-            rec["achieved_gbs"] = algo[kid] / (avg * 1e-3) / 1e9
-            rec["frac_of_measured_hbm"] = rec["achieved_gbs"] / peak
+        for key, table in (("pass_model", model), ("fused_contract", fused)):
+            if kid in table:
+                gbs = table[kid] / per_step / (avg * 1e-3) / 1e9
+                rec[f"{key}_gbs"] = gbs
+                rec[f"{key}_frac"] = gbs / peak
+        tr = traffic_rec.get(KERNEL_NAMES[kid])
+        if tr:
+            rec["dram_bytes_per_launch"] = tr
+            rec["dram_frac"] = tr / (avg * 1e-3) / 1e9 / peak
         kernels[KERNEL_NAMES[kid]] = rec
     dom = max(per_kernel, key=lambda k: per_kernel[k][1])
     n_dom, t_dom = per_kernel[dom]
     avg_dom = t_dom / n_dom
-    achieved = algo[dom] / (avg_dom * 1e-3) / 1e9 if dom in algo else None
-    traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
-        traffic = json.loads(tf.read_text()).get(wl.name, {}).get(KERNEL_NAMES[dom])
+    per_step_dom = n_dom / steps_seen
+
+    def form(table):
+        if dom not in table:
+            return None
+        b = table[dom] / per_step_dom
+        a = b / (avg_dom * 1e-3) / 1e9
+        return {"bytes_per_launch": b, "achieved": a, "frac": a / peak}
+
+    pm, fc = form(model), form(fused)
+    traffic = traffic_rec.get(KERNEL_NAMES[dom])
+    roofline = {"bound": "hbm", "kernel": KERNEL_NAMES[dom],
+                "achieved": pm["achieved"] if pm else None, "peak": peak, "unit": "GB/s",
+                "frac": pm["frac"] if pm else None,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "traffic": traffic, "avg_launch_ms": avg_dom,
+                "algorithmic_bytes_per_launch": pm["bytes_per_launch"] if pm else None,
+                "byte_model": "pass model of the reference (each pass reads its inputs and "
+                              "writes its outputs once, at the storage format used)",
+                "fused_contract": fc,
+                "dram_measured": ({"bytes_per_launch": traffic,
+                                   "achieved": traffic / (avg_dom * 1e-3) / 1e9,
+                                   "frac": traffic / (avg_dom * 1e-3) / 1e9 / peak,
+                                   "source": "ncu dram__bytes_read.sum + "
+                                             "dram__bytes_write.sum (profiles/traffic.json)"}
+                                  if traffic else None)}
 
     # e2e through the C ABI with pinned host buffers
     for _ in range(2):
@@ -841,48 +1048,33 @@ def run_ours(args, world, rank, local):
         wl.step_e2e()
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = max_over_ranks(world, e0.elapsed_time(e1)) / e_steps
+    e2e_ms = reduce_over_ranks(world, e0.elapsed_time(e1), "max") / e_steps
     h2d, d2h = wl.e2e_bytes()
-    e2e_value = world * wl.pixels / (e2e_ms * 1e-3) / 1e6
+    e2e_value = all_pixels / (e2e_ms * 1e-3) / 1e6
 
     fwd_ratio = None
     if hasattr(wl, "forward_only"):
         for _ in range(3):
             wl.forward_only()
         torch.cuda.synchronize()
-        f_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-                for _ in range(args.steps)]
-        for k in range(args.steps):
-            if flush is not None:
-                flush.zero_()
-            f_ev[k][0].record(stream)
-            wl.forward_only()
-            f_ev[k][1].record(stream)
-        torch.cuda.synchronize()
-        fwd_ms = max_over_ranks(world, sum(a.elapsed_time(b) for a, b in f_ev)) / args.steps
+        fwd_ms = reduce_over_ranks(world, _timed_steps(wl.forward_only, stream, args.steps,
+                                                       flush), "max") / args.steps
         fwd_ratio = {"forward_ms": fwd_ms, "fwd_bwd_ms": ms_per_step,
                      "fwd_bwd_over_forward": ms_per_step / fwd_ms}
 
+    config = wl.config(world)
+    if tuning:
+        config["tuning"] = tuning
     line = {
         "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "higher_is_better": True, "scaling": wl.scaling, "vs_baseline": None,
         "dtype": wl.dtype, "data": "synthetic (seeded, shapes of the reference's datasets)",
-        "config": {"workload": wl.name, "pixels_per_step": wl.pixels,
-                   "voxels_per_step": wl.voxels, "iterations": wl.iters,
-                   "l2": ("inputs larger than L2" if big
-                          else "flushed between steps (256 MB write)"),
-                   "parallelism": f"independent instances x{world} GPUs",
-                   "guide_state_reuse": "off (every step recomputes all of it)"},
+        "config": config,
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
                 **({"api": wl.e2e_api} if hasattr(wl, "e2e_api") else {})},
-        "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": achieved,
-                     "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if achieved else None,
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "traffic": traffic, "avg_launch_ms": avg_dom,
-                     "algorithmic_bytes_per_launch": algo.get(dom)},
+        "roofline": roofline,
         "kernels": kernels,
         "profiled_ms_per_step": prof_ms_per_step,
         "gpu_launches": int(round(launches_per_step * args.steps)),
@@ -890,7 +1082,7 @@ def run_ours(args, world, rank, local):
     }
     if fwd_ratio:
         line["fwd_bwd"] = fwd_ratio
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -907,15 +1099,18 @@ def main():
                     help="cfg3 only: shrink every instance (smaller profiling case)")
     ap.add_argument("--e2e-chunks", type=int, default=None,
                     help="chunks of the overlapped host-to-host e2e run (cfg3: 16, cfg4: 4)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default tuning instead of timing the knobs first")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the CPU baseline leg (profiling runs)")
     args = ap.parse_args()
-    args.e2e_chunks_set = args.e2e_chunks is not None
-    if args.e2e_chunks is None:
-        args.e2e_chunks = 16
-    world, rank, local = dist_setup()
     if args.impl == "reference":
-        run_reference(args, world, rank)
-    else:
-        run_ours(args, world, rank, local)
+        # rank 0 alone times the host CPU; no process group is needed
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        run_reference(args, world, int(os.environ.get("RANK", "0")))
+        return
+    world, rank, local = dist_setup()
+    run_ours(args, world, rank, local)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

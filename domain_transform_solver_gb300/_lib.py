@@ -137,6 +137,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_batch_solve_hfbs": ([vp, P(HfbsParams)], i),
         "dtsgb_batch_download": ([vp, i, pvp], i),
         "dtsgb_batch_download_device": ([vp, i, pvp], i),
+        "dtsgb_batch_debug_plane": ([vp, i, i, vp, ll], i),
         "dtsgb_batch_set_tuning": ([vp, i, ll], i),
         "dtsgb_batch_get_tuning": ([vp, i, P(ll)], i),
         "dtsgb_batch_autotune": ([vp, P(FilterParams), P(OptimizeParams), f,

@@ -1312,6 +1312,36 @@ DTSGB_API int dtsgb_batch_download_device(dtsgb_batch_t b, int which,
   return batch_download(b, which, dst, cudaMemcpyDeviceToDevice);
 }
 
+DTSGB_API int dtsgb_batch_debug_plane(dtsgb_batch_t b, int i, int which, void* dst,
+                                      long long dst_bytes) {
+  if (!b || !dst) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  if (i < 0 || i >= b->n) return fail(DTSGB_ERR_INVALID_ARGUMENT, "instance index");
+  if (which == DTSGB_BATCH_PLANE_BOUNDS) {
+    if (b->dts_res < 0) return fail(DTSGB_ERR_INVALID_ARGUMENT, "no DTS solve yet");
+    const Inst& I = b->inst[i];
+    const size_t wb = (size_t)I.w * 4;
+    if (dst_bytes < (long long)wb * I.h)
+      return fail(DTSGB_ERR_INVALID_ARGUMENT, "dst_bytes smaller than W*H*4");
+    DTSGB_CUDA(cudaMemcpy2DAsync(dst, wb, b->bounds + I.off, (size_t)I.pitch * 4, wb, I.h,
+                                 cudaMemcpyDeviceToHost, b->stream));
+  } else if (which >= DTSGB_BATCH_PLANE_COUNT && which <= DTSGB_BATCH_PLANE_B) {
+    if (!b->hfbs_done || (int)b->hinst.size() != b->n)
+      return fail(DTSGB_ERR_INVALID_ARGUMENT, "no HFBS solve yet");
+    const HInst& H = b->hinst[i];
+    const long long n = (long long)H.gx * H.gy * H.gl;
+    if (dst_bytes < n * 4)
+      return fail(DTSGB_ERR_INVALID_ARGUMENT, "dst_bytes smaller than gx*gy*gl*4");
+    const int g = which == DTSGB_BATCH_PLANE_COUNT ? HG_COUNT
+                  : which == DTSGB_BATCH_PLANE_CSUM ? HG_CSUM : HG_B;
+    DTSGB_CUDA(cudaMemcpyAsync(dst, b->hg[g] + H.grid_off, (size_t)n * 4,
+                               cudaMemcpyDeviceToHost, b->stream));
+  } else {
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "which must be a DTSGB_BATCH_PLANE_* value");
+  }
+  DTSGB_CUDA(cudaStreamSynchronize(b->stream));
+  return DTSGB_OK;
+}
+
 
 // ---------------------------------------------------------------------------
 // Overlapped host-to-host solves: chunks of the instances, each a batch on

@@ -18,7 +18,12 @@
 //    host threads) race on it and must be serialised by the caller.  Nothing
 //    in it needs to start at zero: every element a call reads is written
 //    earlier in the same call;
-//  * no cudaMalloc, cudaFree, stream creation or any allocating routine.
+//  * no cudaMalloc, cudaFree, stream creation or any allocating routine;
+//  * sigma_z below DTSGB_NOALLOC_MAX_SIGMA_Z (the iteration's tile and halo
+//    live in shared memory) and 4-byte aligned buffers;
+//  * the array's address is cached per device ordinal: primary context
+//    only, and not across cudaDeviceReset.
+#include <cstdint>
 #include <mutex>
 
 #include "../../include/dtsgb.h"
@@ -218,6 +223,10 @@ extern "C" DTSGB_API int dtsgb_dts_solve_noalloc(
     return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
   if (output == target || (const void*)output == (const void*)confidence)
     return fail(DTSGB_ERR_INVALID_ARGUMENT, "output must not alias an input");
+  if (((uintptr_t)rgba | (uintptr_t)target | (uintptr_t)confidence | (uintptr_t)output) & 3)
+    return fail(DTSGB_ERR_INVALID_ARGUMENT,
+                "dtsgb_dts_solve_noalloc: rgba, target, confidence and output must be "
+                "4-byte aligned");
   if (width <= 0 || height <= 0)
     return fail(DTSGB_ERR_INVALID_DIMS, "image dims must be positive");
   if ((long long)width * height > kNoAllocMaxPixels)
@@ -234,8 +243,11 @@ extern "C" DTSGB_API int dtsgb_dts_solve_noalloc(
     return fail(DTSGB_ERR_INVALID_ARGUMENT, "invalid loss");
   if (optimize->num_iterations < 0)
     return fail(DTSGB_ERR_INVALID_ARGUMENT, "num_iterations < 0");
-  if (!finite_pos(optimize->sigma_z) || optimize->sigma_z >= 254.f)
-    return fail(DTSGB_ERR_UNSUPPORTED, "sigma_z must be in (0, 254)");
+  if (!finite_pos(optimize->sigma_z) || optimize->sigma_z >= DTSGB_NOALLOC_MAX_SIGMA_Z)
+    return fail(DTSGB_ERR_UNSUPPORTED,
+                "dtsgb_dts_solve_noalloc: sigma_z must be in (0, 97): its iteration tile "
+                "of (32 + 2h) x (64 + 2h) floats, h = floor(sigma_z), must fit in 227 KiB "
+                "of shared memory (the allocating entry points take sigma_z below 254)");
   cudaStream_t s = (cudaStream_t)cuda_stream;
   const long long n = (long long)width * height;
   // RobustLoss::L1 runs no kernel in the reference: the result is the target

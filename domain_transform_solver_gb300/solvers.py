@@ -47,6 +47,9 @@ FLAG_STEREO = 0x8
 TUNE_DTS_TILE = 0
 TUNE_HFBS_GROUP_VOXELS = 1
 TUNE_REUSE_GUIDE_STATE = 2
+# knob -> name, for reports
+TUNE_NAMES = {TUNE_DTS_TILE: "dts_tile", TUNE_HFBS_GROUP_VOXELS: "hfbs_group_voxels",
+              TUNE_REUSE_GUIDE_STATE: "reuse_guide_state"}
 
 
 @dataclass
@@ -502,6 +505,28 @@ class Batch:
         check(self._lib.dtsgb_batch_download(self._h, int(which), _ptr_array(outs)))
         return outs
 
+    def debug_bounds(self, i: int):
+        """Windows of instance i's last DTS solve as absolute indices along
+        each axis: (l_x, u_x, l_y, u_y), the window being (l, u]."""
+        w, h = self.sizes[i]
+        packed = np.empty((h, w), np.uint32)
+        check(self._lib.dtsgb_batch_debug_plane(self._h, int(i), 0, _ptr(packed),
+                                                packed.nbytes))
+        xs = np.arange(w, dtype=np.int32)[None, :]
+        ys = np.arange(h, dtype=np.int32)[:, None]
+        b = packed.astype(np.int64)
+        return (xs - (b & 0xFF)).astype(np.int32), (xs + ((b >> 8) & 0xFF)).astype(np.int32), \
+            (ys - ((b >> 16) & 0xFF)).astype(np.int32), (ys + (b >> 24)).astype(np.int32)
+
+    def debug_grid(self, i: int, which: int, grid_dims):
+        """HFBS grid of instance i's last solve, shape (gl, gy, gx): which 1 =
+        splat counts, 2 = splatted confidences, 3 = splatted c * t."""
+        gx, gy, gl = grid_dims
+        out = np.empty((gl, gy, gx), np.float32)
+        check(self._lib.dtsgb_batch_debug_plane(self._h, int(i), int(which), _ptr(out),
+                                                out.nbytes))
+        return out
+
     # ---- device pointers (integers), e.g. from torch tensors ----------------
     def upload_device(self, color_space: COLOR_SPACE, rgba_ptrs, target_ptrs,
                       confidence_ptrs=None) -> None:
@@ -522,6 +547,10 @@ class Batch:
         v = ctypes.c_longlong()
         check(self._lib.dtsgb_batch_get_tuning(self._h, int(knob), ctypes.byref(v)))
         return v.value
+
+    def tuning(self) -> dict:
+        """Every knob's current value, by name."""
+        return {name: self.get_tuning(k) for k, name in TUNE_NAMES.items()}
 
     def autotune(self, filter_params=None, optimize_params=None, grid_params=None,
                  overwrite_target_above_conf: float = -1, reps: int = 3) -> None:

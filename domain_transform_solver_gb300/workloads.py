@@ -173,22 +173,32 @@ def batched_sizes(seed: int = SEED_BASE + 3, n: int = 64):
     return [(int(a), int(b)) for a, b in zip(ws, hs)]
 
 
-def batched_instances(seed: int = SEED_BASE + 3, n: int = 64, scale: float = 1.0):
-    """cfg 3: n ragged instances (scale < 1 shrinks them for quick tests)."""
+def batched_instances(seed: int = SEED_BASE + 3, n: int = 64, scale: float = 1.0,
+                      indices=None):
+    """cfg 3: n ragged instances (scale < 1 shrinks them for quick tests);
+    indices: generate only these instances of the n (one rank's share)."""
     out = []
     for i, (w, h) in enumerate(batched_sizes(seed, n)):
-        w2, h2 = max(16, int(w * scale)), max(16, int(h * scale))
+        if indices is not None and i not in indices:
+            continue
+        w2, h2 = scaled_size(w, h, scale)
         out.append(depth_sr_instance(seed * 1000 + i, w2, h2, sample_frac=0.05))
     return out
 
 
-def grad_instances(seed: int = SEED_BASE + 4, n: int = 16, w: int = 1024, h: int = 768):
+def scaled_size(w: int, h: int, scale: float):
+    return max(16, int(w * scale)), max(16, int(h * scale))
+
+
+def grad_instances(seed: int = SEED_BASE + 4, n: int = 16, w: int = 1024, h: int = 768,
+                   indices=None):
     """cfg 4: n cfg-0-style instances of w x h (samples every 8 px) and one
-    N(0,1) upstream gradient dL/dv per instance."""
-    insts = [depth_sr_instance(seed * 1000 + i, w, h) for i in range(n)]
+    N(0,1) upstream gradient dL/dv per instance; indices: only these."""
+    keep = range(n) if indices is None else sorted(indices)
+    insts = [depth_sr_instance(seed * 1000 + i, w, h) for i in keep]
     rng = np.random.default_rng(seed)
     grads = [rng.standard_normal((h, w)).astype(np.float32) for _ in range(n)]
-    return insts, grads
+    return insts, [grads[i] for i in keep]
 
 
 # ---- solver parameters of each configuration -------------------------------

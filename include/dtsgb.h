@@ -284,10 +284,26 @@ DTSGB_API int dtsgb_hfbs_backward_device(dtsgb_hfbs_t h, const float* grad_out,
  * stream capture.  All calls on a device share the array and it keeps the
  * previous call's contents; nothing in it needs to start at zero, since a
  * call writes every element it reads before reading it.  Calls that overlap
- * on the GPU race on the array and must be serialised by the caller.  The call allocates nothing: no cudaMalloc,
- * cudaFree, stream creation or allocating library routine.
+ * on the GPU race on the array and must be serialised by the caller.  The
+ * call allocates nothing: no cudaMalloc, cudaFree, stream creation or
+ * allocating library routine.
+ *
+ * Limits beyond the allocating path: sigma_z below DTSGB_NOALLOC_MAX_SIGMA_Z
+ * (97; the iteration keeps its 32x32 tile plus a floor(sigma_z) halo on each
+ * side in shared memory, (32 + 2h) * (64 + 2h) * 4 bytes for h =
+ * floor(sigma_z), which must fit in 227 KiB; the allocating path takes any
+ * sigma_z below 254); rgba, target, confidence and output 4-byte aligned
+ * (DTSGB_ERR_INVALID_ARGUMENT otherwise).  The array's address is looked up
+ * once per device ordinal in the primary context: use the call from the
+ * primary context (the runtime API's default) and not across
+ * cudaDeviceReset.  The window bounds sum the edge weights in float, one by
+ * one, where the allocating path takes exact fixed-point prefix
+ * differences: the two agree except at windows whose sum lies within
+ * rounding of sigma_z, so results match the allocating path within the
+ * parity tolerance rather than bit for bit.
  * ===========================================================================*/
 #define DTSGB_NOALLOC_MAX_PIXELS (1LL << 20)
+#define DTSGB_NOALLOC_MAX_SIGMA_Z 97.0f
 DTSGB_API int dtsgb_dts_solve_noalloc(int width, int height, int color_space,
                                       const void* rgba, const float* target,
                                       const float* confidence,
@@ -342,6 +358,23 @@ DTSGB_API int dtsgb_batch_download(dtsgb_batch_t b, int which,
                                    float* const* dst);
 DTSGB_API int dtsgb_batch_download_device(dtsgb_batch_t b, int which,
                                           float* const* dst);
+/* Intermediate state of instance i after the last solve, for parity checks
+ * (new; the reference's FilterStructPtr() exposes the same state through
+ * its device structs, src/domain_transform_filter.h:64).  which:
+ *   DTSGB_BATCH_PLANE_BOUNDS  W*H uint32 packed window offsets of the last
+ *                             DTS solve (bits 0-7 dl_x, 8-15 du_x, 16-23
+ *                             dl_y, 24-31 du_y; the window along an axis is
+ *                             the pixels p-dl+1 .. p+du)
+ *   DTSGB_BATCH_PLANE_COUNT   gx*gy*gl floats, the HFBS splat counts
+ *   DTSGB_BATCH_PLANE_CSUM    gx*gy*gl floats, the splatted confidences
+ *   DTSGB_BATCH_PLANE_B       gx*gy*gl floats, the splatted c * t
+ * (grids x fastest, then y, then luma).  dst_bytes must cover the plane. */
+#define DTSGB_BATCH_PLANE_BOUNDS 0
+#define DTSGB_BATCH_PLANE_COUNT 1
+#define DTSGB_BATCH_PLANE_CSUM 2
+#define DTSGB_BATCH_PLANE_B 3
+DTSGB_API int dtsgb_batch_debug_plane(dtsgb_batch_t b, int i, int which, void* dst,
+                                      long long dst_bytes);
 
 /* ---- Tuning (new).  DTSGB_TUNE_DTS_TILE: tile width of the fused DTS
  * iteration and its adjoint, 64 (64 x 128 tiles) or 32 (32 x 32 tiles;

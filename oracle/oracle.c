@@ -23,6 +23,17 @@
 
 EXPORT int ora_real_bytes(void) { return (int)sizeof(REAL); }
 
+/* Worker threads of the OpenMP loops (timing of the CPU baseline at one
+ * thread and at all host threads); 0 restores the default. */
+#ifdef _OPENMP
+#include <omp.h>
+EXPORT void ora_set_threads(int n) { omp_set_num_threads(n > 0 ? n : omp_get_num_procs()); }
+EXPORT int ora_get_threads(void) { return omp_get_max_threads(); }
+#else
+EXPORT void ora_set_threads(int n) { (void)n; }
+EXPORT int ora_get_threads(void) { return 1; }
+#endif
+
 /* ======================================================================
  * a1. Colour conversion -- src/color_space.cuh:11-40.
  * The reference evaluates double expressions and converts to unsigned char

@@ -45,6 +45,9 @@ enum { ORA_L1 = 0, ORA_L2 = 1, ORA_CHARBONNIER = 2 };
 enum { ORA_CONTRACT_NONE = 0, ORA_CONTRACT_NVCC = 1 };
 
 int ora_real_bytes(void);
+/* OpenMP worker threads of the loops below (n <= 0: all host threads). */
+void ora_set_threads(int n);
+int ora_get_threads(void);
 
 /* ---- a1: colour conversion of n RGBA pixels (in may equal out). -------- */
 void ora_color_convert(int color_space, int contract, const uint8_t* in,

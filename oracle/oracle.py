@@ -47,6 +47,8 @@ def lib(real: str = "f64") -> ctypes.CDLL:
         vp, i, f, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_int64
         sigs = {
             "ora_real_bytes": ([], i),
+            "ora_set_threads": ([i], None),
+            "ora_get_threads": ([], i),
             "ora_color_convert": ([i, i, vp, vp, ll], None),
             "ora_dts_create": ([i, i], vp),
             "ora_dts_destroy": ([vp], None),
@@ -89,6 +91,14 @@ def lib(real: str = "f64") -> ctypes.CDLL:
             fn.restype = res
         _libs[real] = L
     return _libs[real]
+
+
+def set_threads(n: int) -> int:
+    """OpenMP worker threads of both builds (n <= 0: all host threads);
+    returns the count now in effect."""
+    for real in ("f64", "f32"):
+        lib(real).ora_set_threads(int(n))
+    return lib("f32").ora_get_threads()
 
 
 def _p(a):

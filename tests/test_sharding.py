@@ -66,3 +66,63 @@ def test_two_gloo_ranks_agree_on_placement_and_reductions(world):
         assert mine == parts[rank]
         assert total == allpix
         assert t == max(sum(sizes[i][0] * sizes[i][1] for i in p) for p in parts) * 1e-6
+
+
+def _gather_worker(rank, world, port, q):
+    """Each rank solves its share of a small ragged batch with the FP32
+    oracle port (standing in for the per-rank GPU solve) and rank 0 gathers
+    the results."""
+    import sys
+    from pathlib import Path
+    import torch.distributed as dist
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1] / "oracle"))
+    import oracle as O
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        insts = W.batched_instances(n=7, scale=0.06)
+        seen = []
+
+        def solve(share):
+            seen.extend((i.width, i.height) for i in share)
+            return [O.dts_solve(i.rgba, i.target, i.confidence, 1, W.CFG0_FILTER,
+                                dict(W.CFG0_OPT, num_iterations=3), real="f32")[0]
+                    for i in share]
+
+        out = sharding.solve_sharded(insts, solve)
+        q.put((rank, seen, None if out is None else [o.tobytes() for o in out]))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_partition_solve_gather_on_two_gloo_ranks():
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_gather_worker, args=(r, world, port, q))
+             for r in range(world)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    import oracle as O
+    insts = W.batched_instances(n=7, scale=0.06)
+    sizes = [(i.width, i.height) for i in insts]
+    parts = sharding.partition_lpt(sizes, world)
+    (r0, seen0, out0), (r1, seen1, out1) = res
+    assert out1 is None and out0 is not None
+    assert seen0 == [sizes[i] for i in parts[0]] and seen1 == [sizes[i] for i in parts[1]]
+    for inst, got in zip(insts, out0):
+        ref = O.dts_solve(inst.rgba, inst.target, inst.confidence, 1, W.CFG0_FILTER,
+                          dict(W.CFG0_OPT, num_iterations=3), real="f32")[0]
+        assert got == ref.tobytes()
+
+
+def test_solve_sharded_without_a_process_group_solves_everything():
+    insts = W.batched_instances(n=3, scale=0.05)
+    out = sharding.solve_sharded(insts, lambda share: [i.width * i.height for i in share])
+    assert out == [i.width * i.height for i in insts]
