@@ -160,6 +160,12 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_batch_hfbs_grad_info": ([vp, ctypes.POINTER(i), ctypes.POINTER(i)], i),
         "dtsgb_dts_solve_noalloc": ([i, i, i, vp, vp, vp, P(FilterParams),
                                      P(OptimizeParams), f, vp, vp], i),
+        "dtsgb_soft_create": ([i, P(i), P(i), pvp], i),
+        "dtsgb_soft_destroy": ([vp], i),
+        "dtsgb_soft_set_stream": ([vp, vp], i),
+        "dtsgb_soft_edge_weights": ([vp, i, pvp, P(FilterParams), pvp, pvp], i),
+        "dtsgb_soft_solve": ([vp, pvp, pvp, pvp, pvp, P(OptimizeParams), f, pvp], i),
+        "dtsgb_soft_backward": ([vp, pvp, pvp, pvp, pvp, pvp], i),
         "dtsgb_dts_init_right_frame": ([vp, f, i, vp], i),
         "dtsgb_dts_init_right_frame_device": ([vp, f, i, vp], i),
         "dtsgb_dts_process_right_frame": ([vp], i),

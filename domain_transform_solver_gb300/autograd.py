@@ -5,7 +5,9 @@ dtsgb_batch_dts_backward_device and dtsgb_hfbs_backward_device
 (include/dtsgb.h) that let a PyTorch graph differentiate through the
 fixed-iteration solves with respect to the target and the confidence.  DTS
 window bounds and HFBS bins, counts and normalisation come from the guide
-and are held fixed: the guide gets no gradient.
+and are held fixed: the guide gets no gradient.  The soft-window DTS solve
+(soft_dts_solve, over dtsgb_soft_*) also differentiates with respect to the
+edge weights dH, dV that edge_weights derives from the guide.
 
 Tensors stay on the GPU: the solve reads the caller's device buffers and
 writes its result into a tensor allocated by PyTorch.  The library's launch
@@ -22,9 +24,10 @@ import numpy as np
 import torch
 
 from .solvers import (COLOR_SPACE, HFBS, Batch, DomainFilterParams, DomainOptimizeParams,
-                      HFBSGridParams, ImageDim, ImageType)
+                      HFBSGridParams, ImageDim, ImageType, SoftDTS)
 
-__all__ = ["DtsSolveFunction", "dts_solve", "HfbsSolveFunction", "hfbs_solve"]
+__all__ = ["DtsSolveFunction", "dts_solve", "HfbsSolveFunction", "hfbs_solve",
+           "SoftDtsSolveFunction", "soft_dts_solve", "edge_weights"]
 
 _pool: dict = {}
 _pool_lock = threading.Lock()
@@ -218,3 +221,75 @@ def hfbs_solve(rgba: torch.Tensor, target: torch.Tensor, confidence: torch.Tenso
     gp = grid_params or HFBSGridParams()
     return HfbsSolveFunction.apply(target, confidence, rgba, gp, color_space, segment,
                                    max_grid)
+
+
+def edge_weights(rgba: torch.Tensor, filter_params: DomainFilterParams | None = None,
+                 color_space: COLOR_SPACE = COLOR_SPACE.YCbCr):
+    """The guide-derived edge weights (dH, dV), each [B,H,W] float32, as
+    ComputeColorSpaceDifferential computes them (not differentiable: the
+    guide is integer)."""
+    if not rgba.is_cuda or rgba.dtype != torch.uint8 or rgba.shape[-1] != 4:
+        raise ValueError("rgba must be a CUDA uint8 [B,H,W,4] tensor")
+    B, H, W = rgba.shape[:3]
+    g = rgba.contiguous()
+    dh = torch.empty((B, H, W), dtype=torch.float32, device=rgba.device)
+    dv = torch.empty_like(dh)
+    s = SoftDTS([(W, H)] * B)
+    cur = torch.cuda.current_stream(rgba.device)
+    s.set_stream(cur.cuda_stream)
+    s.edge_weights(color_space, _ptrs(g), filter_params or DomainFilterParams(), _ptrs(dh),
+                   _ptrs(dv))
+    s.close()
+    return dh, dv
+
+
+class SoftDtsSolveFunction(torch.autograd.Function):
+    """v = soft-window DTS(dH, dV; target, confidence) for a batch of
+    equal-size images, differentiable in all four inputs.
+
+    forward(dH, dV, target, confidence [B,H,W] f32, optimize_params, tau)
+    -> [B,H,W] f32
+    """
+
+    @staticmethod
+    def forward(ctx, dh, dv, target, confidence, optimize_params, tau=1.0):
+        ts = (dh, dv, target, confidence)
+        if not all(x.is_cuda and x.dtype == torch.float32 for x in ts):
+            raise ValueError("SoftDtsSolveFunction wants CUDA float32 tensors")
+        if not all(x.shape == target.shape for x in ts) or target.dim() != 3:
+            raise ValueError("dH, dV, target and confidence must share one [B,H,W] shape")
+        B, H, W = target.shape
+        dh, dv, t, c = (x.contiguous() for x in ts)
+        s = SoftDTS([(W, H)] * B)
+        cur = torch.cuda.current_stream(t.device)
+        s.set_stream(cur.cuda_stream)
+        out = torch.empty_like(t)
+        s.solve(_ptrs(dh), _ptrs(dv), _ptrs(t), _ptrs(c), optimize_params, float(tau),
+                _ptrs(out))
+        ctx.soft = s
+        ctx.keep = (dh, dv, t, c)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        s = ctx.soft
+        go = grad_out.contiguous().float()
+        grads = [torch.empty_like(go) if need else None for need in ctx.needs_input_grad[:4]]
+        s.set_stream(torch.cuda.current_stream(go.device).cuda_stream)
+        s.backward(_ptrs(go), *[None if g is None else _ptrs(g) for g in grads[2:]],
+                   *[None if g is None else _ptrs(g) for g in grads[:2]])
+        s.close()
+        ctx.soft = ctx.keep = None
+        return (*grads, None, None)
+
+
+def soft_dts_solve(dh: torch.Tensor, dv: torch.Tensor, target: torch.Tensor,
+                   confidence: torch.Tensor,
+                   optimize_params: DomainOptimizeParams | None = None,
+                   tau: float = 1.0) -> torch.Tensor:
+    """Differentiable soft-window DTS Optimize: windows with fractional ends
+    of width tau (transformed-domain units) around the reference's
+    threshold sigma_z, so that the result has gradients with respect to the
+    edge weights dH, dV as well as the target and the confidence."""
+    op = optimize_params or DomainOptimizeParams()
+    return SoftDtsSolveFunction.apply(dh, dv, target, confidence, op, tau)

@@ -21,20 +21,6 @@ namespace dtsgb {
 namespace {
 
 constexpr int kThreads = 256;
-// kINV255Sq, src/domain_transform_common_kernels.cuh:10 (a float constant).
-__device__ __constant__ float c_inv255sq = (float)0.0000153787;
-
-// dH / dV integrand of src/domain_transform_common_kernels.cuh:71-116:
-// sqrt(SSD4(a-b) * kINV255Sq * r * r + 1) with r = sigma_{x|y} / sigma_r,
-// evaluated in the order nvcc compiles the reference expression.
-__device__ __forceinline__ float edge_weight(uchar4 a, uchar4 b, float ratio) {
-  const int d0 = (int)a.x - (int)b.x, d1 = (int)a.y - (int)b.y;
-  const int d2 = (int)a.z - (int)b.z, d3 = (int)a.w - (int)b.w;
-  const float ssd = (float)(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3);
-  float t = __fmul_rn(ssd, c_inv255sq);
-  t = __fmul_rn(t, ratio);
-  return __fsqrt_rn(__fmaf_rn(t, ratio, 1.0f));
-}
 
 __global__ void k_color_convert_flat(uchar4* __restrict__ g, long long n,
                                      int cs) {

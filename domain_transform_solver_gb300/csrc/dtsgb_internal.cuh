@@ -36,6 +36,20 @@ __host__ __device__ inline uint32_t pack_bounds(int dlx, int dux, int dly,
          ((uint32_t)duy << 24);
 }
 
+// dH / dV integrand of src/domain_transform_common_kernels.cuh:71-116
+// (Uchar4SumOfSquaredDiffNormalize inside Compute_dHdx / Compute_dVdy):
+// sqrt(SSD4(a - b) * kINV255Sq * r * r + 1) with r = sigma_{x|y} / sigma_r
+// and kINV255Sq the float constant 0.0000153787 (:10), evaluated in the
+// order nvcc compiles the reference expression.  >= 1 for every input.
+__device__ __forceinline__ float edge_weight(uchar4 a, uchar4 b, float ratio) {
+  const int d0 = (int)a.x - (int)b.x, d1 = (int)a.y - (int)b.y;
+  const int d2 = (int)a.z - (int)b.z, d3 = (int)a.w - (int)b.w;
+  const float ssd = (float)(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3);
+  float t = __fmul_rn(ssd, (float)0.0000153787);
+  t = __fmul_rn(t, ratio);
+  return __fsqrt_rn(__fmaf_rn(t, ratio, 1.0f));
+}
+
 // Storage types for target / confidence.
 enum class Storage : int { F32 = 0, BF16 = 1 };
 

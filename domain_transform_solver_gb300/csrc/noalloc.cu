@@ -44,16 +44,6 @@ constexpr int kMaxDevices = 64;
 void* g_scratch_addr[kMaxDevices] = {};
 std::mutex g_scratch_mu;
 
-__device__ __forceinline__ float na_edge(uchar4 a, uchar4 b, float ratio) {
-  // src/domain_transform_common_kernels.cuh:71-116
-  const int d0 = (int)a.x - (int)b.x, d1 = (int)a.y - (int)b.y;
-  const int d2 = (int)a.z - (int)b.z, d3 = (int)a.w - (int)b.w;
-  const float ssd = (float)(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3);
-  float t = __fmul_rn(ssd, (float)0.0000153787);
-  t = __fmul_rn(t, ratio);
-  return __fsqrt_rn(__fmaf_rn(t, ratio, 1.0f));
-}
-
 __device__ __forceinline__ uchar4 na_guide(const uchar4* g, int W, int x, int y,
                                            int cs) {
   return convert_pixel(g[(long long)y * W + x], cs);
@@ -80,7 +70,7 @@ __global__ void __launch_bounds__(kNaThreads)
     const int x = x0 - r + 1 + c, y = y0 + rr;
     float w = 0.f;
     if (x >= 0 && x < W && y < H)
-      w = na_edge(na_guide(guide, W, x, y, cs),
+      w = edge_weight(na_guide(guide, W, x, y, cs),
                   x > 0 ? na_guide(guide, W, x - 1, y, cs) : zero, ratio_x);
     sH[i] = w;
   }
@@ -89,7 +79,7 @@ __global__ void __launch_bounds__(kNaThreads)
     const int x = x0 + c, y = y0 - r + 1 + rr;
     float w = 0.f;
     if (x < W && y >= 0 && y < H)
-      w = na_edge(na_guide(guide, W, x, y, cs),
+      w = edge_weight(na_guide(guide, W, x, y, cs),
                   y > 0 ? na_guide(guide, W, x, y - 1, cs) : zero, ratio_y);
     sV[i] = w;
   }

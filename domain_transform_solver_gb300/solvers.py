@@ -34,7 +34,7 @@ __all__ = [
     "ImageDim", "ImageType", "COLOR_SPACE", "RobustLoss", "DomainFilterParams",
     "DomainFilterParamsVec1", "DomainOptimizeParams", "HFBSGridParams",
     "DomainTransformFilter", "DomainTransformSolver", "HFBS", "DtsOptions",
-    "HfbsOptions", "Solve", "EdgeAwareOptimize", "DtsgbError",
+    "HfbsOptions", "Solve", "EdgeAwareOptimize", "DtsgbError", "SoftDTS",
     "FLAG_BF16_STORAGE", "FLAG_FIX_Y_LIMIT", "TUNE_DTS_TILE", "TUNE_HFBS_GROUP_VOXELS",
     "TUNE_REUSE_GUIDE_STATE",
     "Batch", "Pipeline", "DomainTransformStereo",
@@ -774,3 +774,58 @@ def EdgeAwareOptimize(rgba_image, target_image, confidence, options, solver):
     Solve(options, confidence is None, solver)
     out = solver.Download(ImageType.OPTIMIZED_QUANTITY)
     return out, (time.perf_counter() - t0) * 1e3
+
+
+class SoftDTS:
+    """Soft-window DTS over device buffers (no reference counterpart): the
+    Optimize iteration with fractional window ends of width tau, so that the
+    result is differentiable in the edge weights dH, dV (the reference's
+    integer windows make that gradient zero almost everywhere).  Arguments
+    are lists of device pointers (ints), one per instance, as in
+    include/dtsgb.h's dtsgb_soft_* calls."""
+
+    def __init__(self, sizes):
+        self._lib = _lib.load()
+        self.sizes = [(int(w), int(h)) for w, h in sizes]
+        n = len(self.sizes)
+        ws = (ctypes.c_int * n)(*[w for w, _ in self.sizes])
+        hs = (ctypes.c_int * n)(*[h for _, h in self.sizes])
+        s = ctypes.c_void_p()
+        check(self._lib.dtsgb_soft_create(n, ws, hs, ctypes.byref(s)))
+        self._h = s
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.dtsgb_soft_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        check(self._lib.dtsgb_soft_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
+
+    def edge_weights(self, color_space, rgba_ptrs, filter_params, dh_ptrs, dv_ptrs) -> None:
+        check(self._lib.dtsgb_soft_edge_weights(self._h, int(color_space),
+                                                _vp_array(rgba_ptrs),
+                                                ctypes.byref(filter_params._c()),
+                                                _vp_array(dh_ptrs), _vp_array(dv_ptrs)))
+
+    def solve(self, dh_ptrs, dv_ptrs, target_ptrs, confidence_ptrs, optimize_params,
+              tau: float, out_ptrs) -> None:
+        conf = None if confidence_ptrs is None else _vp_array(confidence_ptrs)
+        check(self._lib.dtsgb_soft_solve(self._h, _vp_array(dh_ptrs), _vp_array(dv_ptrs),
+                                         _vp_array(target_ptrs), conf,
+                                         ctypes.byref(optimize_params._c()), float(tau),
+                                         _vp_array(out_ptrs)))
+
+    def backward(self, grad_out_ptrs, grad_t_ptrs=None, grad_c_ptrs=None, grad_dh_ptrs=None,
+                 grad_dv_ptrs=None) -> None:
+        def arr(p):
+            return None if p is None else _vp_array(p)
+        check(self._lib.dtsgb_soft_backward(self._h, _vp_array(grad_out_ptrs),
+                                            arr(grad_t_ptrs), arr(grad_c_ptrs),
+                                            arr(grad_dh_ptrs), arr(grad_dv_ptrs)))

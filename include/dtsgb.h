@@ -265,6 +265,57 @@ DTSGB_API int dtsgb_hfbs_backward_device(dtsgb_hfbs_t h, const float* grad_out,
                                          float* grad_target, float* grad_confidence);
 
 /* ===========================================================================
+ * Soft-window DTS: gradients with respect to the edge weights (new; no
+ * reference counterpart).
+ *
+ * The reference's windows are integer (LinearSearchLowerAndUpperBound2DX,
+ * src/domain_transform_filter.cuh:7-28): a pixel q belongs to p's window when
+ * the transformed distance D_pq (the sum of the edge weights dH / dV,
+ * Compute_dHdx / Compute_dVdy, src/domain_transform_common_kernels.cuh:81-116,
+ * between them) is at most sigma_z.  The result is therefore piecewise
+ * constant in the edge weights and their gradient is zero almost everywhere.
+ * This mode relaxes membership to the weight ramp((sigma_z - D_pq) / tau),
+ * ramp(x) = clamp(x + 1/2, 0, 1) -- fractional window ends of width tau in
+ * transformed-domain units -- and solves the Optimize iteration
+ * (src/domain_transform_solver.cuh:12-116) with the weighted box mean and
+ * the summed weights as n.  tau -> 0 gives the integer windows clipped at the
+ * image borders; unlike the reference, windows are clipped (not collapsed to
+ * one side) at the borders and the Y window runs to the image height.
+ *
+ * A handle holds n instances (dense W*H rows).  All image arguments are
+ * host arrays of n DEVICE pointers (W*H floats, or W*H*4 bytes of RGBA);
+ * calls are asynchronous on the handle's stream except where noted.
+ * ===========================================================================*/
+typedef struct dtsgb_soft_s* dtsgb_soft_t;
+DTSGB_API int dtsgb_soft_create(int n, const int* widths, const int* heights,
+                                dtsgb_soft_t* out);
+DTSGB_API int dtsgb_soft_destroy(dtsgb_soft_t s);
+DTSGB_API int dtsgb_soft_set_stream(dtsgb_soft_t s, void* cuda_stream);
+/* The guide-derived edge weights dH, dV of ComputeColorSpaceDifferential
+ * (filter.cu:92-110; colour conversion as InitFrame) for the filter sigmas,
+ * written to dH[i], dV[i]; synchronises. */
+DTSGB_API int dtsgb_soft_edge_weights(dtsgb_soft_t s, int color_space,
+                                      const void* const* rgba,
+                                      const dtsgb_filter_params* filter,
+                                      float* const* dH, float* const* dV);
+/* Soft-window Optimize from given edge weights (finite, > 0; the guide's
+ * are >= 1), target and confidence (NULL: ones) into out.  Keeps every
+ * iterate for dtsgb_soft_backward.  tau in (0, 2 sigma_z]; L1 and zero
+ * iterations return the target.  No confidence overwrite. */
+DTSGB_API int dtsgb_soft_solve(dtsgb_soft_t s, const float* const* dH,
+                               const float* const* dV, const float* const* target,
+                               const float* const* confidence,
+                               const dtsgb_optimize_params* optimize, float tau,
+                               float* const* out);
+/* Adjoint of the last dtsgb_soft_solve: dL/dtarget, dL/dconfidence, dL/ddH,
+ * dL/ddV for the upstream gradient dL/dout (any output array may be NULL);
+ * synchronises. */
+DTSGB_API int dtsgb_soft_backward(dtsgb_soft_t s, const float* const* grad_out,
+                                  float* const* grad_target,
+                                  float* const* grad_confidence,
+                                  float* const* grad_dH, float* const* grad_dV);
+
+/* ===========================================================================
  * Allocation-free DTS solve (no counterpart in the reference).
  *
  * For callers that cannot call cudaMalloc: code that runs inside a CUDA-graph

@@ -1358,3 +1358,181 @@ EXPORT void ora_hfbs_grid(const ora_hfbs* s, int which, REAL* dst) {
   if (which < 0 || which >= ORA_G_COUNT || !s->grids[which]) return;
   memcpy(dst, s->grids[which], (size_t)s->gx * s->gy * s->gl * sizeof(REAL));
 }
+
+/* ======================================================================
+ * Soft-window DTS: the project's relaxation of the reference's integer
+ * windows (src/domain_transform_filter.cuh:7-28), for gradients with
+ * respect to the edge weights dH / dV (Compute_dHdx / Compute_dVdy,
+ * src/domain_transform_common_kernels.cuh:81-116).  Along a line the
+ * transformed distance D_pq is the sum of the edge weights over
+ * (min(p,q), max(p,q)] and q weighs w_pq = ramp((sigma - D_pq) / tau),
+ * ramp(x) = clamp(x + 1/2, 0, 1), in p's window (clipped at the line ends,
+ * the Y window running to the height).  The iteration is
+ * src/domain_transform_solver.cuh:12-116 with B = sum w v / n, n = sum w.
+ * The adjoint here scatters each window pair's derivative onto the edge
+ * weights between the pair, pair by pair.
+ * ====================================================================== */
+static REAL soft_ramp(REAL x) {
+  const REAL r = x + (REAL)0.5;
+  return r < 0 ? 0 : (r > 1 ? 1 : r);
+}
+
+typedef struct {
+  int i, L;
+  size_t st, base;
+} soft_line;
+
+static soft_line soft_line_of(int W, int H, int axis, size_t k) {
+  const int y = (int)(k / (size_t)W), x = (int)(k - (size_t)y * W);
+  soft_line l;
+  if (axis == 0) {
+    l.i = x; l.L = W; l.st = 1; l.base = (size_t)y * W;
+  } else {
+    l.i = y; l.L = H; l.st = (size_t)W; l.base = (size_t)x;
+  }
+  return l;
+}
+
+/* n and sum w*val over pixel k's soft window */
+static void soft_window_sum(const soft_line* l, const REAL* e, const REAL* val, REAL sigma,
+                            REAL tau, REAL* n_out, REAL* s_out) {
+  const REAL wc = soft_ramp(sigma / tau), stop = sigma + tau / 2;
+  REAL n = wc, S = wc * val[l->base + l->i * l->st], D = 0;
+  for (int q = l->i + 1; q < l->L; ++q) {
+    D += e[l->base + q * l->st];
+    if (!(D < stop)) break;
+    const REAL w = soft_ramp((sigma - D) / tau);
+    n += w;
+    S += w * val[l->base + q * l->st];
+  }
+  D = 0;
+  for (int q = l->i - 1; q >= 0; --q) {
+    D += e[l->base + (q + 1) * l->st];
+    if (!(D < stop)) break;
+    const REAL w = soft_ramp((sigma - D) / tau);
+    n += w;
+    S += w * val[l->base + q * l->st];
+  }
+  *n_out = n;
+  *s_out = S;
+}
+
+static void soft_data(int loss, REAL v, REAL t, REAL c, REAL n, REAL* h, REAL* hd, REAL* hc) {
+  const REAL d = v - t, eps = (REAL)0.000001;
+  if (loss == ORA_L2) {
+    *h = c / n * d;
+    *hd = c / n;
+    *hc = d / n;
+  } else {
+    const REAL r = R_SQRT(d * d + eps);
+    *h = (REAL)0.5 * (c / n) * d / r;
+    *hd = (REAL)0.5 * (c / n) * eps / (r * r * r);
+    *hc = (REAL)0.5 * d / (n * r);
+  }
+}
+
+static void soft_half(int W, int H, int axis, const REAL* e, const REAL* vin, REAL* vout,
+                      const REAL* t, const REAL* c, int data, int loss, REAL lam,
+                      REAL sigma, REAL step, REAL tau) {
+  const size_t N = (size_t)W * H;
+#pragma omp parallel for schedule(static)
+  for (size_t k = 0; k < N; ++k) {
+    const soft_line l = soft_line_of(W, H, axis, k);
+    REAL n, S, h = 0, hd, hc;
+    soft_window_sum(&l, e, vin, sigma, tau, &n, &S);
+    if (data) soft_data(loss, vin[k], t[k], c ? c[k] : 1, n, &h, &hd, &hc);
+    vout[k] = vin[k] - step * (lam * (vin[k] - S / n) + h);
+  }
+}
+
+/* adjoint of one half-step: a = dL/dvout -> ain = dL/dvin, ge += dL/de,
+ * gt / gc += the data term's (X only) */
+static void soft_half_adjoint(int W, int H, int axis, const REAL* e, const REAL* vin,
+                              const REAL* t, const REAL* c, int data, int loss, REAL lam,
+                              REAL sigma, REAL step, REAL tau, const REAL* a, REAL* ain,
+                              REAL* ge, REAL* gt, REAL* gc) {
+  const size_t N = (size_t)W * H;
+  const REAL stop = sigma + tau / 2;
+  for (size_t k = 0; k < N; ++k) ain[k] = 0;
+  for (size_t k = 0; k < N; ++k) {
+    const soft_line l = soft_line_of(W, H, axis, k);
+    REAL n, S, h = 0, hd = 0, hc = 0;
+    soft_window_sum(&l, e, vin, sigma, tau, &n, &S);
+    const REAL B = S / n;
+    if (data) {
+      soft_data(loss, vin[k], t[k], c ? c[k] : 1, n, &h, &hd, &hc);
+      gt[k] += a[k] * step * hd;
+      gc[k] -= a[k] * step * hc;
+    }
+    ain[k] += a[k] * (1 - step * lam - step * hd);
+    const REAL coef = a[k] * step / n;
+    ain[k] += coef * lam * soft_ramp(sigma / tau);
+    for (int dir = -1; dir <= 1; dir += 2) {
+      REAL D = 0;
+      for (int q = l.i + dir; q >= 0 && q < l.L; q += dir) {
+        const int jnew = dir > 0 ? q : q + 1;  /* the edge weight D just took */
+        D += e[l.base + jnew * l.st];
+        if (!(D < stop)) break;
+        const REAL x = (sigma - D) / tau;
+        const size_t kq = l.base + q * l.st;
+        ain[kq] += coef * lam * soft_ramp(x);
+        if (x > (REAL)-0.5 && x < (REAL)0.5) {
+          /* dL/dw_pq times dw/dD = -1/tau, onto every edge weight of D */
+          const REAL gD = -coef * (lam * (vin[kq] - B) + h) / tau;
+          const int lo = dir > 0 ? l.i + 1 : q + 1, hi = dir > 0 ? q : l.i;
+          for (int j = lo; j <= hi; ++j) ge[l.base + j * l.st] += gD;
+        }
+      }
+    }
+  }
+}
+
+EXPORT void ora_soft_solve(int W, int H, const REAL* eh, const REAL* ev, const REAL* t,
+                           const REAL* c, int num_iterations, int loss, float lambda,
+                           float sigma_z, float step, float tau, REAL* out) {
+  const size_t N = (size_t)W * H;
+  const int iters = loss == ORA_L1 ? 0 : num_iterations;
+  REAL* v = ora_alloc_real(N);
+  REAL* u = ora_alloc_real(N);
+  memcpy(v, t, N * sizeof(REAL));
+  for (int it = 0; it < iters; ++it) {
+    soft_half(W, H, 0, eh, v, u, t, c, 1, loss, lambda, sigma_z, step, tau);
+    soft_half(W, H, 1, ev, u, v, NULL, NULL, 0, loss, lambda, sigma_z, step, tau);
+  }
+  memcpy(out, v, N * sizeof(REAL));
+  free(v);
+  free(u);
+}
+
+EXPORT void ora_soft_backward(int W, int H, const REAL* eh, const REAL* ev, const REAL* t,
+                              const REAL* c, int num_iterations, int loss, float lambda,
+                              float sigma_z, float step, float tau, const REAL* grad_out,
+                              REAL* grad_t, REAL* grad_c, REAL* grad_eh, REAL* grad_ev) {
+  const size_t N = (size_t)W * H;
+  const int iters = loss == ORA_L1 ? 0 : num_iterations;
+  REAL* vs = ora_alloc_real(N * (size_t)(iters + 1));
+  REAL* u = ora_alloc_real(N);
+  REAL* a = ora_alloc_real(N);
+  REAL* b = ora_alloc_real(N);
+  memcpy(vs, t, N * sizeof(REAL));
+  for (int it = 0; it < iters; ++it) {
+    soft_half(W, H, 0, eh, vs + N * it, u, t, c, 1, loss, lambda, sigma_z, step, tau);
+    soft_half(W, H, 1, ev, u, vs + N * (it + 1), NULL, NULL, 0, loss, lambda, sigma_z, step,
+              tau);
+  }
+  for (size_t k = 0; k < N; ++k) grad_t[k] = grad_c[k] = grad_eh[k] = grad_ev[k] = 0;
+  memcpy(a, grad_out, N * sizeof(REAL));
+  for (int it = iters - 1; it >= 0; --it) {
+    const REAL* v = vs + N * it;
+    soft_half(W, H, 0, eh, v, u, t, c, 1, loss, lambda, sigma_z, step, tau);
+    soft_half_adjoint(W, H, 1, ev, u, NULL, NULL, 0, loss, lambda, sigma_z, step, tau, a, b,
+                      grad_ev, NULL, NULL);
+    soft_half_adjoint(W, H, 0, eh, v, t, c, 1, loss, lambda, sigma_z, step, tau, b, a,
+                      grad_eh, grad_t, grad_c);
+  }
+  for (size_t k = 0; k < N; ++k) grad_t[k] += a[k];
+  free(vs);
+  free(u);
+  free(a);
+  free(b);
+}

@@ -104,6 +104,17 @@ void ora_dts_add_bounds_override(ora_dts* s, int axis, float sigma,
                                  const int32_t* l, const int32_t* u);
 void ora_dts_clear_bounds_override(ora_dts* s);
 
+/* ---- Soft-window DTS (the project's relaxation of the integer windows for
+ * gradients with respect to the edge weights; see oracle.c).  eh / ev: the
+ * edge weights dH / dV (W*H), c may be NULL (ones).  -------------------- */
+void ora_soft_solve(int w, int h, const REAL* eh, const REAL* ev, const REAL* t,
+                    const REAL* c, int num_iterations, int loss, float lambda,
+                    float sigma_z, float step, float tau, REAL* out);
+void ora_soft_backward(int w, int h, const REAL* eh, const REAL* ev, const REAL* t,
+                       const REAL* c, int num_iterations, int loss, float lambda,
+                       float sigma_z, float step, float tau, const REAL* grad_out,
+                       REAL* grad_t, REAL* grad_c, REAL* grad_eh, REAL* grad_ev);
+
 /* ---- HFBS: mirror of class HFBS (src/hfbs.h:99-150). -------------------- */
 typedef struct {
   float sigma_x, sigma_y, sigma_l, lambda, alpha, beta;

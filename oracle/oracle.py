@@ -70,6 +70,9 @@ def lib(real: str = "f64") -> ctypes.CDLL:
             "ora_dts_bounds": ([vp, i, f, vp, vp, vp], None),
             "ora_dts_add_bounds_override": ([vp, i, f, vp, vp], None),
             "ora_dts_clear_bounds_override": ([vp], None),
+            "ora_soft_solve": ([i, i, vp, vp, vp, vp, i, i, f, f, f, f, vp], None),
+            "ora_soft_backward": ([i, i, vp, vp, vp, vp, i, i, f, f, f, f, vp, vp, vp, vp,
+                                   vp], None),
             "ora_hfbs_create": ([i, i, i, i, i], vp),
             "ora_hfbs_destroy": ([vp], None),
             "ora_hfbs_set_compat": ([vp, i], None),
@@ -297,6 +300,50 @@ class OracleHFBS:
         self.L.ora_hfbs_grid(self.h, GRID_NAMES.index(which) if isinstance(which, str)
                              else which, _p(out))
         return out
+
+
+# ---- soft-window DTS ---------------------------------------------------------
+def soft_solve(eh, ev, t, c, opt, tau, real="f64"):
+    """Soft-window Optimize from edge weights eh / ev (HxW), target t and
+    confidence c (None: ones); opt as DomainOptimizeParams fields."""
+    dt = _dtype(real)
+    eh, ev, t = (np.ascontiguousarray(a, dt) for a in (eh, ev, t))
+    c = None if c is None else np.ascontiguousarray(c, dt)
+    h, w = t.shape
+    out = np.empty((h, w), dt)
+    lib(real).ora_soft_solve(w, h, _p(eh), _p(ev), _p(t), _p(c), opt["num_iterations"],
+                             int(opt["loss"]), opt["lambda_"], opt["sigma_z"],
+                             opt["step_size"], tau, _p(out))
+    return out
+
+
+def soft_backward(eh, ev, t, c, opt, tau, grad_out, real="f64"):
+    """(dL/dt, dL/dc, dL/deh, dL/dev) of soft_solve for dL/dout."""
+    dt = _dtype(real)
+    eh, ev, t, g = (np.ascontiguousarray(a, dt) for a in (eh, ev, t, grad_out))
+    c = None if c is None else np.ascontiguousarray(c, dt)
+    h, w = t.shape
+    outs = [np.empty((h, w), dt) for _ in range(4)]
+    lib(real).ora_soft_backward(w, h, _p(eh), _p(ev), _p(t), _p(c), opt["num_iterations"],
+                                int(opt["loss"]), opt["lambda_"], opt["sigma_z"],
+                                opt["step_size"], tau, _p(g), *[_p(o) for o in outs])
+    return tuple(outs)
+
+
+def edge_weights(rgba, color_space, sigma_x, sigma_y, sigma_r, real="f64"):
+    """dH, dV of the guide as ComputeColorSpaceDifferential computes them
+    (through the DTS mirror's DIFFERENTIAL path)."""
+    h, w = rgba.shape[:2]
+    o = OracleDTS(w, h, real=real)
+    o.init_frame(color_space, rgba)
+    o.differential(sigma_x, sigma_y, sigma_r)
+    dh = o.download(1)
+    # dV: the same weights of the transposed guide along its rows
+    ot = OracleDTS(h, w, real=real)
+    ot.init_frame(color_space, np.ascontiguousarray(np.transpose(rgba, (1, 0, 2))))
+    ot.differential(sigma_y, sigma_x, sigma_r)
+    dv = np.ascontiguousarray(ot.download(1).T)
+    return dh, dv
 
 
 # ---- whole-solve conveniences ----------------------------------------------

@@ -102,22 +102,23 @@ def test_noalloc_variants_match_the_allocating_entry_point(gpu_ready, loss, iter
 
 
 def test_noalloc_against_the_fp64_oracle(gpu_ready, oracle_mod):
-    """An instance whose every window decision lies clear of its threshold
-    (no near-ties), so each window the float sums choose must be the
-    oracle's: the output is held to max-abs 1e-4 x range against the FP64
-    oracle on the oracle's own windows."""
+    """An instance whose every window decision lies at least 2.7e-4 from its
+    threshold (a margin some hundred times the FP32 rounding of a window
+    sum), so each window the float sums choose must be the oracle's: the
+    output is held to max-abs 1e-4 x range against the FP64 oracle on the
+    oracle's own windows."""
     D = gpu_ready
     from domain_transform_solver_gb300 import workloads as W
     lib = _lib(D)
-    inst = W.depth_sr_instance(931, 150, 110, n_poly=8, sample_frac=0.2)
+    inst = W.depth_sr_instance(1048, 120, 90, n_poly=8, sample_frac=0.2)
     f, sz = W.CFG0_FILTER, W.CFG0_OPT["sigma_z"]
-    o = oracle_mod.OracleDTS(150, 110)
+    o = oracle_mod.OracleDTS(120, 90)
     o.init_frame(1, inst.rgba, inst.target, inst.confidence)
     o.differential(f["sigma_x"], f["sigma_y"], f["sigma_r"])
     o.integrate()
     for axis in (0, 1):
         _, _, margin = o.bounds(axis, sz)
-        assert np.abs(margin).min() > P.TIE_REL * (sz + 1.0)
+        assert np.abs(margin).min() > 3e-5 * (sz + 1.0)
     for loss, overwrite, use_conf in ((1, -1.0, True), (2, 0.5, True), (1, -1.0, False)):
         opt = dict(W.CFG0_OPT, loss=loss, num_iterations=8)
         o.init_frame(1, inst.rgba, inst.target, inst.confidence if use_conf else None)
