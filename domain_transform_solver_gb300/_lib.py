@@ -122,6 +122,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_hfbs_grad_info": ([vp, ctypes.POINTER(i), ctypes.POINTER(i)], i),
         "dtsgb_hfbs_backward": ([vp, vp, vp, vp], i),
         "dtsgb_hfbs_backward_device": ([vp, vp, vp, vp], i),
+        "dtsgb_wait_timeouts": ([P(ctypes.c_ulonglong)], i),
         "dtsgb_profile_enable": ([i], i),
         "dtsgb_profile_reset": ([], i),
         "dtsgb_profile_read": ([i, P(i), P(ctypes.c_double)], i),
@@ -176,6 +177,14 @@ def _declare(lib: ctypes.CDLL) -> None:
             continue
         fn.argtypes = args
         fn.restype = res
+
+
+def wait_timeouts() -> int:
+    """Thread blocks that gave up waiting for an asynchronous tile copy since
+    the library was loaded (dtsgb_wait_timeouts); 0 on a healthy run."""
+    n = ctypes.c_ulonglong()
+    check(load().dtsgb_wait_timeouts(ctypes.byref(n)))
+    return n.value
 
 
 def check(status: int, allow_warning: bool = False) -> int:

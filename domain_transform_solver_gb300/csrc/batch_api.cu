@@ -19,6 +19,7 @@
 #include "color.cuh"
 #include "dtsgb_internal.cuh"
 #include "hfbs_internal.cuh"
+#include "tma.cuh"
 
 using namespace dtsgb;
 
@@ -78,6 +79,7 @@ struct dtsgb_batch_s {
   int ntb = 0, nti = 0, nti_big = 0, nti_small = 0;
   bool small = false;
   long long hfbs_group_voxels = 0;  // L2-resident HFBS group budget (0: off)
+  int hfbs_solve_steps = 4;         // heavy-ball steps per launch (4 or 1)
   // Guide-derived state kept across solves while the guide is unchanged
   // (video frames that change only the target): the DTS window bounds and
   // the HFBS bistochastized normalisation.
@@ -126,6 +128,9 @@ struct dtsgb_batch_s {
   HfbsBatch hB{};            // that solve's batch description and parameters
   HParams hhp{};
   Graph g_hbwd;
+
+  // tensor maps of the iterate planes (TMA staging of the iteration)
+  TmaCache tma;
 
   size_t tsize() const { return st == Storage::F32 ? 4 : 2; }
 };
@@ -821,7 +826,15 @@ DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b, const dtsgb_filter_params* 
   const bool iterate = p->loss != DTSGB_L1 && p->num_iterations > 0;
   const DtsLaunch Lb{b->d_inst, b->d_tb, b->ntb, b->n};
   const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n, b->small, b->d_ti_small,
-                     b->nti_small};
+                     b->nti_small, &b->tma, b->inst.data()};
+  // the iterate planes' tensor maps exist before any capture (a capture
+  // cannot build them: the kernels would stage by loads)
+  {
+    int bw = 0, bh = 0;
+    dts_iter_tma_box(Li, halo, halo, &bw, &bh);
+    if (bw > 0)
+      for (float* v : b->v) (void)b->tma.get(b->inst.data(), b->n, v, bw, bh, b->stream);
+  }
   const bool over = overwrite > 0.f && overwrite < 1.f;
   const int n_kept = iterate ? p->num_iterations : 0;
   b->grad_n = -1;
@@ -1086,6 +1099,7 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
   B.keep_debug = false;
   B.h_inst = b->hinst.data();
   B.group_voxels = b->hfbs_group_voxels;
+  B.solve_steps = b->hfbs_solve_steps;
   // the bistochastized normalisation depends only on the guide's bins
   const dtsgb_batch_s::NormKey nk{b->guide_gen, p->sigma_x, p->sigma_y, p->sigma_l,
                                   p->bistoch_iter_max};
@@ -1100,6 +1114,7 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
   std::vector<char> key;
   key_append(key, hp);
   key_append(key, b->hfbs_group_voxels);
+  key_append(key, b->hfbs_solve_steps);
   key_append(key, B.reuse_norm);
   key_append(key, b->grad ? b->hgbuf : nullptr);  // the kept iterates' arena
   key_append(key, b->grad ? b->hgrad_seg : 0);
@@ -1209,6 +1224,13 @@ DTSGB_API int dtsgb_batch_set_tuning(dtsgb_batch_t b, int knob, long long value)
     b->reuse = value != 0;
     return DTSGB_OK;
   }
+  if (knob == DTSGB_TUNE_HFBS_SOLVE_STEPS) {
+    if (value != 1 && value != kHfbsTBSteps)
+      return fail(DTSGB_ERR_INVALID_ARGUMENT, "HFBS steps per launch must be 1 or 4");
+    if (value != b->hfbs_solve_steps) b->hgrad_ready = false;  // kept iterates' arithmetic
+    b->hfbs_solve_steps = (int)value;
+    return DTSGB_OK;
+  }
   return fail(DTSGB_ERR_INVALID_ARGUMENT, "unknown tuning knob");
 }
 
@@ -1224,6 +1246,10 @@ DTSGB_API int dtsgb_batch_get_tuning(dtsgb_batch_t b, int knob, long long* value
   }
   if (knob == DTSGB_TUNE_REUSE_GUIDE_STATE) {
     *value = b->reuse ? 1 : 0;
+    return DTSGB_OK;
+  }
+  if (knob == DTSGB_TUNE_HFBS_SOLVE_STEPS) {
+    *value = b->hfbs_solve_steps;
     return DTSGB_OK;
   }
   return fail(DTSGB_ERR_INVALID_ARGUMENT, "unknown tuning knob");

@@ -15,12 +15,16 @@
 #include "color.cuh"
 #include "dtsgb_internal.cuh"
 #include "fixed_point.cuh"
+#include "tma.cuh"
 
 namespace dtsgb {
 
 namespace {
 
 constexpr int kThreads = 256;
+
+// CTAs of this file's kernels that gave up waiting for their TMA staging.
+__device__ unsigned long long g_wait_timeouts = 0;
 
 __global__ void k_color_convert_flat(uchar4* __restrict__ g, long long n,
                                      int cs) {
@@ -247,7 +251,10 @@ __global__ void k_overwrite(const Inst* __restrict__ insts, float* __restrict__ 
 // 2hy rows):
 //  1. stage the iterate over SR rows x SW columns, from HA >= hx + 1
 //     columns left of the tile (SW and HA multiples of 4), and reduce its
-//     largest magnitude (the X scale);
+//     largest magnitude (the X scale).  With a tensor-map table the whole
+//     box arrives by one TMA load (cp.async.bulk.tensor; zeros past the
+//     image) while the threads fetch their first X-step operands; without
+//     one, by 16-byte loads;
 //  2. the rows are converted to fixed point and scanned: a thread per
 //     16-entry segment, then the segment offsets are added;
 //  3. X half-step for the tile columns over all SR rows, four pixels per
@@ -336,10 +343,11 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
                    const float* __restrict__ vin, float* __restrict__ vout,
                    const TS* __restrict__ tgt, const TS* __restrict__ cnf,
                    const uint32_t* __restrict__ bnd, float lambda, float step,
-                   float overwrite, int hx, int hy, StereoArgs sa, VecIterSmem<TW, TH, NT> L) {
+                   float overwrite, int hx, int hy, StereoArgs sa, VecIterSmem<TW, TH, NT> L,
+                   const CUtensorMap* __restrict__ tmaps) {
   constexpr int QW = TW / 4, TQ = TW + 4, RPP = NT / QW, NW = NT / 32;
   static_assert(TW % 32 == 0 && NT % TW == 0 && NW >= QW, "tile shape");
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   const Tile t = tiles[blockIdx.x];
   const Inst in = insts[t.inst];
   const int W = in.w, H = in.h, P = in.pitch;
@@ -357,6 +365,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   float2* rtx = reinterpret_cast<float2*>(smraw + L.rt_off);  // (1/n, 1/n 2^-F)
   float* rsy = reinterpret_cast<float*>(smraw + L.ry_off);     // 1/n 2^-Fy
   unsigned* smax = reinterpret_cast<unsigned*>(smraw + L.mx_off);  // [0] X, [1] Y
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(smraw + L.mx_off + 8);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nrt = 2 * max(hx, hy) + 2;
   for (int i = tid; i < nrt; i += NT) rtx[i].x = i ? __frcp_rn((float)i) : 0.f;
@@ -365,6 +374,20 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
                                                           // overwritten
   const int xs = t.x0 - HA;   // image x of staged column 0
   const int gy0 = t.y0 - hy;  // image y of row 0
+  // TMA staging: the box is SWS x SR (its row stride in shared memory is
+  // the staging stride); the destination must be 128-byte aligned
+  const bool use_tma = tmaps != nullptr && (smem_u32(Xf) & 127u) == 0;
+  if (use_tma) {
+    if (tid == 0) {
+      mbar_init(bar, 1);
+      mbar_fence_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      mbar_arrive_expect_tx(bar, (unsigned)(L.sws * SR * 4));
+      tma_load_2d(Xf, tmaps + t.inst, xs, gy0, bar);
+    }
+  }
   const int lgx = ceil_log2(2 * hx + 1), lgy = ceil_log2(2 * hy + 1);
   // ---- 3'. the X half-step's loads for this thread's first group ------------
   const int cq = tid % QW, r3 = tid / QW;  // group of columns x3 .. x3 + 3
@@ -399,7 +422,23 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   __syncthreads();  // smax initialised
   // ---- 1. stage the iterate, four columns per item, four items in flight -------
   float m = 0.f;
-  {
+  if (use_tma) {
+    // every thread waits for the box; a CTA whose wait ran out (all of its
+    // threads agree through the barrier) records it and leaves its tile
+    const bool ok = mbar_wait_bounded(bar, 0, kTmaWaitPolls);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicAdd(&g_wait_timeouts, 1ull);
+      (void)mbar_wait_bounded(bar, 0, kTmaWaitPolls);  // the copy may still land
+      return;
+    }
+    const int SW4 = SW >> 2, n = SR * SW4;
+    const unsigned mg = L.sw4_magic;
+    for (int i = tid; i < n; i += NT) {
+      const int r = fast_div(i, mg), q = i - r * SW4;
+      const float4 v = *reinterpret_cast<const float4*>(Xf + r * SWS + 4 * q);
+      m = fmaxf(m, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+    }
+  } else {
     constexpr int U = 4;
     const int SW4 = SW >> 2, n = SR * SW4;
     const unsigned mg = L.sw4_magic;
@@ -628,7 +667,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
                       float overwrite, int hx, int hy, StereoArgs sa) {
   static_assert(TW % 32 == 0 && NT % TW == 0, "tile width: whole warps");
   constexpr int NW = NT / 32, NSEG = NT / TW, TWp = TW + 1;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   const Tile t = tiles[blockIdx.x];
   const Inst in = insts[t.inst];
   const int W = in.w, H = in.h, P = in.pitch;
@@ -1060,10 +1099,15 @@ static int launch_iter_shape(const DtsLaunch& L, const float* vin, float* vout,
   }
   int st = set_smem(k_dts_iter_vec<TS, MODE, TW, TH, NT, STEREO>, smem);
   if (st) return st;
+  // TMA staging of the iterate box (SWS x SR, both within the 256-element
+  // box limit) from the owner's tensor-map cache, when it has one
+  const CUtensorMap* tm = nullptr;
+  if (L.tma && L.h_inst && lay.sws <= 256 && lay.sr <= 256)
+    tm = L.tma->get(L.h_inst, L.n_inst, vin, lay.sws, lay.sr, s);
   ProfScope ps(s, DTSGB_K_DTS_ITER);
   k_dts_iter_vec<TS, MODE, TW, TH, NT, STEREO><<<L.n_tiles, NT, smem, s>>>(
       L.d_inst, L.d_tiles, vin, vout, (const TS*)target, (const TS*)conf,
-      bounds, lambda, step, overwrite, hx, hy, sa, lay);
+      bounds, lambda, step, overwrite, hx, hy, sa, lay, tm);
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
 }
@@ -1239,6 +1283,42 @@ int launch_row_prefix(const Inst* h_inst, const Inst* d_inst, int n_inst,
   k_row_prefix<<<grid, kThreads, 0, s>>>(d_inst, in, out);
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
+}
+
+unsigned long long dts_wait_timeouts() {
+  unsigned long long v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_wait_timeouts, sizeof v) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return v;
+}
+
+// Tensor-map boxes the iteration kernel stages for halos hx, hy on the
+// current tile shape (0 x 0: staged by loads).
+void dts_iter_tma_box(const DtsLaunch& L, int hx, int hy, int* box_w, int* box_h) {
+  *box_w = *box_h = 0;
+  int sws = 0, sr = 0;
+  // the tile shape launch_iter_t picks, then the staged kernel's box (the
+  // large-halo kernel, taken when that box does not fit, stages by loads)
+  const VecIterSmem<kIterTW, kIterTH, 512> big(hx, hy);
+  const bool small =
+      L.small || (L.d_tiles_small && (size_t)big.total > kMaxSmem &&
+                  PrefixIterSmem<kIterTW, kIterTH, 512>::bytes(hx, hy) > kMaxSmem);
+  if (small) {
+    const VecIterSmem<kIterSmallTW, kIterSmallTH, 256> lay(hx, hy);
+    if ((size_t)lay.total > kMaxSmem) return;
+    sws = lay.sws;
+    sr = lay.sr;
+  } else {
+    if ((size_t)big.total > kMaxSmem) return;
+    sws = big.sws;
+    sr = big.sr;
+  }
+  if (sws <= 256 && sr <= 256) {
+    *box_w = sws;
+    *box_h = sr;
+  }
 }
 
 int launch_unpack_bounds(const DtsLaunch& L, const uint32_t* bounds, int axis,

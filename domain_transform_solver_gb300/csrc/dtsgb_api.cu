@@ -21,6 +21,7 @@
 #include "../../include/dtsgb.h"
 #include "color.cuh"
 #include "dtsgb_internal.cuh"
+#include "tma.cuh"
 #include "hfbs_internal.cuh"
 
 namespace dtsgb {
@@ -98,16 +99,22 @@ struct dtsgb_dts_s {
   float b_sx = 0.f, b_sy = 0.f;
   int var_idx = -1;
 
+  // tensor maps of the iterate planes (TMA staging of the iteration),
+  // rebuilt when the image dims change
+  mutable TmaCache tma;
+
   size_t tsize() const { return st == Storage::F32 ? 4 : 2; }
   DtsLaunch launch_b() const { return DtsLaunch{d_inst, d_tb, ntb, 1}; }
   bool small = false;
   DtsLaunch launch_i() const {
-    return DtsLaunch{d_inst, d_ti, nti, 1, small, small ? nullptr : d_ti_small, nti_small};
+    return DtsLaunch{d_inst, d_ti, nti, 1, small, small ? nullptr : d_ti_small, nti_small,
+                     &tma, &h_inst};
   }
 };
 
 static int dts_layout(dtsgb_dts_t h) {
   h->h_inst = Inst{h->w, h->h, h->pitch, 0, 0};
+  h->tma.clear();
   std::vector<Tile> tb = make_tiles(h->w, h->h, kBoundsTW, kBoundsTH);
   const long long t64 = (long long)((h->w + kIterTW - 1) / kIterTW) *
                         ((h->h + kIterTH - 1) / kIterTH);
@@ -625,6 +632,12 @@ DTSGB_API int dtsgb_dts_debug_bounds(dtsgb_dts_t h, int axis, float sigma,
   DTSGB_CUDA(cudaMemcpyAsync(u, du, n * 4, cudaMemcpyDeviceToHost, h->stream));
   DTSGB_CUDA(cudaStreamSynchronize(h->stream));
   h->bounds_valid = false;
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_wait_timeouts(unsigned long long* count) {
+  if (!count) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  *count = dts_wait_timeouts();
   return DTSGB_OK;
 }
 

@@ -145,6 +145,8 @@ struct ProfScope {
 // DTS launchers (dts_kernels.cu).  All take device pointers and a stream and
 // return a DTSGB_* status.
 // ---------------------------------------------------------------------------
+class TmaCache;
+
 struct DtsLaunch {
   const Inst* d_inst;   // device instance table
   const Tile* d_tiles;  // device tile table for the tile shape in use
@@ -155,6 +157,10 @@ struct DtsLaunch {
   // shared memory of the big tiles (null: none)
   const Tile* d_tiles_small = nullptr;
   int n_tiles_small = 0;
+  // tensor maps of the iterate planes for TMA staging, and the host copy of
+  // the instance table they describe (null: the kernels stage by loads)
+  TmaCache* tma = nullptr;
+  const Inst* h_inst = nullptr;
   // the same launch on the small tiles
   DtsLaunch as_small() const {
     DtsLaunch s = *this;
@@ -232,6 +238,13 @@ int launch_row_prefix(const Inst* h_inst, const Inst* d_inst, int n_inst,
                       const float* in, float* out, cudaStream_t s);
 int launch_unpack_bounds(const DtsLaunch& L, const uint32_t* bounds, int axis,
                          int32_t* l, int32_t* u, cudaStream_t s);
+// CTAs of the iteration kernels that gave up waiting for their TMA staging
+// since the library was loaded (0 on a healthy run).
+unsigned long long dts_wait_timeouts();
+// The box (columns x rows) of the iteration kernel's TMA staging for halos
+// hx, hy on L's tile shape; 0 x 0 when it stages by loads.  An owner builds
+// its tensor maps for that box before a graph capture.
+void dts_iter_tma_box(const DtsLaunch& L, int hx, int hy, int* box_w, int* box_h);
 
 // ---------------------------------------------------------------------------
 // Adjoint of the fixed-window solve (dts_adjoint.cu).

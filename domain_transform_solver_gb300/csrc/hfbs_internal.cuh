@@ -103,6 +103,10 @@ struct HfbsBatch {
   // group (0: all instances together); see hfbs_enqueue_solve
   const HInst* h_inst = nullptr;
   long long group_voxels = 0;
+  // heavy-ball steps per launch: kHfbsTBSteps (the temporally blocked
+  // kernel, where every grid has at most 16 levels) or 1 (the one-step
+  // kernel for every grid)
+  int solve_steps = 4;
   // the bistochastized normalisation in n0 / n1 (by the parity of
   // bistoch_iter_max) is that of the same guide and grid: skip recomputing it
   bool reuse_norm = false;
@@ -135,7 +139,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s);
 constexpr int kHfbsTBSteps = 4;
 
 // Whether the batch's heavy-ball steps run temporally blocked (every grid
-// at most 16 levels, host instance table given).  Its neighbour sums add
+// at most 16 levels, host instance table given, solve_steps not 1).  Its neighbour sums add
 // rounded z * n products; the one-step kernel's fuse them (FMA).
 bool hfbs_uses_tb(const HfbsBatch& B);
 

@@ -745,7 +745,9 @@ int blocks_for(long long n) {
 
 }  // namespace
 
-bool hfbs_uses_tb(const HfbsBatch& B) { return B.max_gl <= kTBMaxGL && B.h_inst; }
+bool hfbs_uses_tb(const HfbsBatch& B) {
+  return B.max_gl <= kTBMaxGL && B.h_inst && B.solve_steps != 1;
+}
 
 void hfbs_launch_steps(const HfbsBatch& B, const HParams& p, const float* norm,
                        const float* zs, float* zd, const float* hs, float* hd, int steps,
@@ -968,7 +970,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
         it += steps;
       }
     }
-  } else if (B.max_gl <= kTBMaxGL && B.h_inst) {
+  } else if (hfbs_uses_tb(B)) {
     // K heavy-ball steps per pass; h ping-pongs through the free blur
     // temporary t2 (its final value is not needed).  The shared-memory limit
     // is a per-device attribute: set on every call (host-side, cheap).

@@ -36,7 +36,7 @@ __all__ = [
     "DomainTransformFilter", "DomainTransformSolver", "HFBS", "DtsOptions",
     "HfbsOptions", "Solve", "EdgeAwareOptimize", "DtsgbError", "SoftDTS",
     "FLAG_BF16_STORAGE", "FLAG_FIX_Y_LIMIT", "TUNE_DTS_TILE", "TUNE_HFBS_GROUP_VOXELS",
-    "TUNE_REUSE_GUIDE_STATE",
+    "TUNE_REUSE_GUIDE_STATE", "TUNE_HFBS_SOLVE_STEPS",
     "Batch", "Pipeline", "DomainTransformStereo",
 ]
 
@@ -47,9 +47,11 @@ FLAG_STEREO = 0x8
 TUNE_DTS_TILE = 0
 TUNE_HFBS_GROUP_VOXELS = 1
 TUNE_REUSE_GUIDE_STATE = 2
+TUNE_HFBS_SOLVE_STEPS = 3
 # knob -> name, for reports
 TUNE_NAMES = {TUNE_DTS_TILE: "dts_tile", TUNE_HFBS_GROUP_VOXELS: "hfbs_group_voxels",
-              TUNE_REUSE_GUIDE_STATE: "reuse_guide_state"}
+              TUNE_REUSE_GUIDE_STATE: "reuse_guide_state",
+              TUNE_HFBS_SOLVE_STEPS: "hfbs_solve_steps"}
 
 
 @dataclass

@@ -121,6 +121,11 @@ enum {
   DTSGB_K_HFBS_ADJOINT = 10, /* the whole HFBS adjoint                  */
   DTSGB_K_COUNT = 11
 };
+/* (new) Thread blocks of the library's kernels that gave up waiting for an
+ * asynchronous (TMA) copy of their tile since the library was loaded: each
+ * wait polls a bounded number of times, and a block that gives up records
+ * it here and leaves its tile unwritten.  0 on a healthy run. */
+DTSGB_API int dtsgb_wait_timeouts(unsigned long long* count);
 DTSGB_API int dtsgb_profile_enable(int enable);
 DTSGB_API int dtsgb_profile_reset(void);
 DTSGB_API int dtsgb_profile_read(int kernel_id, int* launches, double* total_ms);
@@ -444,6 +449,13 @@ DTSGB_API int dtsgb_batch_debug_plane(dtsgb_batch_t b, int i, int which, void* d
  * and an HFBS solve with the same grid keeps the bistochastized
  * normalisation instead of recomputing them; results are identical. */
 #define DTSGB_TUNE_REUSE_GUIDE_STATE 2
+/* DTSGB_TUNE_HFBS_SOLVE_STEPS: heavy-ball steps per launch, 4 (default:
+ * a temporally blocked kernel, each launch four steps on 24 x 24-column
+ * blocks staged in shared memory, for grids of at most 16 levels) or 1
+ * (one step per launch, any grid; with a group budget its grids can stay in
+ * L2).  The two add a voxel's six neighbour products in different roundings:
+ * results agree to FP32 rounding, and each is differentiated exactly. */
+#define DTSGB_TUNE_HFBS_SOLVE_STEPS 3
 DTSGB_API int dtsgb_batch_set_tuning(dtsgb_batch_t b, int knob, long long value);
 DTSGB_API int dtsgb_batch_get_tuning(dtsgb_batch_t b, int knob, long long* value);
 /* Times the uploaded batch's solves under each tile shape (filter and

@@ -267,3 +267,10 @@ def test_cfg4_adjoint_fp64_central_differences(cfg4, oracle_mod):
     print(f"cfg4 FD: 256 entries in {len(groups)} groups (R = {R}); worst |GPU - FD| / "
           f"max|grad|: dL/dt {worst['t']:.2e}, dL/dc {worst['c']:.2e}")
     assert not bad, bad[:5]
+
+
+def test_no_staging_wait_gave_up(gpu_ready):
+    """Every TMA-staged tile of the solves above arrived: no thread block
+    ran out its bounded wait (dtsgb_wait_timeouts)."""
+    from domain_transform_solver_gb300 import _lib
+    assert _lib.wait_timeouts() == 0
