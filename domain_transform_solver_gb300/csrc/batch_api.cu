@@ -1037,6 +1037,7 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
     H.gx = (int)std::ceil((float)I.w / p->sigma_x);
     H.gy = (int)std::ceil((float)I.h / p->sigma_y);
     H.gl = gl;
+    H.px = round_up(H.gx, 4);
     H.cov_x = H.gx % 8 != 0;
     H.cov_y = H.gy % 8 != 0;
     H.cov_l = H.gl % 8 != 0;
@@ -1047,7 +1048,7 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
     H.slice_off = soff;
     soff += round_up_ll((long long)(H.gx + 1) * (H.gy + 1) * (H.gl + 2), 32);
     const long long vox = (long long)H.gx * H.gy * H.gl;
-    goff += round_up_ll(vox, 32);
+    goff += round_up_ll((long long)H.px * H.gy * H.gl, 32);
     poff += round_up_ll((long long)H.gx * H.gy, 32);
     max_vox = std::max(max_vox, vox);
     max_px = std::max(max_px, (long long)I.w * I.h);
@@ -1359,8 +1360,10 @@ DTSGB_API int dtsgb_batch_debug_plane(dtsgb_batch_t b, int i, int which, void* d
       return fail(DTSGB_ERR_INVALID_ARGUMENT, "dst_bytes smaller than gx*gy*gl*4");
     const int g = which == DTSGB_BATCH_PLANE_COUNT ? HG_COUNT
                   : which == DTSGB_BATCH_PLANE_CSUM ? HG_CSUM : HG_B;
-    DTSGB_CUDA(cudaMemcpyAsync(dst, b->hg[g] + H.grid_off, (size_t)n * 4,
-                               cudaMemcpyDeviceToHost, b->stream));
+    // rows of px voxels on the device, of gx in dst
+    DTSGB_CUDA(cudaMemcpy2DAsync(dst, (size_t)H.gx * 4, b->hg[g] + H.grid_off,
+                                 (size_t)H.px * 4, (size_t)H.gx * 4, (size_t)H.gy * H.gl,
+                                 cudaMemcpyDeviceToHost, b->stream));
   } else {
     return fail(DTSGB_ERR_INVALID_ARGUMENT, "which must be a DTSGB_BATCH_PLANE_* value");
   }

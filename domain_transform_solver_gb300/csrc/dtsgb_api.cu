@@ -720,7 +720,10 @@ static void hfbs_fill_batch(dtsgb_hfbs_t h, const HInst* hi, HfbsBatch& B) {
   B.h_inst = hi;
   B.n_inst = 1;
   B.max_voxels = (long long)I.gx * I.gy * I.gl;
-  B.total_voxels = B.max_voxels;
+  // grid rows of px voxels; planes (and the kept iterates carved from one
+  // arena) start every 32 voxels, as in a batch, so that every grid row
+  // starts on a 16-byte boundary
+  B.total_voxels = round_up_ll((long long)I.px * I.gy * I.gl, 32);
   B.max_pixels = (long long)I.w * I.h;
   B.max_cells = (long long)I.gx * I.gy;
   B.max_rows = (long long)I.gy * I.gl;
@@ -747,7 +750,7 @@ static void hfbs_fill_batch(dtsgb_hfbs_t h, const HInst* hi, HfbsBatch& B) {
   B.sgrid = h->sgrid;
   B.ovf = h->ovf;
   B.keep_debug = true;
-  B.grid_bytes = (size_t)B.max_voxels * 4;
+  B.grid_bytes = (size_t)I.px * I.gy * I.gl * 4;  // pitched
   B.dbg_norm = h->g[G_DBG_NORM];
   B.dbg_blur_c = h->g[G_DBG_BLUR_C];
   B.dbg_z_init = h->g[G_DBG_Z_INIT];
@@ -811,7 +814,7 @@ DTSGB_API int dtsgb_hfbs_create(int max_w, int max_h, int max_gx, int max_gy,
   h->max_gl = max_gl;
   h->flags = flags;
   h->plane = (size_t)h->pitch * max_h;
-  h->gsize = (size_t)max_gx * max_gy * max_gl;
+  h->gsize = (size_t)round_up_ll((long long)round_up(max_gx, 4) * max_gy * max_gl, 32);
   // HFBSGridParams defaults, src/hfbs.h:18-60
   h->p = dtsgb_hfbs_params{8.f, 8.f, 4.f, 8.f, 1.f, 0.9f, 20, 140, 0.9f, 1, 1, 1};
   int st = DTSGB_OK;
@@ -974,6 +977,7 @@ DTSGB_API int dtsgb_hfbs_optimize(dtsgb_hfbs_t h) {
   I.gx = p.grid_x;
   I.gy = p.grid_y;
   I.gl = p.grid_l;
+  I.px = round_up(I.gx, 4);
   I.cov_x = (I.gx % 8 != 0) && (I.gx < h->max_gx);
   I.cov_y = (I.gy % 8 != 0) && (I.gy < h->max_gy);
   I.cov_l = (I.gl % 8 != 0) && (I.gl < h->max_gl);
@@ -1042,9 +1046,10 @@ DTSGB_API int dtsgb_hfbs_debug_grid(dtsgb_hfbs_t h, int which, float* dst) {
                              G_DBG_Z_INIT, G_DBG_Z_FINAL};
   if (which < 0 || which >= 8) return fail(DTSGB_ERR_INVALID_ARGUMENT, "which");
   if (!h->solved) return fail(DTSGB_ERR_INVALID_ARGUMENT, "no solve yet");
-  const size_t n = (size_t)h->gx * h->gy * h->gl;
-  DTSGB_CUDA(cudaMemcpyAsync(dst, h->g[map[which]], n * 4,
-                             cudaMemcpyDeviceToHost, h->stream));
+  // rows of round_up(gx, 4) voxels on the device, of gx in dst
+  DTSGB_CUDA(cudaMemcpy2DAsync(dst, (size_t)h->gx * 4, h->g[map[which]],
+                               (size_t)round_up(h->gx, 4) * 4, (size_t)h->gx * 4,
+                               (size_t)h->gy * h->gl, cudaMemcpyDeviceToHost, h->stream));
   DTSGB_CUDA(cudaStreamSynchronize(h->stream));
   return DTSGB_OK;
 }

@@ -65,7 +65,7 @@ __global__ void k_hb_slice_scale(const HInst* __restrict__ insts,
         float cn = 0.f;
         if (jx < I.gx && jy < I.gy) {
           if (jz < I.gl)
-            cn = count[I.grid_off + ((long long)jz * I.gy + jy) * I.gx + jx];
+            cn = count[I.grid_off + ((long long)jz * I.gy + jy) * I.px + jx];
           else if (jz == I.gl)
             cn = ovf[I.plane_off + (long long)jy * I.gx + jx];  // 0 unless stored
         }
@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(kGatherThreads)
     for (int l = 0; l < I.gl; ++l) {
       const float* r = hcol + l * kGatherThreads;
       const float v = ((r[0] + r[1]) + r[2]) + r[3];
-      const long long g = I.grid_off + ((long long)l * I.gy + iy) * I.gx + ix;
+      const long long g = I.grid_off + ((long long)l * I.gy + iy) * I.px + ix;
       gz[g] = count[g] * v;
     }
   }
@@ -165,14 +165,14 @@ __global__ void k_hb_step_adj(const HInst* __restrict__ insts, const float* __re
   const HInst I = insts[blockIdx.y];
   const int gx = I.gx, gy = I.gy, gl = I.gl;
   const long long nv = (long long)gx * gy * gl;
-  const int sy = gx, sz = gx * gy;
+  const int sy = I.px, sz = I.px * gy;
   const float* nn = norm + I.grid_off;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nv;
        v += (long long)gridDim.x * blockDim.x) {
     const int r = (int)(v / gx), x = (int)(v - (long long)r * gx);
     const int zz = r / gy, y = r - zz * gy;
-    const int i = (int)v;
-    const long long g = I.grid_off + v;
+    const int i = r * sy + x;  // (zz * gy + y) rows of px voxels
+    const long long g = I.grid_off + i;
     float gzv = gz[g];
     const float nc = nn[i];
     if (finish) {
@@ -263,7 +263,7 @@ __global__ void k_hb_splat_adj(const HInst* __restrict__ insts, const uchar4* __
     const int bl = (int)floorf((float)guide[pix].x * 1.0f / p.sigma_l);
     float gt = 0.f, gc = 0.f;
     if (bl < I.gl) {
-      const long long g = I.grid_off + ((long long)bl * I.gy + by) * I.gx + bx;
+      const long long g = I.grid_off + ((long long)bl * I.gy + by) * I.px + bx;
       gt = ld_store(conf + pix) * gb[g];
       gc = ld_store(target + pix) * gb[g] + gcs[g];
     }

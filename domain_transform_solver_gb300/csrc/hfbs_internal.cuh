@@ -10,6 +10,11 @@ namespace dtsgb {
 struct HInst {
   int w, h, pitch;
   int gx, gy, gl;
+  // row pitch of the grids in voxels: gx rounded up to a multiple of 4, so
+  // that every grid row starts on a 16-byte boundary (tensor-map tiles);
+  // voxel (x, y, l) is at grid_off + (l * gy + y) * px + x, and the voxels
+  // x >= gx of a row are padding that no stencil reads
+  int px;
   // pad faces written by the reference's FillGrid (g % 8 != 0 and inside
   // the max-size allocation); they read the last fill value of the buffer
   int cov_x, cov_y, cov_l;

@@ -25,7 +25,7 @@ namespace {
 constexpr int kT = 256;
 
 __device__ __forceinline__ long long gidx(const HInst& I, int x, int y, int z) {
-  return I.grid_off + ((long long)z * I.gy + y) * I.gx + x;
+  return I.grid_off + ((long long)z * I.gy + y) * I.px + x;
 }
 
 // a12: SplatBAndC + BistochastasizeSetup (src/hfbs.cu:72-120).  Bins
@@ -138,13 +138,14 @@ __global__ void k_bistoch(const HInst* __restrict__ insts,
   const float* s = src + I.grid_off;
   const float* cn = count + I.grid_off;
   float* d = dst + I.grid_off;
-  const int sy = gx, sz = gx * gy;
+  const int sy = I.px, sz = I.px * gy;
   // one thread per (x, y) column, marching along l: the l-neighbours come
   // from registers, and the loads of level l+1 are issued before level l is
   // computed
-  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < sz;
-       col += gridDim.x * blockDim.x) {
-    const int y = col / gx, x = col - y * gx;
+  for (int cl = blockIdx.x * blockDim.x + threadIdx.x; cl < gx * gy;
+       cl += gridDim.x * blockDim.x) {
+    const int y = cl / gx, x = cl - y * gx;
+    const int col = y * sy + x;
     const bool xm = x > 0, xp = x + 1 < gx, ym = y > 0, yp = y + 1 < gy;
     auto nb4 = [&](int i, float (&o)[5]) {  // x-1, x+1, y-1, y+1, count
       o[0] = xm ? s[i - 1] : 0.f;
@@ -219,7 +220,7 @@ __global__ void k_laplace_x(const HInst* __restrict__ insts,
   for (int k = lane; k < 32; ++k) brev *= beta;
   for (int line = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; line < nlines;
        line += nwarps) {
-    const long long base = I.grid_off + (long long)line * gx;
+    const long long base = I.grid_off + (long long)line * I.px;
     for (int f = 0; f < 2; ++f) {
       const float* s = (f ? s1 : s0) + base;
       float* d = (f ? d1 : d0) + base;
@@ -272,20 +273,21 @@ __global__ void k_laplace(const HInst* __restrict__ insts, int axis,
   const int gx = I.gx, gy = I.gy, gl = I.gl;
   int len, na, nlines;
   long long stride;
+  const int px = I.px;
   if (axis == 0) {
     len = gx; stride = 1; na = gy; nlines = gy * gl;
   } else if (axis == 1) {
-    len = gy; stride = gx; na = gx; nlines = gx * gl;
+    len = gy; stride = px; na = gx; nlines = gx * gl;
   } else {
-    len = gl; stride = (long long)gx * gy; na = gx; nlines = gx * gy;
+    len = gl; stride = (long long)px * gy; na = gx; nlines = gx * gy;
   }
   for (int line = blockIdx.x * blockDim.x + threadIdx.x; line < nlines;
        line += gridDim.x * blockDim.x) {
     const int a = line % na, bb = line / na;
     long long base;
-    if (axis == 0) base = ((long long)bb * gy + a) * gx;
-    else if (axis == 1) base = (long long)bb * gx * gy + a;
-    else base = (long long)bb * gx + a;
+    if (axis == 0) base = ((long long)bb * gy + a) * px;
+    else if (axis == 1) base = (long long)bb * px * gy + a;
+    else base = (long long)bb * px + a;
     base += I.grid_off;
     for (int f = 0; f < 2; ++f) {
       const float* s = f ? s1 : s0;
@@ -355,14 +357,14 @@ __global__ void k_solve(const HInst* __restrict__ insts,
   const float* ia = invA + I.grid_off;
   float* hh = h + I.grid_off;
   float* zo = zd + I.grid_off;
-  const int sy = gx, sz = gx * gy;
+  const int sy = I.px, sz = I.px * gy;
   // one warp per grid row (fixed y, l); lanes stride along x
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < gy * gl;
        row += nwarps) {
     const int zz = row / gy, y = row - zz * gy;
-    const int base = row * gx;
+    const int base = row * sy;
     // two x positions per lane per pass: their 34 loads are issued before
     // either result is computed
     for (int x0 = lane; x0 < gx; x0 += 64) {
@@ -483,7 +485,7 @@ __global__ void __launch_bounds__(kTBThreads, 1)
   const bool in = x >= 0 && x < gx && y >= 0 && y < gy;
   const bool face = (I.cov_x && x == gx && y >= 0 && y < gy) ||
                     (I.cov_y && y == gy && x >= 0 && x < gx);
-  const int plane = gx * gy, col = in ? y * gx + x : 0;
+  const int plane = I.px * gy, col = in ? y * I.px + x : 0;
   const long long g0 = I.grid_off + col;
 #pragma unroll
   for (int l = 0; l < kTBMaxGL; ++l) {
@@ -551,7 +553,7 @@ __global__ void __launch_bounds__(kTBThreads, 1)
   const int c = threadIdx.x, yy = c / kTBL, xx = c - yy * kTBL;
   const int x = tx * kTBT - kTBK + xx, y = ty * kTBT - kTBK + yy;
   const bool in = x >= 0 && x < gx && y >= 0 && y < gy;
-  const int plane = gx * gy, col = in ? y * gx + x : 0;
+  const int plane = I.px * gy, col = in ? y * I.px + x : 0;
   const long long g0 = I.grid_off + col;
 #pragma unroll
   for (int l = 0; l < kTBMaxGL; ++l) {
