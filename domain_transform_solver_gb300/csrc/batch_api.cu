@@ -129,8 +129,10 @@ struct dtsgb_batch_s {
   HParams hhp{};
   Graph g_hbwd;
 
-  // tensor maps of the iterate planes (TMA staging of the iteration)
+  // tensor maps of the iterate planes (TMA staging of the iteration) and of
+  // the HFBS grid planes (cleared when the grids change)
   TmaCache tma;
+  TmaCache htma;
 
   size_t tsize() const { return st == Storage::F32 ? 4 : 2; }
 };
@@ -1062,6 +1064,7 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
       b->hinst.size() == hi.size() &&
       std::memcmp(b->hinst.data(), hi.data(), hi.size() * sizeof(HInst)) == 0;
   if (!same_tables) {
+    b->htma.clear();
     b->hinst = hi;
     DTSGB_CUDA(cudaMemcpyAsync(b->d_hinst, b->hinst.data(), hi.size() * sizeof(HInst),
                                cudaMemcpyHostToDevice, b->stream));
@@ -1101,6 +1104,7 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
   B.h_inst = b->hinst.data();
   B.group_voxels = b->hfbs_group_voxels;
   B.solve_steps = b->hfbs_solve_steps;
+  B.tma = &b->htma;
   // the bistochastized normalisation depends only on the guide's bins
   const dtsgb_batch_s::NormKey nk{b->guide_gen, p->sigma_x, p->sigma_y, p->sigma_l,
                                   p->bistoch_iter_max};
@@ -1112,6 +1116,7 @@ DTSGB_API int dtsgb_batch_solve_hfbs(dtsgb_batch_t b, const dtsgb_hfbs_params* p
     if ((st = hfbs_prepare_grad(b, p->optim_iter_max, goff))) return st;
     B.grad = &b->hgs;
   }
+  hfbs_prepare_tma(B, b->stream);  // before any capture of the solve
   std::vector<char> key;
   key_append(key, hp);
   key_append(key, b->hfbs_group_voxels);

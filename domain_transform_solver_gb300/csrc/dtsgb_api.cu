@@ -637,7 +637,7 @@ DTSGB_API int dtsgb_dts_debug_bounds(dtsgb_dts_t h, int axis, float sigma,
 
 DTSGB_API int dtsgb_wait_timeouts(unsigned long long* count) {
   if (!count) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
-  *count = dts_wait_timeouts();
+  *count = dts_wait_timeouts() + hfbs_wait_timeouts();
   return DTSGB_OK;
 }
 
@@ -675,6 +675,9 @@ struct dtsgb_hfbs_s {
   uchar4* guide = nullptr;
   float *target = nullptr, *conf = nullptr, *out = nullptr;
   float* g[16] = {};
+  // tensor maps of the grid planes and the grid they describe
+  TmaCache tma;
+  HInst tma_inst{};
   float* ovf = nullptr;
   float2* sgrid = nullptr;  // (max_gx + 1) x (max_gy + 1) x (max_gl + 2)
   HInst* d_inst = nullptr;
@@ -990,6 +993,11 @@ DTSGB_API int dtsgb_hfbs_optimize(dtsgb_hfbs_t h) {
                              cudaMemcpyHostToDevice, h->stream));
   HfbsBatch B{};
   hfbs_fill_batch(h, &I, B);
+  if (std::memcmp(&I, &h->tma_inst, sizeof I) != 0) {  // other grid: other tensor maps
+    h->tma.clear();
+    h->tma_inst = I;
+  }
+  B.tma = &h->tma;
   h->grad_ready = false;
   if (h->grad) {
     int gst = hfbs_prepare_grad(h, p.optim_iter_max, B.total_voxels);

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "dtsgb_internal.cuh"
+#include "tma.cuh"
 
 namespace dtsgb {
 
@@ -112,6 +113,10 @@ struct HfbsBatch {
   // kernel, where every grid has at most 16 levels) or 1 (the one-step
   // kernel for every grid)
   int solve_steps = 4;
+  // tensor maps of the grid planes for the temporally blocked kernels' TMA
+  // staging (null: they stage by 4-byte copies); owned by the caller, which
+  // clears it when the instances' grids change
+  TmaCache* tma = nullptr;
   // the bistochastized normalisation in n0 / n1 (by the parity of
   // bistoch_iter_max) is that of the same guide and grid: skip recomputing it
   bool reuse_norm = false;
@@ -142,6 +147,15 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s);
 
 // Heavy-ball steps per launch of the temporally blocked kernel.
 constexpr int kHfbsTBSteps = 4;
+
+// Builds the grid tensor maps the solve of B will stage from (grid planes
+// b, invA, both z and h buffers, both normalisation buffers, the counts),
+// so that a graph capture of the solve finds them; a no-op without B.tma.
+void hfbs_prepare_tma(const HfbsBatch& B, cudaStream_t s);
+
+// CTAs of the temporally blocked kernels that gave up waiting for their TMA
+// staging since the library was loaded (0 on a healthy run).
+unsigned long long hfbs_wait_timeouts();
 
 // Whether the batch's heavy-ball steps run temporally blocked (every grid
 // at most 16 levels, host instance table given, solve_steps not 1).  Its neighbour sums add

@@ -17,12 +17,16 @@
 #include "../../include/dtsgb.h"
 #include "dtsgb_internal.cuh"
 #include "hfbs_internal.cuh"
+#include "tma.cuh"
 
 namespace dtsgb {
 
 namespace {
 
 constexpr int kT = 256;
+
+// CTAs of this file's kernels that gave up waiting for their TMA staging.
+__device__ unsigned long long g_wait_timeouts = 0;
 
 __device__ __forceinline__ long long gidx(const HInst& I, int x, int y, int z) {
   return I.grid_off + ((long long)z * I.gy + y) * I.px + x;
@@ -422,17 +426,51 @@ __global__ void k_solve(const HInst* __restrict__ insts,
 // because a neighbouring CTA reads the old h of this tile's columns as its
 // halo.
 //
-// The block arrives by 4-byte cp.async copies (zero-filled outside the grid),
-// all in flight at once without holding registers; z, h and n are staged in
-// the space the z * n buffers use afterwards.  Every thread reads and writes
-// only its own column there, so the reuse needs no barrier.
+// The block arrives by TMA: one cp.async.bulk.tensor load per plane of the
+// 24 x 24 x 16 box (tensor maps of the pitched grids, zeros outside the
+// grid and above level gl), issued by one thread and waited for on an
+// mbarrier; without tensor maps, by 4-byte cp.async copies (zero-filled
+// outside the grid).  z, h and n are staged in the space the z * n buffers
+// use afterwards.  Every thread reads and writes only its own column there,
+// so the reuse needs no barrier.
 constexpr int kTBT = 16, kTBK = 4, kTBL = kTBT + 2 * kTBK;
 static_assert(kTBK == kHfbsTBSteps, "steps per temporally blocked launch");
 constexpr int kTBMaxGL = 16;
 constexpr int kTBThreads = kTBL * kTBL;  // one thread per (x, y) column
 constexpr int kTBPlane = kTBMaxGL * kTBThreads;  // floats per staged array
-// b, invA, then z, h, n staged (later z * n, double-buffered)
-constexpr size_t kTBSmem = sizeof(float) * 5 * kTBPlane;
+// b, invA, then z, h, n staged (later z * n, double-buffered), an mbarrier
+constexpr size_t kTBSmem = sizeof(float) * 5 * kTBPlane + 16;
+constexpr unsigned kTBBoxBytes = sizeof(float) * kTBPlane;  // one plane's box
+
+// Tensor-map tables (one entry per instance of the launch) of the planes a
+// temporally blocked launch stages; all null: staged by 4-byte copies.
+struct TBMaps {
+  const CUtensorMap *b, *a, *z, *h, *n;
+};
+
+// Issues the block's TMA loads (thread 0; the mbarrier initialised for one
+// arrival) of np planes into consecutive kTBPlane regions from dst, and
+// waits, bounded.  False (the same in every thread) when the wait ran out.
+__device__ __forceinline__ bool tb_tma_stage(const CUtensorMap* const* maps, int np, float* dst,
+                                             int x0, int y0, unsigned long long* bar) {
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(bar, (unsigned)np * kTBBoxBytes);
+    for (int k = 0; k < np; ++k)
+      tma_load_3d(dst + (size_t)k * kTBPlane, maps[k] + blockIdx.y, x0, y0, 0, bar);
+  }
+  const bool ok = mbar_wait_bounded(bar, 0, kTmaWaitPolls);
+  if (__syncthreads_or(!ok)) {
+    if (threadIdx.x == 0) atomicAdd(&g_wait_timeouts, 1ull);
+    (void)mbar_wait_bounded(bar, 0, kTmaWaitPolls);  // copies may still land
+    return false;
+  }
+  return true;
+}
 
 // True when column (xx, yy) of a temporally blocked block is updated at step
 // k: it lies at least k columns inside the block.
@@ -458,7 +496,8 @@ __device__ __forceinline__ void cp_async_f32(float* dst, const float* src, bool 
 // even iterations, 0 on odd ones), everything else 0.  The neighbour order
 // and the arithmetic are k_bistoch's, so the result is bitwise that of the
 // one-step passes.  it0: the global index of the pass's first iteration.
-constexpr size_t kTBBistochSmem = sizeof(float) * 3 * kTBPlane;  // v x 2, count
+// v x 2 (the first also the staged src), count, an mbarrier
+constexpr size_t kTBBistochSmem = sizeof(float) * 3 * kTBPlane + 16;
 // Small grids only: there one-step passes are launch-latency-bound (about
 // 12 us each on GB300 whatever the size) and four iterations per pass win
 // (a 640x480 colorization's two 80x60x16 grids: 0.097 against 0.246 ms).  At 11.7 M voxels
@@ -472,9 +511,11 @@ constexpr long long kBistochTBMaxVoxels = 1ll << 18;
 __global__ void __launch_bounds__(kTBThreads, 1)
     k_bistoch_tb(const HInst* __restrict__ insts, const float* __restrict__ src,
                  float* __restrict__ dst, const float* __restrict__ count, int it0,
-                 int steps) {
-  extern __shared__ float tb_s[];
+                 int steps, const CUtensorMap* __restrict__ msrc,
+                 const CUtensorMap* __restrict__ mcnt) {
+  extern __shared__ __align__(128) float tb_s[];
   float* Cs = tb_s + 2 * kTBPlane;  // counts of the block's columns
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(tb_s + 3 * kTBPlane);
   const HInst I = insts[blockIdx.y];
   const int gx = I.gx, gy = I.gy, gl = I.gl;  // gl <= kTBMaxGL (host checks)
   const int tiles_x = (gx + kTBT - 1) / kTBT;
@@ -487,14 +528,35 @@ __global__ void __launch_bounds__(kTBThreads, 1)
                     (I.cov_y && y == gy && x >= 0 && x < gx);
   const int plane = I.px * gy, col = in ? y * I.px + x : 0;
   const long long g0 = I.grid_off + col;
+  if (msrc && mcnt && (smem_u32(tb_s) & 127u) == 0) {
+    // src into plane 0 (the first step's exchange then writes plane 1),
+    // the counts into plane 2
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_arrive_expect_tx(bar, 2u * kTBBoxBytes);
+      tma_load_3d(tb_s, msrc + blockIdx.y, tx * kTBT - kTBK, ty * kTBT - kTBK, 0, bar);
+      tma_load_3d(Cs, mcnt + blockIdx.y, tx * kTBT - kTBK, ty * kTBT - kTBK, 0, bar);
+    }
+    const bool ok = mbar_wait_bounded(bar, 0, kTmaWaitPolls);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicAdd(&g_wait_timeouts, 1ull);
+      (void)mbar_wait_bounded(bar, 0, kTmaWaitPolls);
+      return;
+    }
+  } else {
 #pragma unroll
-  for (int l = 0; l < kTBMaxGL; ++l) {
-    const bool v = in && l < gl;
-    const long long i = g0 + (v ? (long long)l * plane : 0);
-    cp_async_f32(tb_s + l * kTBThreads + c, src + i, v);
-    cp_async_f32(Cs + l * kTBThreads + c, count + i, v);
+    for (int l = 0; l < kTBMaxGL; ++l) {
+      const bool v = in && l < gl;
+      const long long i = g0 + (v ? (long long)l * plane : 0);
+      cp_async_f32(tb_s + l * kTBThreads + c, src + i, v);
+      cp_async_f32(Cs + l * kTBThreads + c, count + i, v);
+    }
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
   }
-  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
   float v[kTBMaxGL];
 #pragma unroll
   for (int l = 0; l < kTBMaxGL; ++l) v[l] = tb_s[l * kTBThreads + c];
@@ -540,11 +602,13 @@ __global__ void __launch_bounds__(kTBThreads, 1)
                float* __restrict__ zd, const float* __restrict__ hs, float* __restrict__ hd,
                const float* __restrict__ norm, const float* __restrict__ b,
                const float* __restrict__ invA, float lambda, float alpha, float beta,
-               int steps, float* __restrict__ rec, long long rec_stride, int rec_steps) {
-  extern __shared__ float tb_s[];
+               int steps, float* __restrict__ rec, long long rec_stride, int rec_steps,
+               TBMaps m) {
+  extern __shared__ __align__(128) float tb_s[];
   float* Bs = tb_s;
   float* As = Bs + kTBPlane;
   float* R = As + kTBPlane;  // z, h, n staging; then z * n [2]
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(tb_s + 5 * kTBPlane);
   const HInst I = insts[blockIdx.y];
   const int gx = I.gx, gy = I.gy, gl = I.gl;  // gl <= kTBMaxGL (host checks)
   const int tiles_x = (gx + kTBT - 1) / kTBT;
@@ -555,17 +619,23 @@ __global__ void __launch_bounds__(kTBThreads, 1)
   const bool in = x >= 0 && x < gx && y >= 0 && y < gy;
   const int plane = I.px * gy, col = in ? y * I.px + x : 0;
   const long long g0 = I.grid_off + col;
+  if (m.b && (smem_u32(tb_s) & 127u) == 0) {
+    // b, invA, z, h, n: the five consecutive plane regions from Bs
+    const CUtensorMap* maps[5] = {m.b, m.a, m.z, m.h, m.n};
+    if (!tb_tma_stage(maps, 5, Bs, tx * kTBT - kTBK, ty * kTBT - kTBK, bar)) return;
+  } else {
 #pragma unroll
-  for (int l = 0; l < kTBMaxGL; ++l) {
-    const bool v = in && l < gl;
-    const long long i = g0 + (v ? (long long)l * plane : 0);
-    cp_async_f32(R + l * kTBThreads + c, zs + i, v);
-    cp_async_f32(R + kTBPlane + l * kTBThreads + c, hs + i, v);
-    cp_async_f32(R + 2 * kTBPlane + l * kTBThreads + c, norm + i, v);
-    cp_async_f32(Bs + l * kTBThreads + c, b + i, v);
-    cp_async_f32(As + l * kTBThreads + c, invA + i, v);
+    for (int l = 0; l < kTBMaxGL; ++l) {
+      const bool v = in && l < gl;
+      const long long i = g0 + (v ? (long long)l * plane : 0);
+      cp_async_f32(R + l * kTBThreads + c, zs + i, v);
+      cp_async_f32(R + kTBPlane + l * kTBThreads + c, hs + i, v);
+      cp_async_f32(R + 2 * kTBPlane + l * kTBThreads + c, norm + i, v);
+      cp_async_f32(Bs + l * kTBThreads + c, b + i, v);
+      cp_async_f32(As + l * kTBThreads + c, invA + i, v);
+    }
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
   }
-  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
   float z[kTBMaxGL], h[kTBMaxGL], n[kTBMaxGL];
 #pragma unroll
   for (int l = 0; l < kTBMaxGL; ++l) {
@@ -739,6 +809,29 @@ __global__ void k_slice(const HInst* __restrict__ insts,
   }
 }
 
+// The table of tensor maps of grid plane `plane` over B's instances (TMA
+// boxes of the temporally blocked kernels), or null.
+const CUtensorMap* grid_map(const HfbsBatch& B, const float* plane, cudaStream_t s) {
+  if (!B.tma || !B.h_inst || B.max_gl > kTBMaxGL) return nullptr;
+  std::vector<TmaGrid> g(B.n_inst);
+  for (int i = 0; i < B.n_inst; ++i) {
+    const HInst& H = B.h_inst[i];
+    g[i] = TmaGrid{H.grid_off, H.gx, H.gy, H.gl, H.px};
+  }
+  return B.tma->get_grid(g.data(), B.n_inst, plane, kTBL, kTBL, kTBMaxGL, s);
+}
+
+// The five tables of a temporally blocked heavy-ball launch over the
+// instances from `first`; all null when any is missing.
+TBMaps tb_maps(const HfbsBatch& B, int first, const float* zs, const float* hs,
+               const float* norm, cudaStream_t s) {
+  const float* planes[5] = {B.b, B.invA, zs, hs, norm};
+  const CUtensorMap* t[5];
+  for (int k = 0; k < 5; ++k)
+    if (!(t[k] = grid_map(B, planes[k], s))) return TBMaps{};
+  return TBMaps{t[0] + first, t[1] + first, t[2] + first, t[3] + first, t[4] + first};
+}
+
 int blocks_for(long long n) {
   long long b = (n + kT - 1) / kT;
   if (b > 152 * 8) b = 152 * 8;
@@ -746,6 +839,22 @@ int blocks_for(long long n) {
 }
 
 }  // namespace
+
+unsigned long long hfbs_wait_timeouts() {
+  unsigned long long v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_wait_timeouts, sizeof v) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return v;
+}
+
+void hfbs_prepare_tma(const HfbsBatch& B, cudaStream_t s) {
+  for (const float* p : {(const float*)B.b, (const float*)B.invA, (const float*)B.z0,
+                         (const float*)B.z1, (const float*)B.h, (const float*)B.t2,
+                         (const float*)B.n0, (const float*)B.n1, (const float*)B.count})
+    (void)grid_map(B, p, s);
+}
 
 bool hfbs_uses_tb(const HfbsBatch& B) {
   return B.max_gl <= kTBMaxGL && B.h_inst && B.solve_steps != 1;
@@ -764,7 +873,7 @@ void hfbs_launch_steps(const HfbsBatch& B, const HParams& p, const float* norm,
     cudaFuncSetAttribute(k_solve_tb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTBSmem);
     k_solve_tb<<<dim3((unsigned)tiles, B.n_inst), kTBThreads, kTBSmem, s>>>(
         B.d_inst, zs, zd, hs, hd, norm, B.b, B.invA, p.lambda, p.alpha, p.beta, steps, rec,
-        B.total_voxels, rec_steps);
+        B.total_voxels, rec_steps, tb_maps(B, 0, zs, hs, norm, s));
   } else {
     // one step; h in place (hs == hd)
     const dim3 gr((unsigned)std::min<long long>((B.max_rows + 7) / 8, 4096), B.n_inst);
@@ -889,9 +998,13 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
                                       (int)kTBBistochSmem));
       int it0 = 0;
       for (int steps : plan) {
+        const CUtensorMap* ms = grid_map(B, src, s);
+        const CUtensorMap* mc = ms ? grid_map(B, B.count, s) : nullptr;
+        if (!mc) ms = nullptr;
         prof_begin(s, DTSGB_K_HFBS_BISTOCH);
         k_bistoch_tb<<<dim3((unsigned)tiles, g.count), kTBThreads, kTBBistochSmem, s>>>(
-            B.d_inst + g.first, src, dst, B.count, it0, steps);
+            B.d_inst + g.first, src, dst, B.count, it0, steps, ms ? ms + g.first : nullptr,
+            mc ? mc + g.first : nullptr);
         prof_end(s, DTSGB_K_HFBS_BISTOCH);
         std::swap(src, dst);
         it0 += steps;
@@ -994,7 +1107,8 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
         prof_begin(s, DTSGB_K_HFBS_SOLVE);
         k_solve_tb<<<gt, kTBThreads, kTBSmem, s>>>(B.d_inst + g.first, zs, zd, hs, hd, norm,
                                                     B.b, B.invA, p.lambda, p.alpha, p.beta,
-                                                    steps, nullptr, 0, 0);
+                                                    steps, nullptr, 0, 0,
+                                                    tb_maps(B, g.first, zs, hs, norm, s));
         prof_end(s, DTSGB_K_HFBS_SOLVE);
         std::swap(zs, zd);
         std::swap(hs, hd);

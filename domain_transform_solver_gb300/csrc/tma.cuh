@@ -73,6 +73,18 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tmap, 
       : "memory");
 }
 
+// 3D tiled load of the box at (x, y, z) of tensor map `tmap` into shared
+// memory at dst (128-byte aligned), completing on `bar`.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tmap, int x, int y,
+                                            int z, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(tmap)), "r"(x), "r"(y), "r"(z),
+      "r"(smem_u32(bar))
+      : "memory");
+}
+
 // Polls of a staging wait before a kernel gives up (about a second at the
 // hardware's try_wait suspend time); a CTA that gives up counts the event
 // in its translation unit's wait-timeout counter (dtsgb_wait_timeouts) and
@@ -88,9 +100,23 @@ constexpr unsigned kTmaWaitPolls = 1u << 22;
 int tma_encode_plane(CUtensorMap* out, const void* base, int w, int h, int pitch, int box_w,
                      int box_h);
 
+// One instance's 3D grid inside a grid plane: gx x gy x gl 4-byte voxels at
+// element offset off, rows of px voxels (px a multiple of 4).
+struct TmaGrid {
+  long long off;
+  int gx, gy, gl, px;
+};
+
+// Encodes a tensor map of one grid (dims gx, gy, gl; row pitch px voxels,
+// level pitch px * gy) with a box of bx x by x bl voxels.
+int tma_encode_grid(CUtensorMap* out, const void* base, const TmaGrid& g, int bx, int by,
+                    int bl);
+
 // Device tables of tensor maps, one entry per instance, for a source plane
-// (the arena base of a per-pixel plane) and a box shape; built on first use
-// (never while the stream is being captured) and kept until destruction.
+// (the arena base of a per-pixel plane or of a grid plane) and a box shape;
+// built on first use (never while the stream is being captured) and kept
+// until clear() or destruction.  The owner clears the cache when the
+// instances' geometry changes.
 class TmaCache {
  public:
   TmaCache() = default;
@@ -101,10 +127,15 @@ class TmaCache {
   // not built and cannot be built now (capture in progress, failure)
   const CUtensorMap* get(const Inst* h_inst, int n, const float* plane, int box_w, int box_h,
                          cudaStream_t s);
+  // the same for grids (3D boxes of bx x by x bl voxels)
+  const CUtensorMap* get_grid(const TmaGrid* grids, int n, const float* plane, int bx, int by,
+                              int bl, cudaStream_t s);
   void clear();
 
  private:
-  std::map<std::tuple<const float*, int, int>, CUtensorMap*> tables_;
+  const CUtensorMap* upload(const std::vector<CUtensorMap>& maps,
+                            const std::tuple<const float*, int, int, int>& key);
+  std::map<std::tuple<const float*, int, int, int>, CUtensorMap*> tables_;
 };
 
 }  // namespace dtsgb

@@ -51,7 +51,67 @@ int tma_encode_plane(CUtensorMap* out, const void* base, int w, int h, int pitch
   return DTSGB_OK;
 }
 
+int tma_encode_grid(CUtensorMap* out, const void* base, const TmaGrid& g, int bx, int by,
+                    int bl) {
+  auto fn = encode_fn();
+  if (!fn) return fail(DTSGB_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+  if (bx <= 0 || bx > 256 || by <= 0 || by > 256 || bl <= 0 || bl > 256 ||
+      (bx * 4) % 16 != 0 || ((uintptr_t)base & 15) != 0 || (g.px * 4) % 16 != 0)
+    return fail(DTSGB_ERR_UNSUPPORTED, "grid or box outside the TMA limits");
+  const cuuint64_t dims[3] = {(cuuint64_t)g.gx, (cuuint64_t)g.gy, (cuuint64_t)g.gl};
+  const cuuint64_t strides[2] = {(cuuint64_t)g.px * 4, (cuuint64_t)g.px * g.gy * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bl};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims,
+                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return fail(DTSGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return DTSGB_OK;
+}
+
 TmaCache::~TmaCache() { clear(); }
+
+const CUtensorMap* TmaCache::upload(const std::vector<CUtensorMap>& maps,
+                                    const std::tuple<const float*, int, int, int>& key) {
+  CUtensorMap* d = nullptr;
+  if (cudaMalloc((void**)&d, sizeof(CUtensorMap) * maps.size()) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  if (cudaMemcpy(d, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice) !=
+      cudaSuccess) {
+    (void)cudaGetLastError();
+    cudaFree(d);
+    return nullptr;
+  }
+  tables_[key] = d;
+  return d;
+}
+
+// No synchronous copies inside a capture: the caller then stages by loads.
+static bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return true;
+  }
+  return cs != cudaStreamCaptureStatusNone;
+}
+
+const CUtensorMap* TmaCache::get_grid(const TmaGrid* grids, int n, const float* plane, int bx,
+                                      int by, int bl, cudaStream_t s) {
+  if (!grids || n <= 0 || !plane) return nullptr;
+  const auto key = std::make_tuple(plane, bx, by, 1000 + bl);
+  auto it = tables_.find(key);
+  if (it != tables_.end()) return it->second;
+  if (capturing(s)) return nullptr;
+  std::vector<CUtensorMap> maps(n);
+  for (int i = 0; i < n; ++i)
+    if (tma_encode_grid(&maps[i], plane + grids[i].off, grids[i], bx, by, bl)) return nullptr;
+  return upload(maps, key);
+}
 
 void TmaCache::clear() {
   for (auto& kv : tables_) cudaFree(kv.second);
@@ -61,32 +121,16 @@ void TmaCache::clear() {
 const CUtensorMap* TmaCache::get(const Inst* h_inst, int n, const float* plane, int box_w,
                                  int box_h, cudaStream_t s) {
   if (!h_inst || n <= 0 || !plane) return nullptr;
-  const auto key = std::make_tuple(plane, box_w, box_h);
+  const auto key = std::make_tuple(plane, box_w, box_h, 0);
   auto it = tables_.find(key);
   if (it != tables_.end()) return it->second;
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
-    (void)cudaGetLastError();
-    return nullptr;  // no synchronous copies inside a capture: the caller stages itself
-  }
+  if (capturing(s)) return nullptr;
   std::vector<CUtensorMap> maps(n);
   for (int i = 0; i < n; ++i)
     if (tma_encode_plane(&maps[i], plane + h_inst[i].off, h_inst[i].w, h_inst[i].h,
                          h_inst[i].pitch, box_w, box_h))
       return nullptr;
-  CUtensorMap* d = nullptr;
-  if (cudaMalloc((void**)&d, sizeof(CUtensorMap) * n) != cudaSuccess) {
-    (void)cudaGetLastError();
-    return nullptr;
-  }
-  if (cudaMemcpy(d, maps.data(), sizeof(CUtensorMap) * n, cudaMemcpyHostToDevice) !=
-      cudaSuccess) {
-    (void)cudaGetLastError();
-    cudaFree(d);
-    return nullptr;
-  }
-  tables_[key] = d;
-  return d;
+  return upload(maps, key);
 }
 
 }  // namespace dtsgb
