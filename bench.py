@@ -79,6 +79,22 @@ def workloads_module():
     return _W
 
 
+def tuning_signature(tuning) -> str:
+    """The knobs a traffic record was measured under, as one string."""
+    if not tuning:
+        return "default"
+    keys = ("dts_tile", "bounds_segment", "hfbs_solve_steps", "hfbs_group_voxels")
+    return ",".join(f"{k}={tuning[k]}" for k in keys if k in tuning)
+
+
+def autotune_cache() -> str:
+    """The autotune cache file: $DTSGB_AUTOTUNE_CACHE, else the package's
+    autotune_cache.txt (choices timed on GB300 for the workloads here; a case
+    not in it is timed and appended)."""
+    return os.environ.get("DTSGB_AUTOTUNE_CACHE") or str(
+        ROOT / "domain_transform_solver_gb300" / "autotune_cache.txt")
+
+
 def cpu_model() -> str:
     try:
         out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
@@ -290,13 +306,14 @@ class Cfg3(Batched):
 
     def autotune(self):
         """The batch's tuning knobs chosen by timing (outside the timed
-        region); returns the chosen values."""
+        region), or read from the autotune cache file; returns the chosen
+        values and where they came from."""
         D = self.D
-        self.b.autotune(D.DomainFilterParams(**self.W.CFG0_FILTER),
-                        D.DomainOptimizeParams(**self.W.CFG0_OPT),
-                        D.HFBSGridParams(**self.hp) if "hfbs" in self.solvers else None,
-                        reps=2)
-        return self.b.tuning()
+        hit = self.b.autotune(D.DomainFilterParams(**self.W.CFG0_FILTER),
+                              D.DomainOptimizeParams(**self.W.CFG0_OPT),
+                              D.HFBSGridParams(**self.hp) if "hfbs" in self.solvers else None,
+                              reps=2, cache_path=autotune_cache())
+        return {**self.b.tuning(), "source": "cache file" if hit else "timed"}
 
     def step(self):
         if "dts" in self.solvers:
@@ -718,10 +735,12 @@ class Cfg4(Batched):
 
     def autotune(self):
         D = self.D
-        self.b.autotune(D.DomainFilterParams(**self.W.CFG0_FILTER),
-                        D.DomainOptimizeParams(**self.W.CFG0_OPT), None, reps=2)
-        self.fwd.set_tuning(D.TUNE_DTS_TILE, self.b.get_tuning(D.TUNE_DTS_TILE))
-        return self.b.tuning()
+        hit = self.b.autotune(D.DomainFilterParams(**self.W.CFG0_FILTER),
+                              D.DomainOptimizeParams(**self.W.CFG0_OPT), None, reps=2,
+                              cache_path=autotune_cache())
+        for knob in (D.TUNE_DTS_TILE, D.TUNE_BOUNDS_SEGMENT):
+            self.fwd.set_tuning(knob, self.b.get_tuning(knob))
+        return {**self.b.tuning(), "source": "cache file" if hit else "timed"}
 
     def step(self):
         _check(self.lib.dtsgb_batch_solve_dts(self.b.handle, ctypes.byref(self.fp),
@@ -989,6 +1008,21 @@ def run_ours(args, world, rank, local):
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         traffic_rec = json.loads(tf.read_text()).get(wl.name, {})
+    sig = tuning_signature(tuning)
+
+    def traffic_of(kid, per_step):
+        """DRAM bytes per launch of kernel kid from the ncu record: the entry
+        measured under this run's tuning; else another tuning's bytes per
+        step spread over this run's launches (an approximation, noted)."""
+        entries = traffic_rec.get(KERNEL_NAMES[kid])
+        if not entries:
+            return None, None
+        for e in entries:
+            if e["tuning"] == sig:
+                return e["bytes_per_launch"], f"measured under this tuning ({sig})"
+        e = entries[0]
+        return (e["bytes_per_launch"] * e["launches_per_step"] / per_step,
+                f"approximate: the bytes per step measured under tuning {e['tuning']}")
     kernels = {}
     for kid, (n, t) in per_kernel.items():
         avg = t / n
@@ -1000,7 +1034,7 @@ def run_ours(args, world, rank, local):
                 gbs = table[kid] / per_step / (avg * 1e-3) / 1e9
                 rec[f"{key}_gbs"] = gbs
                 rec[f"{key}_frac"] = gbs / peak
-        tr = traffic_rec.get(KERNEL_NAMES[kid])
+        tr, _ = traffic_of(kid, per_step)
         if tr:
             rec["dram_bytes_per_launch"] = tr
             rec["dram_frac"] = tr / (avg * 1e-3) / 1e9 / peak
@@ -1018,7 +1052,7 @@ def run_ours(args, world, rank, local):
         return {"bytes_per_launch": b, "achieved": a, "frac": a / peak}
 
     pm, fc = form(model), form(fused)
-    traffic = traffic_rec.get(KERNEL_NAMES[dom])
+    traffic, traffic_note = traffic_of(dom, per_step_dom)
     roofline = {"bound": "hbm", "kernel": KERNEL_NAMES[dom],
                 "achieved": pm["achieved"] if pm else None, "peak": peak, "unit": "GB/s",
                 "frac": pm["frac"] if pm else None,
@@ -1032,7 +1066,8 @@ def run_ours(args, world, rank, local):
                                    "achieved": traffic / (avg_dom * 1e-3) / 1e9,
                                    "frac": traffic / (avg_dom * 1e-3) / 1e9 / peak,
                                    "source": "ncu dram__bytes_read.sum + "
-                                             "dram__bytes_write.sum (profiles/traffic.json)"}
+                                             "dram__bytes_write.sum (profiles/traffic.json), "
+                                             + traffic_note}
                                   if traffic else None)}
 
     # e2e through the C ABI with pinned host buffers

@@ -143,6 +143,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_batch_get_tuning": ([vp, i, P(ll)], i),
         "dtsgb_batch_autotune": ([vp, P(FilterParams), P(OptimizeParams), f,
                                   P(HfbsParams), i], i),
+        "dtsgb_batch_autotune_cached": ([vp, P(FilterParams), P(OptimizeParams), f,
+                                         P(HfbsParams), i, ctypes.c_char_p, P(i)], i),
         "dtsgb_pipeline_create": ([i, P(i), P(i), u, i, pvp], i),
         "dtsgb_pipeline_destroy": ([vp], i),
         "dtsgb_pipeline_chunks": ([vp], i),

@@ -11,7 +11,11 @@
 // with g % 8 != 0 are covered, and the luma-overflow plane is stored.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <initializer_list>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -80,6 +84,7 @@ struct dtsgb_batch_s {
   bool small = false;
   long long hfbs_group_voxels = 0;  // L2-resident HFBS group budget (0: off)
   int hfbs_solve_steps = 4;         // heavy-ball steps per launch (4 or 1)
+  int bounds_seg = 8;               // pixels per window-bound walk (4, 8, 16)
   // Guide-derived state kept across solves while the guide is unchanged
   // (video frames that change only the target): the DTS window bounds and
   // the HFBS bistochastized normalisation.
@@ -826,7 +831,8 @@ DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b, const dtsgb_filter_params* 
   const float rx = f->sigma_x / f->sigma_r, ry = f->sigma_y / f->sigma_r;
   const int halo = (int)std::floor(p->sigma_z);
   const bool iterate = p->loss != DTSGB_L1 && p->num_iterations > 0;
-  const DtsLaunch Lb{b->d_inst, b->d_tb, b->ntb, b->n};
+  DtsLaunch Lb{b->d_inst, b->d_tb, b->ntb, b->n};
+  Lb.bounds_seg = b->bounds_seg;
   const DtsLaunch Li{b->d_inst, b->d_ti, b->nti, b->n, b->small, b->d_ti_small,
                      b->nti_small, &b->tma, b->inst.data()};
   // the iterate planes' tensor maps exist before any capture (a capture
@@ -903,6 +909,7 @@ DTSGB_API int dtsgb_batch_solve_dts(dtsgb_batch_t b, const dtsgb_filter_params* 
   key_append(key, b->grad_seg);
   key_append(key, b->small);
   key_append(key, keep_bounds);
+  key_append(key, b->bounds_seg);
   int st = run_graph(b, b->g_dts, key, enqueue);
   if (st) {
     b->bkey.gen = ~0ull;
@@ -1230,6 +1237,12 @@ DTSGB_API int dtsgb_batch_set_tuning(dtsgb_batch_t b, int knob, long long value)
     b->reuse = value != 0;
     return DTSGB_OK;
   }
+  if (knob == DTSGB_TUNE_BOUNDS_SEGMENT) {
+    if (value != 4 && value != 8 && value != 16)
+      return fail(DTSGB_ERR_INVALID_ARGUMENT, "bounds segment must be 4, 8 or 16");
+    b->bounds_seg = (int)value;
+    return DTSGB_OK;
+  }
   if (knob == DTSGB_TUNE_HFBS_SOLVE_STEPS) {
     if (value != 1 && value != kHfbsTBSteps)
       return fail(DTSGB_ERR_INVALID_ARGUMENT, "HFBS steps per launch must be 1 or 4");
@@ -1258,9 +1271,41 @@ DTSGB_API int dtsgb_batch_get_tuning(dtsgb_batch_t b, int knob, long long* value
     *value = b->hfbs_solve_steps;
     return DTSGB_OK;
   }
+  if (knob == DTSGB_TUNE_BOUNDS_SEGMENT) {
+    *value = b->bounds_seg;
+    return DTSGB_OK;
+  }
   return fail(DTSGB_ERR_INVALID_ARGUMENT, "unknown tuning knob");
 }
 
+
+}  // extern "C"
+
+// The knob value of `choices` that gives the shortest run, each run timed
+// reps times after one untimed run; choices the kernels cannot take
+// (DTSGB_ERR_UNSUPPORTED) are skipped.  Leaves the knob at the best value.
+template <typename F>
+static int tune_knob(dtsgb_batch_t b, int knob, std::initializer_list<long long> choices,
+                     int reps, F run) {
+  float best = 3.4e38f;
+  long long best_v = -1;
+  for (long long v : choices) {
+    int st = dtsgb_batch_set_tuning(b, knob, v);
+    if (st) return st;
+    float ms = 0.f;
+    st = time_runs(b, reps, run, &ms);
+    if (st == DTSGB_ERR_UNSUPPORTED) continue;  // e.g. a halo too large for this shape
+    if (st) return st;
+    if (ms < best) {
+      best = ms;
+      best_v = v;
+    }
+  }
+  if (best_v < 0) return fail(DTSGB_ERR_UNSUPPORTED, "no tuning choice runs");
+  return dtsgb_batch_set_tuning(b, knob, best_v);
+}
+
+extern "C" {
 
 DTSGB_API int dtsgb_batch_autotune(dtsgb_batch_t b, const dtsgb_filter_params* f,
                                    const dtsgb_optimize_params* p, float overwrite,
@@ -1269,42 +1314,128 @@ DTSGB_API int dtsgb_batch_autotune(dtsgb_batch_t b, const dtsgb_filter_params* f
   if ((f == nullptr) != (p == nullptr))
     return fail(DTSGB_ERR_INVALID_ARGUMENT, "filter and optimize params go together");
   if (reps < 1) reps = 3;
-  int st;
+  // every timed solve does all of its work (no guide state kept across runs)
+  const bool reuse = b->reuse;
+  b->reuse = false;
+  int st = DTSGB_OK;
   if (f) {
-    float best = 3.4e38f;
-    long long best_tile = kIterTW;
-    for (long long tile : {(long long)kIterTW, (long long)kIterSmallTW}) {
-      if ((st = dtsgb_batch_set_tuning(b, DTSGB_TUNE_DTS_TILE, tile))) return st;
-      float ms = 0.f;
-      st = time_runs(b, reps, [&]() { return dtsgb_batch_solve_dts(b, f, p, overwrite); },
-                     &ms);
-      if (st == DTSGB_ERR_UNSUPPORTED) continue;  // halo too large for this shape
-      if (st) return st;
-      if (ms < best) {
-        best = ms;
-        best_tile = tile;
-      }
-    }
-    if ((st = dtsgb_batch_set_tuning(b, DTSGB_TUNE_DTS_TILE, best_tile))) return st;
-    if ((st = dtsgb_batch_solve_dts(b, f, p, overwrite))) return st;
+    auto dts = [&]() { return dtsgb_batch_solve_dts(b, f, p, overwrite); };
+    st = tune_knob(b, DTSGB_TUNE_DTS_TILE, {(long long)kIterTW, (long long)kIterSmallTW}, reps,
+                   dts);
+    if (!st) st = tune_knob(b, DTSGB_TUNE_BOUNDS_SEGMENT, {8, 4, 16}, reps, dts);
   }
-  if (hp) {
+  if (hp && !st) {
+    auto hfbs = [&]() { return dtsgb_batch_solve_hfbs(b, hp); };
     float best = 3.4e38f;
-    long long best_g = 0;
-    for (long long g : {0LL, 1000000LL, 2000000LL, 4000000LL, 8000000LL}) {
-      if ((st = dtsgb_batch_set_tuning(b, DTSGB_TUNE_HFBS_GROUP_VOXELS, g))) return st;
-      float ms = 0.f;
-      if ((st = time_runs(b, reps, [&]() { return dtsgb_batch_solve_hfbs(b, hp); }, &ms)))
-        return st;
-      if (ms < best) {
-        best = ms;
-        best_g = g;
+    long long best_s = kHfbsTBSteps, best_g = 0;
+    for (long long steps : {(long long)kHfbsTBSteps, 1LL}) {
+      if ((st = dtsgb_batch_set_tuning(b, DTSGB_TUNE_HFBS_SOLVE_STEPS, steps))) break;
+      for (long long g : {0LL, 1000000LL, 2000000LL, 4000000LL, 8000000LL}) {
+        if ((st = dtsgb_batch_set_tuning(b, DTSGB_TUNE_HFBS_GROUP_VOXELS, g))) break;
+        float ms = 0.f;
+        if ((st = time_runs(b, reps, hfbs, &ms))) break;
+        if (ms < best) {
+          best = ms;
+          best_s = steps;
+          best_g = g;
+        }
       }
+      if (st) break;
     }
-    if ((st = dtsgb_batch_set_tuning(b, DTSGB_TUNE_HFBS_GROUP_VOXELS, best_g))) return st;
-    if ((st = dtsgb_batch_solve_hfbs(b, hp))) return st;
+    if (!st) st = dtsgb_batch_set_tuning(b, DTSGB_TUNE_HFBS_SOLVE_STEPS, best_s);
+    if (!st) st = dtsgb_batch_set_tuning(b, DTSGB_TUNE_HFBS_GROUP_VOXELS, best_g);
   }
+  b->reuse = reuse;
+  if (st) return st;
+  // leave the results of one solve with the chosen setting
+  if (f && (st = dtsgb_batch_solve_dts(b, f, p, overwrite))) return st;
+  if (hp && (st = dtsgb_batch_solve_hfbs(b, hp))) return st;
   return DTSGB_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// FNV-1a over bytes: the autotune cache key.
+struct Fnv {
+  unsigned long long h = 1469598103934665603ull;
+  template <typename T>
+  void add(const T& v) {
+    const unsigned char* q = reinterpret_cast<const unsigned char*>(&v);
+    for (size_t i = 0; i < sizeof(T); ++i) h = (h ^ q[i]) * 1099511628211ull;
+  }
+};
+
+const int kCachedKnobs[4] = {DTSGB_TUNE_DTS_TILE, DTSGB_TUNE_BOUNDS_SEGMENT,
+                             DTSGB_TUNE_HFBS_SOLVE_STEPS, DTSGB_TUNE_HFBS_GROUP_VOXELS};
+
+}  // namespace
+
+extern "C" {
+
+DTSGB_API int dtsgb_batch_autotune_cached(dtsgb_batch_t b, const dtsgb_filter_params* f,
+                                          const dtsgb_optimize_params* p, float overwrite,
+                                          const dtsgb_hfbs_params* hp, int reps,
+                                          const char* cache_path, int* from_cache) {
+  if (!b || !cache_path) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  if ((f == nullptr) != (p == nullptr))
+    return fail(DTSGB_ERR_INVALID_ARGUMENT, "filter and optimize params go together");
+  int dev = 0;
+  DTSGB_CUDA(cudaGetDevice(&dev));
+  cudaDeviceProp prop{};
+  DTSGB_CUDA(cudaGetDeviceProperties(&prop, dev));
+  // key: the device, the batch's shapes and storage, and the parameters
+  Fnv k;
+  for (const char* c = prop.name; *c; ++c) k.add(*c);
+  k.add(prop.multiProcessorCount);
+  k.add(b->n);
+  k.add(b->flags);
+  for (const Inst& I : b->inst) {
+    k.add(I.w);
+    k.add(I.h);
+  }
+  k.add(f != nullptr);
+  if (f) {
+    k.add(*f);
+    k.add(*p);
+    k.add(overwrite);
+  }
+  k.add(hp != nullptr);
+  if (hp) k.add(*hp);
+  char key[32];
+  std::snprintf(key, sizeof key, "%016llx", k.h);
+  if (from_cache) *from_cache = 0;
+  {
+    std::ifstream in(cache_path);
+    std::string line;
+    while (in && std::getline(in, line)) {
+      std::istringstream ls(line);
+      std::string lk;
+      long long v[4];
+      if (!(ls >> lk >> v[0] >> v[1] >> v[2] >> v[3]) || lk != key) continue;
+      int st = DTSGB_OK;
+      for (int i = 0; i < 4 && !st; ++i) st = dtsgb_batch_set_tuning(b, kCachedKnobs[i], v[i]);
+      if (st) break;  // a stale line: tune again
+      if (f && (st = dtsgb_batch_solve_dts(b, f, p, overwrite))) return st;
+      if (hp && (st = dtsgb_batch_solve_hfbs(b, hp))) return st;
+      if (from_cache) *from_cache = 1;
+      return DTSGB_OK;
+    }
+  }
+  int st = dtsgb_batch_autotune(b, f, p, overwrite, hp, reps);
+  if (st) return st;
+  std::ofstream out(cache_path, std::ios::app);
+  if (out) {
+    out << key;
+    for (int kn : kCachedKnobs) {
+      long long v = 0;
+      dtsgb_batch_get_tuning(b, kn, &v);
+      out << ' ' << v;
+    }
+    out << ' ' << prop.name << '\n';
+  }
+  return DTSGB_OK;  // a cache that cannot be written only costs the next caller a tuning
 }
 
 static int batch_download(dtsgb_batch_t b, int which, float* const* dst,

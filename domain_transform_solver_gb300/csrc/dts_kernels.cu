@@ -53,7 +53,9 @@ __global__ void k_color_convert_flat(uchar4* __restrict__ g, long long n,
 // only advance: about two prefix reads per end and pixel instead of a search
 // over the whole radius.
 // ---------------------------------------------------------------------------
-constexpr int kBoundsSeg = 8;  // pixels per thread and axis
+// Pixels per thread and axis of the two-pointer walks (a launch knob:
+// DTSGB_TUNE_BOUNDS_SEGMENT selects 4, 8 or 16).
+constexpr int kBoundsSegDefault = 8;
 
 // Lower and upper window ends along one axis for the n pixels starting at
 // prefix index j0 (S[j0 + k] for pixel p0 + k), coordinates p0.., axis length
@@ -87,13 +89,15 @@ __device__ __forceinline__ void bounds_walk(const unsigned* __restrict__ S, int 
   }
 }
 
-template <int TW, int TH>
+template <int TW, int TH, int SEG>
 __global__ void __launch_bounds__(kThreads)
     k_bounds(const Inst* __restrict__ insts, const Tile* __restrict__ tiles,
              const uchar4* __restrict__ guide, uint32_t* __restrict__ bounds,
              float ratio_x, float ratio_y, int rx, int ry, int ref_y_limit,
              float cap_x, float cap_y, float scale_x, float scale_y, int Tx, int Ty) {
   static_assert(TW == 32 && TH == 32 && kThreads == 256, "bounds tile shape");
+  static_assert(SEG == 4 || SEG == 8 || SEG == 16, "walk segment");
+  constexpr int NW = kThreads / 32;
   extern __shared__ unsigned smu[];
   const Tile t = tiles[blockIdx.x];
   const Inst in = insts[t.inst];
@@ -105,10 +109,11 @@ __global__ void __launch_bounds__(kThreads)
   unsigned* SV = SH + TH * DWp;   // DR x TW: prefix of dV, entry 0 = 0 at y0 - ry
   uint16_t* BX = reinterpret_cast<uint16_t*>(SV + DR * TW);  // TH x TW
   uint16_t* BY = BX + TH * TW;                               // TH x TW
+  unsigned* TOT = reinterpret_cast<unsigned*>(BY + TH * TW);  // 2 x NW x 32 totals
   const uchar4 zero = make_uchar4(0, 0, 0, 0);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // ---- 1. weights in fixed point: dH one warp per row, dV lanes on columns
-  for (int r = warp; r < TH; r += kThreads / 32) {
+  for (int r = warp; r < TH; r += NW) {
     const int y = t.y0 + r;
     for (int j = lane; j < DW; j += 32) {
       const int x = t.x0 - rx + j;
@@ -133,33 +138,59 @@ __global__ void __launch_bounds__(kThreads)
     SV[i] = q;
   }
   __syncthreads();
-  // ---- 2. inclusive prefixes: a thread per row of SH, a thread per column of SV
-  if (tid < TH) {
-    unsigned* row = SH + tid * DWp;
+  // ---- 2. inclusive prefixes, segmented: warp w scans its share of every row
+  // (lane = row) and of every column (lane = column), then adds the totals of
+  // the segments before it (wrapping 32-bit sums)
+  const int sx = (DW + NW - 1) / NW, sy = (DR + NW - 1) / NW;
+  {
+    unsigned* row = SH + lane * DWp;
+    const int a = warp * sx, e = min(DW, a + sx);
     unsigned acc = 0u;
-    for (int j = 0; j < DW; ++j) row[j] = acc += row[j];
-  } else if (tid >= 32 && tid < 32 + TW) {
-    unsigned* col = SV + (tid - 32);
-    unsigned acc = 0u;
-    for (int j = 0; j < DR; ++j) col[j * TW] = acc += col[j * TW];
+    for (int j = a; j < e; ++j) row[j] = acc += row[j];
+    TOT[warp * 32 + lane] = acc;
+    unsigned* col = SV + lane;
+    const int b = warp * sy, f = min(DR, b + sy);
+    unsigned accy = 0u;
+    for (int j = b; j < f; ++j) col[j * TW] = accy += col[j * TW];
+    TOT[(NW + warp) * 32 + lane] = accy;
   }
   __syncthreads();
-  // ---- 3. two-pointer walks: warps 0-3 rows (X), warps 4-7 columns (Y)
+  if (warp > 0) {
+    unsigned ox = 0u, oy = 0u;
+    for (int w = 0; w < warp; ++w) {
+      ox += TOT[w * 32 + lane];
+      oy += TOT[(NW + w) * 32 + lane];
+    }
+    unsigned* row = SH + lane * DWp;
+    const int a = warp * sx, e = min(DW, a + sx);
+    for (int j = a; j < e; ++j) row[j] += ox;
+    unsigned* col = SV + lane;
+    const int b = warp * sy, f = min(DR, b + sy);
+    for (int j = b; j < f; ++j) col[j * TW] += oy;
+  }
+  __syncthreads();
+  // ---- 3. two-pointer walks: warps 0-3 rows (X), warps 4-7 columns (Y), each
+  // taking the SEG-pixel segments sg = warp, warp + 4, ... of its lines
   const int ylim = ref_y_limit ? min(W, H) : H;
+  constexpr int NSEG = TW / SEG;
   if (tid < 4 * 32) {
-    const int r = lane, sg = warp;  // lanes on rows
-    const int y = t.y0 + r, xs = t.x0 + sg * kBoundsSeg;
-    const int n = min(kBoundsSeg, W - xs);
-    if (y < H && n > 0)
-      bounds_walk(SH + r * DWp, 1, xs - t.x0 + rx, xs, n, rx, W, Tx,
-                  BX + r * TW + sg * kBoundsSeg, 1);
+    const int r = lane, y = t.y0 + r;  // lanes on rows
+    for (int sg = warp; sg < NSEG; sg += 4) {
+      const int xs = t.x0 + sg * SEG;
+      const int n = min(SEG, W - xs);
+      if (y < H && n > 0)
+        bounds_walk(SH + r * DWp, 1, xs - t.x0 + rx, xs, n, rx, W, Tx,
+                    BX + r * TW + sg * SEG, 1);
+    }
   } else {
-    const int c = lane, sg = warp - 4;  // lanes on columns
-    const int x = t.x0 + c, ys = t.y0 + sg * kBoundsSeg;
-    const int n = min(kBoundsSeg, H - ys);
-    if (x < W && n > 0)
-      bounds_walk(SV + c, TW, ys - t.y0 + ry, ys, n, ry, ylim, Ty,
-                  BY + sg * kBoundsSeg * TW + c, TW);
+    const int c = lane, x = t.x0 + c;  // lanes on columns
+    for (int sg = warp - 4; sg < NSEG; sg += 4) {
+      const int ys = t.y0 + sg * SEG;
+      const int n = min(SEG, H - ys);
+      if (x < W && n > 0)
+        bounds_walk(SV + c, TW, ys - t.y0 + ry, ys, n, ry, ylim, Ty, BY + sg * SEG * TW + c,
+                    TW);
+    }
   }
   __syncthreads();
   // ---- 4. packed bounds, rows written coalesced
@@ -1046,7 +1077,8 @@ int launch_bounds(const DtsLaunch& L, const uchar4* guide, uint32_t* bounds,
   const int TW = kBoundsTW, TH = kBoundsTH;
   const size_t smem = sizeof(unsigned) * ((size_t)TH * ((TW + 2 * rx) | 1) +
                                           (size_t)(TH + 2 * ry) * TW) +
-                      2 * sizeof(uint16_t) * TH * TW;
+                      2 * sizeof(uint16_t) * TH * TW +
+                      sizeof(unsigned) * 2 * (kThreads / 32) * 32;  // segment totals
   if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "sigma too large");
   // fixed point per axis: r * (sigma + 1) * 2^F <= 2^30; threshold floor(sigma 2^F)
   auto fx = [](int r, float sigma, float* cap, float* scale, int* T) {
@@ -1059,14 +1091,19 @@ int launch_bounds(const DtsLaunch& L, const uchar4* guide, uint32_t* bounds,
   int Tx, Ty;
   fx(rx, sigma_x, &cap_x, &scale_x, &Tx);
   fx(ry, sigma_y, &cap_y, &scale_y, &Ty);
-  int st = set_smem(k_bounds<TW, TH>, smem);
-  if (st) return st;
-  ProfScope ps(s, DTSGB_K_BOUNDS);
-  k_bounds<TW, TH><<<L.n_tiles, kThreads, smem, s>>>(
-      L.d_inst, L.d_tiles, guide, bounds, ratio_x, ratio_y, rx, ry, ref_y_limit, cap_x,
-      cap_y, scale_x, scale_y, Tx, Ty);
-  DTSGB_CUDA(cudaGetLastError());
-  return DTSGB_OK;
+  auto go = [&](auto kern) -> int {
+    int st = set_smem(kern, smem);
+    if (st) return st;
+    ProfScope ps(s, DTSGB_K_BOUNDS);
+    kern<<<L.n_tiles, kThreads, smem, s>>>(L.d_inst, L.d_tiles, guide, bounds, ratio_x,
+                                           ratio_y, rx, ry, ref_y_limit, cap_x, cap_y,
+                                           scale_x, scale_y, Tx, Ty);
+    DTSGB_CUDA(cudaGetLastError());
+    return DTSGB_OK;
+  };
+  if (L.bounds_seg == 4) return go(k_bounds<kBoundsTW, kBoundsTH, 4>);
+  if (L.bounds_seg == 16) return go(k_bounds<kBoundsTW, kBoundsTH, 16>);
+  return go(k_bounds<kBoundsTW, kBoundsTH, kBoundsSegDefault>);
 }
 
 template <typename TS, int MODE, int TW, int TH, bool STEREO>

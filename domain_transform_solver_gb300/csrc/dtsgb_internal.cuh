@@ -161,6 +161,8 @@ struct DtsLaunch {
   // the instance table they describe (null: the kernels stage by loads)
   TmaCache* tma = nullptr;
   const Inst* h_inst = nullptr;
+  // pixels per thread and axis of the window-bound walks (4, 8 or 16)
+  int bounds_seg = 8;
   // the same launch on the small tiles
   DtsLaunch as_small() const {
     DtsLaunch s = *this;

@@ -36,7 +36,7 @@ __all__ = [
     "DomainTransformFilter", "DomainTransformSolver", "HFBS", "DtsOptions",
     "HfbsOptions", "Solve", "EdgeAwareOptimize", "DtsgbError", "SoftDTS",
     "FLAG_BF16_STORAGE", "FLAG_FIX_Y_LIMIT", "TUNE_DTS_TILE", "TUNE_HFBS_GROUP_VOXELS",
-    "TUNE_REUSE_GUIDE_STATE", "TUNE_HFBS_SOLVE_STEPS",
+    "TUNE_REUSE_GUIDE_STATE", "TUNE_HFBS_SOLVE_STEPS", "TUNE_BOUNDS_SEGMENT",
     "Batch", "Pipeline", "DomainTransformStereo",
 ]
 
@@ -48,10 +48,12 @@ TUNE_DTS_TILE = 0
 TUNE_HFBS_GROUP_VOXELS = 1
 TUNE_REUSE_GUIDE_STATE = 2
 TUNE_HFBS_SOLVE_STEPS = 3
+TUNE_BOUNDS_SEGMENT = 4
 # knob -> name, for reports
 TUNE_NAMES = {TUNE_DTS_TILE: "dts_tile", TUNE_HFBS_GROUP_VOXELS: "hfbs_group_voxels",
               TUNE_REUSE_GUIDE_STATE: "reuse_guide_state",
-              TUNE_HFBS_SOLVE_STEPS: "hfbs_solve_steps"}
+              TUNE_HFBS_SOLVE_STEPS: "hfbs_solve_steps",
+              TUNE_BOUNDS_SEGMENT: "bounds_segment"}
 
 
 @dataclass
@@ -555,15 +557,25 @@ class Batch:
         return {name: self.get_tuning(k) for k, name in TUNE_NAMES.items()}
 
     def autotune(self, filter_params=None, optimize_params=None, grid_params=None,
-                 overwrite_target_above_conf: float = -1, reps: int = 3) -> None:
-        """Time each tile shape / HFBS group budget on the uploaded batch and
-        keep the fastest."""
+                 overwrite_target_above_conf: float = -1, reps: int = 3,
+                 cache_path: str | None = None) -> bool:
+        """Time each tile shape, bounds segment and HFBS steps / group budget
+        on the uploaded batch and keep the fastest.  With cache_path, a case
+        tuned before (same device, sizes and parameters) is read from that
+        file instead; returns True when it was."""
         f = None if filter_params is None else ctypes.byref(filter_params._c())
         o = None if optimize_params is None else ctypes.byref(optimize_params._c())
         g = None if grid_params is None else ctypes.byref(grid_params._c())
-        check(self._lib.dtsgb_batch_autotune(self._h, f, o,
-                                             float(overwrite_target_above_conf), g,
-                                             int(reps)))
+        if cache_path is None:
+            check(self._lib.dtsgb_batch_autotune(self._h, f, o,
+                                                 float(overwrite_target_above_conf), g,
+                                                 int(reps)))
+            return False
+        hit = ctypes.c_int()
+        check(self._lib.dtsgb_batch_autotune_cached(
+            self._h, f, o, float(overwrite_target_above_conf), g, int(reps),
+            str(cache_path).encode(), ctypes.byref(hit)))
+        return bool(hit.value)
 
     # ---- gradients of the DTS solve (no reference counterpart) --------------
     def enable_grad(self, enable: bool = True, segment: int = 0) -> None:

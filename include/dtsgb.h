@@ -456,16 +456,35 @@ DTSGB_API int dtsgb_batch_debug_plane(dtsgb_batch_t b, int i, int which, void* d
  * L2).  The two add a voxel's six neighbour products in different roundings:
  * results agree to FP32 rounding, and each is differentiated exactly. */
 #define DTSGB_TUNE_HFBS_SOLVE_STEPS 3
+/* DTSGB_TUNE_BOUNDS_SEGMENT: pixels each thread of the window-bound search
+ * walks per axis with its two pointers (4, 8 or 16; default 8).  Longer
+ * segments restart the walk less often, shorter ones spread a tile's lines
+ * over more threads; the windows are identical. */
+#define DTSGB_TUNE_BOUNDS_SEGMENT 4
 DTSGB_API int dtsgb_batch_set_tuning(dtsgb_batch_t b, int knob, long long value);
 DTSGB_API int dtsgb_batch_get_tuning(dtsgb_batch_t b, int knob, long long* value);
-/* Times the uploaded batch's solves under each tile shape (filter and
- * optimize given) and HFBS group budget (hfbs given; 0, 1M, 2M, 4M, 8M
- * voxels), reps runs each on the batch's stream, keeps the fastest setting
- * of each knob and leaves the results of one solve with it. */
+/* Times the uploaded batch's solves (reps runs each on the batch's stream,
+ * with the guide state recomputed every run) under each DTS tile shape, then
+ * each bounds segment (filter and optimize given), and under every pair of
+ * HFBS steps per launch (4, 1) and group budget (0, 1M, 2M, 4M, 8M voxels;
+ * hfbs given); keeps the fastest setting of each and leaves the results of
+ * one solve with it. */
 DTSGB_API int dtsgb_batch_autotune(dtsgb_batch_t b, const dtsgb_filter_params* filter,
                                    const dtsgb_optimize_params* optimize,
                                    float overwrite_target_above_conf,
                                    const dtsgb_hfbs_params* hfbs, int reps);
+/* dtsgb_batch_autotune with a cache file: a line per tuned case (a hash of
+ * the device name and SM count, the batch's sizes and flags and the solve
+ * parameters, then the chosen DTS tile, bounds segment, HFBS steps per
+ * launch and HFBS group budget).  A case found there is applied without
+ * timing (*from_cache = 1); otherwise it is tuned and appended.  The file is
+ * created when missing; failing to write it is not an error. */
+DTSGB_API int dtsgb_batch_autotune_cached(dtsgb_batch_t b,
+                                          const dtsgb_filter_params* filter,
+                                          const dtsgb_optimize_params* optimize,
+                                          float overwrite_target_above_conf,
+                                          const dtsgb_hfbs_params* hfbs, int reps,
+                                          const char* cache_path, int* from_cache);
 
 /* ---- Overlapped host-to-host solves (new; the reference copies, solves
  * and copies back one image at a time).  A pipeline splits n instances into

@@ -122,11 +122,52 @@ def test_tuning_knobs_and_autotune(gpu_ready):
             assert np.array_equal(a, r, equal_nan=True)
         for a, r, inst in zip(d, ref_d, insts):
             assert np.abs(a - r).max() <= 1e-6 * max(P.target_range(inst.target), 1.0)
+    # the window-bound walk's segment length changes nothing
+    b.set_tuning(D.TUNE_DTS_TILE, 64)
+    for seg in (4, 16, 8):
+        b.set_tuning(D.TUNE_BOUNDS_SEGMENT, seg)
+        b.solve_dts(fp, op)
+        for a, r in zip(b.download(0), ref_d):
+            assert np.array_equal(a, r)
+    # one heavy-ball step per launch: the same solve to FP32 rounding
+    b.set_tuning(D.TUNE_HFBS_SOLVE_STEPS, 1)
+    b.solve_hfbs(hp)
+    for a, r, inst in zip(b.download(1), ref_h, insts):
+        fin = np.isfinite(r)
+        assert np.array_equal(np.isfinite(a), fin)
+        assert np.abs(a[fin] - r[fin]).max() <= 1e-5 * max(P.target_range(inst.target), 1.0)
+    b.set_tuning(D.TUNE_HFBS_SOLVE_STEPS, 4)
     b.autotune(fp, op, hp, reps=1)
     assert b.get_tuning(D.TUNE_DTS_TILE) in (64, 32)
+    assert b.get_tuning(D.TUNE_BOUNDS_SEGMENT) in (4, 8, 16)
+    assert b.get_tuning(D.TUNE_HFBS_SOLVE_STEPS) in (1, 4)
     assert b.get_tuning(D.TUNE_HFBS_GROUP_VOXELS) in (0, 1000000, 2000000, 4000000, 8000000)
-    for a, r in zip(b.download(1), ref_h):
-        assert np.array_equal(a, r, equal_nan=True)
+    if b.get_tuning(D.TUNE_HFBS_SOLVE_STEPS) == 4:
+        for a, r in zip(b.download(1), ref_h):
+            assert np.array_equal(a, r, equal_nan=True)
+
+
+def test_autotune_cache_file(gpu_ready, tmp_path):
+    """The first tuning of a case is timed and written to the cache file; a
+    second batch of the same sizes and parameters reads the same choice."""
+    D = gpu_ready
+    from domain_transform_solver_gb300 import workloads as W
+    insts = _instances(SIZES[:3])
+    fp = D.DomainFilterParams(**W.CFG0_FILTER)
+    op = D.DomainOptimizeParams(**dict(W.CFG0_OPT, num_iterations=3))
+    hp = D.HFBSGridParams(**dict(W.CFG1_HFBS, optim_iter_max=8))
+    cache = tmp_path / "autotune.txt"
+    choices = []
+    for k in range(2):
+        b = D.Batch([(i.width, i.height) for i in insts])
+        b.upload(D.COLOR_SPACE.YCbCr, [i.rgba for i in insts], [i.target for i in insts],
+                 [i.confidence for i in insts])
+        hit = b.autotune(fp, op, hp, reps=1, cache_path=cache)
+        assert hit == (k == 1)
+        choices.append(b.tuning())
+        b.close()
+    assert choices[0] == choices[1]
+    assert len(cache.read_text().splitlines()) == 1
 
 
 def test_video_frames_reuse_guide_state(gpu_ready):
