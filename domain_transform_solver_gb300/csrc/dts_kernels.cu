@@ -451,8 +451,22 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   Quad QA, QB;
   fetch(r3, QA);
   __syncthreads();  // smax initialised
+  // A non-finite value in the staged box (or among the X results) has no
+  // fixed-point form: the tile's outputs are then NaN, as every pixel of it
+  // can reach that value within the iteration (the reference's float prefix
+  // sums carry it along rows and columns likewise).  Never finite garbage.
+  auto poison = [&]() {
+    if (x3 >= W) return;
+    const int jmax = min(TH, H - t.y0);
+    for (int j = r3; j < jmax; j += RPP) {
+      float* dst = vout_i + (t.y0 + j) * P + x3;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (x3 + k < W) dst[k] = __int_as_float(0x7fc00000);
+    }
+  };
   // ---- 1. stage the iterate, four columns per item, four items in flight -------
-  float m = 0.f;
+  unsigned mb = 0u;  // magnitude bits (mag_bits)
   if (use_tma) {
     // every thread waits for the box; a CTA whose wait ran out (all of its
     // threads agree through the barrier) records it and leaves its tile
@@ -467,7 +481,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
     for (int i = tid; i < n; i += NT) {
       const int r = fast_div(i, mg), q = i - r * SW4;
       const float4 v = *reinterpret_cast<const float4*>(Xf + r * SWS + 4 * q);
-      m = fmaxf(m, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+      mb = max(mb, max(max(mag_bits(v.x), mag_bits(v.y)), max(mag_bits(v.z), mag_bits(v.w))));
     }
   } else {
     constexpr int U = 4;
@@ -494,14 +508,18 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         if (dst[u] >= 0) *reinterpret_cast<float4*>(Xf + dst[u]) = v[u];
-        m = fmaxf(m, fmaxf(fmaxf(fabsf(v[u].x), fabsf(v[u].y)),
-                           fmaxf(fabsf(v[u].z), fabsf(v[u].w))));
+        mb = max(mb, max(max(mag_bits(v[u].x), mag_bits(v[u].y)),
+                         max(mag_bits(v[u].z), mag_bits(v[u].w))));
       }
     }
   }
-  m = warp_max_nonneg(m);
-  if (lane == 0) atomicMax(&smax[0], __float_as_uint(m));
+  mb = __reduce_max_sync(0xffffffffu, mb);
+  if (lane == 0) atomicMax(&smax[0], mb);
   __syncthreads();
+  if (smax[0] >= kNonFiniteBits) {
+    poison();
+    return;
+  }
   // ---- 2. X prefix: a thread per 16-entry segment of a row, then offsets -------
   {
     const float sF = pow2f(fx_shift(__uint_as_float(smax[0]), lgx));
@@ -553,7 +571,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
   __syncthreads();
   // ---- 3. X half-step for the tile columns over all rows -----------------------
   {
-    float mloc = 0.f;
+    unsigned mloc = 0u;  // magnitude bits of the X results
     auto compute = [&](int r, const Quad& Q) {
       const unsigned* e0 = XP + r * SWS + HA + 4 * cq;  // e0[k]: prefix at x3 + k
       float o[4];
@@ -574,7 +592,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
           o[k] = x_update<MODE, STEREO>(vv, B, tv, cv, rn, lambda, step, extra);
           if (over && cv > overwrite) o[k] = tv;
         }
-        mloc = fmaxf(mloc, fabsf(o[k]));
+        mloc = max(mloc, mag_bits(o[k]));
       }
       *reinterpret_cast<float4*>(sx + r * TQ + 4 * cq) = make_float4(o[0], o[1], o[2], o[3]);
       // the Y bytes (b >> 16) of the four pixels as four u16
@@ -591,10 +609,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
       compute(r, QB);
       r += RPP;
     }
-    mloc = warp_max_nonneg(mloc);
-    if (lane == 0) atomicMax(&smax[1], __float_as_uint(mloc));
+    mloc = __reduce_max_sync(0xffffffffu, mloc);
+    if (lane == 0) atomicMax(&smax[1], mloc);
   }
   __syncthreads();
+  if (smax[1] >= kNonFiniteBits) {
+    poison();
+    return;
+  }
   // ---- 4. Y prefix: a warp per group of four columns, a lane per segment ---------
   const int Fy = fx_shift(__uint_as_float(smax[1]), lgy);
   const float sFy = pow2f(Fy), isFy = pow2f(-Fy);
@@ -754,7 +776,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
       }
     }
   };
-  float mloc = 0.f;
+  unsigned mloc = 0u;  // magnitude bits of the X results
   unsigned* xb = Xb + warp * SWX;
   RowIn cur, nxt;
   if (warp < SR) fetch(warp, cur);
@@ -763,12 +785,15 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
     const int y = gy0 + r;
     const bool yok = (unsigned)y < (unsigned)H;
     const long long row = in.off + (long long)y * P;
-    float m = fmaxf(fmaxf(fabsf(cur.v4[0]), fabsf(cur.v4[1])),
-                    fmaxf(fabsf(cur.v4[2]), fabsf(cur.v4[3])));
+    unsigned mb = max(max(mag_bits(cur.v4[0]), mag_bits(cur.v4[1])),
+                      max(mag_bits(cur.v4[2]), mag_bits(cur.v4[3])));
     for (int base = 128; base < SWX; base += 128)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) m = fmaxf(m, fabsf(load_v(yok, row, base + 4 * lane + j)));
-    const int F = fx_shift(warp_max_nonneg(m), lgx);
+      for (int j = 0; j < 4; ++j) mb = max(mb, mag_bits(load_v(yok, row, base + 4 * lane + j)));
+    mb = __reduce_max_sync(0xffffffffu, mb);
+    // a non-finite value in the row: its X results are NaN (see below)
+    const bool row_bad = mb >= kNonFiniteBits;
+    const int F = fx_shift(__uint_as_float(row_bad ? 0u : mb), lgx);
     const float sF = pow2f(F), isF = pow2f(-F);
     unsigned carry = 0;
     for (int base = 0; base < SWX; base += 128) {
@@ -807,17 +832,27 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
         if (STEREO) extra = photometric(sa, row, x, W, v);
         o = x_update<MODE, STEREO>(v, B, tv, cv, rn, lambda, step, extra);
         if (over && cv > overwrite) o = tv;
+        if (row_bad) o = __int_as_float(0x7fc00000);
         if (r >= hy && r < hy + TH) sby[(r - hy) * TW + c] = (uint16_t)(b >> 16);
       }
       sx[r * TWp + c] = o;
-      mloc = fmaxf(mloc, fabsf(o));
+      mloc = max(mloc, mag_bits(o));
     }
     __syncwarp();  // the warp's prefix buffer is rewritten for its next row
     cur = nxt;
   }
-  mloc = warp_max_nonneg(mloc);
-  if (lane == 0) atomicMax(smax, __float_as_uint(mloc));
+  mloc = __reduce_max_sync(0xffffffffu, mloc);
+  if (lane == 0) atomicMax(smax, mloc);
   __syncthreads();
+  if (*smax >= kNonFiniteBits) {
+    // a non-finite value reached the X results: the tile's outputs are NaN
+    // (every pixel of it can reach that value), never finite garbage
+    const int x = t.x0 + tid % TW;
+    for (int j = tid / TW; j < TH; j += NT / TW)
+      if (t.y0 + j < H && x < W)
+        vout[in.off + (long long)(t.y0 + j) * P + x] = __int_as_float(0x7fc00000);
+    return;
+  }
   // ---- Y half-step ----------------------------------------------------------
   const int Fy = fx_shift(__uint_as_float(*smax), lgy);
   const float sFy = pow2f(Fy), isFy = pow2f(-Fy);

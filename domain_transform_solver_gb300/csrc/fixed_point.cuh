@@ -53,6 +53,15 @@ __device__ __forceinline__ unsigned warp_incl_scan(unsigned v, int lane) {
   return v;
 }
 
+// Bits of |v|: they order like the magnitude, and every infinity or NaN
+// lies at or above kNonFiniteBits, so an integer max over them both finds the
+// fixed-point scale and flags a non-finite value (a float max would skip a
+// NaN, whose conversion to fixed point is then undefined).
+__device__ __forceinline__ unsigned mag_bits(float v) {
+  return __float_as_uint(v) & 0x7fffffffu;
+}
+constexpr unsigned kNonFiniteBits = 0x7f800000u;
+
 // Largest of a non-negative float over the warp (all lanes active).
 __device__ __forceinline__ float warp_max_nonneg(float m) {
   return __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(m)));
