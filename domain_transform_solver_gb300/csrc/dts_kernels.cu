@@ -109,64 +109,60 @@ __global__ void __launch_bounds__(kThreads)
   unsigned* SV = SH + TH * DWp;   // DR x TW: prefix of dV, entry 0 = 0 at y0 - ry
   uint16_t* BX = reinterpret_cast<uint16_t*>(SV + DR * TW);  // TH x TW
   uint16_t* BY = BX + TH * TW;                               // TH x TW
-  unsigned* TOT = reinterpret_cast<unsigned*>(BY + TH * TW);  // 2 x NW x 32 totals
-  const uchar4 zero = make_uchar4(0, 0, 0, 0);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // ---- 1. weights in fixed point: dH one warp per row, dV lanes on columns
+  // ---- 1. weights in fixed point.  dH: a warp per row, lanes on columns; a
+  // lane's left neighbour comes from the lane before it (one load per pixel).
+  // dV: eight threads per column, each down a run of rows, the pixel above
+  // carried in a register.  Pixels outside the image read as zero.
+  auto load_g = [&](int x, int y) -> unsigned {
+    return (x >= 0 && x < W && y >= 0 && y < H)
+               ? *reinterpret_cast<const unsigned*>(g + (long long)y * P + x)
+               : 0u;
+  };
+  auto as_px = [](unsigned v) { return *reinterpret_cast<const uchar4*>(&v); };
   for (int r = warp; r < TH; r += NW) {
     const int y = t.y0 + r;
-    for (int j = lane; j < DW; j += 32) {
-      const int x = t.x0 - rx + j;
+    for (int j0 = 0; j0 < DW; j0 += 32) {
+      const int j = j0 + lane, x = t.x0 - rx + j;
+      const unsigned cur = j < DW ? load_g(x, y) : 0u;
+      unsigned prev = __shfl_up_sync(0xffffffffu, cur, 1);
+      if (lane == 0) prev = load_g(x - 1, y);
       unsigned q = 0u;
-      if (j > 0 && x >= 0 && x < W && y < H && ratio_x >= 0.f) {
-        const uchar4 cur = g[y * P + x];
-        const uchar4 prev = x > 0 ? g[y * P + x - 1] : zero;
-        q = (unsigned)__float2int_rn(fminf(edge_weight(cur, prev, ratio_x), cap_x) * scale_x);
-      }
-      SH[r * DWp + j] = q;
+      if (j > 0 && x >= 0 && x < W && y < H && ratio_x >= 0.f)
+        q = (unsigned)__float2int_rn(
+            fminf(edge_weight(as_px(cur), as_px(prev), ratio_x), cap_x) * scale_x);
+      if (j < DW) SH[r * DWp + j] = q;
     }
   }
-  for (int i = tid; i < DR * TW; i += kThreads) {
-    const int j = i / TW, c = i % TW;
-    const int x = t.x0 + c, y = t.y0 - ry + j;
-    unsigned q = 0u;
-    if (j > 0 && x < W && y >= 0 && y < H && ratio_y >= 0.f) {
-      const uchar4 cur = g[y * P + x];
-      const uchar4 prev = y > 0 ? g[(y - 1) * P + x] : zero;
-      q = (unsigned)__float2int_rn(fminf(edge_weight(cur, prev, ratio_y), cap_y) * scale_y);
-    }
-    SV[i] = q;
-  }
-  __syncthreads();
-  // ---- 2. inclusive prefixes, segmented: warp w scans its share of every row
-  // (lane = row) and of every column (lane = column), then adds the totals of
-  // the segments before it (wrapping 32-bit sums)
-  const int sx = (DW + NW - 1) / NW, sy = (DR + NW - 1) / NW;
   {
-    unsigned* row = SH + lane * DWp;
-    const int a = warp * sx, e = min(DW, a + sx);
-    unsigned acc = 0u;
-    for (int j = a; j < e; ++j) row[j] = acc += row[j];
-    TOT[warp * 32 + lane] = acc;
-    unsigned* col = SV + lane;
-    const int b = warp * sy, f = min(DR, b + sy);
-    unsigned accy = 0u;
-    for (int j = b; j < f; ++j) col[j * TW] = accy += col[j * TW];
-    TOT[(NW + warp) * 32 + lane] = accy;
+    const int c = tid % TW, sgi = tid / TW, nsg = kThreads / TW;
+    const int seg = (DR + nsg - 1) / nsg;
+    const int j0 = sgi * seg, j1 = min(DR, j0 + seg);
+    const int x = t.x0 + c;
+    unsigned prev = load_g(x, t.y0 - ry + j0 - 1);
+    for (int j = j0; j < j1; ++j) {
+      const int y = t.y0 - ry + j;
+      const unsigned cur = load_g(x, y);
+      unsigned q = 0u;
+      if (j > 0 && x < W && y >= 0 && y < H && ratio_y >= 0.f)
+        q = (unsigned)__float2int_rn(
+            fminf(edge_weight(as_px(cur), as_px(prev), ratio_y), cap_y) * scale_y);
+      SV[j * TW + c] = q;
+      prev = cur;
+    }
   }
   __syncthreads();
-  if (warp > 0) {
-    unsigned ox = 0u, oy = 0u;
-    for (int w = 0; w < warp; ++w) {
-      ox += TOT[w * 32 + lane];
-      oy += TOT[(NW + w) * 32 + lane];
-    }
-    unsigned* row = SH + lane * DWp;
-    const int a = warp * sx, e = min(DW, a + sx);
-    for (int j = a; j < e; ++j) row[j] += ox;
-    unsigned* col = SV + lane;
-    const int b = warp * sy, f = min(DR, b + sy);
-    for (int j = b; j < f; ++j) col[j * TW] += oy;
+  // ---- 2. inclusive prefixes: a thread per row of SH, a thread per column of SV
+  // (a segmented scan over all warps was slower: its extra pass costs more
+  // issue slots than the serial chains, which the other resident blocks hide)
+  if (tid < TH) {
+    unsigned* row = SH + tid * DWp;
+    unsigned acc = 0u;
+    for (int j = 0; j < DW; ++j) row[j] = acc += row[j];
+  } else if (tid >= 32 && tid < 32 + TW) {
+    unsigned* col = SV + (tid - 32);
+    unsigned acc = 0u;
+    for (int j = 0; j < DR; ++j) col[j * TW] = acc += col[j * TW];
   }
   __syncthreads();
   // ---- 3. two-pointer walks: warps 0-3 rows (X), warps 4-7 columns (Y), each
@@ -1112,8 +1108,7 @@ int launch_bounds(const DtsLaunch& L, const uchar4* guide, uint32_t* bounds,
   const int TW = kBoundsTW, TH = kBoundsTH;
   const size_t smem = sizeof(unsigned) * ((size_t)TH * ((TW + 2 * rx) | 1) +
                                           (size_t)(TH + 2 * ry) * TW) +
-                      2 * sizeof(uint16_t) * TH * TW +
-                      sizeof(unsigned) * 2 * (kThreads / 32) * 32;  // segment totals
+                      2 * sizeof(uint16_t) * TH * TW;
   if (smem > kMaxSmem) return fail(DTSGB_ERR_UNSUPPORTED, "sigma too large");
   // fixed point per axis: r * (sigma + 1) * 2^F <= 2^30; threshold floor(sigma 2^F)
   auto fx = [](int r, float sigma, float* cap, float* scale, int* T) {

@@ -41,10 +41,12 @@ __host__ __device__ inline uint32_t pack_bounds(int dlx, int dux, int dly,
 // sqrt(SSD4(a - b) * kINV255Sq * r * r + 1) with r = sigma_{x|y} / sigma_r
 // and kINV255Sq the float constant 0.0000153787 (:10), evaluated in the
 // order nvcc compiles the reference expression.  >= 1 for every input.
+// The sum of squared channel differences is exact integer arithmetic: the
+// four |a - b| bytes (one SIMD byte instruction) dotted with themselves.
 __device__ __forceinline__ float edge_weight(uchar4 a, uchar4 b, float ratio) {
-  const int d0 = (int)a.x - (int)b.x, d1 = (int)a.y - (int)b.y;
-  const int d2 = (int)a.z - (int)b.z, d3 = (int)a.w - (int)b.w;
-  const float ssd = (float)(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3);
+  const unsigned d = __vabsdiffu4(*reinterpret_cast<const unsigned*>(&a),
+                                  *reinterpret_cast<const unsigned*>(&b));
+  const float ssd = (float)__dp4a(d, d, 0u);
   float t = __fmul_rn(ssd, (float)0.0000153787);
   t = __fmul_rn(t, ratio);
   return __fsqrt_rn(__fmaf_rn(t, ratio, 1.0f));
