@@ -1,7 +1,7 @@
 """Benchmark of the DTS / HFBS hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg3|cfg3dts|cfg0|cfg1|cfg2|cfg4|cfg1grad]
+                    [--workload cfg3|cfg3dts|cfg0|cfg1|cfg2|cfg4|cfg1grad|cfg4soft]
 
 One JSON line on stdout (rank 0).  A step is one pass of the workload's
 solves with inputs already resident in HBM: for DTS the reference's timed
@@ -51,7 +51,7 @@ L2_FLUSH_BYTES = 256 << 20
 KERNEL_NAMES = {0: "k_bounds", 1: "k_dts_iter", 2: "k_filter", 3: "k_splat",
                 4: "k_bistoch", 5: "k_solve (HFBS heavy-ball)", 6: "hfbs setup kernels",
                 7: "k_slice", 8: "k_to_float", 9: "k_dts_adjoint",
-                10: "hfbs adjoint (whole backward)"}
+                10: "hfbs adjoint (whole backward)", 11: "soft-window kernels"}
 HFBS_TB_STEPS = 4  # heavy-ball steps per launch of the temporally blocked kernel
 
 
@@ -383,9 +383,9 @@ class Cfg3(Batched):
         what = " + ".join(s.upper() for s in self.solvers)
         if subset is None or len(idx) == len(self.insts):
             return px, f"all {len(self.insts)} instances, {what} each"
-        return px, (f"{len(idx)} of the {len(self.insts)} instances (every "
-                    f"{max(1, round(len(self.insts) / max(1, len(idx))))}th by pixel "
-                    f"count), {what} each")
+        step = max(1, round(len(self.insts) / max(1, len(idx))))
+        return px, (f"{len(idx)} of the {len(self.insts)} instances (one in "
+                    f"{step} by pixel count), {what} each")
 
 
 class Cfg3Dts(Cfg3):
@@ -803,8 +803,117 @@ class Cfg4(Batched):
         return px, f"{len(idx)} of the {len(self.insts)} instances, forward + adjoint"
 
 
+class Cfg4Soft(Batched):
+    """Config 4 with gradients with respect to the guide-derived edge
+    weights: 16 x 1024x768, FP32, L2, 10 iterations of the soft-window solve
+    (window ends ramped over tau = 1 transformed-domain unit around sigma_z)
+    from the guides' edge weights dH, dV, plus its adjoint dL/dtarget,
+    dL/dconfidence, dL/ddH, dL/ddV for an N(0,1) upstream gradient.  One
+    step = forward + backward (every iterate kept)."""
+
+    name = "cfg4soft_dts_soft_window_fwd_bwd_16x1024x768_f32"
+    dtype = "f32"
+    tau = 1.0
+
+    def __init__(self, rank: int = 0, world: int = 1):
+        W = workloads_module()
+        self.W = W
+        n, w, h = 16, 1024, 768
+        self.n_total = n
+        if world > 1:
+            from domain_transform_solver_gb300.sharding import partition_lpt
+            share = partition_lpt([(w, h)] * n, world)[rank]
+        else:
+            share = list(range(n))
+        self.insts, self.grads = W.grad_instances(indices=share)
+        self.sizes = [(i.width, i.height) for i in self.insts]
+        self.pixels = sum(a * b for a, b in self.sizes)
+        self.total_pixels = n * w * h
+        self.iters = W.CFG0_OPT["num_iterations"]
+        self.voxels = self.total_voxels = 0
+
+    def setup(self, stream_handle: int):
+        import torch
+        import domain_transform_solver_gb300 as D
+        W = self.W
+        dev = torch.device("cuda")
+        n = len(self.sizes)
+        h, w = self.insts[0].target.shape
+        self.s = D.SoftDTS(self.sizes)
+        self.s.set_stream(stream_handle)
+        self.op = D.DomainOptimizeParams(**W.CFG0_OPT)
+        self.rgba = torch.from_numpy(np.stack([i.rgba for i in self.insts])).to(dev)
+        self.t = torch.from_numpy(np.stack([i.target for i in self.insts])).to(dev)
+        self.c = torch.from_numpy(np.stack([i.confidence for i in self.insts])).to(dev)
+        self.g = torch.from_numpy(np.stack(self.grads)).to(dev)
+        self.dh = torch.empty_like(self.t)
+        self.dv = torch.empty_like(self.t)
+        self.out = torch.empty_like(self.t)
+        self.grad_planes = [torch.empty_like(self.t) for _ in range(4)]
+        p = lambda x: [x[i].data_ptr() for i in range(n)]  # noqa: E731
+        self.p = p
+        self.s.edge_weights(D.COLOR_SPACE.YCbCr, p(self.rgba), D.DomainFilterParams(**W.CFG0_FILTER),
+                            p(self.dh), p(self.dv))
+        # pinned host copies for the end-to-end form
+        self.h_in = [_pinned_copy(a.cpu().numpy()) for a in (self.dh, self.dv, self.t, self.c,
+                                                             self.g)]
+        self.h_out = [_pinned_empty((n, h, w)) for _ in range(5)]
+        self.e2e_api = "dtsgb_soft_solve, dtsgb_soft_backward (device buffers filled from pinned host memory)"
+        torch.cuda.synchronize()
+
+    def _solve(self):
+        p = self.p
+        self.s.solve(p(self.dh), p(self.dv), p(self.t), p(self.c), self.op, self.tau, p(self.out))
+
+    def step(self):
+        p = self.p
+        self._solve()
+        self.s.backward(p(self.g), *[p(x) for x in self.grad_planes])
+
+    def forward_only(self):
+        self._solve()
+
+    def step_e2e(self):
+        import torch
+        for dst, src in zip((self.dh, self.dv, self.t, self.c, self.g), self.h_in):
+            dst.copy_(torch.from_numpy(src), non_blocking=True)
+        self.step()
+        for dst, src in zip(self.h_out, [self.out] + self.grad_planes):
+            torch.from_numpy(dst).copy_(src, non_blocking=True)
+
+    def e2e_bytes(self):
+        return self.pixels * 20, self.pixels * 20
+
+    def fused_bytes(self):
+        return {}
+
+    def pass_model_bytes(self):
+        return {}
+
+    def reference_subset(self):
+        return [0]  # the oracle's soft adjoint is serial: one instance per step
+
+    def cpu_sizes(self):
+        return self.sizes
+
+    def cpu_sample(self, real="f32", subset=None):
+        """The soft-window forward + adjoint restated by the oracle (FP32
+        build), from the oracle's own edge weights."""
+        import oracle as O
+        W = self.W
+        idx = range(len(self.insts)) if subset is None else subset
+        px = 0
+        for i in idx:
+            inst, g = self.insts[i], self.grads[i]
+            eh, ev = O.edge_weights(inst.rgba, 1, real=real, **W.CFG0_FILTER)
+            O.soft_backward(eh, ev, inst.target, inst.confidence, W.CFG0_OPT, self.tau, g,
+                            real=real)
+            px += inst.width * inst.height
+        return px, f"{len(idx)} of the {len(self.insts)} instances, forward + adjoint"
+
+
 WORKLOADS = {"cfg3": Cfg3, "cfg3dts": Cfg3Dts, "cfg0": Cfg0, "cfg1": Cfg1, "cfg2": Cfg2,
-             "cfg4": Cfg4, "cfg1grad": Cfg1Grad}
+             "cfg4": Cfg4, "cfg1grad": Cfg1Grad, "cfg4soft": Cfg4Soft}
 
 
 # ---- arms ----------------------------------------------------------------------

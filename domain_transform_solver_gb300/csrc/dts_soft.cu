@@ -49,6 +49,14 @@ namespace {
 
 constexpr int kST = 256;
 
+// Launches of this file's kernels, timed by the library's profiler as one
+// kind (DTSGB_K_SOFT) when it is on.
+#define SOFT_LAUNCH(kernel, grid, stream, ...)            \
+  do {                                                    \
+    ProfScope ps_((stream), DTSGB_K_SOFT);                \
+    kernel<<<(grid), kST, 0, (stream)>>>(__VA_ARGS__);    \
+  } while (0)
+
 struct SInst {
   int w, h;
   long long off;  // element offset of pixel (0,0); rows dense (pitch = w)
@@ -441,10 +449,10 @@ DTSGB_API int dtsgb_soft_solve(dtsgb_soft_t s, const float* const* dH, const flo
   const dim3 g = soft_grid(s);
   const int mode = p->loss == DTSGB_L2 ? 0 : 1;
   for (int k = 0; k < N; ++k) {
-    k_soft_half<<<g, kST, 0, s->stream>>>(s->d_inst, s->plane(P_ITER + k), s->plane(P_U),
+    SOFT_LAUNCH(k_soft_half, g, s->stream, s->d_inst, s->plane(P_ITER + k), s->plane(P_U),
                                           s->plane(P_EH), s->plane(P_T), s->plane(P_C), 0,
                                           1, mode, p->sigma_z, tau, p->lambda, p->step_size);
-    k_soft_half<<<g, kST, 0, s->stream>>>(s->d_inst, s->plane(P_U), s->plane(P_ITER + k + 1),
+    SOFT_LAUNCH(k_soft_half, g, s->stream, s->d_inst, s->plane(P_U), s->plane(P_ITER + k + 1),
                                           s->plane(P_EV), nullptr, nullptr, 1, 0, mode,
                                           p->sigma_z, tau, p->lambda, p->step_size);
   }
@@ -473,34 +481,34 @@ DTSGB_API int dtsgb_soft_backward(dtsgb_soft_t s, const float* const* grad_out,
   for (int k = N - 1; k >= 0; --k) {
     float* vk = s->plane(P_ITER + k);
     // u = X half-step of v_k (the Y half-step's input)
-    k_soft_half<<<g, kST, 0, s->stream>>>(s->d_inst, vk, s->plane(P_U), s->plane(P_EH),
+    SOFT_LAUNCH(k_soft_half, g, s->stream, s->d_inst, vk, s->plane(P_U), s->plane(P_EH),
                                           s->plane(P_T), s->plane(P_C), 0, 1, mode, sg, tau,
                                           lam, step);
     // Y^T: a = dL/dv_{k+1} -> b = dL/du, and dL/ddV
-    k_soft_pre<<<g, kST, 0, s->stream>>>(s->d_inst, s->plane(P_U), a, s->plane(P_EV),
+    SOFT_LAUNCH(k_soft_pre, g, s->stream, s->d_inst, s->plane(P_U), a, s->plane(P_EV),
                                          nullptr, nullptr, s->plane(P_COEF), s->plane(P_B),
                                          s->plane(P_HV), s->plane(P_DIAG), nullptr, nullptr,
                                          1, 0, mode, sg, tau, lam, step);
-    k_soft_scatter<<<g, kST, 0, s->stream>>>(s->d_inst, a, s->plane(P_COEF),
+    SOFT_LAUNCH(k_soft_scatter, g, s->stream, s->d_inst, a, s->plane(P_COEF),
                                              s->plane(P_DIAG), s->plane(P_EV), b, 1, sg, tau,
                                              lam);
-    k_soft_edge<<<g, kST, 0, s->stream>>>(s->d_inst, s->plane(P_U), s->plane(P_COEF),
+    SOFT_LAUNCH(k_soft_edge, g, s->stream, s->d_inst, s->plane(P_U), s->plane(P_COEF),
                                           s->plane(P_B), s->plane(P_HV), s->plane(P_EV),
                                           s->plane(P_GEV), 1, sg, tau, lam);
     // X^T: b = dL/du -> a = dL/dv_k, dL/dt, dL/dc and dL/ddH
-    k_soft_pre<<<g, kST, 0, s->stream>>>(s->d_inst, vk, b, s->plane(P_EH), s->plane(P_T),
+    SOFT_LAUNCH(k_soft_pre, g, s->stream, s->d_inst, vk, b, s->plane(P_EH), s->plane(P_T),
                                          s->plane(P_C), s->plane(P_COEF), s->plane(P_B),
                                          s->plane(P_HV), s->plane(P_DIAG), s->plane(P_GT),
                                          s->plane(P_GC), 0, 1, mode, sg, tau, lam, step);
-    k_soft_scatter<<<g, kST, 0, s->stream>>>(s->d_inst, b, s->plane(P_COEF),
+    SOFT_LAUNCH(k_soft_scatter, g, s->stream, s->d_inst, b, s->plane(P_COEF),
                                              s->plane(P_DIAG), s->plane(P_EH), a, 0, sg, tau,
                                              lam);
-    k_soft_edge<<<g, kST, 0, s->stream>>>(s->d_inst, vk, s->plane(P_COEF), s->plane(P_B),
+    SOFT_LAUNCH(k_soft_edge, g, s->stream, s->d_inst, vk, s->plane(P_COEF), s->plane(P_B),
                                           s->plane(P_HV), s->plane(P_EH), s->plane(P_GEH), 0,
                                           sg, tau, lam);
   }
   // v_0 = t
-  k_soft_axpy<<<g, kST, 0, s->stream>>>(s->d_inst, a, s->plane(P_GT));
+  SOFT_LAUNCH(k_soft_axpy, g, s->stream, s->d_inst, a, s->plane(P_GT));
   DTSGB_CUDA(cudaGetLastError());
   const struct {
     float* const* dst;

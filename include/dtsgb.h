@@ -119,7 +119,8 @@ enum {
   DTSGB_K_DTS_OTHER = 8, /* iterate init, conversions                 */
   DTSGB_K_DTS_ADJOINT = 9, /* adjoint of one fused iteration          */
   DTSGB_K_HFBS_ADJOINT = 10, /* the whole HFBS adjoint                  */
-  DTSGB_K_COUNT = 11
+  DTSGB_K_SOFT = 11,         /* soft-window half-steps and adjoint passes */
+  DTSGB_K_COUNT = 12
 };
 /* (new) Thread blocks of the library's kernels that gave up waiting for an
  * asynchronous (TMA) copy of their tile since the library was loaded: each
