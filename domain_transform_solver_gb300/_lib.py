@@ -93,6 +93,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_dts_set_image_dim": ([vp, i, i], i),
         "dtsgb_dts_init_frame": ([vp, i, vp, vp, vp], i),
         "dtsgb_dts_init_frame_device": ([vp, i, vp, vp, vp], i),
+        "dtsgb_dts_upload_targets": ([vp, vp, vp], i),
+        "dtsgb_dts_upload_targets_device": ([vp, vp, vp], i),
         "dtsgb_dts_compute_differential": ([vp, P(FilterParams)], i),
         "dtsgb_dts_integrate": ([vp], i),
         "dtsgb_dts_filter": ([vp, P(FilterParams), vp, vp, i], i),
@@ -109,6 +111,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "dtsgb_hfbs_set_image_dim": ([vp, i, i], i),
         "dtsgb_hfbs_init_frame": ([vp, i, vp, vp, vp], i),
         "dtsgb_hfbs_init_frame_device": ([vp, i, vp, vp, vp], i),
+        "dtsgb_hfbs_upload_targets": ([vp, vp, vp], i),
+        "dtsgb_hfbs_upload_targets_device": ([vp, vp, vp], i),
         "dtsgb_hfbs_set_filter_params": ([vp, P(HfbsParams)], i),
         "dtsgb_hfbs_clear_all": ([vp], i),
         "dtsgb_hfbs_optimize": ([vp], i),

@@ -306,6 +306,32 @@ DTSGB_API int dtsgb_dts_init_frame_device(dtsgb_dts_t h, int cs,
   return dts_init_frame(h, cs, rgba, target, conf, cudaMemcpyDeviceToDevice);
 }
 
+// A new target and confidence for the guide already in place (video frames
+// with a fixed guide): the guide, its domain transform and the cached window
+// bounds stay, so the next Optimize with the same sigma_z skips the
+// window-bound search.  Results equal InitFrame with the same guide.
+static int dts_upload_targets(dtsgb_dts_t h, const float* target, const float* conf,
+                              cudaMemcpyKind kind) {
+  if (!h || !target) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  int st = dts_upload_plane(h, target, h->target, kind);
+  if (st) return st;
+  st = conf ? dts_upload_plane(h, conf, h->conf, kind)
+            : launch_fill_storage(h->st, h->conf, (long long)h->plane, 1.f, h->stream);
+  if (st) return st;
+  if (kind == cudaMemcpyHostToDevice) DTSGB_CUDA(cudaStreamSynchronize(h->stream));
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_dts_upload_targets(dtsgb_dts_t h, const float* target,
+                                       const float* conf) {
+  return dts_upload_targets(h, target, conf, cudaMemcpyHostToDevice);
+}
+
+DTSGB_API int dtsgb_dts_upload_targets_device(dtsgb_dts_t h, const float* target,
+                                              const float* conf) {
+  return dts_upload_targets(h, target, conf, cudaMemcpyDeviceToDevice);
+}
+
 static int check_filter_params(float sx, float sy, float sr) {
   if (!finite_pos(sx) || !finite_pos(sy) || !finite_pos(sr))
     return fail(DTSGB_ERR_INVALID_ARGUMENT,
@@ -695,6 +721,18 @@ struct dtsgb_hfbs_s {
   HfbsGradState gs{};
   HInst inst{};
   bool grad_ready = false;  // the last optimize kept its iterates
+  // guide-state reuse: the bistochastized normalisation depends only on the
+  // guide's bins, so a solve whose guide (generation), grid and
+  // bistochastization parameters equal the last one's keeps it
+  struct NormKey {
+    unsigned long long guide_gen;
+    HInst inst;
+    float sigma_x, sigma_y, sigma_l;
+    int bistoch_iter_max;
+  };
+  unsigned long long guide_gen = 0;
+  NormKey nkey{};
+  bool nkey_valid = false;
 };
 
 enum {
@@ -883,6 +921,7 @@ DTSGB_API int dtsgb_hfbs_set_image_dim(dtsgb_hfbs_t h, int w, int hh) {
   h->w = w;
   h->h = hh;
   h->grad_ready = false;
+  ++h->guide_gen;
   return DTSGB_OK;
 }
 
@@ -910,8 +949,39 @@ static int hfbs_init_frame(dtsgb_hfbs_t h, int cs, const void* rgba,
     if (st) return st;
   }
   h->grad_ready = false;
+  ++h->guide_gen;
   if (kind == cudaMemcpyHostToDevice) DTSGB_CUDA(cudaStreamSynchronize(h->stream));
   return DTSGB_OK;
+}
+
+// A new target and confidence for the guide already in place: the next
+// Optimize with the same grid parameters keeps the bistochastized
+// normalisation (results equal InitFrame with the same guide).
+static int hfbs_upload_targets(dtsgb_hfbs_t h, const float* target, const float* conf,
+                               cudaMemcpyKind kind) {
+  if (!h || !target) return fail(DTSGB_ERR_INVALID_ARGUMENT, "null argument");
+  const size_t wb = (size_t)h->w * 4, pb = (size_t)h->pitch * 4;
+  DTSGB_CUDA(cudaMemcpy2DAsync(h->target, pb, target, wb, wb, h->h, kind, h->stream));
+  if (conf) {
+    DTSGB_CUDA(cudaMemcpy2DAsync(h->conf, pb, conf, wb, wb, h->h, kind, h->stream));
+  } else {
+    int st = launch_fill_storage(Storage::F32, h->conf, (long long)h->plane, 1.f,
+                                 h->stream);
+    if (st) return st;
+  }
+  h->grad_ready = false;
+  if (kind == cudaMemcpyHostToDevice) DTSGB_CUDA(cudaStreamSynchronize(h->stream));
+  return DTSGB_OK;
+}
+
+DTSGB_API int dtsgb_hfbs_upload_targets(dtsgb_hfbs_t h, const float* target,
+                                        const float* conf) {
+  return hfbs_upload_targets(h, target, conf, cudaMemcpyHostToDevice);
+}
+
+DTSGB_API int dtsgb_hfbs_upload_targets_device(dtsgb_hfbs_t h, const float* target,
+                                               const float* conf) {
+  return hfbs_upload_targets(h, target, conf, cudaMemcpyDeviceToDevice);
 }
 
 DTSGB_API int dtsgb_hfbs_init_frame(dtsgb_hfbs_t h, int cs, const void* rgba,
@@ -944,6 +1014,7 @@ DTSGB_API int dtsgb_hfbs_clear_all(dtsgb_hfbs_t h) {
                              h->stream));
   h->solved = false;
   h->grad_ready = false;
+  ++h->guide_gen;
   return DTSGB_OK;
 }
 
@@ -962,6 +1033,8 @@ DTSGB_API int dtsgb_hfbs_optimize(dtsgb_hfbs_t h) {
   h->gy = p.grid_y;
   h->gl = p.grid_l;
   h->solved = false;
+  const bool had_norm = h->nkey_valid;
+  h->nkey_valid = false;
   if (p.grid_x > h->max_gx || p.grid_y > h->max_gy || p.grid_l > h->max_gl) {
     // src/hfbs.cu:594-611: the target becomes the output
     const size_t pb = (size_t)h->pitch * 4;
@@ -1006,8 +1079,18 @@ DTSGB_API int dtsgb_hfbs_optimize(dtsgb_hfbs_t h) {
   }
   HParams hp{p.sigma_x, p.sigma_y, p.sigma_l, p.lambda, p.alpha, p.beta,
              p.bistoch_iter_max, p.optim_iter_max, p.neg_exp_beta};
+  dtsgb_hfbs_s::NormKey nk{};  // zero padding, so that memcmp compares fields
+  nk.guide_gen = h->guide_gen;
+  nk.inst = I;
+  nk.sigma_x = p.sigma_x;
+  nk.sigma_y = p.sigma_y;
+  nk.sigma_l = p.sigma_l;
+  nk.bistoch_iter_max = p.bistoch_iter_max;
+  B.reuse_norm = had_norm && std::memcmp(&nk, &h->nkey, sizeof nk) == 0;
   int st = hfbs_enqueue_solve(B, hp, h->stream);
   if (st) return st;
+  h->nkey = nk;
+  h->nkey_valid = true;
   h->inst = I;
   h->solved = true;
   h->grad_ready = h->grad;

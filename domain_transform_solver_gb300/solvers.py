@@ -265,6 +265,15 @@ class DomainTransformSolver(DomainTransformFilter):
         check(self._lib.dtsgb_dts_init_frame(self._h, int(color_space), _ptr(rgba),
                                              _ptr(t), _ptr(c)))
 
+    def UploadTargets(self, target, confidence=None) -> None:
+        """New target and confidence for the guide in place (video frames
+        with a fixed guide); the next Optimize with the same sigma_z keeps
+        the window bounds (dtsgb_dts_upload_targets)."""
+        shape = self._shape()
+        t = _f32(target, shape)
+        c = _f32(confidence, shape) if confidence is not None else None
+        check(self._lib.dtsgb_dts_upload_targets(self._h, _ptr(t), _ptr(c)))
+
     def Optimize(self, optimize_params: DomainOptimizeParams,
                  overwrite_target_above_conf: float = -1) -> None:
         check(self._lib.dtsgb_dts_optimize(self._h, ctypes.byref(optimize_params._c()),
@@ -341,6 +350,15 @@ class HFBS:
         c = _f32(confidence, shape) if confidence is not None else None
         check(self._lib.dtsgb_hfbs_init_frame(self._h, int(color_space), _ptr(rgba),
                                               _ptr(t), _ptr(c)))
+
+    def UploadTargets(self, target, confidence=None) -> None:
+        """New target and confidence for the guide in place; the next
+        Optimize with the same grid parameters keeps the bistochastized
+        normalisation (dtsgb_hfbs_upload_targets)."""
+        shape = self._shape()
+        t = _f32(target, shape)
+        c = _f32(confidence, shape) if confidence is not None else None
+        check(self._lib.dtsgb_hfbs_upload_targets(self._h, _ptr(t), _ptr(c)))
 
     def SetFilterParams(self, grid_params: HFBSGridParams) -> None:
         self.grid_params_ = grid_params

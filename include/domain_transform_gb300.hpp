@@ -165,6 +165,11 @@ class DomainTransformSolver : public DomainTransformFilter {
  public:
   explicit DomainTransformSolver(const ImageDim& max_image_dims, unsigned flags = 0)
       : DomainTransformFilter(max_image_dims, flags & ~DTSGB_FLAG_FILTER_ONLY) {}
+  // Guide-state reuse (extension): a new target / confidence for the guide
+  // in place; the next Optimize with the same sigma_z keeps its windows.
+  void UploadTargets(const float* target, const float* confidence = nullptr) {
+    detail::on_status(dtsgb_dts_upload_targets(h_, target, confidence));
+  }
   void InitFrame(const COLOR_SPACE& color_space, void* color_image, float* target,
                  float* confidence = nullptr) {
     detail::on_status(dtsgb_dts_init_frame(h_, static_cast<int>(color_space),
@@ -233,6 +238,11 @@ class HFBS {
     const int st = dtsgb_hfbs_set_image_dim(h_, image_dim.width, image_dim.height);
     if (st == DTSGB_OK) image_dim_ = image_dim;
     detail::on_status(st, true);
+  }
+  // Guide-state reuse (extension): a new target / confidence for the guide
+  // in place; the next Optimize with the same grid keeps the normalisation.
+  void UploadTargets(const float* target, const float* confidence = nullptr) {
+    detail::on_status(dtsgb_hfbs_upload_targets(h_, target, confidence));
   }
   void InitFrame(const COLOR_SPACE& color_space, void* color_image, float* target,
                  float* confidence = nullptr) {

@@ -162,6 +162,17 @@ DTSGB_API int dtsgb_dts_init_frame_device(dtsgb_dts_t h, int color_space,
                                           const void* rgba,
                                           const float* target,
                                           const float* confidence);
+/* Guide-state reuse (no reference counterpart; its InitFrame always
+ * re-uploads the guide, src/domain_transform_solver.cu:46-60): a new target
+ * and confidence (null: all ones) for the guide already in place, as for
+ * video frames with a fixed guide.  The guide, its domain transform and the
+ * window bounds of the last Optimize stay, so the next Optimize with the
+ * same sigma_z skips the window-bound search; results equal InitFrame with
+ * the same guide. */
+DTSGB_API int dtsgb_dts_upload_targets(dtsgb_dts_t h, const float* target,
+                                       const float* confidence);
+DTSGB_API int dtsgb_dts_upload_targets_device(dtsgb_dts_t h, const float* target,
+                                              const float* confidence);
 /* ComputeColorSpaceDifferential, filter.h:53 / solver.h:57. */
 DTSGB_API int dtsgb_dts_compute_differential(dtsgb_dts_t h,
                                              const dtsgb_filter_params* p);
@@ -229,6 +240,16 @@ DTSGB_API int dtsgb_hfbs_init_frame_device(dtsgb_hfbs_t h, int color_space,
                                            const void* rgba,
                                            const float* target,
                                            const float* confidence);
+/* Guide-state reuse for HFBS (src/hfbs.cu:540-554 re-uploads the guide
+ * with every InitFrame): a new target and confidence for the guide in
+ * place.  The next Optimize with the same grid parameters keeps the
+ * bistochastized normalisation of the last one (it depends only on the
+ * guide's bins, src/hfbs.cu:626-665); results equal InitFrame with the same
+ * guide. */
+DTSGB_API int dtsgb_hfbs_upload_targets(dtsgb_hfbs_t h, const float* target,
+                                        const float* confidence);
+DTSGB_API int dtsgb_hfbs_upload_targets_device(dtsgb_hfbs_t h, const float* target,
+                                               const float* confidence);
 /* SetFilterParams, hfbs.h:125. */
 DTSGB_API int dtsgb_hfbs_set_filter_params(dtsgb_hfbs_t h,
                                            const dtsgb_hfbs_params* p);

@@ -108,13 +108,31 @@ def test_filter_against_the_reference(gpu_ready, oracle_mod, name):
     params = D.DomainFilterParams(m["sigma_x"], m["sigma_y"], m["sigma_r"])
     out = s.Filter(params, d["input"], m["num_iter"])
     b = d["bounds"].astype(np.int32)
+    o = oracle_mod.OracleDTS(w, h)
+    o.init_frame(m["color_space"], d["rgba"])
+    o.differential(m["sigma_x"], m["sigma_y"], m["sigma_r"])
+    o.integrate()
     same = True
     for it, (sx, sy) in enumerate(P.filter_sigmas(m["sigma_x"], m["sigma_y"], m["num_iter"])):
         for axis, sg in ((0, sx), (1, sy)):
             gl, gu = s.DebugBounds(axis, sg)
-            same = same and np.array_equal(gl, b[it, ..., 2 * axis]) and \
-                np.array_equal(gu, b[it, ..., 2 * axis + 1])
-    _held(out, d["output"], P.target_range(d["input"]), same)
+            diff = (gl != b[it, ..., 2 * axis]) | (gu != b[it, ..., 2 * axis + 1])
+            _, _, marg = o.bounds(axis, sg)
+            assert not (diff & (np.abs(marg) > P.TIE_REL * (sg + 1.0))).any(), (it, axis)
+            same = same and not diff.any()
+            o.add_bounds_override(axis, sg, gl, gu)
+    rng_x = P.target_range(d["input"])
+    if same:
+        _held(out, d["output"], rng_x, True)
+    else:
+        # a near-tie window of any of the six passes moves its neighbourhood:
+        # RMSE and 99.5% of pixels against the reference, every pixel against
+        # the FP64 oracle run on the GPU's windows
+        err = np.abs(out.astype(np.float64) - d["output"])
+        assert float(np.sqrt(np.mean(err ** 2))) <= P.TOL_REL * rng_x
+        assert float(np.mean(err <= P.TOL_REL * rng_x)) >= 0.995
+        own = o.filter(m["sigma_x"], m["sigma_y"], m["sigma_r"], d["input"], m["num_iter"])
+        assert float(np.abs(out - own).max()) <= P.TOL_REL * rng_x
 
 
 @pytest.mark.parametrize("name", _cases("stereo"))
