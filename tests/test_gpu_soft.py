@@ -95,6 +95,51 @@ def test_soft_forward_and_adjoint_match_the_oracle(gpu_ready, oracle_mod, loss, 
             assert float(np.mean(err > bar)) <= 1e-3, (float(err.max()), bar)
 
 
+def _check_against_oracle(O, data, eh_all, ev_all, opt, res):
+    out, gt, gc, geh, gev = res
+    for i, (_, t, c, g) in enumerate(data):
+        eh, ev = eh_all[i], ev_all[i]
+        ref = O.soft_solve(eh, ev, t, c, opt, TAU)
+        assert np.abs(out[i] - ref).max() <= P.TOL_REL * P.target_range(t)
+        rgrads = O.soft_backward(eh, ev, t, c, opt, TAU, g)
+        for got, r in zip((gt[i], gc[i], geh[i], gev[i]), rgrads):
+            err = np.abs(got - r)
+            bar = TOL_GRAD * max(float(np.abs(r).max()), 1e-12)
+            assert float(np.mean(err > bar)) <= 1e-3, (float(err.max()), bar)
+
+
+@pytest.mark.parametrize("scale", [1.0, 0.1])
+def test_soft_ragged_tiles_and_small_weights(gpu_ready, oracle_mod, scale):
+    """Instances that span several shared-memory tiles, with partial ones
+    (300 x 70, 45 x 130), and the same with edge weights scaled by 0.1, whose
+    windows reach past the tiles' largest halo: those solves run the
+    global-memory kernels.  Both are held to the oracle's bars."""
+    D = gpu_ready
+    import torch
+    sizes = [(300, 70), (45, 130)]
+    data = [_inputs(800 + i, w, h) for i, (w, h) in enumerate(sizes)]
+    opt = dict(num_iterations=4, loss=1, lambda_=0.99, sigma_z=8.0, step_size=0.99)
+    s = D.SoftDTS(sizes)
+    ehs, evs, ptrs = [], [], {}
+    for i, (rgba, t, c, g) in enumerate(data):
+        dh, dv = _gpu_edges(D, [rgba])
+        ehs.append(dh[0].cpu().numpy() * np.float32(scale))
+        evs.append(dv[0].cpu().numpy() * np.float32(scale))
+    dev = {k: [_dev(x) for x in v] for k, v in
+           (("eh", ehs), ("ev", evs), ("t", [d[1] for d in data]), ("c", [d[2] for d in data]),
+            ("g", [d[3] for d in data]))}
+    p = lambda xs: [x.data_ptr() for x in xs]  # noqa: E731
+    out = [torch.empty_like(x) for x in dev["t"]]
+    s.solve(p(dev["eh"]), p(dev["ev"]), p(dev["t"]), p(dev["c"]),
+            D.DomainOptimizeParams(**opt), TAU, p(out))
+    grads = [[torch.empty_like(x) for x in dev["t"]] for _ in range(4)]
+    s.backward(p(dev["g"]), *[p(gr) for gr in grads])
+    torch.cuda.synchronize()
+    s.close()
+    res = [[x.cpu().numpy() for x in out]] + [[x.cpu().numpy() for x in gr] for gr in grads]
+    _check_against_oracle(oracle_mod, data, ehs, evs, opt, res)
+
+
 def test_soft_edge_gradients_match_fp64_central_differences(gpu_ready, oracle_mod):
     """256 entries (128 of dH, 128 of dV) of one 64x48 instance: d/de sum(g*v)
     by central differences of the FP64 oracle's soft forward."""
