@@ -79,8 +79,8 @@ struct SInst {
 enum {
   P_EH = 0, P_EV, P_FH, P_FV, P_T, P_C, P_U, P_COEF, P_ALPHA, P_BETA, P_ADIAG, P_DIFF,
   P_G0, P_G1, P_GT, P_GC, P_GEH, P_GEV,
-  // window plans (k_soft_plan): n, counts, and four planes of float4 weights per axis
-  P_PNX, P_PCX, P_PWX, P_PNY = P_PWX + 4, P_PCY, P_PWY, P_ITER = P_PWY + 4
+  // window plans (k_soft_plan): n, counts, and two planes of float2 weights per axis
+  P_PNX, P_PCX, P_PWX, P_PNY = P_PWX + 2, P_PCY, P_PWY, P_ITER = P_PWY + 2
 };
 
 __device__ __forceinline__ float ramp(float x) { return fminf(fmaxf(x + 0.5f, 0.f), 1.f); }
@@ -632,17 +632,20 @@ __global__ void __launch_bounds__(1024)
 // ---- window plans ------------------------------------------------------------
 // The edge weights stay fixed through a solve and its adjoint, and so do the
 // soft windows: a plan of one axis records, per pixel, the full-weight
-// pixels on each side (dl, du), the ramp pixels beyond them (nrl, nru, at
-// most kPlanRamp a side) with their weights, and n.  Sums over a planned
-// window add the same terms in the same order as a walk, so a planned
-// half-step or adjoint gives bitwise the walk's results while skipping its
-// distance arithmetic.  counts = dl | du << 8 | nrl << 16 | nru << 24,
-// weights = (left ramp 1, 2, right ramp 1, 2).
-constexpr int kPlanRamp = 2;
+// pixels on each side (dl, du), the ramp pixel beyond them (nrl, nru: 0 or
+// 1 a side) with its weight, and n.  One ramp pixel a side is all a window
+// can hold when tau does not exceed the smallest edge weight (the ramp band
+// is tau wide and consecutive distances differ by an edge weight; the
+// guide's are at least 1 and tau is 1 by default); other windows keep the
+// walking kernels.  Sums over a planned window add the same terms in the
+// same order as a walk, so a planned half-step or adjoint gives bitwise the
+// walk's results while skipping its distance arithmetic.  counts = dl |
+// du << 8 | nrl << 16 | nru << 24, weights = (left ramp, right ramp).
+constexpr int kPlanRamp = 1;
 
 __global__ void k_soft_plan(const SInst* __restrict__ insts, const float* __restrict__ e,
                             int axis, Ramp R, float* __restrict__ nout,
-                            unsigned* __restrict__ counts, float4* __restrict__ wts,
+                            unsigned* __restrict__ counts, float2* __restrict__ wts,
                             int* __restrict__ stat) {
   __shared__ int bext, bovf;
   if (threadIdx.x == 0) bext = bovf = 0;
@@ -657,7 +660,7 @@ __global__ void k_soft_plan(const SInst* __restrict__ insts, const float* __rest
     const GlobalLine ln{e + l.base, nullptr, nullptr, nullptr, nullptr, l.st, l.L};
     float n = R.wc;
     int full[2] = {0, 0}, nr[2] = {0, 0};
-    float wr[2][kPlanRamp] = {{0.f, 0.f}, {0.f, 0.f}};
+    float wr[2] = {0.f, 0.f};
 #pragma unroll
     for (int side = 0; side < 2; ++side) {  // right, then left: the walks' order
       int D = 0;
@@ -671,7 +674,7 @@ __global__ void k_soft_plan(const SInst* __restrict__ insts, const float* __rest
         if (D <= R.loF) {
           ++full[side];
         } else {
-          if (nr[side] < kPlanRamp) wr[side][nr[side]] = w;
+          if (nr[side] == 0) wr[side] = w;
           ++nr[side];
         }
       }
@@ -682,7 +685,7 @@ __global__ void k_soft_plan(const SInst* __restrict__ insts, const float* __rest
     nout[p] = n;
     counts[p] = (unsigned)min(full[1], 255) | (unsigned)min(full[0], 255) << 8 |
                 (unsigned)min(nr[1], 3) << 16 | (unsigned)min(nr[0], 3) << 24;
-    wts[p] = make_float4(wr[1][0], wr[1][1], wr[0][0], wr[0][1]);
+    wts[p] = make_float2(wr[1], wr[0]);
   }
   atomicMax(&bext, ext);
   if (ovf) atomicOr(&bovf, 1);
@@ -693,18 +696,30 @@ __global__ void k_soft_plan(const SInst* __restrict__ insts, const float* __rest
   }
 }
 
-// sum_q w_pq V(q) over pixel i's planned window, in the walks' order.
+// sum_q w_pq V(q) over pixel i's planned window, and its weight n, in the
+// walks' order.
 template <class LN>
-__device__ __forceinline__ float plan_sum(const LN& ln, int i, unsigned cnt, float4 w4,
-                                          float wc) {
+__device__ __forceinline__ float plan_sum(const LN& ln, int i, unsigned cnt, float2 w2,
+                                          float wc, float* n_out = nullptr) {
   const int dl = cnt & 255, du = (cnt >> 8) & 255, nrl = (cnt >> 16) & 255, nru = cnt >> 24;
-  float S = wc * ln.V(i);
-  for (int m = 1; m <= du; ++m) S += ln.V(i + m);
-  if (nru > 0) S = __fmaf_rn(w4.z, ln.V(i + du + 1), S);
-  if (nru > 1) S = __fmaf_rn(w4.w, ln.V(i + du + 2), S);
-  for (int m = 1; m <= dl; ++m) S += ln.V(i - m);
-  if (nrl > 0) S = __fmaf_rn(w4.x, ln.V(i - dl - 1), S);
-  if (nrl > 1) S = __fmaf_rn(w4.y, ln.V(i - dl - 2), S);
+  float S = wc * ln.V(i), n = wc;
+  for (int m = 1; m <= du; ++m) {
+    S += ln.V(i + m);
+    n += 1.f;
+  }
+  if (nru) {
+    S = __fmaf_rn(w2.y, ln.V(i + du + 1), S);
+    n += w2.y;
+  }
+  for (int m = 1; m <= dl; ++m) {
+    S += ln.V(i - m);
+    n += 1.f;
+  }
+  if (nrl) {
+    S = __fmaf_rn(w2.x, ln.V(i - dl - 1), S);
+    n += w2.x;
+  }
+  if (n_out) *n_out = n;
   return S;
 }
 
@@ -712,7 +727,7 @@ template <int AXIS>
 __global__ void __launch_bounds__(256)
     k_soft_half_plan(const SInst* __restrict__ insts, const float* __restrict__ vin,
                      float* __restrict__ vout, const unsigned* __restrict__ counts,
-                     const float4* __restrict__ wts, const float* __restrict__ nplan,
+                     const float2* __restrict__ wts,
                      const float* __restrict__ t, const float* __restrict__ c,
                      float* __restrict__ Bout, int data, int mode, float wc, float lambda,
                      float step, int halo) {
@@ -732,9 +747,9 @@ __global__ void __launch_bounds__(256)
                       AXIS == 0 ? 1 : kTYC, AXIS == 0 ? 0 : (int)threadIdx.x,
                       AXIS == 0 ? I.w : I.h};
     auto one = [&](int i, long long p) {
-      const float S = plan_sum(ln, i, counts[p], wts[p], wc);
-      half_update(p, ln.V(i), nplan[p], S, t, c, vout, nullptr, Bout, data, mode, lambda,
-                  step);
+      float n;
+      const float S = plan_sum(ln, i, counts[p], wts[p], wc, &n);
+      half_update(p, ln.V(i), n, S, t, c, vout, nullptr, Bout, data, mode, lambda, step);
     };
     if (AXIS == 0) {
       const int x = l0 + threadIdx.x;
@@ -750,9 +765,9 @@ __global__ void __launch_bounds__(256)
 }
 
 // The planned adjoint with its pointwise first pass fused in: the tile
-// stages a = dL/d(output), n, B, the input x (and t, c on X), each thread
-// first takes its own pixels' a * diag and dL/dt, dL/dc, then every staged
-// entry becomes (coef, alpha, beta) in place, and the window sums (over
+// stages a = dL/d(output), n, B, the input x (and t, c on X), every staged
+// entry becomes (coef, alpha, beta) in place (its owner taking a * diag and
+// dL/dt, dL/dc on the way), and the window sums (over
 // coef, plan_sum) and the ramp band's pair terms (diff) follow, in
 // soft_window_adj's order.  The same expressions as k_soft_pre +
 // k_soft_adjoint_tile, without their four intermediate planes.
@@ -762,7 +777,7 @@ __global__ void __launch_bounds__(256)
                          const float* __restrict__ nplan, const float* __restrict__ Bk,
                          const float* __restrict__ val, const float* __restrict__ t,
                          const float* __restrict__ c, const unsigned* __restrict__ counts,
-                         const float4* __restrict__ wts, float* __restrict__ aout,
+                         const float2* __restrict__ wts, float* __restrict__ aout,
                          float* __restrict__ diff, float* __restrict__ gt,
                          float* __restrict__ gc, int data, int mode, float lambda, float step,
                          float wc, int halo) {
@@ -775,8 +790,6 @@ __global__ void __launch_bounds__(256)
   const int nf = data ? 6 : 4;
   float* F[6] = {smf, smf + TS, smf + 2 * TS, smf + 3 * TS, smf + 4 * TS, smf + 5 * TS};
   const float* srcs[6] = {a, nplan, Bk, val, t, c};
-  const int tid = threadIdx.x + (AXIS == 0 ? 0 : kTYC * threadIdx.y);
-  const int nthr = AXIS == 0 ? kTX : kTYC * kTYT;
   for (int tile = blockIdx.x; tile < G.n0 * G.n1; tile += gridDim.x) {
     const int t1 = tile / G.n0, t0 = tile - t1 * G.n0;
     const int l0 = t0 * len, cross = AXIS == 0 ? t1 : t1 * kTYC;
@@ -786,66 +799,90 @@ __global__ void __launch_bounds__(256)
     const TileLine ln{nullptr, F[0], F[1], F[2], F[3], l0 - halo,
                       AXIS == 0 ? 1 : kTYC, AXIS == 0 ? 0 : (int)threadIdx.x,
                       AXIS == 0 ? I.w : I.h};
-    // own pixels: line index, global index (p < 0: none)
-    int li[OWN];
-    long long pp[OWN];
-#pragma unroll
-    for (int k = 0; k < OWN; ++k) {
+    // own pixel k: line index and global index (< 0: outside the image)
+    auto own_i = [&](int k) -> int {
+      return AXIS == 0 ? l0 + (int)threadIdx.x : l0 + (int)threadIdx.y + kTYT * k;
+    };
+    auto own_p = [&](int k) -> long long {
       if (AXIS == 0) {
-        li[k] = l0 + threadIdx.x;
-        pp[k] = li[k] < I.w ? I.off + (long long)cross * I.w + li[k] : -1;
-      } else {
-        const int x = cross + threadIdx.x, y = l0 + threadIdx.y + kTYT * k;
-        li[k] = y;
-        pp[k] = (x < I.w && y < I.h) ? I.off + (long long)y * I.w + x : -1;
+        const int x = l0 + threadIdx.x;
+        return x < I.w ? I.off + (long long)cross * I.w + x : -1;
       }
-    }
-    float adg[OWN];
-#pragma unroll
-    for (int k = 0; k < OWN; ++k) {
-      adg[k] = 0.f;
-      if (pp[k] < 0) continue;
-      const int at = ln.at(li[k]);
-      const float ap = F[0][at], n = F[1][at];
-      float h = 0.f, hd = 0.f, hc = 0.f;
-      if (data) {
-        data_term(mode, F[3][at], F[4][at], F[5][at], 1.f / n, &h, &hd, &hc);
-        gt[pp[k]] += ap * step * hd;
-        gc[pp[k]] -= ap * step * hc;
-      }
-      adg[k] = ap * (1.f - step * lambda - step * hd);
-    }
-    __syncthreads();
-    for (int e = tid; e < TS; e += nthr) {
+      const int x = cross + threadIdx.x, y = l0 + threadIdx.y + kTYT * k;
+      return (x < I.w && y < I.h) ? I.off + (long long)y * I.w + x : -1;
+    };
+    // Every staged entry becomes (coef, alpha, beta) in place; a thread
+    // transforms its own pixels' entries (taking their a * diag and dL/dt,
+    // dL/dc on the way) and a share of the halo's.
+    // returns a * diag of an own pixel (p >= 0)
+    auto transform = [&](int e, long long p) -> float {
       const float ap = F[0][e], n = F[1][e];
-      float h = 0.f, hd, hc;
+      float h = 0.f, hd = 0.f, hc = 0.f;
       const float rn = 1.f / n;
       if (data) data_term(mode, F[3][e], F[4][e], F[5][e], rn, &h, &hd, &hc);
+      float adg = 0.f;
+      if (p >= 0) {
+        if (data) {
+          gt[p] += ap * step * hd;  // dh/dt = -dh/dd, and v' has -s*h
+          gc[p] -= ap * step * hc;
+        }
+        adg = ap * (1.f - step * lambda - step * hd);
+      }
       const float cf = ap * step * rn;
       F[0][e] = cf;
       F[1][e] = lambda * cf;
       F[2][e] = cf * (h - lambda * F[2][e]);
+      return adg;
+    };
+    float adg[OWN];
+    if (AXIS == 0) {
+      // one own pixel a thread: transformed with its a * diag, the halo
+      // shared out over the first 2 halo threads
+      adg[0] = transform(ln.at(own_i(0)), own_p(0));
+      const int t = threadIdx.x;
+      if (t < 2 * halo) (void)transform(t < halo ? t : kTX + t, -1);
+    } else {
+      // eight own pixels a thread: their a * diag (and dL/dt, dL/dc) first,
+      // then the whole tile transformed, entries spread over the threads
+#pragma unroll
+      for (int k = 0; k < OWN; ++k) {
+        const long long p = own_p(k);
+        adg[k] = 0.f;
+        if (p < 0) continue;
+        const int e = ln.at(own_i(k));
+        const float ap = F[0][e];
+        float hd = 0.f;
+        if (data) {
+          float h, hc;
+          data_term(mode, F[3][e], F[4][e], F[5][e], 1.f / F[1][e], &h, &hd, &hc);
+          gt[p] += ap * step * hd;
+          gc[p] -= ap * step * hc;
+        }
+        adg[k] = ap * (1.f - step * lambda - step * hd);
+      }
+      __syncthreads();
+      const int tid = threadIdx.x + kTYC * threadIdx.y;
+      for (int e = tid; e < TS; e += kTYC * kTYT) (void)transform(e, -1);
     }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < OWN; ++k) {
-      if (pp[k] < 0) continue;
-      const long long p = pp[k];
-      const int i = li[k];
+      const long long p = own_p(k);
+      if (p < 0) continue;
+      const int i = own_i(k);
       const unsigned cnt = counts[p];
-      const float4 w4 = wts[p];
-      const float S = plan_sum(ln, i, cnt, w4, wc);
+      const float S = plan_sum(ln, i, cnt, wts[p], wc);
       aout[p] = __fmaf_rn(lambda, S, adg[k]);
       const int dl = cnt & 255, du = (cnt >> 8) & 255, nrl = (cnt >> 16) & 255,
                 nru = cnt >> 24;
       const float ai = ln.A(i), bi = ln.Bt(i), xi = ln.X(i);
       float d = 0.f;
-      for (int r = 1; r <= nru; ++r) {
-        const int b = i + du + r;
+      if (nru) {
+        const int b = i + du + 1;
         d += __fmaf_rn(ai, ln.X(b), bi) + __fmaf_rn(ln.A(b), xi, ln.Bt(b));
       }
-      for (int r = 1; r <= nrl; ++r) {
-        const int aa = i - dl - r;
+      if (nrl) {
+        const int aa = i - dl - 1;
         d -= __fmaf_rn(ln.A(aa), xi, ln.Bt(aa)) + __fmaf_rn(ai, ln.X(aa), bi);
       }
       diff[p] = d;
@@ -1031,7 +1068,7 @@ int plan_windows(dtsgb_soft_t s) {
     k_soft_plan<<<soft_grid(s), kST, 0, s->stream>>>(
         s->d_inst, s->plane(axis == 0 ? P_FH : P_FV), axis, s->ramp, s->plane(base),
         reinterpret_cast<unsigned*>(s->plane(base + 1)),
-        reinterpret_cast<float4*>(s->plane(base + 2)), s->d_stat);
+        reinterpret_cast<float2*>(s->plane(base + 2)), s->d_stat);
   }
   DTSGB_CUDA(cudaGetLastError());
   int st[2] = {0, 0};
@@ -1051,16 +1088,15 @@ int launch_half(dtsgb_soft_t s, const float* vin, float* vout, const float* e, c
   if (s->use_plan) {
     const int PH = s->plan_halo, base = axis == 0 ? P_PNX : P_PNY;
     const unsigned* cnt = reinterpret_cast<const unsigned*>(s->plane(base + 1));
-    const float4* wts = reinterpret_cast<const float4*>(s->plane(base + 2));
+    const float2* wts = reinterpret_cast<const float2*>(s->plane(base + 2));
     const dim3 g((unsigned)std::min<long long>(max_tiles(s, axis), 152 * 16), s->n);
     if (axis == 0)
       k_soft_half_plan<0><<<g, kTX, sizeof(float) * (kTX + 2 * PH), s->stream>>>(
-          s->d_inst, vin, vout, cnt, wts, s->plane(base), t, c, Bout, data, mode, R.wc, lambda,
-          step, PH);
+          s->d_inst, vin, vout, cnt, wts, t, c, Bout, data, mode, R.wc, lambda, step, PH);
     else
       k_soft_half_plan<1><<<g, dim3(kTYC, kTYT), sizeof(float) * (kTYR + 2 * PH) * kTYC,
-                            s->stream>>>(s->d_inst, vin, vout, cnt, wts, s->plane(base), t, c,
-                                         Bout, data, mode, R.wc, lambda, step, PH);
+                            s->stream>>>(s->d_inst, vin, vout, cnt, wts, t, c, Bout, data, mode,
+                                         R.wc, lambda, step, PH);
   } else if (H > kMaxHalo) {
     k_soft_half<<<soft_grid(s), kST, 0, s->stream>>>(s->d_inst, vin, vout, e, t, c, nout, Bout,
                                                      axis, data, mode, R, lambda, step);
@@ -1132,7 +1168,7 @@ int launch_adjoint_fused(dtsgb_soft_t s, const float* a, const float* Bk, const 
   float* diff = s->plane(P_DIFF);
   const int PH = s->plan_halo, base = axis == 0 ? P_PNX : P_PNY;
   const unsigned* cnt = reinterpret_cast<const unsigned*>(s->plane(base + 1));
-  const float4* wts = reinterpret_cast<const float4*>(s->plane(base + 2));
+  const float2* wts = reinterpret_cast<const float2*>(s->plane(base + 2));
   const float* nplan = s->plane(base);
   const float wc = s->ramp.wc;
   const int nf = data ? 6 : 4;
