@@ -363,9 +363,9 @@ constexpr int kTX = 256, kTYC = 32, kTYR = 64, kTYT = 8;  // Y: kTYC x kTYT thre
 template <int AXIS>
 struct TileGeom {
   int n0, n1;  // tiles along the line and across lines of an instance
-  __device__ TileGeom(const SInst& I) {
+  __device__ TileGeom(const SInst& I, int len = AXIS == 0 ? kTX : kTYR) {
     if (AXIS == 0) {
-      n0 = (I.w + kTX - 1) / kTX;
+      n0 = (I.w + len - 1) / len;
       n1 = I.h;
     } else {
       n0 = (I.h + kTYR - 1) / kTYR;
@@ -696,6 +696,111 @@ __global__ void k_soft_plan(const SInst* __restrict__ insts, const float* __rest
   }
 }
 
+// The plan from shared-memory tiles of the edge weights, converted to fixed
+// point as they are staged (the conversion of k_soft_fix, so the plan is the
+// global kernel's): a window side that would reach past the tile's halo
+// flags the plan as overflowing (stat[1]) and the solve falls back to the
+// global-memory plan.
+constexpr int kPlanHalo = 24;
+
+template <int AXIS>
+__global__ void __launch_bounds__(256)
+    k_soft_plan_tile(const SInst* __restrict__ insts, const float* __restrict__ e, Ramp R,
+                     float cap, float scale, float* __restrict__ nout,
+                     unsigned* __restrict__ counts, float2* __restrict__ wts,
+                     int* __restrict__ stat) {
+  extern __shared__ float smf[];
+  __shared__ int bext, bovf;
+  if (threadIdx.x == 0 && threadIdx.y == 0) bext = bovf = 0;
+  const SInst I = insts[blockIdx.y];
+  const TileGeom<AXIS> G(I);
+  const int len = AXIS == 0 ? kTX : kTYR, halo = kPlanHalo;
+  int ext = 0, ovf = 0;
+  for (int tile = blockIdx.x; tile < G.n0 * G.n1; tile += gridDim.x) {
+    const int t1 = tile / G.n0, t0 = tile - t1 * G.n0;
+    const int l0 = t0 * len, cross = AXIS == 0 ? t1 : t1 * kTYC;
+    __syncthreads();
+    {  // stage the fixed-point weights (zero outside the image)
+      const int TL = len + 2 * halo;
+      if (AXIS == 0) {
+        const long long row = I.off + (long long)cross * I.w;
+        for (int i = threadIdx.x; i < TL; i += kTX) {
+          const int x = l0 - halo + i;
+          smf[i] = __int_as_float(
+              x >= 0 && x < I.w
+                  ? (int)rintf(fmaxf(fminf(e[row + x], cap), 0.f) * scale)
+                  : 0);
+        }
+      } else {
+        const int x = cross + threadIdx.x;
+        for (int i = threadIdx.y; i < TL; i += kTYT) {
+          const int y = l0 - halo + i;
+          const bool in = x < I.w && y >= 0 && y < I.h;
+          smf[i * kTYC + threadIdx.x] = __int_as_float(
+              in ? (int)rintf(fmaxf(fminf(e[I.off + (long long)y * I.w + x], cap), 0.f) *
+                              scale)
+                 : 0);
+        }
+      }
+    }
+    __syncthreads();
+    const TileLine ln{smf, nullptr, nullptr, nullptr, nullptr, l0 - halo,
+                      AXIS == 0 ? 1 : kTYC, AXIS == 0 ? 0 : (int)threadIdx.x,
+                      AXIS == 0 ? I.w : I.h};
+    auto one = [&](int i, long long p) {
+      float n = R.wc;
+      int full[2] = {0, 0}, nr[2] = {0, 0};
+      float wr[2] = {0.f, 0.f};
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {  // right, then left: the walks' order
+        int D = 0;
+        for (int m = 1;; ++m) {
+          const int q = side == 0 ? i + m : i - m;
+          if (side == 0 ? q >= ln.L : q < 0) break;
+          if (m > halo - 1) {  // past the staged halo
+            ovf = 1;
+            break;
+          }
+          D += side == 0 ? ln.E(q) : ln.E(q + 1);
+          if (D >= R.hiF) break;
+          const float w = R.w(D);
+          n += w;
+          if (D <= R.loF) {
+            ++full[side];
+          } else {
+            if (nr[side] == 0) wr[side] = w;
+            ++nr[side];
+          }
+        }
+      }
+      if (nr[0] > kPlanRamp || nr[1] > kPlanRamp) ovf = 1;
+      ext = max(ext, max(full[0] + nr[0], full[1] + nr[1]));
+      nout[p] = n;
+      counts[p] = (unsigned)min(full[1], 255) | (unsigned)min(full[0], 255) << 8 |
+                  (unsigned)min(nr[1], 3) << 16 | (unsigned)min(nr[0], 3) << 24;
+      wts[p] = make_float2(wr[1], wr[0]);
+    };
+    if (AXIS == 0) {
+      const int x = l0 + threadIdx.x;
+      if (x < I.w) one(x, I.off + (long long)cross * I.w + x);
+    } else {
+      const int x = cross + threadIdx.x;
+      for (int y = l0 + threadIdx.y; y < min(l0 + kTYR, I.h); y += kTYT) {
+        if (x >= I.w) break;
+        one(y, I.off + (long long)y * I.w + x);
+      }
+    }
+  }
+  __syncthreads();
+  atomicMax(&bext, ext);
+  if (ovf) atomicOr(&bovf, 1);
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    atomicMax(&stat[0], bext);
+    if (bovf) atomicOr(&stat[1], 1);
+  }
+}
+
 // sum_q w_pq V(q) over pixel i's planned window, and its weight n, in the
 // walks' order.
 template <class LN>
@@ -723,7 +828,9 @@ __device__ __forceinline__ float plan_sum(const LN& ln, int i, unsigned cnt, flo
   return S;
 }
 
-template <int AXIS>
+// X tiles of PX x 256 pixels (a thread takes pixels t, t + 256, ...): more
+// loads in flight per thread on wide images.
+template <int AXIS, int PX = 1>
 __global__ void __launch_bounds__(256)
     k_soft_half_plan(const SInst* __restrict__ insts, const float* __restrict__ vin,
                      float* __restrict__ vout, const unsigned* __restrict__ counts,
@@ -733,8 +840,8 @@ __global__ void __launch_bounds__(256)
                      float step, int halo) {
   extern __shared__ float smf[];
   const SInst I = insts[blockIdx.y];
-  const TileGeom<AXIS> G(I);
-  const int len = AXIS == 0 ? kTX : kTYR;
+  const int len = AXIS == 0 ? kTX * PX : kTYR;
+  const TileGeom<AXIS> G(I, len);
   const float* srcs[1] = {vin};
   float* dsts[1] = {smf};
   for (int tile = blockIdx.x; tile < G.n0 * G.n1; tile += gridDim.x) {
@@ -752,8 +859,11 @@ __global__ void __launch_bounds__(256)
       half_update(p, ln.V(i), n, S, t, c, vout, nullptr, Bout, data, mode, lambda, step);
     };
     if (AXIS == 0) {
-      const int x = l0 + threadIdx.x;
-      if (x < I.w) one(x, I.off + (long long)cross * I.w + x);
+#pragma unroll
+      for (int k = 0; k < PX; ++k) {
+        const int x = l0 + threadIdx.x + kTX * k;
+        if (x < I.w) one(x, I.off + (long long)cross * I.w + x);
+      }
     } else {
       const int x = cross + threadIdx.x;
       for (int y = l0 + threadIdx.y; y < min(l0 + kTYR, I.h); y += kTYT) {
@@ -771,7 +881,7 @@ __global__ void __launch_bounds__(256)
 // coef, plan_sum) and the ramp band's pair terms (diff) follow, in
 // soft_window_adj's order.  The same expressions as k_soft_pre +
 // k_soft_adjoint_tile, without their four intermediate planes.
-template <int AXIS>
+template <int AXIS, int PX = 1>
 __global__ void __launch_bounds__(256)
     k_soft_adjoint_fused(const SInst* __restrict__ insts, const float* __restrict__ a,
                          const float* __restrict__ nplan, const float* __restrict__ Bk,
@@ -782,10 +892,10 @@ __global__ void __launch_bounds__(256)
                          float* __restrict__ gc, int data, int mode, float lambda, float step,
                          float wc, int halo) {
   extern __shared__ float smf[];
-  constexpr int OWN = AXIS == 0 ? 1 : kTYR / kTYT;  // pixels per thread
+  constexpr int OWN = AXIS == 0 ? PX : kTYR / kTYT;  // pixels per thread
   const SInst I = insts[blockIdx.y];
-  const TileGeom<AXIS> G(I);
-  const int len = AXIS == 0 ? kTX : kTYR;
+  const int len = AXIS == 0 ? kTX * PX : kTYR;
+  const TileGeom<AXIS> G(I, len);
   const int TL = len + 2 * halo, TS = AXIS == 0 ? TL : TL * kTYC;
   const int nf = data ? 6 : 4;
   float* F[6] = {smf, smf + TS, smf + 2 * TS, smf + 3 * TS, smf + 4 * TS, smf + 5 * TS};
@@ -801,11 +911,11 @@ __global__ void __launch_bounds__(256)
                       AXIS == 0 ? I.w : I.h};
     // own pixel k: line index and global index (< 0: outside the image)
     auto own_i = [&](int k) -> int {
-      return AXIS == 0 ? l0 + (int)threadIdx.x : l0 + (int)threadIdx.y + kTYT * k;
+      return AXIS == 0 ? l0 + (int)threadIdx.x + kTX * k : l0 + (int)threadIdx.y + kTYT * k;
     };
     auto own_p = [&](int k) -> long long {
       if (AXIS == 0) {
-        const int x = l0 + threadIdx.x;
+        const int x = l0 + threadIdx.x + kTX * k;
         return x < I.w ? I.off + (long long)cross * I.w + x : -1;
       }
       const int x = cross + threadIdx.x, y = l0 + threadIdx.y + kTYT * k;
@@ -836,11 +946,12 @@ __global__ void __launch_bounds__(256)
     };
     float adg[OWN];
     if (AXIS == 0) {
-      // one own pixel a thread: transformed with its a * diag, the halo
-      // shared out over the first 2 halo threads
-      adg[0] = transform(ln.at(own_i(0)), own_p(0));
+      // own pixels transformed with their a * diag, the halo shared out
+      // over the first 2 halo threads
+#pragma unroll
+      for (int k = 0; k < OWN; ++k) adg[k] = transform(ln.at(own_i(k)), own_p(k));
       const int t = threadIdx.x;
-      if (t < 2 * halo) (void)transform(t < halo ? t : kTX + t, -1);
+      if (t < 2 * halo) (void)transform(t < halo ? t : len + t, -1);
     } else {
       // eight own pixels a thread: their a * diag (and dL/dt, dL/dc) first,
       // then the whole tile transformed, entries spread over the threads
@@ -1003,12 +1114,21 @@ int ensure_planes(dtsgb_soft_t s, int planes) {
 // holds 5 x 32 x (64 + 80) floats, 92 KB).
 constexpr int kMaxHalo = 40;
 
-long long max_tiles(const dtsgb_soft_s* s, int axis) {
+long long max_tiles(const dtsgb_soft_s* s, int axis, int px = 1) {
   long long m = 1;
+  const int lx = kTX * px;
   for (const SInst& I : s->inst)
-    m = std::max(m, axis == 0 ? (long long)((I.w + kTX - 1) / kTX) * I.h
+    m = std::max(m, axis == 0 ? (long long)((I.w + lx - 1) / lx) * I.h
                               : (long long)((I.h + kTYR - 1) / kTYR) * ((I.w + kTYC - 1) / kTYC));
   return m;
+}
+
+// Pixels per thread of the planned X kernels: 4 when the widest image spans
+// 1024 pixels.
+int plan_px(const dtsgb_soft_s* s) {
+  int w = 0;
+  for (const SInst& I : s->inst) w = std::max(w, I.w);
+  return w >= 4 * kTX ? 4 : 1;
 }
 
 // The tiles' halo for this solve's edge weights and sigma, tau: every walk
@@ -1059,6 +1179,37 @@ int fix_edges(dtsgb_soft_t s, float sigma, float tau) {
   return DTSGB_OK;
 }
 
+// Plans both axes' windows from shared-memory tiles of the float edge
+// weights (no fixed-point planes, no e_min); true when no window overflows.
+int plan_windows_tiled(dtsgb_soft_t s, float sigma, float tau, bool* ok) {
+  s->ramp = make_ramp(sigma, tau);
+  const float cap = (float)((double)sigma + 0.5 * (double)tau + 1.0);
+  const float scale = 1.f / s->ramp.scl;
+  DTSGB_CUDA(cudaMemsetAsync(s->d_stat, 0, 2 * sizeof(int), s->stream));
+  for (int axis = 0; axis < 2; ++axis) {
+    const int base = axis == 0 ? P_PNX : P_PNY;
+    const dim3 g((unsigned)std::min<long long>(max_tiles(s, axis), 152 * 16), s->n);
+    float* e = s->plane(axis == 0 ? P_EH : P_EV);
+    unsigned* cnt = reinterpret_cast<unsigned*>(s->plane(base + 1));
+    float2* wts = reinterpret_cast<float2*>(s->plane(base + 2));
+    if (axis == 0)
+      k_soft_plan_tile<0><<<g, kTX, sizeof(float) * (kTX + 2 * kPlanHalo), s->stream>>>(
+          s->d_inst, e, s->ramp, cap, scale, s->plane(base), cnt, wts, s->d_stat);
+    else
+      k_soft_plan_tile<1><<<g, dim3(kTYC, kTYT),
+                            sizeof(float) * (kTYR + 2 * kPlanHalo) * kTYC, s->stream>>>(
+          s->d_inst, e, s->ramp, cap, scale, s->plane(base), cnt, wts, s->d_stat);
+  }
+  DTSGB_CUDA(cudaGetLastError());
+  int st[2] = {0, 0};
+  DTSGB_CUDA(cudaMemcpyAsync(st, s->d_stat, sizeof st, cudaMemcpyDeviceToHost, s->stream));
+  DTSGB_CUDA(cudaStreamSynchronize(s->stream));
+  *ok = st[1] == 0;
+  s->plan_halo = st[0];
+  s->use_plan = *ok;
+  return DTSGB_OK;
+}
+
 // Plans both axes' windows; they are used when no side of any window has
 // more than kPlanRamp ramp pixels and every window fits the tiles' halo.
 int plan_windows(dtsgb_soft_t s) {
@@ -1089,8 +1240,12 @@ int launch_half(dtsgb_soft_t s, const float* vin, float* vout, const float* e, c
     const int PH = s->plan_halo, base = axis == 0 ? P_PNX : P_PNY;
     const unsigned* cnt = reinterpret_cast<const unsigned*>(s->plane(base + 1));
     const float2* wts = reinterpret_cast<const float2*>(s->plane(base + 2));
-    const dim3 g((unsigned)std::min<long long>(max_tiles(s, axis), 152 * 16), s->n);
-    if (axis == 0)
+    const int px = axis == 0 ? plan_px(s) : 1;
+    const dim3 g((unsigned)std::min<long long>(max_tiles(s, axis, px), 152 * 16), s->n);
+    if (axis == 0 && px == 4)
+      k_soft_half_plan<0, 4><<<g, kTX, sizeof(float) * (4 * kTX + 2 * PH), s->stream>>>(
+          s->d_inst, vin, vout, cnt, wts, t, c, Bout, data, mode, R.wc, lambda, step, PH);
+    else if (axis == 0)
       k_soft_half_plan<0><<<g, kTX, sizeof(float) * (kTX + 2 * PH), s->stream>>>(
           s->d_inst, vin, vout, cnt, wts, t, c, Bout, data, mode, R.wc, lambda, step, PH);
     else
@@ -1172,8 +1327,18 @@ int launch_adjoint_fused(dtsgb_soft_t s, const float* a, const float* Bk, const 
   const float* nplan = s->plane(base);
   const float wc = s->ramp.wc;
   const int nf = data ? 6 : 4;
-  const dim3 g((unsigned)std::min<long long>(max_tiles(s, axis), 152 * 16), s->n);
-  if (axis == 0) {
+  const int px = axis == 0 ? plan_px(s) : 1;
+  const dim3 g((unsigned)std::min<long long>(max_tiles(s, axis, px), 152 * 16), s->n);
+  int max_w = 1, max_h = 1;
+  for (const SInst& I : s->inst) {
+    max_w = std::max(max_w, I.w);
+    max_h = std::max(max_h, I.h);
+  }
+  if (axis == 0 && px == 4) {
+    k_soft_adjoint_fused<0, 4><<<g, kTX, sizeof(float) * nf * (4 * kTX + 2 * PH), s->stream>>>(
+        s->d_inst, a, nplan, Bk, val, t, c, cnt, wts, aout, diff, gt, gc, data, mode, lambda,
+        step, wc, PH);
+  } else if (axis == 0) {
     k_soft_adjoint_fused<0><<<g, kTX, sizeof(float) * nf * (kTX + 2 * PH), s->stream>>>(
         s->d_inst, a, nplan, Bk, val, t, c, cnt, wts, aout, diff, gt, gc, data, mode, lambda,
         step, wc, PH);
@@ -1186,11 +1351,6 @@ int launch_adjoint_fused(dtsgb_soft_t s, const float* a, const float* Bk, const 
         step, wc, PH);
   }
   DTSGB_CUDA(cudaGetLastError());
-  int max_w = 1, max_h = 1;
-  for (const SInst& I : s->inst) {
-    max_w = std::max(max_w, I.w);
-    max_h = std::max(max_h, I.h);
-  }
   if (axis == 0)
     k_soft_edge_scan_x<<<dim3((unsigned)std::min(1024, (max_h + 7) / 8), s->n), kST, 0,
                          s->stream>>>(s->d_inst, diff, ge, tau);
@@ -1348,9 +1508,13 @@ DTSGB_API int dtsgb_soft_solve(dtsgb_soft_t s, const float* const* dH, const flo
   const dim3 g = soft_grid(s);
   const int mode = p->loss == DTSGB_L2 ? 0 : 1;
   if (N > 0) {
-    if (int st = soft_halo(s, p->sigma_z, tau, &s->halo)) return st;
-    if (int st = fix_edges(s, p->sigma_z, tau)) return st;
-    if (int st = plan_windows(s)) return st;
+    bool planned = false;
+    if (int st = plan_windows_tiled(s, p->sigma_z, tau, &planned)) return st;
+    if (!planned) {  // the walking kernels' fixed-point planes and halo, and a global plan
+      if (int st = soft_halo(s, p->sigma_z, tau, &s->halo)) return st;
+      if (int st = fix_edges(s, p->sigma_z, tau)) return st;
+      if (int st = plan_windows(s)) return st;
+    }
   }
   for (int k = 0; k < N; ++k) {
     if (int st = launch_half(s, s->plane(P_ITER + k), s->kept(0, k), s->plane(P_FH),

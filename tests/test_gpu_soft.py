@@ -108,15 +108,17 @@ def _check_against_oracle(O, data, eh_all, ev_all, opt, res):
             assert float(np.mean(err > bar)) <= 1e-3, (float(err.max()), bar)
 
 
+@pytest.mark.parametrize("sizes", [[(1100, 40), (45, 130)], [(1024, 30), (300, 70)]])
 @pytest.mark.parametrize("scale", [1.0, 0.1])
-def test_soft_ragged_tiles_and_small_weights(gpu_ready, oracle_mod, scale):
+def test_soft_ragged_tiles_and_small_weights(gpu_ready, oracle_mod, scale, sizes):
     """Instances that span several shared-memory tiles, with partial ones
-    (300 x 70, 45 x 130), and the same with edge weights scaled by 0.1, whose
-    windows reach past the tiles' largest halo: those solves run the
-    global-memory kernels.  Both are held to the oracle's bars."""
+    (1100 x 40: rows wider than 1024 pixels, whose X kernels take four pixels
+    a thread; 45 x 130), rows of exactly 1024 pixels, and the same with
+    edge weights scaled by 0.1, whose windows reach past the tiles' largest
+    halo: those solves run the global-memory kernels.  All are held to the
+    oracle's bars."""
     D = gpu_ready
     import torch
-    sizes = [(300, 70), (45, 130)]
     data = [_inputs(800 + i, w, h) for i, (w, h) in enumerate(sizes)]
     opt = dict(num_iterations=4, loss=1, lambda_=0.99, sigma_z=8.0, step_size=0.99)
     s = D.SoftDTS(sizes)
