@@ -40,11 +40,14 @@
 // result and each half-step's n and B, so the adjoint of a half-step is a
 // pointwise pass (coef, alpha, beta, a * diag) and one window walk per pixel
 // (k_soft_adjoint*), which also collects the ramp-band pair terms of its
-// own pixel (diff); dL/de is then a prefix of diff along each line
-// (k_soft_edge_scan, FP64).  When every window ends within 40 pixels (the
-// smallest edge weight bounds it) the walks read shared-memory tiles of the
-// lines (k_*_tile: 256 pixels of a row, or 32 columns x 64 rows, staged once
-// with their halo); otherwise a thread per pixel reads global memory.
+// own pixel (diff, summed over the iterations); dL/de is then one prefix of
+// diff along each line (k_soft_edge_scan, compensated).  The edge weights
+// are fixed through a solve, so each pixel's window is planned once
+// (k_soft_plan*) and the half-steps and adjoints sum planned windows over
+// shared-memory tiles of the lines (rows of 256 or 1024 pixels, or 32
+// columns x 64 rows, staged once with their halo).  Windows a plan cannot
+// hold are walked: from tiles when the smallest edge weight bounds them
+// within 40 pixels, otherwise by a thread per pixel over global memory.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -78,6 +81,7 @@ struct SInst {
 // weights n and means B of both half-steps (kept for the adjoint)
 enum {
   P_EH = 0, P_EV, P_FH, P_FV, P_T, P_C, P_U, P_COEF, P_ALPHA, P_BETA, P_ADIAG, P_DIFF,
+  P_DIFFY,
   P_G0, P_G1, P_GT, P_GC, P_GEH, P_GEV,
   // window plans (k_soft_plan): n, counts, and two planes of float2 weights per axis
   P_PNX, P_PCX, P_PWX, P_PNY = P_PWX + 2, P_PCY, P_PWY, P_ITER = P_PWY + 2
@@ -500,7 +504,7 @@ __global__ void k_soft_adjoint(const SInst* __restrict__ insts, const float* __r
     soft_window_adj(ln, l.i, R, &n, &S, &d);
     const long long p = I.off + k;
     aout[p] = __fmaf_rn(lambda, S, adiag[p]);
-    diff[p] = d;
+    diff[p] += d;
   }
 }
 
@@ -531,7 +535,7 @@ __global__ void __launch_bounds__(256)
       float n, S, d;
       soft_window_adj(ln, i, R, &n, &S, &d);
       aout[p] = __fmaf_rn(lambda, S, adiag[p]);
-      diff[p] = d;
+      diff[p] += d;
     };
     if (AXIS == 0) {
       const int x = l0 + threadIdx.x;
@@ -996,7 +1000,7 @@ __global__ void __launch_bounds__(256)
         const int aa = i - dl - 1;
         d -= __fmaf_rn(ln.A(aa), xi, ln.Bt(aa)) + __fmaf_rn(ai, ln.X(aa), bi);
       }
-      diff[p] = d;
+      diff[p] += d;
     }
   }
 }
@@ -1276,7 +1280,7 @@ int launch_adjoint(dtsgb_soft_t s, const float* adiag, const float* coef, const 
                    const float* beta, const float* val, const float* e, float* aout, float* ge,
                    int axis, float tau, float lambda) {
   ProfScope ps(s->stream, DTSGB_K_SOFT);
-  float* diff = s->plane(P_DIFF);
+  float* diff = s->plane(axis == 0 ? P_DIFF : P_DIFFY);
   const int H = s->halo;
   const Ramp R = s->ramp;
   if (H > kMaxHalo) {
@@ -1298,29 +1302,17 @@ int launch_adjoint(dtsgb_soft_t s, const float* adiag, const float* coef, const 
     }
   }
   DTSGB_CUDA(cudaGetLastError());
-  int max_w = 1, max_h = 1;
-  for (const SInst& I : s->inst) {
-    max_w = std::max(max_w, I.w);
-    max_h = std::max(max_h, I.h);
-  }
-  if (axis == 0)
-    k_soft_edge_scan_x<<<dim3((unsigned)std::min(1024, (max_h + 7) / 8), s->n), kST, 0,
-                         s->stream>>>(s->d_inst, diff, ge, tau);
-  else
-    k_soft_edge_scan_y<<<dim3((unsigned)std::min(1024, (max_w + 31) / 32), s->n), dim3(32, 32),
-                         0, s->stream>>>(s->d_inst, diff, ge, tau);
-  DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
 }
 
 // The planned adjoint of one half-step with its pointwise pass fused in
-// (k_soft_adjoint_fused), then the edge-weight prefix.
+// (k_soft_adjoint_fused); its band pair terms add into the axis's diff plane.
 int launch_adjoint_fused(dtsgb_soft_t s, const float* a, const float* Bk, const float* val,
                          const float* t, const float* c, float* aout, float* ge, float* gt,
                          float* gc, int axis, int data, int mode, float tau, float lambda,
                          float step) {
   ProfScope ps(s->stream, DTSGB_K_SOFT);
-  float* diff = s->plane(P_DIFF);
+  float* diff = s->plane(axis == 0 ? P_DIFF : P_DIFFY);
   const int PH = s->plan_halo, base = axis == 0 ? P_PNX : P_PNY;
   const unsigned* cnt = reinterpret_cast<const unsigned*>(s->plane(base + 1));
   const float2* wts = reinterpret_cast<const float2*>(s->plane(base + 2));
@@ -1329,11 +1321,6 @@ int launch_adjoint_fused(dtsgb_soft_t s, const float* a, const float* Bk, const 
   const int nf = data ? 6 : 4;
   const int px = axis == 0 ? plan_px(s) : 1;
   const dim3 g((unsigned)std::min<long long>(max_tiles(s, axis, px), 152 * 16), s->n);
-  int max_w = 1, max_h = 1;
-  for (const SInst& I : s->inst) {
-    max_w = std::max(max_w, I.w);
-    max_h = std::max(max_h, I.h);
-  }
   if (axis == 0 && px == 4) {
     k_soft_adjoint_fused<0, 4><<<g, kTX, sizeof(float) * nf * (4 * kTX + 2 * PH), s->stream>>>(
         s->d_inst, a, nplan, Bk, val, t, c, cnt, wts, aout, diff, gt, gc, data, mode, lambda,
@@ -1351,12 +1338,22 @@ int launch_adjoint_fused(dtsgb_soft_t s, const float* a, const float* Bk, const 
         step, wc, PH);
   }
   DTSGB_CUDA(cudaGetLastError());
-  if (axis == 0)
-    k_soft_edge_scan_x<<<dim3((unsigned)std::min(1024, (max_h + 7) / 8), s->n), kST, 0,
-                         s->stream>>>(s->d_inst, diff, ge, tau);
-  else
-    k_soft_edge_scan_y<<<dim3((unsigned)std::min(1024, (max_w + 31) / 32), s->n), dim3(32, 32),
-                         0, s->stream>>>(s->d_inst, diff, ge, tau);
+  return DTSGB_OK;
+}
+
+// The edge-weight gradients from the band pair terms summed over all the
+// iterations (the prefix is linear, so one per axis serves them all).
+int launch_edge_scans(dtsgb_soft_t s, float tau) {
+  ProfScope ps(s->stream, DTSGB_K_SOFT);
+  int max_w = 1, max_h = 1;
+  for (const SInst& I : s->inst) {
+    max_w = std::max(max_w, I.w);
+    max_h = std::max(max_h, I.h);
+  }
+  k_soft_edge_scan_x<<<dim3((unsigned)std::min(1024, (max_h + 7) / 8), s->n), kST, 0,
+                       s->stream>>>(s->d_inst, s->plane(P_DIFF), s->plane(P_GEH), tau);
+  k_soft_edge_scan_y<<<dim3((unsigned)std::min(1024, (max_w + 31) / 32), s->n), dim3(32, 32), 0,
+                       s->stream>>>(s->d_inst, s->plane(P_DIFFY), s->plane(P_GEV), tau);
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
 }
@@ -1543,7 +1540,7 @@ DTSGB_API int dtsgb_soft_backward(dtsgb_soft_t s, const float* const* grad_out,
   const int N = s->n_iter, mode = p.loss == DTSGB_L2 ? 0 : 1;
   const float tau = s->tau, sg = p.sigma_z, lam = p.lambda, step = p.step_size;
   if (int st = copy_planes(s, grad_out, P_G0, true)) return st;
-  for (int k : {P_GT, P_GC, P_GEH, P_GEV})
+  for (int k : {P_GT, P_GC, P_GEH, P_GEV, P_DIFF, P_DIFFY})
     DTSGB_CUDA(cudaMemsetAsync(s->plane(k), 0, (size_t)s->total * 4, s->stream));
   const dim3 g = soft_grid(s);
   float* a = s->plane(P_G0);
@@ -1582,6 +1579,7 @@ DTSGB_API int dtsgb_soft_backward(dtsgb_soft_t s, const float* const* grad_out,
                                 tau, lam))
       return st;
   }
+  if (int st = launch_edge_scans(s, tau)) return st;
   // v_0 = t
   SOFT_LAUNCH(k_soft_axpy, g, s->stream, s->d_inst, a, s->plane(P_GT));
   DTSGB_CUDA(cudaGetLastError());
