@@ -11,7 +11,10 @@ by instance with the FP64 oracle.
   batch's windows, RMSE <= 1e-4 x range against the oracle's own windows;
 * HFBS result: against the oracle on the BF16-rounded inputs (bar below);
 * adjoint: dL/dtarget, dL/dconfidence against the oracle's adjoint, and
-  FP64 central differences of the oracle's forward on 256 entries.
+  FP64 central differences of the oracle's forward on 256 entries;
+* the same 16 x 1024x768 batch through the soft-window solve with its
+  edge-weight gradients (bench.py's cfg4soft): forward and all four
+  gradients against the oracle's soft-window restatement.
 
 A line per instance is printed (pytest -s shows them)."""
 import numpy as np
@@ -267,6 +270,55 @@ def test_cfg4_adjoint_fp64_central_differences(cfg4, oracle_mod):
     print(f"cfg4 FD: 256 entries in {len(groups)} groups (R = {R}); worst |GPU - FD| / "
           f"max|grad|: dL/dt {worst['t']:.2e}, dL/dc {worst['c']:.2e}")
     assert not bad, bad[:5]
+
+
+def test_cfg4soft_forward_and_gradients_against_oracle(gpu_ready, oracle_mod):
+    """Every instance of the 16 x 1024x768 batch: the soft-window forward
+    within 1e-4 x target range, and dL/dt, dL/dc, dL/ddH, dL/ddV with at
+    most 0.1% of entries past 1e-4 x max |gradient| (a pair whose FP32
+    distance lands on the other side of a ramp end than the FP64 one moves
+    that entry by its pair term)."""
+    torch = pytest.importorskip("torch")
+    D = gpu_ready
+    from domain_transform_solver_gb300 import workloads as W
+    insts, grads = W.grad_instances()
+    n = len(insts)
+    sizes = [(i.width, i.height) for i in insts]
+    s = D.SoftDTS(sizes)
+    dev = torch.device("cuda")
+    rgba = torch.from_numpy(np.stack([i.rgba for i in insts])).to(dev)
+    t = torch.from_numpy(np.stack([i.target for i in insts])).to(dev)
+    c = torch.from_numpy(np.stack([i.confidence for i in insts])).to(dev)
+    g = torch.from_numpy(np.stack(grads)).to(dev)
+    dh, dv, out = torch.empty_like(t), torch.empty_like(t), torch.empty_like(t)
+    gr = [torch.empty_like(t) for _ in range(4)]
+    p = lambda x: [x[k].data_ptr() for k in range(n)]  # noqa: E731
+    opt = dict(W.CFG0_OPT)
+    s.edge_weights(D.COLOR_SPACE.YCbCr, p(rgba), D.DomainFilterParams(**W.CFG0_FILTER),
+                   p(dh), p(dv))
+    s.solve(p(dh), p(dv), p(t), p(c), D.DomainOptimizeParams(**opt), 1.0, p(out))
+    s.backward(p(g), *[p(x) for x in gr])
+    torch.cuda.synchronize()
+    s.close()
+    eh, ev, v = dh.cpu().numpy(), dv.cpu().numpy(), out.cpu().numpy()
+    grs = [x.cpu().numpy() for x in gr]
+    worst = [0.0] * 5
+    for k, inst in enumerate(insts):
+        rng_t = P.target_range(inst.target)
+        ref = oracle_mod.soft_solve(eh[k], ev[k], inst.target, inst.confidence, opt, 1.0)
+        e = float(np.abs(v[k] - ref).max()) / rng_t
+        assert e <= P.TOL_REL, (k, e)
+        worst[0] = max(worst[0], e)
+        rg = oracle_mod.soft_backward(eh[k], ev[k], inst.target, inst.confidence, opt, 1.0,
+                                      grads[k])
+        for j, (got, r) in enumerate(zip((x[k] for x in grs), rg)):
+            bar = TOL_GRAD * max(float(np.abs(r).max()), 1e-12)
+            frac = float(np.mean(np.abs(got - r) > bar))
+            assert frac <= 1e-3, (k, j, frac)
+            worst[j + 1] = max(worst[j + 1], frac)
+        print(f"cfg4soft instance {k}: result {e:.1e} x range")
+    print("cfg4soft worst: result %.1e x range; entries past the bar: t %.1e, c %.1e, "
+          "dH %.1e, dV %.1e" % tuple(worst))
 
 
 def test_no_staging_wait_gave_up(gpu_ready):
