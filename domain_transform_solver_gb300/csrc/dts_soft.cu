@@ -1277,8 +1277,8 @@ int launch_half(dtsgb_soft_t s, const float* vin, float* vout, const float* e, c
 }
 
 int launch_adjoint(dtsgb_soft_t s, const float* adiag, const float* coef, const float* alpha,
-                   const float* beta, const float* val, const float* e, float* aout, float* ge,
-                   int axis, float tau, float lambda) {
+                   const float* beta, const float* val, const float* e, float* aout, int axis,
+                   float lambda) {
   ProfScope ps(s->stream, DTSGB_K_SOFT);
   float* diff = s->plane(axis == 0 ? P_DIFF : P_DIFFY);
   const int H = s->halo;
@@ -1308,9 +1308,8 @@ int launch_adjoint(dtsgb_soft_t s, const float* adiag, const float* coef, const 
 // The planned adjoint of one half-step with its pointwise pass fused in
 // (k_soft_adjoint_fused); its band pair terms add into the axis's diff plane.
 int launch_adjoint_fused(dtsgb_soft_t s, const float* a, const float* Bk, const float* val,
-                         const float* t, const float* c, float* aout, float* ge, float* gt,
-                         float* gc, int axis, int data, int mode, float tau, float lambda,
-                         float step) {
+                         const float* t, const float* c, float* aout, float* gt, float* gc,
+                         int axis, int data, int mode, float lambda, float step) {
   ProfScope ps(s->stream, DTSGB_K_SOFT);
   float* diff = s->plane(axis == 0 ? P_DIFF : P_DIFFY);
   const int PH = s->plan_halo, base = axis == 0 ? P_PNX : P_PNY;
@@ -1538,7 +1537,7 @@ DTSGB_API int dtsgb_soft_backward(dtsgb_soft_t s, const float* const* grad_out,
   if (s->n_iter < 0) return fail(DTSGB_ERR_INVALID_ARGUMENT, "no soft solve to differentiate");
   const dtsgb_optimize_params& p = s->opt;
   const int N = s->n_iter, mode = p.loss == DTSGB_L2 ? 0 : 1;
-  const float tau = s->tau, sg = p.sigma_z, lam = p.lambda, step = p.step_size;
+  const float tau = s->tau, lam = p.lambda, step = p.step_size;
   if (int st = copy_planes(s, grad_out, P_G0, true)) return st;
   for (int k : {P_GT, P_GC, P_GEH, P_GEV, P_DIFF, P_DIFFY})
     DTSGB_CUDA(cudaMemsetAsync(s->plane(k), 0, (size_t)s->total * 4, s->stream));
@@ -1551,13 +1550,12 @@ DTSGB_API int dtsgb_soft_backward(dtsgb_soft_t s, const float* const* grad_out,
     if (s->use_plan) {
       // Y^T: a = dL/dv_{k+1} -> b = dL/du, and dL/ddV; X^T: b -> a = dL/dv_k,
       // dL/dt, dL/dc and dL/ddH
-      if (int st = launch_adjoint_fused(s, a, s->kept(4, k), uk, nullptr, nullptr, b,
-                                        s->plane(P_GEV), nullptr, nullptr, 1, 0, mode, tau, lam,
-                                        step))
+      if (int st = launch_adjoint_fused(s, a, s->kept(4, k), uk, nullptr, nullptr, b, nullptr,
+                                        nullptr, 1, 0, mode, lam, step))
         return st;
       if (int st = launch_adjoint_fused(s, b, s->kept(2, k), vk, s->plane(P_T), s->plane(P_C),
-                                        a, s->plane(P_GEH), s->plane(P_GT), s->plane(P_GC), 0, 1,
-                                        mode, tau, lam, step))
+                                        a, s->plane(P_GT), s->plane(P_GC), 0, 1, mode, lam,
+                                        step))
         return st;
       continue;
     }
@@ -1566,8 +1564,7 @@ DTSGB_API int dtsgb_soft_backward(dtsgb_soft_t s, const float* const* grad_out,
                 nullptr, nullptr, s->plane(P_COEF), s->plane(P_ALPHA), s->plane(P_BETA),
                 s->plane(P_ADIAG), nullptr, nullptr, 0, mode, lam, step);
     if (int st = launch_adjoint(s, s->plane(P_ADIAG), s->plane(P_COEF), s->plane(P_ALPHA),
-                                s->plane(P_BETA), uk, s->plane(P_FV), b, s->plane(P_GEV), 1,
-                                tau, lam))
+                                s->plane(P_BETA), uk, s->plane(P_FV), b, 1, lam))
       return st;
     // X^T: b = dL/du -> a = dL/dv_k, dL/dt, dL/dc and dL/ddH
     SOFT_LAUNCH(k_soft_pre, g, s->stream, s->d_inst, vk, b, s->kept(1, k), s->kept(2, k),
@@ -1575,8 +1572,7 @@ DTSGB_API int dtsgb_soft_backward(dtsgb_soft_t s, const float* const* grad_out,
                 s->plane(P_BETA), s->plane(P_ADIAG), s->plane(P_GT), s->plane(P_GC), 1, mode,
                 lam, step);
     if (int st = launch_adjoint(s, s->plane(P_ADIAG), s->plane(P_COEF), s->plane(P_ALPHA),
-                                s->plane(P_BETA), vk, s->plane(P_FH), a, s->plane(P_GEH), 0,
-                                tau, lam))
+                                s->plane(P_BETA), vk, s->plane(P_FH), a, 0, lam))
       return st;
   }
   if (int st = launch_edge_scans(s, tau)) return st;

@@ -268,11 +268,16 @@ __global__ void k_laplace_x(const HInst* __restrict__ insts,
 // a15: Laplace sweep along one axis for two fields at once (src/hfbs.cu:
 // 355-427): d(i) = sum_j beta^|i-j| s(j), forward then backward recursion,
 // one thread per grid line (used along y and l, where consecutive threads
-// take consecutive x and the accesses coalesce).
+// take consecutive x and the accesses coalesce).  The recursions are serial,
+// their loads are not: each thread loads kLapChunk elements of a line before
+// it runs the recursion over them, so that a chunk's loads are in flight
+// together instead of one load latency per element.
+constexpr int kLapChunk = 8;
 __global__ void k_laplace(const HInst* __restrict__ insts, int axis,
                           const float* __restrict__ s0, float* __restrict__ d0,
                           const float* __restrict__ s1, float* __restrict__ d1,
                           float beta) {
+  constexpr int U = kLapChunk;
   const HInst I = insts[blockIdx.y];
   const int gx = I.gx, gy = I.gy, gl = I.gl;
   int len, na, nlines;
@@ -294,19 +299,43 @@ __global__ void k_laplace(const HInst* __restrict__ insts, int axis,
     else base = (long long)bb * px + a;
     base += I.grid_off;
     for (int f = 0; f < 2; ++f) {
-      const float* s = f ? s1 : s0;
-      float* d = f ? d1 : d0;
-      float r = s[base];
-      d[base] = r;
-      for (int i = 1; i < len; ++i) {
-        r = __fmaf_rn(beta, r, s[base + i * stride]);
-        d[base + i * stride] = r;
+      const float* s = (f ? s1 : s0) + base;
+      float* d = (f ? d1 : d0) + base;
+      // forward: d(0) = s(0), d(i) = beta * d(i-1) + s(i)
+      float r = 0.f;
+      for (int i0 = 0; i0 < len; i0 += U) {
+        float v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) v[u] = i0 + u < len ? s[(i0 + u) * stride] : 0.f;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = i0 + u;
+          if (i < len) {
+            r = i == 0 ? v[u] : __fmaf_rn(beta, r, v[u]);
+            d[i * stride] = r;
+          }
+        }
       }
-      r = s[base + (long long)(len - 1) * stride];
-      for (int i = len - 2; i >= 0; --i) {
-        r = beta * r;
-        d[base + i * stride] = d[base + i * stride] + r;
-        r = r + s[base + i * stride];
+      // backward: r(len-1) = s(len-1); for i < len-1: r = beta * r,
+      // d(i) += r, r += s(i)
+      r = s[(long long)(len - 1) * stride];
+      for (int i0 = len - 2; i0 >= 0; i0 -= U) {
+        float v[U], w[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = i0 - u;
+          v[u] = i >= 0 ? s[i * stride] : 0.f;
+          w[u] = i >= 0 ? d[i * stride] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = i0 - u;
+          if (i >= 0) {
+            r = beta * r;
+            d[i * stride] = w[u] + r;
+            r = r + v[u];
+          }
+        }
       }
     }
   }
@@ -956,7 +985,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
   } else {
     groups.push_back(Group{0, ni, B.max_cells});
   }
-  // column kernels (bistochastization, heavy-ball): one thread per (x, y)
+  // column kernels (bistochastization): one thread per (x, y)
   auto col_grid = [](const Group& g) {
     return dim3((unsigned)std::min<long long>((g.cols + kT - 1) / kT, 4096), g.count);
   };
