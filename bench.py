@@ -51,7 +51,10 @@ L2_FLUSH_BYTES = 256 << 20
 KERNEL_NAMES = {0: "k_bounds", 1: "k_dts_iter", 2: "k_filter", 3: "k_splat",
                 4: "k_bistoch", 5: "k_solve (HFBS heavy-ball)", 6: "hfbs setup kernels",
                 7: "k_slice", 8: "k_to_float", 9: "k_dts_adjoint",
-                10: "hfbs adjoint (whole backward)", 11: "soft-window kernels"}
+                10: "hfbs adjoint (whole backward)",
+                11: "soft-window plans, line scans and other",
+                12: "k_soft_half_plan (X and Y)", 13: "k_soft_adjoint_fused X",
+                14: "k_soft_adjoint_fused Y"}
 HFBS_TB_STEPS = 4  # heavy-ball steps per launch of the temporally blocked kernel
 
 
@@ -885,10 +888,18 @@ class Cfg4Soft(Batched):
         return self.pixels * 20, self.pixels * 20
 
     def fused_bytes(self):
-        return {}
+        """Per step: the planned half-steps (X reads v, the plan's counts and
+        ramp weights, t, c and writes v, B: 32 B/px; Y 24 B/px) and adjoints
+        (X reads a, n, B, x, t, c and the plan, reads and writes dL/dt, dL/dc
+        and the band pair sums, writes a': 64 B/px; Y 40 B/px), once per
+        iteration each."""
+        px, it = self.pixels, self.iters
+        return {12: px * (32 + 24) * it, 13: px * 64 * it, 14: px * 40 * it}
 
     def pass_model_bytes(self):
-        return {}
+        # the reference has no soft-window form: its pass model is the
+        # fused contract
+        return self.fused_bytes()
 
     def reference_subset(self):
         return [0]  # the oracle's soft adjoint is serial: one instance per step

@@ -63,8 +63,9 @@ namespace {
 
 constexpr int kST = 256;
 
-// Launches of this file's kernels, timed by the library's profiler as one
-// kind (DTSGB_K_SOFT) when it is on.
+// Launches of this file's kernels, timed by the library's profiler when it
+// is on: the planned half-steps (DTSGB_K_SOFT_HALF) and adjoints
+// (DTSGB_K_SOFT_ADJ_X, _Y) by kind, everything else as DTSGB_K_SOFT.
 #define SOFT_LAUNCH(kernel, grid, stream, ...)            \
   do {                                                    \
     ProfScope ps_((stream), DTSGB_K_SOFT);                \
@@ -1237,7 +1238,7 @@ int plan_windows(dtsgb_soft_t s) {
 int launch_half(dtsgb_soft_t s, const float* vin, float* vout, const float* e, const float* t,
                 const float* c, float* nout, float* Bout, int axis, int data, int mode,
                 float lambda, float step) {
-  ProfScope ps(s->stream, DTSGB_K_SOFT);
+  ProfScope ps(s->stream, s->use_plan ? DTSGB_K_SOFT_HALF : DTSGB_K_SOFT);
   const int H = s->halo;
   const Ramp R = s->ramp;
   if (s->use_plan) {
@@ -1310,7 +1311,7 @@ int launch_adjoint(dtsgb_soft_t s, const float* adiag, const float* coef, const 
 int launch_adjoint_fused(dtsgb_soft_t s, const float* a, const float* Bk, const float* val,
                          const float* t, const float* c, float* aout, float* gt, float* gc,
                          int axis, int data, int mode, float lambda, float step) {
-  ProfScope ps(s->stream, DTSGB_K_SOFT);
+  ProfScope ps(s->stream, axis == 0 ? DTSGB_K_SOFT_ADJ_X : DTSGB_K_SOFT_ADJ_Y);
   float* diff = s->plane(axis == 0 ? P_DIFF : P_DIFFY);
   const int PH = s->plan_halo, base = axis == 0 ? P_PNX : P_PNY;
   const unsigned* cnt = reinterpret_cast<const unsigned*>(s->plane(base + 1));
