@@ -818,10 +818,15 @@ class Cfg4Soft(Batched):
     dtype = "f32"
     tau = 1.0
 
-    def __init__(self, rank: int = 0, world: int = 1):
+    def __init__(self, rank: int = 0, world: int = 1, instances: int = None):
         W = workloads_module()
         self.W = W
         n, w, h = 16, 1024, 768
+        # instances < 16 keeps the first ones (profiling captures of a
+        # smaller case); the reported workload is all 16
+        if instances is not None and instances < n:
+            n = max(1, instances)
+            self.name = f"{self.name}_first{n}"
         self.n_total = n
         if world > 1:
             from domain_transform_solver_gb300.sharding import partition_lpt
@@ -934,6 +939,8 @@ def make_workload(args, rank, world):
                                         e2e_chunks=args.e2e_chunks or 16)
     if args.workload == "cfg4":
         return Cfg4(rank, world, e2e_chunks=args.e2e_chunks or 4)
+    if args.workload == "cfg4soft":
+        return Cfg4Soft(rank, world, instances=args.instances)
     return WORKLOADS[args.workload](rank, world)
 
 
@@ -1252,6 +1259,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="cfg3")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="cfg3 only: shrink every instance (smaller profiling case)")
+    ap.add_argument("--instances", type=int, default=None,
+                    help="cfg4soft only: the first N of the 16 instances (smaller profiling case)")
     ap.add_argument("--e2e-chunks", type=int, default=None,
                     help="chunks of the overlapped host-to-host e2e run (cfg3: 16, cfg4: 4)")
     ap.add_argument("--no-autotune", action="store_true",

@@ -63,8 +63,8 @@ namespace {
 
 constexpr int kST = 256;
 
-// Launches of this file's kernels, timed by the library's profiler when it
-// is on: the planned half-steps (DTSGB_K_SOFT_HALF) and adjoints
+// Every launch of this file's kernels is timed by the library's profiler
+// when it is on: the planned half-steps (DTSGB_K_SOFT_HALF) and adjoints
 // (DTSGB_K_SOFT_ADJ_X, _Y) by kind, everything else as DTSGB_K_SOFT.
 #define SOFT_LAUNCH(kernel, grid, stream, ...)            \
   do {                                                    \
@@ -379,27 +379,58 @@ struct TileGeom {
   }
 };
 
-// Stages `nf` planes of one tile (line positions [l0 - halo, l0 + len +
+// Stages NF planes of one tile (line positions [l0 - halo, l0 + len +
 // halo) of the lines of the tile) into shared memory, zero outside the image.
-template <int AXIS>
+// A thread loads U entries of every plane into registers before it stores
+// any: the stores go through generic pointers that the compiler cannot tell
+// apart from the planes' addresses, so a store between two loads would
+// serialise them (one memory latency per entry and plane).
+template <int AXIS, int NF>
 __device__ __forceinline__ void stage_tile(const SInst& I, int l0, int cross,
-                                           const float* const* src, float* const* dst, int nf,
+                                           const float* const* src, float* const* dst,
                                            int halo, int len) {
+  constexpr int U = NF > 4 ? 2 : 4;  // line positions per batch
   const int TL = len + 2 * halo;
   if (AXIS == 0) {  // one row `cross`
     const long long row = I.off + (long long)cross * I.w;
-    for (int i = threadIdx.x; i < TL; i += kTX) {
-      const int x = l0 - halo + i;
-      const bool in = x >= 0 && x < I.w;
-      for (int f = 0; f < nf; ++f) dst[f][i] = in ? src[f][row + x] : 0.f;
+    for (int i0 = threadIdx.x; i0 < TL; i0 += U * kTX) {
+      float v[U][NF];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int x = l0 - halo + i0 + u * kTX;
+        const bool in = i0 + u * kTX < TL && x >= 0 && x < I.w;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) v[u][f] = in ? src[f][row + x] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * kTX;
+        if (i < TL) {
+#pragma unroll
+          for (int f = 0; f < NF; ++f) dst[f][i] = v[u][f];
+        }
+      }
     }
   } else {  // columns cross .. cross + kTYC - 1
     const int x = cross + threadIdx.x;
-    for (int i = threadIdx.y; i < TL; i += kTYT) {
-      const int y = l0 - halo + i;
-      const bool in = x < I.w && y >= 0 && y < I.h;
-      const long long p = I.off + (long long)y * I.w + x;
-      for (int f = 0; f < nf; ++f) dst[f][i * kTYC + threadIdx.x] = in ? src[f][p] : 0.f;
+    for (int i0 = threadIdx.y; i0 < TL; i0 += U * kTYT) {
+      float v[U][NF];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int y = l0 - halo + i0 + u * kTYT;
+        const bool in = i0 + u * kTYT < TL && x < I.w && y >= 0 && y < I.h;
+        const long long p = I.off + (long long)y * I.w + x;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) v[u][f] = in ? src[f][p] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * kTYT;
+        if (i < TL) {
+#pragma unroll
+          for (int f = 0; f < NF; ++f) dst[f][i * kTYC + threadIdx.x] = v[u][f];
+        }
+      }
     }
   }
 }
@@ -424,7 +455,7 @@ __global__ void __launch_bounds__(256)
     const int t1 = tile / G.n0, t0 = tile - t1 * G.n0;
     const int l0 = t0 * len, cross = AXIS == 0 ? t1 : t1 * kTYC;
     __syncthreads();  // the previous tile's walks are done
-    stage_tile<AXIS>(I, l0, cross, srcs, dsts, 2, halo, len);
+    stage_tile<AXIS, 2>(I, l0, cross, srcs, dsts, halo, len);
     __syncthreads();
     if (AXIS == 0) {
       const int x = l0 + threadIdx.x;
@@ -527,7 +558,7 @@ __global__ void __launch_bounds__(256)
     const int t1 = tile / G.n0, t0 = tile - t1 * G.n0;
     const int l0 = t0 * len, cross = AXIS == 0 ? t1 : t1 * kTYC;
     __syncthreads();
-    stage_tile<AXIS>(I, l0, cross, srcs, sm, 5, halo, len);
+    stage_tile<AXIS, 5>(I, l0, cross, srcs, sm, halo, len);
     __syncthreads();
     const TileLine ln{sm[0], sm[1], sm[2], sm[3], sm[4], l0 - halo,
                       AXIS == 0 ? 1 : kTYC, AXIS == 0 ? 0 : (int)threadIdx.x,
@@ -853,7 +884,7 @@ __global__ void __launch_bounds__(256)
     const int t1 = tile / G.n0, t0 = tile - t1 * G.n0;
     const int l0 = t0 * len, cross = AXIS == 0 ? t1 : t1 * kTYC;
     __syncthreads();
-    stage_tile<AXIS>(I, l0, cross, srcs, dsts, 1, halo, len);
+    stage_tile<AXIS, 1>(I, l0, cross, srcs, dsts, halo, len);
     __syncthreads();
     const TileLine ln{nullptr, smf, nullptr, nullptr, nullptr, l0 - halo,
                       AXIS == 0 ? 1 : kTYC, AXIS == 0 ? 0 : (int)threadIdx.x,
@@ -909,7 +940,10 @@ __global__ void __launch_bounds__(256)
     const int t1 = tile / G.n0, t0 = tile - t1 * G.n0;
     const int l0 = t0 * len, cross = AXIS == 0 ? t1 : t1 * kTYC;
     __syncthreads();
-    stage_tile<AXIS>(I, l0, cross, srcs, F, nf, halo, len);
+    if (data)
+      stage_tile<AXIS, 6>(I, l0, cross, srcs, F, halo, len);
+    else
+      stage_tile<AXIS, 4>(I, l0, cross, srcs, F, halo, len);
     __syncthreads();
     const TileLine ln{nullptr, F[0], F[1], F[2], F[3], l0 - halo,
                       AXIS == 0 ? 1 : kTYC, AXIS == 0 ? 0 : (int)threadIdx.x,
@@ -1143,8 +1177,11 @@ int plan_px(const dtsgb_soft_s* s) {
 int soft_halo(dtsgb_soft_t s, float sigma, float tau, int* halo) {
   const unsigned inf_bits = 0x7f800000u;
   DTSGB_CUDA(cudaMemcpyAsync(s->d_emin, &inf_bits, 4, cudaMemcpyHostToDevice, s->stream));
-  k_soft_emin<<<soft_grid(s), kST, 0, s->stream>>>(s->d_inst, s->plane(P_EH), s->plane(P_EV),
-                                                   s->d_emin);
+  {
+    ProfScope ps(s->stream, DTSGB_K_SOFT);
+    k_soft_emin<<<soft_grid(s), kST, 0, s->stream>>>(s->d_inst, s->plane(P_EH), s->plane(P_EV),
+                                                     s->d_emin);
+  }
   DTSGB_CUDA(cudaGetLastError());
   unsigned bits = 0;
   DTSGB_CUDA(cudaMemcpyAsync(&bits, s->d_emin, 4, cudaMemcpyDeviceToHost, s->stream));
@@ -1176,10 +1213,12 @@ int fix_edges(dtsgb_soft_t s, float sigma, float tau) {
   s->ramp = make_ramp(sigma, tau);
   const float cap = (float)((double)sigma + 0.5 * (double)tau + 1.0);
   const float scale = 1.f / s->ramp.scl;
-  k_soft_fix<<<soft_grid(s), kST, 0, s->stream>>>(
-      s->d_inst, s->plane(P_EH), reinterpret_cast<int*>(s->plane(P_FH)), cap, scale);
-  k_soft_fix<<<soft_grid(s), kST, 0, s->stream>>>(
-      s->d_inst, s->plane(P_EV), reinterpret_cast<int*>(s->plane(P_FV)), cap, scale);
+  for (int axis = 0; axis < 2; ++axis) {
+    ProfScope ps(s->stream, DTSGB_K_SOFT);
+    k_soft_fix<<<soft_grid(s), kST, 0, s->stream>>>(
+        s->d_inst, s->plane(axis == 0 ? P_EH : P_EV),
+        reinterpret_cast<int*>(s->plane(axis == 0 ? P_FH : P_FV)), cap, scale);
+  }
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
 }
@@ -1197,6 +1236,7 @@ int plan_windows_tiled(dtsgb_soft_t s, float sigma, float tau, bool* ok) {
     float* e = s->plane(axis == 0 ? P_EH : P_EV);
     unsigned* cnt = reinterpret_cast<unsigned*>(s->plane(base + 1));
     float2* wts = reinterpret_cast<float2*>(s->plane(base + 2));
+    ProfScope ps(s->stream, DTSGB_K_SOFT);
     if (axis == 0)
       k_soft_plan_tile<0><<<g, kTX, sizeof(float) * (kTX + 2 * kPlanHalo), s->stream>>>(
           s->d_inst, e, s->ramp, cap, scale, s->plane(base), cnt, wts, s->d_stat);
@@ -1221,6 +1261,7 @@ int plan_windows(dtsgb_soft_t s) {
   DTSGB_CUDA(cudaMemsetAsync(s->d_stat, 0, 2 * sizeof(int), s->stream));
   for (int axis = 0; axis < 2; ++axis) {
     const int base = axis == 0 ? P_PNX : P_PNY;
+    ProfScope ps(s->stream, DTSGB_K_SOFT);
     k_soft_plan<<<soft_grid(s), kST, 0, s->stream>>>(
         s->d_inst, s->plane(axis == 0 ? P_FH : P_FV), axis, s->ramp, s->plane(base),
         reinterpret_cast<unsigned*>(s->plane(base + 1)),
@@ -1344,16 +1385,22 @@ int launch_adjoint_fused(dtsgb_soft_t s, const float* a, const float* Bk, const 
 // The edge-weight gradients from the band pair terms summed over all the
 // iterations (the prefix is linear, so one per axis serves them all).
 int launch_edge_scans(dtsgb_soft_t s, float tau) {
-  ProfScope ps(s->stream, DTSGB_K_SOFT);
   int max_w = 1, max_h = 1;
   for (const SInst& I : s->inst) {
     max_w = std::max(max_w, I.w);
     max_h = std::max(max_h, I.h);
   }
-  k_soft_edge_scan_x<<<dim3((unsigned)std::min(1024, (max_h + 7) / 8), s->n), kST, 0,
-                       s->stream>>>(s->d_inst, s->plane(P_DIFF), s->plane(P_GEH), tau);
-  k_soft_edge_scan_y<<<dim3((unsigned)std::min(1024, (max_w + 31) / 32), s->n), dim3(32, 32), 0,
-                       s->stream>>>(s->d_inst, s->plane(P_DIFFY), s->plane(P_GEV), tau);
+  {
+    ProfScope ps(s->stream, DTSGB_K_SOFT);
+    k_soft_edge_scan_x<<<dim3((unsigned)std::min(1024, (max_h + 7) / 8), s->n), kST, 0,
+                         s->stream>>>(s->d_inst, s->plane(P_DIFF), s->plane(P_GEH), tau);
+  }
+  {
+    ProfScope ps(s->stream, DTSGB_K_SOFT);
+    k_soft_edge_scan_y<<<dim3((unsigned)std::min(1024, (max_w + 31) / 32), s->n),
+                         dim3(32, 32), 0, s->stream>>>(s->d_inst, s->plane(P_DIFFY),
+                                                       s->plane(P_GEV), tau);
+  }
   DTSGB_CUDA(cudaGetLastError());
   return DTSGB_OK;
 }
@@ -1465,8 +1512,11 @@ DTSGB_API int dtsgb_soft_edge_weights(dtsgb_soft_t s, int color_space,
   }
   if (int st = launch_color_convert_flat(g, s->total, color_space, s->stream)) return st;
   const float rx = f->sigma_x / f->sigma_r, ry = f->sigma_y / f->sigma_r;
-  k_soft_edges<<<soft_grid(s), kST, 0, s->stream>>>(s->d_inst, g, rx, ry, s->plane(P_EH),
-                                                    s->plane(P_EV));
+  {
+    ProfScope ps(s->stream, DTSGB_K_SOFT);
+    k_soft_edges<<<soft_grid(s), kST, 0, s->stream>>>(s->d_inst, g, rx, ry, s->plane(P_EH),
+                                                      s->plane(P_EV));
+  }
   DTSGB_CUDA(cudaGetLastError());
   if (int st = copy_planes(s, dH, P_EH, false)) return st;
   if (int st = copy_planes(s, dV, P_EV, false)) return st;
@@ -1498,6 +1548,7 @@ DTSGB_API int dtsgb_soft_solve(dtsgb_soft_t s, const float* const* dH, const flo
   if (confidence) {
     if (int st = copy_planes(s, confidence, P_C, true)) return st;
   } else {
+    ProfScope ps(s->stream, DTSGB_K_SOFT);
     k_soft_fill<<<152 * 8, kST, 0, s->stream>>>(s->plane(P_C), s->total, 1.f);
   }
   DTSGB_CUDA(cudaMemcpyAsync(s->plane(P_ITER), s->plane(P_T), (size_t)s->total * 4,
