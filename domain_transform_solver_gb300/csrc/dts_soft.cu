@@ -389,7 +389,7 @@ template <int AXIS, int NF>
 __device__ __forceinline__ void stage_tile(const SInst& I, int l0, int cross,
                                            const float* const* src, float* const* dst,
                                            int halo, int len) {
-  constexpr int U = NF > 4 ? 2 : 4;  // line positions per batch
+  constexpr int U = 4;  // line positions per batch
   const int TL = len + 2 * halo;
   if (AXIS == 0) {  // one row `cross`
     const long long row = I.off + (long long)cross * I.w;
