@@ -53,8 +53,8 @@ KERNEL_NAMES = {0: "k_bounds", 1: "k_dts_iter", 2: "k_filter", 3: "k_splat",
                 7: "k_slice", 8: "k_to_float", 9: "k_dts_adjoint",
                 10: "hfbs adjoint (whole backward)",
                 11: "soft-window plans, line scans and other",
-                12: "k_soft_half_plan (X and Y)", 13: "k_soft_adjoint_fused X",
-                14: "k_soft_adjoint_fused Y"}
+                12: "k_soft_half_plan X", 13: "k_soft_adjoint_fused X",
+                14: "k_soft_adjoint_fused Y", 15: "k_soft_half_plan Y"}
 HFBS_TB_STEPS = 4  # heavy-ball steps per launch of the temporally blocked kernel
 
 
@@ -899,7 +899,7 @@ class Cfg4Soft(Batched):
         and the band pair sums, writes a': 64 B/px; Y 40 B/px), once per
         iteration each."""
         px, it = self.pixels, self.iters
-        return {12: px * (32 + 24) * it, 13: px * 64 * it, 14: px * 40 * it}
+        return {12: px * 32 * it, 15: px * 24 * it, 13: px * 64 * it, 14: px * 40 * it}
 
     def pass_model_bytes(self):
         # the reference has no soft-window form: its pass model is the

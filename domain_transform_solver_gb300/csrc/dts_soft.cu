@@ -64,8 +64,8 @@ namespace {
 constexpr int kST = 256;
 
 // Every launch of this file's kernels is timed by the library's profiler
-// when it is on: the planned half-steps (DTSGB_K_SOFT_HALF) and adjoints
-// (DTSGB_K_SOFT_ADJ_X, _Y) by kind, everything else as DTSGB_K_SOFT.
+// when it is on: the planned half-steps (DTSGB_K_SOFT_HALF_X, _Y) and
+// adjoints (DTSGB_K_SOFT_ADJ_X, _Y) by kind, everything else as DTSGB_K_SOFT.
 #define SOFT_LAUNCH(kernel, grid, stream, ...)            \
   do {                                                    \
     ProfScope ps_((stream), DTSGB_K_SOFT);                \
@@ -323,19 +323,29 @@ __device__ __forceinline__ void soft_window_adj(const LN& ln, int i, const Ramp&
 // ---- the half-step ----------------------------------------------------------
 // vout = half-step(vin) along `axis`; data term on X.  nout / Bout (nullable)
 // keep each pixel's window weight n and mean B for the adjoint.
+// tv, cv: t[p] and c[p] (read only when data)
+__device__ __forceinline__ void half_update_v(long long p, float v, float n, float S, float tv,
+                                              float cv, float* __restrict__ vout,
+                                              float* __restrict__ nout,
+                                              float* __restrict__ Bout, int data, int mode,
+                                              float lambda, float step) {
+  const float rn = 1.f / n;
+  const float B = S * rn;
+  float h = 0.f, hd, hc;
+  if (data) data_term(mode, v, tv, cv, rn, &h, &hd, &hc);
+  vout[p] = v - step * (lambda * (v - B) + h);
+  if (nout) nout[p] = n;
+  if (Bout) Bout[p] = B;
+}
+
 __device__ __forceinline__ void half_update(long long p, float v, float n, float S,
                                             const float* __restrict__ t,
                                             const float* __restrict__ c,
                                             float* __restrict__ vout, float* __restrict__ nout,
                                             float* __restrict__ Bout, int data, int mode,
                                             float lambda, float step) {
-  const float rn = 1.f / n;
-  const float B = S * rn;
-  float h = 0.f, hd, hc;
-  if (data) data_term(mode, v, t[p], c[p], rn, &h, &hd, &hc);
-  vout[p] = v - step * (lambda * (v - B) + h);
-  if (nout) nout[p] = n;
-  if (Bout) Bout[p] = B;
+  half_update_v(p, v, n, S, data ? t[p] : 0.f, data ? c[p] : 0.f, vout, nout, Bout, data,
+                mode, lambda, step);
 }
 
 // Global-memory form: any edge weights.
@@ -880,31 +890,64 @@ __global__ void __launch_bounds__(256)
   const TileGeom<AXIS> G(I, len);
   const float* srcs[1] = {vin};
   float* dsts[1] = {smf};
+  constexpr int OWN = AXIS == 0 ? PX : kTYR / kTYT;  // pixels per thread
   for (int tile = blockIdx.x; tile < G.n0 * G.n1; tile += gridDim.x) {
     const int t1 = tile / G.n0, t0 = tile - t1 * G.n0;
     const int l0 = t0 * len, cross = AXIS == 0 ? t1 : t1 * kTYC;
+    // own pixel k: line index and global index (< 0: outside the image)
+    auto own_i = [&](int k) -> int {
+      return AXIS == 0 ? l0 + (int)threadIdx.x + kTX * k : l0 + (int)threadIdx.y + kTYT * k;
+    };
+    auto own_p = [&](int k) -> long long {
+      if (AXIS == 0) {
+        const int x = l0 + threadIdx.x + kTX * k;
+        return x < I.w ? I.off + (long long)cross * I.w + x : -1;
+      }
+      const int x = cross + threadIdx.x, y = l0 + threadIdx.y + kTYT * k;
+      return (x < I.w && y < I.h) ? I.off + (long long)y * I.w + x : -1;
+    };
+    // X: the own pixels' plan, t and c, loaded before the tile is staged, so
+    // that these loads are in flight with the staging's (Y's eight pixels a
+    // thread load after the staging)
+    constexpr int OP = AXIS == 0 ? OWN : 1;
+    unsigned cn[OP];
+    float2 w2[OP];
+    float tv[OP], cv[OP];
+    if (AXIS == 0) {
+#pragma unroll
+      for (int k = 0; k < OP; ++k) {
+        const long long p = own_p(k);
+        cn[k] = p >= 0 ? counts[p] : 0u;
+        w2[k] = p >= 0 ? wts[p] : make_float2(0.f, 0.f);
+        tv[k] = p >= 0 && data ? t[p] : 0.f;
+        cv[k] = p >= 0 && data ? c[p] : 0.f;
+      }
+    }
     __syncthreads();
     stage_tile<AXIS, 1>(I, l0, cross, srcs, dsts, halo, len);
     __syncthreads();
     const TileLine ln{nullptr, smf, nullptr, nullptr, nullptr, l0 - halo,
                       AXIS == 0 ? 1 : kTYC, AXIS == 0 ? 0 : (int)threadIdx.x,
                       AXIS == 0 ? I.w : I.h};
-    auto one = [&](int i, long long p) {
-      float n;
-      const float S = plan_sum(ln, i, counts[p], wts[p], wc, &n);
-      half_update(p, ln.V(i), n, S, t, c, vout, nullptr, Bout, data, mode, lambda, step);
-    };
     if (AXIS == 0) {
 #pragma unroll
-      for (int k = 0; k < PX; ++k) {
-        const int x = l0 + threadIdx.x + kTX * k;
-        if (x < I.w) one(x, I.off + (long long)cross * I.w + x);
+      for (int k = 0; k < OP; ++k) {
+        const long long p = own_p(k);
+        if (p < 0) continue;
+        const int i = own_i(k);
+        float n;
+        const float S = plan_sum(ln, i, cn[k], w2[k], wc, &n);
+        half_update_v(p, ln.V(i), n, S, tv[k], cv[k], vout, nullptr, Bout, data, mode, lambda,
+                      step);
       }
     } else {
       const int x = cross + threadIdx.x;
       for (int y = l0 + threadIdx.y; y < min(l0 + kTYR, I.h); y += kTYT) {
         if (x >= I.w) break;
-        one(y, I.off + (long long)y * I.w + x);
+        const long long p = I.off + (long long)y * I.w + x;
+        float n;
+        const float S = plan_sum(ln, y, counts[p], wts[p], wc, &n);
+        half_update(p, ln.V(y), n, S, t, c, vout, nullptr, Bout, data, mode, lambda, step);
       }
     }
   }
@@ -939,15 +982,6 @@ __global__ void __launch_bounds__(256)
   for (int tile = blockIdx.x; tile < G.n0 * G.n1; tile += gridDim.x) {
     const int t1 = tile / G.n0, t0 = tile - t1 * G.n0;
     const int l0 = t0 * len, cross = AXIS == 0 ? t1 : t1 * kTYC;
-    __syncthreads();
-    if (data)
-      stage_tile<AXIS, 6>(I, l0, cross, srcs, F, halo, len);
-    else
-      stage_tile<AXIS, 4>(I, l0, cross, srcs, F, halo, len);
-    __syncthreads();
-    const TileLine ln{nullptr, F[0], F[1], F[2], F[3], l0 - halo,
-                      AXIS == 0 ? 1 : kTYC, AXIS == 0 ? 0 : (int)threadIdx.x,
-                      AXIS == 0 ? I.w : I.h};
     // own pixel k: line index and global index (< 0: outside the image)
     auto own_i = [&](int k) -> int {
       return AXIS == 0 ? l0 + (int)threadIdx.x + kTX * k : l0 + (int)threadIdx.y + kTYT * k;
@@ -960,20 +994,48 @@ __global__ void __launch_bounds__(256)
       const int x = cross + threadIdx.x, y = l0 + threadIdx.y + kTYT * k;
       return (x < I.w && y < I.h) ? I.off + (long long)y * I.w + x : -1;
     };
+    // X: the own pixels' plan, pair sums, dL/dt and dL/dc, loaded before
+    // the tile is staged, so that these loads are in flight with the
+    // staging's (on Y, eight pixels a thread, the same preloads took more
+    // time than they saved: 0.202 against 0.183 ms at 16 x 1024x768)
+    constexpr int OP = AXIS == 0 ? OWN : 1;
+    unsigned cn[OP];
+    float2 w2[OP];
+    float dv[OP], gtv[OP], gcv[OP];
+    if (AXIS == 0) {
+#pragma unroll
+      for (int k = 0; k < OP; ++k) {
+        const long long p = own_p(k);
+        cn[k] = p >= 0 ? counts[p] : 0u;
+        w2[k] = p >= 0 ? wts[p] : make_float2(0.f, 0.f);
+        dv[k] = p >= 0 ? diff[p] : 0.f;
+        gtv[k] = p >= 0 && data ? gt[p] : 0.f;
+        gcv[k] = p >= 0 && data ? gc[p] : 0.f;
+      }
+    }
+    __syncthreads();
+    if (data)
+      stage_tile<AXIS, 6>(I, l0, cross, srcs, F, halo, len);
+    else
+      stage_tile<AXIS, 4>(I, l0, cross, srcs, F, halo, len);
+    __syncthreads();
+    const TileLine ln{nullptr, F[0], F[1], F[2], F[3], l0 - halo,
+                      AXIS == 0 ? 1 : kTYC, AXIS == 0 ? 0 : (int)threadIdx.x,
+                      AXIS == 0 ? I.w : I.h};
     // Every staged entry becomes (coef, alpha, beta) in place; a thread
     // transforms its own pixels' entries (taking their a * diag and dL/dt,
-    // dL/dc on the way) and a share of the halo's.
-    // returns a * diag of an own pixel (p >= 0)
-    auto transform = [&](int e, long long p) -> float {
+    // dL/dc on the way, X only) and a share of the halo's.
+    // returns a * diag of own pixel k (p >= 0)
+    auto transform = [&](int e, long long p, int k) -> float {
       const float ap = F[0][e], n = F[1][e];
       float h = 0.f, hd = 0.f, hc = 0.f;
       const float rn = 1.f / n;
       if (data) data_term(mode, F[3][e], F[4][e], F[5][e], rn, &h, &hd, &hc);
       float adg = 0.f;
-      if (p >= 0) {
+      if (AXIS == 0 && p >= 0) {
         if (data) {
-          gt[p] += ap * step * hd;  // dh/dt = -dh/dd, and v' has -s*h
-          gc[p] -= ap * step * hc;
+          gt[p] = gtv[k % OP] + ap * step * hd;  // dh/dt = -dh/dd, and v' has -s*h
+          gc[p] = gcv[k % OP] - ap * step * hc;
         }
         adg = ap * (1.f - step * lambda - step * hd);
       }
@@ -988,9 +1050,9 @@ __global__ void __launch_bounds__(256)
       // own pixels transformed with their a * diag, the halo shared out
       // over the first 2 halo threads
 #pragma unroll
-      for (int k = 0; k < OWN; ++k) adg[k] = transform(ln.at(own_i(k)), own_p(k));
+      for (int k = 0; k < OWN; ++k) adg[k] = transform(ln.at(own_i(k)), own_p(k), k);
       const int t = threadIdx.x;
-      if (t < 2 * halo) (void)transform(t < halo ? t : len + t, -1);
+      if (t < 2 * halo) (void)transform(t < halo ? t : len + t, -1, 0);
     } else {
       // eight own pixels a thread: their a * diag (and dL/dt, dL/dc) first,
       // then the whole tile transformed, entries spread over the threads
@@ -1012,7 +1074,7 @@ __global__ void __launch_bounds__(256)
       }
       __syncthreads();
       const int tid = threadIdx.x + kTYC * threadIdx.y;
-      for (int e = tid; e < TS; e += kTYC * kTYT) (void)transform(e, -1);
+      for (int e = tid; e < TS; e += kTYC * kTYT) (void)transform(e, -1, 0);
     }
     __syncthreads();
 #pragma unroll
@@ -1020,8 +1082,8 @@ __global__ void __launch_bounds__(256)
       const long long p = own_p(k);
       if (p < 0) continue;
       const int i = own_i(k);
-      const unsigned cnt = counts[p];
-      const float S = plan_sum(ln, i, cnt, wts[p], wc);
+      const unsigned cnt = AXIS == 0 ? cn[k % OP] : counts[p];
+      const float S = plan_sum(ln, i, cnt, AXIS == 0 ? w2[k % OP] : wts[p], wc);
       aout[p] = __fmaf_rn(lambda, S, adg[k]);
       const int dl = cnt & 255, du = (cnt >> 8) & 255, nrl = (cnt >> 16) & 255,
                 nru = cnt >> 24;
@@ -1035,7 +1097,7 @@ __global__ void __launch_bounds__(256)
         const int aa = i - dl - 1;
         d -= __fmaf_rn(ln.A(aa), xi, ln.Bt(aa)) + __fmaf_rn(ai, ln.X(aa), bi);
       }
-      diff[p] += d;
+      diff[p] = (AXIS == 0 ? dv[k % OP] : diff[p]) + d;
     }
   }
 }
@@ -1279,7 +1341,9 @@ int plan_windows(dtsgb_soft_t s) {
 int launch_half(dtsgb_soft_t s, const float* vin, float* vout, const float* e, const float* t,
                 const float* c, float* nout, float* Bout, int axis, int data, int mode,
                 float lambda, float step) {
-  ProfScope ps(s->stream, s->use_plan ? DTSGB_K_SOFT_HALF : DTSGB_K_SOFT);
+  ProfScope ps(s->stream, !s->use_plan ? DTSGB_K_SOFT
+                          : axis == 0 ? DTSGB_K_SOFT_HALF_X
+                                      : DTSGB_K_SOFT_HALF_Y);
   const int H = s->halo;
   const Ramp R = s->ramp;
   if (s->use_plan) {

@@ -120,10 +120,11 @@ enum {
   DTSGB_K_DTS_ADJOINT = 9, /* adjoint of one fused iteration          */
   DTSGB_K_HFBS_ADJOINT = 10, /* the whole HFBS adjoint                  */
   DTSGB_K_SOFT = 11,         /* soft-window plans, line scans, unplanned forms */
-  DTSGB_K_SOFT_HALF = 12,    /* planned soft half-steps, X and Y            */
+  DTSGB_K_SOFT_HALF_X = 12,  /* planned soft X half-step                    */
   DTSGB_K_SOFT_ADJ_X = 13,   /* planned soft adjoint of the X half-step     */
   DTSGB_K_SOFT_ADJ_Y = 14,   /* planned soft adjoint of the Y half-step     */
-  DTSGB_K_COUNT = 15
+  DTSGB_K_SOFT_HALF_Y = 15,  /* planned soft Y half-step                    */
+  DTSGB_K_COUNT = 16
 };
 /* (new) Thread blocks of the library's kernels that gave up waiting for an
  * asynchronous (TMA) copy of their tile since the library was loaded: each
