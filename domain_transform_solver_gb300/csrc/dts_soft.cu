@@ -994,25 +994,27 @@ __global__ void __launch_bounds__(256)
       const int x = cross + threadIdx.x, y = l0 + threadIdx.y + kTYT * k;
       return (x < I.w && y < I.h) ? I.off + (long long)y * I.w + x : -1;
     };
-    // X: the own pixels' plan, pair sums, dL/dt and dL/dc, loaded before
-    // the tile is staged, so that these loads are in flight with the
-    // staging's (on Y, eight pixels a thread, the same preloads took more
-    // time than they saved: 0.202 against 0.183 ms at 16 x 1024x768)
-    constexpr int OP = AXIS == 0 ? OWN : 1;
-    unsigned cn[OP];
-    float2 w2[OP];
-    float dv[OP], gtv[OP], gcv[OP];
-    if (AXIS == 0) {
-#pragma unroll
-      for (int k = 0; k < OP; ++k) {
-        const long long p = own_p(k);
-        cn[k] = p >= 0 ? counts[p] : 0u;
-        w2[k] = p >= 0 ? wts[p] : make_float2(0.f, 0.f);
-        dv[k] = p >= 0 ? diff[p] : 0.f;
-        gtv[k] = p >= 0 && data ? gt[p] : 0.f;
-        gcv[k] = p >= 0 && data ? gc[p] : 0.f;
+    // The own pixels' plan and pair sums (and on X their dL/dt, dL/dc) are
+    // loaded ahead of their use: on X all four before the tile is staged,
+    // so that these loads are in flight with the staging's; on Y (eight
+    // pixels a thread: registers) a ring of RING pixels, the first ones
+    // before the staging and each later one when its slot frees up.
+    constexpr int RING = AXIS == 0 ? OWN : 2, OG = AXIS == 0 ? OWN : 1;
+    unsigned cn[RING];
+    float2 w2[RING];
+    float dv[RING], gtv[OG], gcv[OG];
+    auto load_own = [&](int k, int slot) {
+      const long long p = own_p(k);
+      cn[slot] = p >= 0 ? counts[p] : 0u;
+      w2[slot] = p >= 0 ? wts[p] : make_float2(0.f, 0.f);
+      dv[slot] = p >= 0 ? diff[p] : 0.f;
+      if (AXIS == 0) {
+        gtv[slot % OG] = p >= 0 && data ? gt[p] : 0.f;
+        gcv[slot % OG] = p >= 0 && data ? gc[p] : 0.f;
       }
-    }
+    };
+#pragma unroll
+    for (int k = 0; k < RING; ++k) load_own(k, k);
     __syncthreads();
     if (data)
       stage_tile<AXIS, 6>(I, l0, cross, srcs, F, halo, len);
@@ -1034,8 +1036,8 @@ __global__ void __launch_bounds__(256)
       float adg = 0.f;
       if (AXIS == 0 && p >= 0) {
         if (data) {
-          gt[p] = gtv[k % OP] + ap * step * hd;  // dh/dt = -dh/dd, and v' has -s*h
-          gc[p] = gcv[k % OP] - ap * step * hc;
+          gt[p] = gtv[k % OG] + ap * step * hd;  // dh/dt = -dh/dd, and v' has -s*h
+          gc[p] = gcv[k % OG] - ap * step * hc;
         }
         adg = ap * (1.f - step * lambda - step * hd);
       }
@@ -1077,13 +1079,11 @@ __global__ void __launch_bounds__(256)
       for (int e = tid; e < TS; e += kTYC * kTYT) (void)transform(e, -1, 0);
     }
     __syncthreads();
-#pragma unroll
-    for (int k = 0; k < OWN; ++k) {
-      const long long p = own_p(k);
-      if (p < 0) continue;
+    // window sum and band pair terms of own pixel k (p >= 0) from its ring slot
+    auto finish = [&](int k, long long p, int slot) {
       const int i = own_i(k);
-      const unsigned cnt = AXIS == 0 ? cn[k % OP] : counts[p];
-      const float S = plan_sum(ln, i, cnt, AXIS == 0 ? w2[k % OP] : wts[p], wc);
+      const unsigned cnt = cn[slot];
+      const float S = plan_sum(ln, i, cnt, w2[slot], wc);
       aout[p] = __fmaf_rn(lambda, S, adg[k]);
       const int dl = cnt & 255, du = (cnt >> 8) & 255, nrl = (cnt >> 16) & 255,
                 nru = cnt >> 24;
@@ -1097,7 +1097,21 @@ __global__ void __launch_bounds__(256)
         const int aa = i - dl - 1;
         d -= __fmaf_rn(ln.A(aa), xi, ln.Bt(aa)) + __fmaf_rn(ai, ln.X(aa), bi);
       }
-      diff[p] = (AXIS == 0 ? dv[k % OP] : diff[p]) + d;
+      diff[p] = dv[slot] + d;
+    };
+    if (AXIS == 0) {
+#pragma unroll
+      for (int k = 0; k < OWN; ++k) {
+        const long long p = own_p(k);
+        if (p >= 0) finish(k, p, k);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < OWN; ++k) {
+        const long long p = own_p(k);
+        if (p >= 0) finish(k, p, k % RING);
+        if (k + RING < OWN) load_own(k + RING, k % RING);
+      }
     }
   }
 }
