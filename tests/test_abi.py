@@ -46,3 +46,23 @@ def test_gradient_entry_points_reject_null_handles(dts):
     assert lib.dtsgb_batch_hfbs_backward(None, None, None, None) == bad
     assert lib.dtsgb_batch_hfbs_backward_device(None, None, None, None) == bad
     assert lib.dtsgb_batch_hfbs_grad_info(None, None, None) == bad
+
+
+def test_bench_names_every_profiler_kind():
+    """bench.py reports every kernel kind the header's profiler enum holds
+    (DTSGB_K_* below DTSGB_K_COUNT), each under its own name."""
+    import ast
+    import re
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    header = (root / "include" / "dtsgb.h").read_text()
+    kinds = {int(v) for n, v in re.findall(r"\b(DTSGB_K_\w+)\s*=\s*(\d+)", header)
+             if n != "DTSGB_K_COUNT"}
+    count = int(re.search(r"DTSGB_K_COUNT\s*=\s*(\d+)", header).group(1))
+    assert kinds == set(range(count))
+    tree = ast.parse((root / "bench.py").read_text())
+    names = next(ast.literal_eval(node.value) for node in tree.body
+                 if isinstance(node, ast.Assign)
+                 and any(getattr(t, "id", None) == "KERNEL_NAMES" for t in node.targets))
+    assert set(names) == kinds
+    assert len(set(names.values())) == len(names)
