@@ -716,6 +716,168 @@ __global__ void __launch_bounds__(kTBThreads, 1)
   }
 }
 
+// a16 as k_solve_tb (the same K-step blocks, the same arithmetic in the
+// same order: bitwise the same z and h), in a persistent form that keeps the
+// SM busy while a block is staged.  One CTA per SM walks the launch's
+// blocks L = blockIdx.x, + gridDim.x, ... (the blocks of the (tile,
+// instance) grid that lie inside their instance).  Shared memory: the z, h,
+// n staging area (three planes), the current block's b and invA (two
+// planes) and one z * n exchange plane (two barriers a step).  As soon as a
+// block's z, h, n are in registers, the next block's are requested by TMA
+// into the staging area, so that they arrive while this block is solved;
+// the next b and invA are requested after this block's last step.  Each of
+// the two mbarriers completes once per block, so both are waited for with
+// the parity of the block's position in the CTA's walk.  A wait that runs
+// out (bounded) is counted in g_wait_timeouts (as is a shared-memory base
+// that TMA cannot write to); the CTA then waits, bounded, for its copies in
+// flight and returns.
+constexpr size_t kTBPSmem = sizeof(float) * 6 * kTBPlane + 32;
+
+__global__ void __launch_bounds__(kTBThreads, 1)
+    k_solve_tbp(const HInst* __restrict__ insts, int n_inst, int tiles_max,
+                float* __restrict__ zd, float* __restrict__ hd, float lambda, float alpha,
+                float beta, int steps, TBMaps m) {
+  extern __shared__ __align__(128) float tb_s[];
+  float* ZS = tb_s;                 // z, h, n of the block being staged
+  float* Bs = tb_s + 3 * kTBPlane;  // b, invA of the current block
+  float* As = Bs + kTBPlane;
+  float* P = tb_s + 5 * kTBPlane;   // z * n of a step
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(tb_s + 6 * kTBPlane);
+  const int c = threadIdx.x, yy = c / kTBL, xx = c - yy * kTBL;
+  const long long total = (long long)tiles_max * n_inst;
+  // block L: instance and tile
+  auto decode = [&](long long L, int& inst, int& tx, int& ty) -> bool {
+    inst = (int)(L / tiles_max);
+    const int t = (int)(L - (long long)inst * tiles_max);
+    const int gx = insts[inst].gx, gy = insts[inst].gy;
+    const int tiles_x = (gx + kTBT - 1) / kTBT;
+    ty = t / tiles_x;
+    tx = t - ty * tiles_x;
+    return t < tiles_x * ((gy + kTBT - 1) / kTBT);
+  };
+  // the first block inside its instance at or after L in this CTA's walk
+  auto next_block = [&](long long L) -> long long {
+    int i, tx, ty;
+    for (; L < total; L += gridDim.x)
+      if (decode(L, i, tx, ty)) return L;
+    return -1;
+  };
+  auto issue_zhn = [&](long long L) {  // thread 0
+    int i, tx, ty;
+    decode(L, i, tx, ty);
+    const int x0 = tx * kTBT - kTBK, y0 = ty * kTBT - kTBK;
+    mbar_arrive_expect_tx(&bar[0], 3u * kTBBoxBytes);
+    tma_load_3d(ZS, m.z + i, x0, y0, 0, &bar[0]);
+    tma_load_3d(ZS + kTBPlane, m.h + i, x0, y0, 0, &bar[0]);
+    tma_load_3d(ZS + 2 * kTBPlane, m.n + i, x0, y0, 0, &bar[0]);
+  };
+  auto issue_ba = [&](long long L) {  // thread 0
+    int i, tx, ty;
+    decode(L, i, tx, ty);
+    const int x0 = tx * kTBT - kTBK, y0 = ty * kTBT - kTBK;
+    mbar_arrive_expect_tx(&bar[1], 2u * kTBBoxBytes);
+    tma_load_3d(Bs, m.b + i, x0, y0, 0, &bar[1]);
+    tma_load_3d(As, m.a + i, x0, y0, 0, &bar[1]);
+  };
+  long long L = next_block(blockIdx.x);
+  if (L < 0) return;
+  if ((smem_u32(tb_s) & 127u) != 0) {  // TMA destinations need 128-byte alignment
+    if (c == 0) atomicAdd(&g_wait_timeouts, 1ull);
+    return;
+  }
+  if (c == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (c == 0) {
+    issue_zhn(L);
+    issue_ba(L);
+  }
+  unsigned ph = 0;  // parity of this block's phase of both barriers
+  for (;;) {
+    int inst, tx, ty;
+    decode(L, inst, tx, ty);
+    const HInst& I = insts[inst];
+    const int gx = I.gx, gy = I.gy, gl = I.gl;
+    const int x = tx * kTBT - kTBK + xx, y = ty * kTBT - kTBK + yy;
+    const bool in = x >= 0 && x < gx && y >= 0 && y < gy;
+    const int plane = I.px * gy, col = in ? y * I.px + x : 0;
+    const long long g0 = I.grid_off + col;
+    // this block's z, h, n
+    const bool ok0 = mbar_wait_bounded(&bar[0], ph, kTmaWaitPolls);
+    if (__syncthreads_or(!ok0)) {
+      if (c == 0) atomicAdd(&g_wait_timeouts, 1ull);
+      (void)mbar_wait_bounded(&bar[0], ph, kTmaWaitPolls);  // copies may still land
+      (void)mbar_wait_bounded(&bar[1], ph, kTmaWaitPolls);
+      return;
+    }
+    float z[kTBMaxGL], h[kTBMaxGL], n[kTBMaxGL];
+#pragma unroll
+    for (int l = 0; l < kTBMaxGL; ++l) {
+      z[l] = ZS[l * kTBThreads + c];
+      h[l] = ZS[kTBPlane + l * kTBThreads + c];
+      n[l] = ZS[2 * kTBPlane + l * kTBThreads + c];
+    }
+    __syncthreads();  // the staging area is free
+    const long long Ln = next_block(L + gridDim.x);
+    if (c == 0 && Ln >= 0) {
+      fence_proxy_async_shared();
+      issue_zhn(Ln);
+    }
+    // this block's b, invA
+    const bool ok1 = mbar_wait_bounded(&bar[1], ph, kTmaWaitPolls);
+    if (__syncthreads_or(!ok1)) {
+      if (c == 0) atomicAdd(&g_wait_timeouts, 1ull);
+      (void)mbar_wait_bounded(&bar[1], ph, kTmaWaitPolls);
+      if (Ln >= 0) (void)mbar_wait_bounded(&bar[0], ph ^ 1u, kTmaWaitPolls);
+      return;
+    }
+    for (int k = 1; k <= steps; ++k) {
+#pragma unroll
+      for (int l = 0; l < kTBMaxGL; ++l) P[l * kTBThreads + c] = z[l] * n[l];
+      __syncthreads();
+      if (in && tb_active(xx, yy, k)) {
+        float below = 0.f, cur = z[0] * n[0];
+#pragma unroll
+        for (int l = 0; l < kTBMaxGL; ++l) {
+          const float above = l + 1 < kTBMaxGL ? z[l + 1] * n[l + 1] : 0.f;
+          const float* q = P + l * kTBThreads + c;
+          const float d = q[-1] + q[1] + q[-kTBL] + q[kTBL] + below + above;
+          const float qb = (Bs[l * kTBThreads + c] + lambda * n[l] * d) * As[l * kTBThreads + c];
+          const float grad = z[l] - qb;
+          // |grad| > 1.345 with the double threshold of the reference: the
+          // smallest float above 1.345 (double) is 1.345f
+          const float gc = fabsf(grad) >= 1.345f ? copysignf(1.f, grad) : grad;
+          h[l] = __fmaf_rn(beta, h[l], gc);
+          z[l] = z[l] - alpha * h[l];
+          below = cur;
+          cur = above;
+        }
+      }
+      __syncthreads();  // P (and after the last step b, invA) read
+    }
+    if (c == 0 && Ln >= 0) {
+      fence_proxy_async_shared();
+      issue_ba(Ln);
+    }
+    if (in && xx >= kTBK && xx < kTBK + kTBT && yy >= kTBK && yy < kTBK + kTBT) {
+      float* zo = zd + g0;
+      float* ho = hd + g0;
+#pragma unroll
+      for (int l = 0; l < kTBMaxGL; ++l)
+        if (l < gl) {
+          zo[l * plane] = z[l];
+          ho[l * plane] = h[l];
+        }
+    }
+    if (Ln < 0) return;
+    L = Ln;
+    ph ^= 1u;
+  }
+}
+
 constexpr int kSliceXTable = 2048;
 
 // The slice's corner values, once per solve: (count * z, count) at every
@@ -1120,6 +1282,17 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
     // is a per-device attribute: set on every call (host-side, cheap).
     DTSGB_CUDA(cudaFuncSetAttribute(k_solve_tb, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kTBSmem));
+    DTSGB_CUDA(cudaFuncSetAttribute(k_solve_tbp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kTBPSmem));
+    static const int sms = [] {
+      int dev = 0, n = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0;
+      }
+      return n;
+    }();
     for (const Group& g : groups) {
       zs = B.z0;
       zd = B.z1;
@@ -1131,13 +1304,21 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
         tiles = std::max(tiles, (long long)((H.gx + kTBT - 1) / kTBT) * ((H.gy + kTBT - 1) / kTBT));
       }
       const dim3 gt((unsigned)tiles, g.count);
+      // the persistent form with tensor maps, one CTA per SM; else one CTA
+      // per block
+      const unsigned gp = (unsigned)std::min<long long>(tiles * g.count, sms > 0 ? sms : 1);
       for (int it = 0; it < p.optim_iter_max; it += kTBK) {
         const int steps = std::min(kTBK, p.optim_iter_max - it);
+        const TBMaps maps = tb_maps(B, g.first, zs, hs, norm, s);
         prof_begin(s, DTSGB_K_HFBS_SOLVE);
-        k_solve_tb<<<gt, kTBThreads, kTBSmem, s>>>(B.d_inst + g.first, zs, zd, hs, hd, norm,
-                                                    B.b, B.invA, p.lambda, p.alpha, p.beta,
-                                                    steps, nullptr, 0, 0,
-                                                    tb_maps(B, g.first, zs, hs, norm, s));
+        if (maps.b && sms > 0)
+          k_solve_tbp<<<gp, kTBThreads, kTBPSmem, s>>>(B.d_inst + g.first, g.count, (int)tiles,
+                                                        zd, hd, p.lambda, p.alpha, p.beta,
+                                                        steps, maps);
+        else
+          k_solve_tb<<<gt, kTBThreads, kTBSmem, s>>>(B.d_inst + g.first, zs, zd, hs, hd, norm,
+                                                      B.b, B.invA, p.lambda, p.alpha, p.beta,
+                                                      steps, nullptr, 0, 0, maps);
         prof_end(s, DTSGB_K_HFBS_SOLVE);
         std::swap(zs, zd);
         std::swap(hs, hd);

@@ -85,6 +85,13 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tmap, 
       : "memory");
 }
 
+// Orders this thread's earlier generic-proxy accesses of shared memory
+// before later async-proxy (TMA) accesses: issued by the thread that reuses
+// a buffer for a TMA load after a barrier with the threads that read it.
+__device__ __forceinline__ void fence_proxy_async_shared() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // Polls of a staging wait before a kernel gives up (about a second at the
 // hardware's try_wait suspend time); a CTA that gives up counts the event
 // in its translation unit's wait-timeout counter (dtsgb_wait_timeouts) and
