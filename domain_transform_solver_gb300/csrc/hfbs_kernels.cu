@@ -720,28 +720,34 @@ __global__ void __launch_bounds__(kTBThreads, 1)
 // same order: bitwise the same z and h), in a persistent form that keeps the
 // SM busy while a block is staged.  One CTA per SM walks the launch's
 // blocks L = blockIdx.x, + gridDim.x, ... (the blocks of the (tile,
-// instance) grid that lie inside their instance).  Shared memory: the z, h,
-// n staging area (three planes), the current block's b and invA (two
-// planes) and one z * n exchange plane (two barriers a step).  As soon as a
-// block's z, h, n are in registers, the next block's are requested by TMA
+// instance) grid that lie inside their instance).  Shared memory: the z, n
+// staging area (two planes), the current block's b and invA (two planes)
+// and the z * n exchange (two planes, alternating by step).  As soon as a
+// block's z and n are in registers, the next block's are requested by TMA
 // into the staging area, so that they arrive while this block is solved;
-// the next b and invA are requested after this block's last step.  Each of
-// the two mbarriers completes once per block, so both are waited for with
-// the parity of the block's position in the CTA's walk.  A wait that runs
-// out (bounded) is counted in g_wait_timeouts (as is a shared-memory base
-// that TMA cannot write to); the CTA then waits, bounded, for its copies in
-// flight and returns.
+// the next b and invA are requested after this block's last step, and a
+// block's h (read by its own column's thread only) comes straight from
+// global memory into registers, in flight during the first exchange.  Each
+// of the two mbarriers completes once per block, so both are waited for
+// with the parity of the block's position in the CTA's walk.  A wait that
+// runs out (bounded) is counted in g_wait_timeouts (as is a shared-memory
+// base that TMA cannot write to); the CTA then waits, bounded, for its
+// copies in flight and returns.
 constexpr size_t kTBPSmem = sizeof(float) * 6 * kTBPlane + 32;
+// registers a thread: warps take registers in groups of four, so the 18
+// warps of a block count as 20 and 65536 / 640 leaves 96
+constexpr int kTBPRegs = 96;
+static_assert(kTBPRegs * 640 <= 65536, "one CTA per SM");
 
-__global__ void __launch_bounds__(kTBThreads, 1)
+__global__ void __maxnreg__(kTBPRegs)
     k_solve_tbp(const HInst* __restrict__ insts, int n_inst, int tiles_max,
-                float* __restrict__ zd, float* __restrict__ hd, float lambda, float alpha,
-                float beta, int steps, TBMaps m) {
+                float* __restrict__ zd, const float* __restrict__ hs, float* __restrict__ hd,
+                float lambda, float alpha, float beta, int steps, TBMaps m) {
   extern __shared__ __align__(128) float tb_s[];
-  float* ZS = tb_s;                 // z, h, n of the block being staged
-  float* Bs = tb_s + 3 * kTBPlane;  // b, invA of the current block
+  float* ZS = tb_s;                 // z, n of the block being staged
+  float* Bs = tb_s + 2 * kTBPlane;  // b, invA of the current block
   float* As = Bs + kTBPlane;
-  float* P = tb_s + 5 * kTBPlane;   // z * n of a step
+  float* PP = tb_s + 4 * kTBPlane;  // z * n of a step, two buffers
   unsigned long long* bar = reinterpret_cast<unsigned long long*>(tb_s + 6 * kTBPlane);
   const int c = threadIdx.x, yy = c / kTBL, xx = c - yy * kTBL;
   const long long total = (long long)tiles_max * n_inst;
@@ -762,14 +768,13 @@ __global__ void __launch_bounds__(kTBThreads, 1)
       if (decode(L, i, tx, ty)) return L;
     return -1;
   };
-  auto issue_zhn = [&](long long L) {  // thread 0
+  auto issue_zn = [&](long long L) {  // thread 0
     int i, tx, ty;
     decode(L, i, tx, ty);
     const int x0 = tx * kTBT - kTBK, y0 = ty * kTBT - kTBK;
-    mbar_arrive_expect_tx(&bar[0], 3u * kTBBoxBytes);
+    mbar_arrive_expect_tx(&bar[0], 2u * kTBBoxBytes);
     tma_load_3d(ZS, m.z + i, x0, y0, 0, &bar[0]);
-    tma_load_3d(ZS + kTBPlane, m.h + i, x0, y0, 0, &bar[0]);
-    tma_load_3d(ZS + 2 * kTBPlane, m.n + i, x0, y0, 0, &bar[0]);
+    tma_load_3d(ZS + kTBPlane, m.n + i, x0, y0, 0, &bar[0]);
   };
   auto issue_ba = [&](long long L) {  // thread 0
     int i, tx, ty;
@@ -792,7 +797,7 @@ __global__ void __launch_bounds__(kTBThreads, 1)
   }
   __syncthreads();
   if (c == 0) {
-    issue_zhn(L);
+    issue_zn(L);
     issue_ba(L);
   }
   unsigned ph = 0;  // parity of this block's phase of both barriers
@@ -805,7 +810,12 @@ __global__ void __launch_bounds__(kTBThreads, 1)
     const bool in = x >= 0 && x < gx && y >= 0 && y < gy;
     const int plane = I.px * gy, col = in ? y * I.px + x : 0;
     const long long g0 = I.grid_off + col;
-    // this block's z, h, n
+    // h straight into registers (zero outside the grid and above level gl,
+    // as the staged planes read there)
+    float h[kTBMaxGL];
+#pragma unroll
+    for (int l = 0; l < kTBMaxGL; ++l) h[l] = in && l < gl ? hs[g0 + (long long)l * plane] : 0.f;
+    // this block's z, n
     const bool ok0 = mbar_wait_bounded(&bar[0], ph, kTmaWaitPolls);
     if (__syncthreads_or(!ok0)) {
       if (c == 0) atomicAdd(&g_wait_timeouts, 1ull);
@@ -813,18 +823,17 @@ __global__ void __launch_bounds__(kTBThreads, 1)
       (void)mbar_wait_bounded(&bar[1], ph, kTmaWaitPolls);
       return;
     }
-    float z[kTBMaxGL], h[kTBMaxGL], n[kTBMaxGL];
+    float z[kTBMaxGL], n[kTBMaxGL];
 #pragma unroll
     for (int l = 0; l < kTBMaxGL; ++l) {
       z[l] = ZS[l * kTBThreads + c];
-      h[l] = ZS[kTBPlane + l * kTBThreads + c];
-      n[l] = ZS[2 * kTBPlane + l * kTBThreads + c];
+      n[l] = ZS[kTBPlane + l * kTBThreads + c];
     }
     __syncthreads();  // the staging area is free
     const long long Ln = next_block(L + gridDim.x);
     if (c == 0 && Ln >= 0) {
       fence_proxy_async_shared();
-      issue_zhn(Ln);
+      issue_zn(Ln);
     }
     // this block's b, invA
     const bool ok1 = mbar_wait_bounded(&bar[1], ph, kTmaWaitPolls);
@@ -835,6 +844,7 @@ __global__ void __launch_bounds__(kTBThreads, 1)
       return;
     }
     for (int k = 1; k <= steps; ++k) {
+      float* P = PP + (k & 1) * kTBPlane;
 #pragma unroll
       for (int l = 0; l < kTBMaxGL; ++l) P[l * kTBThreads + c] = z[l] * n[l];
       __syncthreads();
@@ -856,8 +866,8 @@ __global__ void __launch_bounds__(kTBThreads, 1)
           cur = above;
         }
       }
-      __syncthreads();  // P (and after the last step b, invA) read
     }
+    __syncthreads();  // b, invA and the exchange buffers read
     if (c == 0 && Ln >= 0) {
       fence_proxy_async_shared();
       issue_ba(Ln);
@@ -1284,14 +1294,18 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
                                     (int)kTBSmem));
     DTSGB_CUDA(cudaFuncSetAttribute(k_solve_tbp, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kTBPSmem));
+    // SMs for the persistent form, 0 when it cannot be resident (then the
+    // kernel with one CTA per block runs)
     static const int sms = [] {
-      int dev = 0, n = 0;
+      int dev = 0, n = 0, per_sm = 0;
       if (cudaGetDevice(&dev) != cudaSuccess ||
-          cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+          cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_tbp, kTBThreads,
+                                                        kTBPSmem) != cudaSuccess) {
         (void)cudaGetLastError();
         return 0;
       }
-      return n;
+      return per_sm >= 1 ? n : 0;
     }();
     for (const Group& g : groups) {
       zs = B.z0;
@@ -1313,7 +1327,7 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
         prof_begin(s, DTSGB_K_HFBS_SOLVE);
         if (maps.b && sms > 0)
           k_solve_tbp<<<gp, kTBThreads, kTBPSmem, s>>>(B.d_inst + g.first, g.count, (int)tiles,
-                                                        zd, hd, p.lambda, p.alpha, p.beta,
+                                                        zd, hs, hd, p.lambda, p.alpha, p.beta,
                                                         steps, maps);
         else
           k_solve_tb<<<gt, kTBThreads, kTBSmem, s>>>(B.d_inst + g.first, zs, zd, hs, hd, norm,
