@@ -374,6 +374,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT)
                    const CUtensorMap* __restrict__ tmaps) {
   constexpr int QW = TW / 4, TQ = TW + 4, RPP = NT / QW, NW = NT / 32;
   static_assert(TW % 32 == 0 && NT % TW == 0 && NW >= QW, "tile shape");
+  pdl_wait_then_release();  // launched as a dependent of the previous iteration
   extern __shared__ __align__(128) unsigned char smraw[];
   const Tile t = tiles[blockIdx.x];
   const Inst in = insts[t.inst];
@@ -1172,10 +1173,10 @@ static int launch_iter_shape(const DtsLaunch& L, const float* vin, float* vout,
   if (L.tma && L.h_inst && lay.sws <= 256 && lay.sr <= 256)
     tm = L.tma->get(L.h_inst, L.n_inst, vin, lay.sws, lay.sr, s);
   ProfScope ps(s, DTSGB_K_DTS_ITER);
-  k_dts_iter_vec<TS, MODE, TW, TH, NT, STEREO><<<L.n_tiles, NT, smem, s>>>(
-      L.d_inst, L.d_tiles, vin, vout, (const TS*)target, (const TS*)conf,
-      bounds, lambda, step, overwrite, hx, hy, sa, lay, tm);
-  DTSGB_CUDA(cudaGetLastError());
+  DTSGB_CUDA(launch_dependent(k_dts_iter_vec<TS, MODE, TW, TH, NT, STEREO>, dim3(L.n_tiles),
+                              dim3(NT), smem, s, L.d_inst, L.d_tiles, vin, vout,
+                              (const TS*)target, (const TS*)conf, bounds, lambda, step,
+                              overwrite, hx, hy, sa, lay, tm));
   return DTSGB_OK;
 }
 

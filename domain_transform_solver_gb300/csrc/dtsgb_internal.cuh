@@ -91,6 +91,36 @@ int cuda_fail(cudaError_t e, const char* what);
   } while (0)
 
 // ---------------------------------------------------------------------------
+// Programmatic dependent launch: a chain of kernels on one stream (solver
+// iterations, heavy-ball and bistochastization passes) launches each kernel
+// as a dependent of the one before it, so that its launch overlaps the
+// predecessor's last blocks.  Every such kernel starts with
+// pdl_wait_then_release(): it waits for the predecessor's grid to complete
+// (its writes visible) before touching memory, then lets its own dependent
+// launch.  In a plain launch both instructions are no-ops.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_wait_then_release() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block,
+                                    size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchAttribute a[1];
+  a[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  a[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t c = {};
+  c.gridDim = grid;
+  c.blockDim = block;
+  c.dynamicSmemBytes = smem;
+  c.stream = s;
+  c.attrs = a;
+  c.numAttrs = 1;
+  return cudaLaunchKernelEx(&c, kernel, static_cast<KArgs>(args)...);
+}
+
+// ---------------------------------------------------------------------------
 // Host helpers shared by the API translation units.
 // ---------------------------------------------------------------------------
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }

@@ -162,6 +162,7 @@ __global__ void k_hb_step_adj(const HInst* __restrict__ insts, const float* __re
                               const float* __restrict__ invA, float* __restrict__ gb,
                               float* __restrict__ ginv, float lambda, float alpha, float beta,
                               int finish, int step) {
+  pdl_wait_then_release();  // launched as a dependent of the previous step
   const HInst I = insts[blockIdx.y];
   const int gx = I.gx, gy = I.gy, gl = I.gl;
   const long long nv = (long long)gx * gy * gl;
@@ -316,21 +317,20 @@ int hfbs_enqueue_backward(const HfbsBatch& B, const HParams& p, const float* gou
   float* pg[2] = {G.gg, G.gg2};
   float* pw[2] = {G.gw, G.gw2};
   int cur = 0, launched = 0;
-  auto step_adj = [&](const float* zk) {
+  // the steps' launches are programmatic dependents of one another
+  auto step_adj = [&](const float* zk) -> int {
     const int fin = launched > 0, nx = cur ^ 1;
-    if (tb)
-      k_hb_step_adj<true><<<gv, kA, 0, s>>>(B.d_inst, zk, G.gz, G.gh, pg[cur], pw[cur], pg[nx],
-                                            pw[nx], norm, B.b, B.invA, G.gb, G.ginv,
-                                            p.lambda, p.alpha, p.beta, fin, 1);
-    else
-      k_hb_step_adj<false><<<gv, kA, 0, s>>>(B.d_inst, zk, G.gz, G.gh, pg[cur], pw[cur],
-                                             pg[nx], pw[nx], norm, B.b, B.invA, G.gb,
-                                             G.ginv, p.lambda, p.alpha, p.beta, fin, 1);
+    DTSGB_CUDA(launch_dependent(tb ? k_hb_step_adj<true> : k_hb_step_adj<false>, gv, dim3(kA),
+                                0, s, B.d_inst, zk, G.gz, G.gh, pg[cur], pw[cur], pg[nx],
+                                pw[nx], norm, B.b, B.invA, G.gb, G.ginv, p.lambda, p.alpha,
+                                p.beta, fin, 1));
     cur = nx;
     ++launched;
+    return DTSGB_OK;
   };
   if (S == 1) {
-    for (int k = K - 1; k >= 0; --k) step_adj(G.hist + (size_t)k * tv);
+    for (int k = K - 1; k >= 0; --k)
+      if (int st = step_adj(G.hist + (size_t)k * tv)) return st;
   } else {
     const int nseg = (K + S - 1) / S;
     for (int j = nseg - 1; j >= 0; --j) {
@@ -355,7 +355,8 @@ int hfbs_enqueue_backward(const HfbsBatch& B, const HParams& p, const float* gou
         hb ^= 1;
         k += steps;
       }
-      for (int k = end - 1; k >= start; --k) step_adj(zk(k));
+      for (int k = end - 1; k >= start; --k)
+        if (int st = step_adj(zk(k))) return st;
     }
   }
   if (launched > 0) {  // finish step 0

@@ -135,6 +135,7 @@ __global__ void k_fill_ones(float* __restrict__ a, long long n) {
 __global__ void k_bistoch(const HInst* __restrict__ insts,
                           const float* __restrict__ src, float* __restrict__ dst,
                           const float* __restrict__ count, float pad) {
+  pdl_wait_then_release();  // launched as a dependent of the previous pass
   const HInst I = insts[blockIdx.y];
   const int gx = I.gx, gy = I.gy, gl = I.gl;
   const float px = I.cov_x ? pad : 0.f, py = I.cov_y ? pad : 0.f,
@@ -542,6 +543,7 @@ __global__ void __launch_bounds__(kTBThreads, 1)
                  float* __restrict__ dst, const float* __restrict__ count, int it0,
                  int steps, const CUtensorMap* __restrict__ msrc,
                  const CUtensorMap* __restrict__ mcnt) {
+  pdl_wait_then_release();  // launched as a dependent of the previous pass
   extern __shared__ __align__(128) float tb_s[];
   float* Cs = tb_s + 2 * kTBPlane;  // counts of the block's columns
   unsigned long long* bar = reinterpret_cast<unsigned long long*>(tb_s + 3 * kTBPlane);
@@ -633,6 +635,7 @@ __global__ void __launch_bounds__(kTBThreads, 1)
                const float* __restrict__ invA, float lambda, float alpha, float beta,
                int steps, float* __restrict__ rec, long long rec_stride, int rec_steps,
                TBMaps m) {
+  pdl_wait_then_release();  // launched as a dependent of the previous pass
   extern __shared__ __align__(128) float tb_s[];
   float* Bs = tb_s;
   float* As = Bs + kTBPlane;
@@ -743,6 +746,7 @@ __global__ void __maxnreg__(kTBPRegs)
     k_solve_tbp(const HInst* __restrict__ insts, int n_inst, int tiles_max,
                 float* __restrict__ zd, const float* __restrict__ hs, float* __restrict__ hd,
                 float lambda, float alpha, float beta, int steps, TBMaps m) {
+  pdl_wait_then_release();  // launched as a dependent of the previous pass
   extern __shared__ __align__(128) float tb_s[];
   float* ZS = tb_s;                 // z, n of the block being staged
   float* Bs = tb_s + 2 * kTBPlane;  // b, invA of the current block
@@ -1203,9 +1207,10 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
         const CUtensorMap* mc = ms ? grid_map(B, B.count, s) : nullptr;
         if (!mc) ms = nullptr;
         prof_begin(s, DTSGB_K_HFBS_BISTOCH);
-        k_bistoch_tb<<<dim3((unsigned)tiles, g.count), kTBThreads, kTBBistochSmem, s>>>(
-            B.d_inst + g.first, src, dst, B.count, it0, steps, ms ? ms + g.first : nullptr,
-            mc ? mc + g.first : nullptr);
+        DTSGB_CUDA(launch_dependent(k_bistoch_tb, dim3((unsigned)tiles, g.count),
+                                    dim3(kTBThreads), kTBBistochSmem, s, B.d_inst + g.first,
+                                    src, dst, B.count, it0, steps, ms ? ms + g.first : nullptr,
+                                    mc ? mc + g.first : nullptr));
         prof_end(s, DTSGB_K_HFBS_BISTOCH);
         std::swap(src, dst);
         it0 += steps;
@@ -1213,8 +1218,8 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
     } else {
       for (int it = 0; it < p.bistoch_iter_max; ++it) {
         prof_begin(s, DTSGB_K_HFBS_BISTOCH);
-        k_bistoch<<<col_grid(g), kT, 0, s>>>(B.d_inst + g.first, src, dst, B.count,
-                                             (it % 2 == 0) ? 1.f : 0.f);
+        DTSGB_CUDA(launch_dependent(k_bistoch, col_grid(g), dim3(kT), 0, s, B.d_inst + g.first,
+                                    src, dst, B.count, (it % 2 == 0) ? 1.f : 0.f));
         prof_end(s, DTSGB_K_HFBS_BISTOCH);
         std::swap(src, dst);
       }
@@ -1326,13 +1331,14 @@ int hfbs_enqueue_solve(const HfbsBatch& B, const HParams& p, cudaStream_t s) {
         const TBMaps maps = tb_maps(B, g.first, zs, hs, norm, s);
         prof_begin(s, DTSGB_K_HFBS_SOLVE);
         if (maps.b && sms > 0)
-          k_solve_tbp<<<gp, kTBThreads, kTBPSmem, s>>>(B.d_inst + g.first, g.count, (int)tiles,
-                                                        zd, hs, hd, p.lambda, p.alpha, p.beta,
-                                                        steps, maps);
+          DTSGB_CUDA(launch_dependent(k_solve_tbp, dim3(gp), dim3(kTBThreads), kTBPSmem, s,
+                                      B.d_inst + g.first, g.count, (int)tiles, zd, hs, hd,
+                                      p.lambda, p.alpha, p.beta, steps, maps));
         else
-          k_solve_tb<<<gt, kTBThreads, kTBSmem, s>>>(B.d_inst + g.first, zs, zd, hs, hd, norm,
-                                                      B.b, B.invA, p.lambda, p.alpha, p.beta,
-                                                      steps, nullptr, 0, 0, maps);
+          DTSGB_CUDA(launch_dependent(k_solve_tb, gt, dim3(kTBThreads), kTBSmem, s,
+                                      B.d_inst + g.first, zs, zd, hs, hd, norm, B.b, B.invA,
+                                      p.lambda, p.alpha, p.beta, steps, (float*)nullptr, 0LL,
+                                      0, maps));
         prof_end(s, DTSGB_K_HFBS_SOLVE);
         std::swap(zs, zd);
         std::swap(hs, hd);
